@@ -1,0 +1,321 @@
+"""Synthetic problem setups with the shapes of the five benchmark configurations.
+
+Every setup is deterministic (config 4 draws from our own splitmix64 stream
+with seed 0x5EED2026).  Initial states follow the reference initialisers'
+semantics (init/InitTwoFluidShockTube.cpp, init/InitShockBubble.cpp,
+init/InitDropletAdvection.cpp, init/InitTriplePoint.cpp): per-region
+primitive states (alpha_0, alpha_rho_k, p, velocity) converted to the
+conservative vector with the stiffened-gas mixture EOS.
+
+Variable ids (models/FiveEq.h:35-50): 2D ID=0 IE=1 IU=2 IV=3 IA0=4 IAD0=5
+IA1=6 IAD1=7; 3D adds IW=4 and shifts the material ids by one.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .mesh import BC_PERIODIC, BC_WALL, BC_ZERO_GRADIENT, BlockMesh, BlockTable, cell_centers, concat_tables
+
+INTEGRATOR = {"HANCOCK": 0, "RK1": 1, "RK2_SSP": 2}
+SOURCE_TERM = {"ALLAIRE_KOKH": 0, "MILLER_PUCKETT": 1}
+INDICATOR = {"SIMPLE_GRADIENT": 0, "LOHNER_UNSPLIT": 1, "LOHNER_SPLIT": 2}
+
+
+def ids(dim: int) -> dict:
+    hc = 4 if dim == 2 else 5
+    d = {"ID": 0, "IE": 1, "IP": 1, "IU": 2, "IV": 3, "IA0": hc, "IAD0": hc + 1, "IA1": hc + 2, "IAD1": hc + 3, "NV": hc + 4}
+    d["IW"] = 4 if dim == 3 else 3
+    return d
+
+
+@dataclass
+class HydroParams:
+    """Scheme parameters (HydroSettings, THINCParams, time integrator, EOS, BCs)."""
+
+    dim: int = 2
+    bsize: int = 16
+    gamma: tuple = (1.4, 1.4)
+    pinf: tuple = (0.0, 0.0)
+    smallr: float = 1e-10  # models/HydroSettings.cpp:18-29 defaults
+    smallc: float = 1e-10
+    slope_type: float = 1.0
+    cfl: float = 0.5
+    integrator: int = 0  # HANCOCK
+    thinc: int = 0
+    thinc_beta: float = 1.6
+    thinc_eps: float = 1e-3
+    source_term: int = 0  # ALLAIRE_KOKH
+    prolongation: int = 0  # SIMPLE_COPY
+    bc: tuple = (BC_PERIODIC,) * 6
+    level_dx: np.ndarray = field(default_factory=lambda: np.zeros(32))
+
+
+def prim_to_cons(dim, params: HydroParams, a0, ar0, ar1, p, vel):
+    """Conservative vector [nv, ...] from primitive fields (stiffened-gas mixture)."""
+    I = ids(dim)
+    a0 = np.asarray(a0, dtype=np.float64)
+    shape = np.broadcast_shapes(a0.shape, np.shape(ar0), np.shape(ar1), np.shape(p), *[np.shape(v) for v in vel])
+    U = np.zeros((I["NV"],) + shape)
+    xi = [1.0 / (g - 1.0) for g in params.gamma]
+    gpx = [params.gamma[k] * params.pinf[k] * xi[k] for k in range(2)]
+    a1 = 1.0 - a0
+    S = a0 * xi[0] + a1 * xi[1]
+    PI = a0 * gpx[0] + a1 * gpx[1]
+    rho = ar0 + ar1
+    rhoe = p * S + PI
+    ek = 0.0
+    for v in vel:
+        ek = ek + v * v
+    U[I["ID"]] = rho
+    U[I["IE"]] = rhoe + 0.5 * rho * ek
+    U[I["IU"]] = rho * vel[0]
+    U[I["IV"]] = rho * vel[1]
+    if dim == 3:
+        U[I["IW"]] = rho * vel[2]
+    U[I["IA0"]] = a0
+    U[I["IAD0"]] = ar0
+    U[I["IA1"]] = a1
+    U[I["IAD1"]] = ar1
+    return U
+
+
+def _alloc_U(table: BlockTable) -> np.ndarray:
+    return np.zeros((table.n_total, table.nv, table.ncell), dtype=np.float64)
+
+
+def rankine_hugoniot(gamma, rho1, p1, mach):
+    """Post-shock state of a shock moving at Mach `mach` into gas at rest
+    (standard Rankine-Hugoniot relations, as in app/tools/moving_shock.py:79-163)."""
+    c1 = math.sqrt(gamma * p1 / rho1)
+    m2 = mach * mach
+    p2 = p1 * (1.0 + 2.0 * gamma / (gamma + 1.0) * (m2 - 1.0))
+    rho2 = rho1 * (gamma + 1.0) * m2 / ((gamma - 1.0) * m2 + 2.0)
+    u2 = c1 * 2.0 * (m2 - 1.0) / ((gamma + 1.0) * mach)
+    return rho2, p2, u2
+
+
+# ----------------------------------------------------------------------------
+# config 1: 2D gas-water two-fluid shock tube, 512x32 cells, 32x2 blocks of 16^2
+# ----------------------------------------------------------------------------
+def gas_water_shock_tube(bsize=16, nx_blocks=32, ny_blocks=2):
+    """Water (stiffened gas 4.4 / 6e8) at x<0.5 against air (ideal 1.4) at x>0.5."""
+    level = 1
+    trees_x = nx_blocks >> level
+    trees_y = max(1, ny_blocks >> level)
+    mesh = BlockMesh(2, bsize, (trees_x, trees_y), (False, True), level, level, scaling=1.0 / trees_x)
+    table = mesh.build()
+    params = HydroParams(
+        dim=2,
+        bsize=bsize,
+        gamma=(4.4, 1.4),
+        pinf=(6e8, 0.0),
+        slope_type=1.0,
+        cfl=0.4,
+        integrator=INTEGRATOR["HANCOCK"],
+        bc=(BC_ZERO_GRADIENT, BC_ZERO_GRADIENT, BC_PERIODIC, BC_PERIODIC, BC_PERIODIC, BC_PERIODIC),
+        level_dx=table.level_dx,
+    )
+    U = _alloc_U(table)
+    xc = cell_centers(mesh, table)
+    left = xc[:, 0] < 0.5
+    eps = 1e-6
+    a0 = np.where(left, 1.0 - eps, eps)
+    ar0 = a0 * 1000.0
+    ar1 = (1.0 - a0) * 50.0
+    p = np.where(left, 1e9, 1e5)
+    U[: table.n_owned] = np.moveaxis(prim_to_cons(2, params, a0, ar0, ar1, p, (0.0 * p, 0.0 * p)), 0, 1)
+    return mesh, table, params, U
+
+
+# ----------------------------------------------------------------------------
+# configs 2 / 3: 2D shock-bubble (air-helium, air-R22) on a 3-level block AMR
+# ----------------------------------------------------------------------------
+def _shock_bubble_prim(params, xc, dxf, bubble_gamma_rho, mach=1.22):
+    x, y = xc[:, 0], xc[:, 1]
+    eps = 1e-6
+    r = np.sqrt((x - 1.0) ** 2 + (y - 0.5) ** 2)
+    # alpha_bubble ramps over 2 finest cells around r = 0.25
+    phi = 0.5 * (1.0 - np.tanh((r - 0.25) / (2.0 * dxf)))
+    a_b = eps + (1.0 - 2.0 * eps) * phi
+    a0 = 1.0 - a_b  # material 0 = air
+    rho_b = bubble_gamma_rho[1]
+    rho2, p2, u2 = rankine_hugoniot(params.gamma[0], 1.0, 1.0, mach)
+    post = x < 0.6
+    ar0 = np.where(post, a0 * rho2, a0 * 1.0)
+    ar1 = np.where(post, (1.0 - a0) * rho_b * rho2, (1.0 - a0) * rho_b)
+    p = np.where(post, p2, 1.0)
+    u = np.where(post, u2, 0.0)
+    return a0, ar0, ar1, p, u
+
+
+def shock_bubble(bubble="helium", thinc=False, level_min=4, level_max=6, bsize=16, flag_fn=None, slope_type=1.0):
+    """Mach 1.22 shock in air hitting a helium (or R22) bubble; domain [0,4]x[0,1].
+
+    The mesh is refined from ``level_min`` by the refine flags evaluated on the
+    initial condition (``flag_fn(table, params, U, level_min, level_max) -> int8
+    flags``; SIMPLE_GRADIENT on alpha_rho_k, eps_refine 0.1, eps_coarsen
+    0.0125), level by level, with 2:1 balance; the mesh then stays fixed.
+    """
+    gb = {"helium": (1.648, 0.138), "r22": (1.249, 3.1538)}[bubble]
+    mesh = BlockMesh(2, bsize, (4, 1), (False, False), level_min, level_max, scaling=1.0)
+    params = HydroParams(
+        dim=2,
+        bsize=bsize,
+        gamma=(1.4, gb[0]),
+        pinf=(0.0, 0.0),
+        slope_type=slope_type,
+        cfl=0.4,
+        integrator=INTEGRATOR["HANCOCK"],
+        thinc=1 if thinc else 0,
+        thinc_beta=1.6,
+        thinc_eps=1e-3,
+        bc=(BC_ZERO_GRADIENT, BC_ZERO_GRADIENT, BC_WALL, BC_WALL, BC_PERIODIC, BC_PERIODIC),
+    )
+    dxf = mesh.cell_length(level_max)
+
+    def init(table):
+        params.level_dx = table.level_dx
+        U = _alloc_U(table)
+        xc = cell_centers(mesh, table)
+        a0, ar0, ar1, p, u = _shock_bubble_prim(params, xc, dxf, gb)
+        U[: table.n_owned] = np.moveaxis(prim_to_cons(2, params, a0, ar0, ar1, p, (u, 0.0 * u)), 0, 1)
+        return U
+
+    table, U = refine_from_initial_condition(mesh, params, init, flag_fn, level_min, level_max)
+    return mesh, table, params, U
+
+
+def refine_from_initial_condition(mesh, params, init, flag_fn, level_min, level_max):
+    """Static AMR: refine by flags on the analytic initial condition, one level
+    at a time, then 2:1 balance, until no block asks for refinement."""
+    table = mesh.build()
+    U = init(table)
+    if flag_fn is None:
+        return table, U
+    for _ in range(level_max - level_min):
+        flags = flag_fn(table, params, U, level_min, level_max)
+        keys = [
+            (int(table.level[n]),) + tuple(int(v) for v in table.coord[n])
+            for n in range(table.n_owned)
+            if flags[n] == 2
+        ]
+        if not keys:
+            break
+        mesh.refine(keys)
+        mesh.balance()
+        table = mesh.build()
+        U = init(table)
+    return table, U
+
+
+# ----------------------------------------------------------------------------
+# config 4: batched droplet advection instances
+# ----------------------------------------------------------------------------
+class SplitMix64:
+    """splitmix64 stream (Steele, Lea & Flood 2014); uniform doubles from the top 53 bits."""
+
+    MASK = (1 << 64) - 1
+
+    def __init__(self, seed: int):
+        self.state = seed & self.MASK
+
+    def next_u64(self) -> int:
+        self.state = (self.state + 0x9E3779B97F4A7C15) & self.MASK
+        z = self.state
+        z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & self.MASK
+        z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & self.MASK
+        return z ^ (z >> 31)
+
+    def uniform(self, lo=0.0, hi=1.0) -> float:
+        return lo + (hi - lo) * ((self.next_u64() >> 11) * (1.0 / (1 << 53)))
+
+
+def droplet_instances(n_inst=256, sides=(64, 128, 256, 512), bsize=16, seed=0x5EED2026):
+    """Independent periodic droplet-advection runs of uneven sizes in one table."""
+    rng = SplitMix64(seed)
+    tables, meshes, Us = [], [], []
+    params = HydroParams(
+        dim=2,
+        bsize=bsize,
+        gamma=(4.4, 1.4),
+        pinf=(6e8, 0.0),
+        slope_type=1.0,
+        cfl=0.4,
+        integrator=INTEGRATOR["HANCOCK"],
+        bc=(BC_PERIODIC,) * 6,
+    )
+    specs = []
+    for _ in range(n_inst):
+        side = sides[min(int(rng.uniform() * len(sides)), len(sides) - 1)]
+        radius = rng.uniform(0.15, 0.3)
+        u = rng.uniform(-1.0, 1.0)
+        v = rng.uniform(-1.0, 1.0)
+        specs.append((side, radius, u, v))
+    for side, radius, u, v in specs:
+        # one tree of unit length at level log2(side / bsize)
+        level = int(round(math.log2(side // bsize)))
+        mesh = BlockMesh(2, bsize, (1, 1), (True, True), level, level, scaling=1.0)
+        t = mesh.build()
+        # all instances share the level -> dx table of a unit tree
+        xc = cell_centers(mesh, t)
+        r = np.sqrt((xc[:, 0] - 0.5) ** 2 + (xc[:, 1] - 0.5) ** 2)
+        dx = mesh.cell_length(level)
+        phi = 0.5 * (1.0 - np.tanh((r - radius) / (2.0 * dx)))
+        eps = 1e-6
+        a0 = eps + (1.0 - 2.0 * eps) * phi  # material 0 = droplet (water)
+        ar0 = a0 * 1000.0
+        ar1 = (1.0 - a0) * 1.0
+        p = np.full_like(a0, 1e5)
+        Ui = np.zeros((t.n_total, t.nv, t.ncell))
+        Ui[: t.n_owned] = np.moveaxis(prim_to_cons(2, params, a0, ar0, ar1, p, (u + 0 * p, v + 0 * p)), 0, 1)
+        tables.append(t)
+        meshes.append(mesh)
+        Us.append(Ui)
+    table = concat_tables(tables)
+    params.level_dx = table.level_dx
+    U = np.concatenate([Ui[: t.n_owned] for Ui, t in zip(Us, tables)])
+    return meshes, table, params, U, specs
+
+
+# ----------------------------------------------------------------------------
+# config 5: 3D triple point
+# ----------------------------------------------------------------------------
+def triple_point_3d(level_min=0, level_max=3, bsize=8, nbrick=(14, 6, 3), scaling=0.5, thinc=True, flag_fn=None):
+    """Three-region triple-point problem on [0,7]x[0,3]x[0,1.5]."""
+    mesh = BlockMesh(3, bsize, nbrick, (False, False, False), level_min, level_max, scaling=scaling)
+    params = HydroParams(
+        dim=3,
+        bsize=bsize,
+        gamma=(1.5, 1.4),
+        pinf=(0.0, 0.0),
+        slope_type=1.0,
+        cfl=0.4,
+        integrator=INTEGRATOR["HANCOCK"],
+        thinc=1 if thinc else 0,
+        thinc_beta=1.6,
+        thinc_eps=1e-3,
+        bc=(BC_ZERO_GRADIENT,) * 6,
+    )
+
+    def init(table):
+        params.level_dx = table.level_dx
+        U = _alloc_U(table)
+        xc = cell_centers(mesh, table)
+        x, y = xc[:, 0], xc[:, 1]
+        eps = 1e-6
+        left = x < 1.0
+        top = (~left) & (y > 1.5)
+        a0 = np.where(top, eps, 1.0 - eps)
+        rho = np.where(left, 1.0, np.where(top, 0.125, 1.0))
+        p = np.where(left, 1.0, 0.1)
+        ar0 = a0 * rho
+        ar1 = (1.0 - a0) * rho
+        z = 0.0 * p
+        U[: table.n_owned] = np.moveaxis(prim_to_cons(3, params, a0, ar0, ar1, p, (z, z, z)), 0, 1)
+        return U
+
+    table, U = refine_from_initial_condition(mesh, params, init, flag_fn, level_min, level_max)
+    return mesh, table, params, U

@@ -1,0 +1,99 @@
+/*
+ * g5_oracle.h — CPU restatement of the godunov_five_eq per-block timestep.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the parity checker of the GPU
+ * path: only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg
+ * may load it.  The product (godunov_five_eq_gb300) never links or calls it.
+ *
+ * Parity status: partially pinned.  The HLLC solver and the
+ * conservative->primitive conversion are pinned against the reference's own
+ * header code (models/RiemannSolvers.h, models/utils.h) compiled from the
+ * reference tree with shim headers (oracle/refpin/), through golden vectors
+ * committed under tests/golden/.  The mixture EOS, the Youngs normal, the
+ * AMR stencil semantics (restriction / prolongation / face sibling sums),
+ * the cell length and tree ordering live in the external kalypsso core,
+ * which is not available; they are restated from published mathematics and
+ * are "parity unpinned".
+ *
+ * Layout of every conservative array U: [n_blocks][nv][b^dim] (cells x
+ * fastest), owned blocks first, then "outside" blocks (the reference's
+ * outside quadrants that carry the boundary conditions).
+ */
+#ifndef G5_ORACLE_H_
+#define G5_ORACLE_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct G5OParams
+{
+  int32_t dim;          /* 2 or 3 */
+  int32_t b;            /* cells per block edge (bx = by = bz) */
+  int32_t integrator;   /* 0 HANCOCK, 1 RK1 */
+  int32_t thinc;        /* 0 MUSCL, 1 THINC */
+  int32_t source_term;  /* 0 ALLAIRE_KOKH, 1 MILLER_PUCKETT */
+  int32_t prolongation; /* 0 SIMPLE_COPY */
+  int32_t bc[6];        /* per face (xmin,xmax,ymin,ymax,zmin,zmax): 0 NONE 1 PERIODIC 2 ZERO_GRADIENT 3 WALL */
+  double  gamma[2];
+  double  pinf[2];
+  double  smallr;
+  double  smallc;
+  double  slope_type;
+  double  cfl;
+  double  thinc_beta;
+  double  thinc_eps;
+  double  level_dx[32]; /* cell length per AMR level (already scaled) */
+} G5OParams;
+
+typedef struct G5OMesh
+{
+  int32_t         n_owned;
+  int32_t         n_outside;
+  int32_t         n_inst;     /* number of independent instances (>= 1) */
+  int32_t         pad;
+  const int32_t * level;      /* [n_total] */
+  const int32_t * coord;      /* [n_total*3] block coords at own level */
+  const int32_t * nbr;        /* [n_owned * 3^dim * 2^dim] */
+  const int8_t *  nbr_rel;    /* [n_owned * 3^dim] : -1 coarser, 0 same, +1 finer */
+  const int32_t * out_src;    /* [n_outside] inside block mirrored by each outside block */
+  const int8_t *  out_normal; /* [n_outside*3] outside direction per dim */
+  const int8_t *  out_border; /* [n_outside*6] inside block touches domain face f */
+  const int32_t * inst;       /* [n_total] instance id, NULL => 0 */
+} G5OMesh;
+
+/* whole-step API (one context per mesh) */
+void * g5o_create(const G5OMesh * mesh, const G5OParams * prm, int nthreads);
+void   g5o_destroy(void * ctx);
+/* U2 owned blocks <- one step of U; dt[inst] per instance.  returns 0 */
+int    g5o_step(void * ctx, const double * U, double * U2, const double * dt);
+/* max over owned cells of sum_d (c+|u_d|)/dx, per instance */
+int    g5o_inv_dt(void * ctx, const double * U, double * inv_dt);
+/* fill outside blocks of U from inside blocks (boundary conditions) */
+int    g5o_fill_outside(void * ctx, double * U);
+/* refine flags per owned block (int8: -1 init, 0 coarsen, 1 nothing, 2 refine) */
+int    g5o_refine_flags(void * ctx,
+                        const double * U,
+                        int            indicator, /* 0 SIMPLE_GRADIENT 1 LOHNER_UNSPLIT 2 LOHNER_SPLIT */
+                        double         eps_refine,
+                        double         eps_coarsen,
+                        double         eps_lohner,
+                        int            level_min,
+                        int            level_max,
+                        int8_t *       flags);
+
+/* point functions (used by the golden-vector pins) */
+double g5o_compute_primitives(const G5OParams * prm, const double * u, double * q);
+void   g5o_riemann_hllc(const G5OParams * prm, const double * qL, const double * qR, double * out);
+double g5o_slope(const G5OParams * prm, double q, double qp, double qm);
+double g5o_tanh(double x);
+double g5o_mixture_pressure(const G5OParams * prm, double rho, double eint, double a0);
+double g5o_mixture_sound_speed(const G5OParams * prm, double rho, double p, double a0);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

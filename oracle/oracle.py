@@ -1,0 +1,211 @@
+"""ctypes binding of the CPU oracle (test infrastructure only).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import
+this module; it is the checker, never the measured or shipped path.
+Parity status: partially pinned (see g5_oracle.h).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libg5oracle.so")
+
+
+def build(force: bool = False) -> str:
+    src = os.path.join(HERE, "g5_oracle.cpp")
+    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(src):
+        subprocess.run(["make", "-C", HERE, "-s"], check=True)
+    return LIB_PATH
+
+
+class G5OParams(ctypes.Structure):
+    _fields_ = [
+        ("dim", ctypes.c_int32),
+        ("b", ctypes.c_int32),
+        ("integrator", ctypes.c_int32),
+        ("thinc", ctypes.c_int32),
+        ("source_term", ctypes.c_int32),
+        ("prolongation", ctypes.c_int32),
+        ("bc", ctypes.c_int32 * 6),
+        ("gamma", ctypes.c_double * 2),
+        ("pinf", ctypes.c_double * 2),
+        ("smallr", ctypes.c_double),
+        ("smallc", ctypes.c_double),
+        ("slope_type", ctypes.c_double),
+        ("cfl", ctypes.c_double),
+        ("thinc_beta", ctypes.c_double),
+        ("thinc_eps", ctypes.c_double),
+        ("level_dx", ctypes.c_double * 32),
+    ]
+
+
+class G5OMesh(ctypes.Structure):
+    _fields_ = [
+        ("n_owned", ctypes.c_int32),
+        ("n_outside", ctypes.c_int32),
+        ("n_inst", ctypes.c_int32),
+        ("pad", ctypes.c_int32),
+        ("level", ctypes.c_void_p),
+        ("coord", ctypes.c_void_p),
+        ("nbr", ctypes.c_void_p),
+        ("nbr_rel", ctypes.c_void_p),
+        ("out_src", ctypes.c_void_p),
+        ("out_normal", ctypes.c_void_p),
+        ("out_border", ctypes.c_void_p),
+        ("inst", ctypes.c_void_p),
+    ]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB_PATH)
+        vp, dp = ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)
+        L.g5o_create.restype = vp
+        L.g5o_create.argtypes = [ctypes.POINTER(G5OMesh), ctypes.POINTER(G5OParams), ctypes.c_int]
+        L.g5o_destroy.argtypes = [vp]
+        L.g5o_step.argtypes = [vp, vp, vp, vp]
+        L.g5o_inv_dt.argtypes = [vp, vp, vp]
+        L.g5o_fill_outside.argtypes = [vp, vp]
+        L.g5o_refine_flags.argtypes = [vp, vp, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int, vp]
+        L.g5o_compute_primitives.restype = ctypes.c_double
+        L.g5o_compute_primitives.argtypes = [ctypes.POINTER(G5OParams), vp, vp]
+        L.g5o_riemann_hllc.argtypes = [ctypes.POINTER(G5OParams), vp, vp, vp]
+        L.g5o_slope.restype = ctypes.c_double
+        L.g5o_slope.argtypes = [ctypes.POINTER(G5OParams), ctypes.c_double, ctypes.c_double, ctypes.c_double]
+        L.g5o_tanh.restype = ctypes.c_double
+        L.g5o_tanh.argtypes = [ctypes.c_double]
+        L.g5o_mixture_pressure.restype = ctypes.c_double
+        L.g5o_mixture_pressure.argtypes = [ctypes.POINTER(G5OParams), ctypes.c_double, ctypes.c_double, ctypes.c_double]
+        L.g5o_mixture_sound_speed.restype = ctypes.c_double
+        L.g5o_mixture_sound_speed.argtypes = [ctypes.POINTER(G5OParams), ctypes.c_double, ctypes.c_double, ctypes.c_double]
+        _lib = L
+    return _lib
+
+
+def make_params(p) -> G5OParams:
+    """From a godunov_five_eq_gb300.configs.HydroParams-like object."""
+    o = G5OParams()
+    o.dim = p.dim
+    o.b = p.bsize
+    o.integrator = p.integrator
+    o.thinc = p.thinc
+    o.source_term = p.source_term
+    o.prolongation = p.prolongation
+    for i in range(6):
+        o.bc[i] = int(p.bc[i])
+    for k in range(2):
+        o.gamma[k] = p.gamma[k]
+        o.pinf[k] = p.pinf[k]
+    o.smallr = p.smallr
+    o.smallc = p.smallc
+    o.slope_type = p.slope_type
+    o.cfl = p.cfl
+    o.thinc_beta = p.thinc_beta
+    o.thinc_eps = p.thinc_eps
+    for i in range(32):
+        o.level_dx[i] = float(p.level_dx[i])
+    return o
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+class Oracle:
+    """One oracle context per (mesh, params)."""
+
+    def __init__(self, table, params, nthreads: int = 0):
+        self.table = table
+        self.params = params
+        self._keep = dict(
+            level=np.ascontiguousarray(table.level, np.int32),
+            coord=np.ascontiguousarray(table.coord, np.int32),
+            nbr=np.ascontiguousarray(table.nbr, np.int32),
+            nbr_rel=np.ascontiguousarray(table.nbr_rel, np.int8),
+            out_src=np.ascontiguousarray(table.out_src, np.int32),
+            out_normal=np.ascontiguousarray(table.out_normal, np.int8),
+            out_border=np.ascontiguousarray(table.out_border, np.int8),
+            inst=np.ascontiguousarray(table.inst, np.int32),
+        )
+        m = G5OMesh()
+        m.n_owned = table.n_owned
+        m.n_outside = table.n_outside
+        m.n_inst = table.n_inst
+        for k, v in self._keep.items():
+            setattr(m, k, _ptr(v))
+        self._mesh = m
+        self._prm = make_params(params)
+        self.ctx = lib().g5o_create(ctypes.byref(m), ctypes.byref(self._prm), int(nthreads))
+        if not self.ctx:
+            raise RuntimeError("g5o_create failed")
+
+    def close(self):
+        if self.ctx:
+            lib().g5o_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def fill_outside(self, U: np.ndarray) -> None:
+        assert U.dtype == np.float64 and U.flags.c_contiguous
+        lib().g5o_fill_outside(self.ctx, _ptr(U))
+
+    def inv_dt(self, U: np.ndarray) -> np.ndarray:
+        out = np.zeros(self.table.n_inst)
+        lib().g5o_inv_dt(self.ctx, _ptr(U), _ptr(out))
+        return out
+
+    def dt(self, U: np.ndarray) -> np.ndarray:
+        return self.params.cfl / self.inv_dt(U)
+
+    def step(self, U: np.ndarray, dt) -> np.ndarray:
+        """One do_time_step: returns U2 (owned blocks updated, outside blocks copied from U)."""
+        assert U.dtype == np.float64 and U.flags.c_contiguous
+        dt = np.ascontiguousarray(np.broadcast_to(np.asarray(dt, np.float64), (self.table.n_inst,)))
+        U2 = U.copy()
+        lib().g5o_step(self.ctx, _ptr(U), _ptr(U2), _ptr(dt))
+        return U2
+
+    def refine_flags(self, U, indicator=0, eps_refine=0.1, eps_coarsen=0.0125, eps_lohner=0.02, level_min=0, level_max=30):
+        flags = np.zeros(self.table.n_owned, np.int8)
+        lib().g5o_refine_flags(self.ctx, _ptr(U), int(indicator), eps_refine, eps_coarsen, eps_lohner, level_min, level_max, _ptr(flags))
+        return flags
+
+    def run(self, U: np.ndarray, nsteps: int, fill_first: bool = True):
+        """Solver loop of SolverGodunovFiveEq (HANCOCK/RK1): fill outside, dt, step."""
+        U = U.copy()
+        dts = []
+        for _ in range(nsteps):
+            self.fill_outside(U)
+            dt = self.dt(U)
+            dts.append(dt)
+            U = self.step(U, dt)
+        self.fill_outside(U)
+        return U, np.array(dts)
+
+
+def oracle_flag_fn(indicator=0, eps_refine=0.1, eps_coarsen=0.0125, eps_lohner=0.02):
+    """Refine-flag callback for configs.refine_from_initial_condition (tests only)."""
+
+    def fn(table, params, U, level_min, level_max):
+        o = Oracle(table, params)
+        o.fill_outside(U)
+        f = o.refine_flags(U, indicator, eps_refine, eps_coarsen, eps_lohner, level_min, level_max)
+        o.close()
+        return f
+
+    return fn
