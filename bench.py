@@ -1,0 +1,416 @@
+#!/usr/bin/env python
+"""Benchmark of the five-equation block timestep on GB300.
+
+Workload (default): the 2D air-helium shock-bubble on a 3-level block AMR
+(levels 4..6 of a 4x1 brick, 16x16 blocks, finest dx = 1/1024, refined from
+the initial condition by the SIMPLE_GRADIENT flags), synthetic data with the
+shape of the reference's shock-bubble deck.  One "step" is one solver step of
+the whole mesh: dt = cfl / inv_dt, the fused timestep kernel (+ coarse/fine
+reflux pass), the boundary fill and the fused CFL reduction, replayed from a
+CUDA graph (g5_advance).  The L2 cache (129 MB) is flushed before every timed
+step (the mesh state fits in L2), and steps are timed with CUDA events on the
+launching stream.
+
+value            mixed-precision cell-updates/s (all ranks, replicas)
+fp64_plain       the same for the FP64 reference method
+e2e              g5_step through the C ABI with host buffers: H2D of U, the
+                 step, D2H of U2 inside the timed region
+roofline         fused step kernel: 128 B/cell-update (read U + write U2,
+                 8 FP64 variables) / kernel time, against the measured HBM copy
+                 bandwidth of MEASURED_PEAKS.json
+cpu_baseline     the CPU oracle (FP64 restatement, OpenMP) on the host cores,
+                 bounded sample of the same workload
+
+--impl reference times the CPU restatement of the reference method (the
+reference's own Kokkos build cannot be built: its kalypsso core, Kokkos and
+p4est dependencies are absent) with all host threads.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "cell-updates/s, 1 GB300: mixed vs FP64 plain at L1 err<=1e-5 vs FP64; %HBM peak"
+BYTES_PER_CELL_2D = 2 * 8 * 8  # read U + write U2, 8 FP64 variables
+L1_STEPS = {"shock_bubble": 500, "gas_water": 200, "droplets": 100, "shock_bubble_r22_thinc": 500}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--workload", choices=list(L1_STEPS), default="shock_bubble")
+    ap.add_argument("--no-l1", action="store_true", help="skip the 500-step accuracy run")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    return ap.parse_args()
+
+
+def build_workload(name, flag_fn):
+    from godunov_five_eq_gb300 import configs
+
+    if name == "shock_bubble":
+        mesh, t, p, U = configs.shock_bubble("helium", thinc=False, flag_fn=flag_fn)
+        desc = "shock_bubble_air_helium_2d_amr_levels4-6_16x16"
+    elif name == "shock_bubble_r22_thinc":
+        mesh, t, p, U = configs.shock_bubble("r22", thinc=True, flag_fn=flag_fn)
+        desc = "shock_bubble_air_r22_thinc_2d_amr_levels4-6_16x16"
+    elif name == "gas_water":
+        mesh, t, p, U = configs.gas_water_shock_tube()
+        desc = "gas_water_shock_tube_2d_512x32_16x16"
+    else:
+        _, t, p, U, _ = configs.droplet_instances()
+        U = np.ascontiguousarray(U)
+        desc = "droplet_advection_2d_256_instances_16x16"
+    return desc, t, p, U
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE,
+                stderr=subprocess.DEVNULL,
+                text=True,
+            )
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = max(smax, float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(workload, mode):
+    """Per-launch DRAM bytes of the step kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", f"ncu_step2d_{workload}.md")
+    if not os.path.exists(path):
+        return None
+    m = re.search(rf"traffic_bytes_per_launch_{mode}:\s*([0-9.eE+]+)", open(path).read())
+    return float(m.group(1)) if m else None
+
+
+def cpu_baseline(t, p, U, max_seconds=20.0):
+    from oracle.oracle import Oracle
+
+    cores = os.cpu_count() or 1
+    o = Oracle(t, p, nthreads=cores)
+    A = U.copy()
+    o.fill_outside(A)
+    dt = o.dt(A)
+    A = o.step(A, dt)  # warm-up (first-touch of the work arrays)
+    n, t0 = 0, time.perf_counter()
+    while True:
+        o.fill_outside(A)
+        A = o.step(A, o.dt(A))
+        n += 1
+        el = time.perf_counter() - t0
+        if el > max_seconds / 4 or n >= 20:
+            break
+    cells = t.n_owned * t.ncell
+    o.close()
+    return {
+        "value": cells * n / el,
+        "unit": "cell-updates/s",
+        "cores": cores,
+        "kind": "port",
+        "sample": f"{n} solver steps (fill outside, dt reduction, step) of the same mesh, {cells} cells, FP64 oracle with OpenMP",
+    }
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    from oracle.oracle import Oracle, oracle_flag_fn
+
+    desc, t, p, U = build_workload(args.workload, oracle_flag_fn())
+    cores = os.cpu_count() or 1
+    o = Oracle(t, p, nthreads=cores)
+    A = U.copy()
+    for _ in range(max(args.warmup, 1)):
+        o.fill_outside(A)
+        A = o.step(A, o.dt(A))
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        o.fill_outside(A)
+        A = o.step(A, o.dt(A))
+    el = time.perf_counter() - t0
+    cells = t.n_owned * t.ncell
+    value = cells * args.steps / el
+    line = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": value,
+        "unit": "cell-updates/s",
+        "n_gpus": args.gpus,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": el / args.steps * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": desc, "blocks": int(t.n_owned), "cells": int(cells), "parallelism": "host threads"},
+        "cpu_baseline": {
+            "value": value,
+            "unit": "cell-updates/s",
+            "cores": cores,
+            "kind": "port",
+            "sample": f"{args.steps} solver steps of the full mesh ({cells} cells); CPU restatement of the reference method (the reference's Kokkos build is unavailable: kalypsso core, Kokkos and p4est are absent)",
+        },
+        "e2e": {"value": value, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def time_steps(impl, A, B, mode, steps, flush, stream):
+    """K solver steps, each timed alone after an L2 flush; returns (total ms, launches, A, B)."""
+    import torch
+
+    total, launches = 0.0, 0
+    for _ in range(steps):
+        flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        impl.advance(A, B, mode, stream=stream)
+        e1.record(stream)
+        launches += impl.last_launch_count()
+        e1.synchronize()
+        total += e0.elapsed_time(e1)
+        A, B = B, A
+    return total, launches, A, B
+
+
+def time_kernel(impl, A, B, d_dt, mode, steps, flush, stream):
+    """The fused step kernel alone (g5_step_dev), L2 flushed before each launch."""
+    import torch
+
+    ts = []
+    for _ in range(steps):
+        flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        impl.do_time_step_dev(A, B, d_dt, mode, stream=stream)
+        e1.record(stream)
+        e1.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    return float(np.mean(ts))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    import torch
+    import torch.distributed as dist
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from godunov_five_eq_gb300 import GodunovImplemGB300, gpu_flag_fn
+
+    desc, t, p, U = build_workload(args.workload, gpu_flag_fn())
+    cells = t.n_owned * t.ncell
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float64, device="cuda")  # 512 MB > L2
+    res = {}
+    for mode in ("fp64", "mixed"):
+        impl = GodunovImplemGB300(p, t)
+        A = torch.from_numpy(U.copy()).cuda()
+        B = torch.zeros_like(A)
+        impl.begin(A)
+        for _ in range(args.warmup):
+            impl.advance(A, B, mode)
+            A, B = B, A
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        sampler = ClockSampler(local) if mode == "mixed" else None
+        if sampler:
+            sampler.start()
+        total_ms, launches, A, B = time_steps(impl, A, B, mode, args.steps, flush, stream)
+        clocks = sampler.stop() if sampler else None
+        if world > 1:
+            tt = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            total_ms = float(tt.item())
+        d_dt = impl.compute_dt_local(A)
+        kern_ms = time_kernel(impl, A, B, d_dt, mode, max(5, min(args.steps, 20)), flush, stream)
+        res[mode] = dict(total_ms=total_ms, launches=launches, clocks=clocks, kern_ms=kern_ms, impl=impl)
+    value = world * cells * args.steps / (res["mixed"]["total_ms"] * 1e-3)
+    value64 = world * cells * args.steps / (res["fp64"]["total_ms"] * 1e-3)
+
+    # accuracy of the mixed path: L1 against the FP64 path after the config's step count
+    l1 = None
+    if not args.no_l1:
+        nst = L1_STEPS[args.workload]
+        outs = {}
+        for mode in ("fp64", "mixed"):
+            impl = res[mode]["impl"]
+            A = torch.from_numpy(U.copy()).cuda()
+            B = torch.zeros_like(A)
+            impl.run(A, B, nst, mode)
+            torch.cuda.synchronize()
+            outs[mode] = A.cpu().numpy()
+        from godunov_five_eq_gb300.metrics import l1_relative
+
+        errs = [float(e) for e in l1_relative(t, outs["mixed"], outs["fp64"])]
+        l1 = {"steps": nst, "max": max(errs), "per_variable": errs, "norm": "volume-weighted relative L1 (momentum by |rho u|)"}
+
+    # end to end through the C ABI: pinned host U -> device, g5_step (host dt), U2 -> pinned host
+    impl = res["mixed"]["impl"]
+    hU = torch.from_numpy(U.copy()).pin_memory()
+    hO = torch.empty_like(hU).pin_memory()
+    A = torch.empty_like(hU, device="cuda")
+    B = torch.zeros_like(A)
+    A.copy_(hU)
+    impl.fill_outside_quadrants(A)
+    hU.copy_(A.cpu())
+    dt_host = impl.compute_dt_local(A).cpu().numpy()
+    e2e_ms = 0.0
+    for k in range(args.warmup + args.steps):
+        flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        A.copy_(hU, non_blocking=True)
+        impl.do_time_step(A, B, dt_host, mode="mixed", stream=stream)
+        hO.copy_(B, non_blocking=True)
+        e1.record(stream)
+        e1.synchronize()
+        if k >= args.warmup:
+            e2e_ms += e0.elapsed_time(e1)
+    e2e = {
+        "value": world * cells * args.steps / (e2e_ms * 1e-3),
+        "unit": "cell-updates/s",
+        "h2d_bytes_per_step": int(hU.numel() * 8),
+        "d2h_bytes_per_step": int(hO.numel() * 8),
+    }
+    peak, peak_kind = measured_peaks()
+    kern_s = res["mixed"]["kern_ms"] * 1e-3
+    achieved = cells * BYTES_PER_CELL_2D / kern_s / 1e9
+    roofline = {
+        "bound": "hbm",
+        "achieved": achieved,
+        "peak": peak,
+        "unit": "GB/s",
+        "frac": achieved / peak,
+        "traffic": ncu_traffic(args.workload, "mixed"),
+        "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback 6.8 TB/s",
+        "kernel": "step2d_kernel<16,mixed> (+reflux2d)",
+        "kernel_ms": res["mixed"]["kern_ms"],
+        "algorithmic_bytes_per_launch": cells * BYTES_PER_CELL_2D,
+        "fp64_kernel_ms": res["fp64"]["kern_ms"],
+        "fp64_frac": cells * BYTES_PER_CELL_2D / (res["fp64"]["kern_ms"] * 1e-3) / 1e9 / peak,
+    }
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_baseline(t, p, U)
+    if rank == 0:
+        line = {
+            "metric": METRIC,
+            "value": value,
+            "unit": "cell-updates/s",
+            "n_gpus": world,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": res["mixed"]["total_ms"] / args.steps,
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f32+f64",
+            "data": "synthetic",
+            "config": {
+                "workload": desc,
+                "blocks": int(t.n_owned),
+                "outside_blocks": int(t.n_outside),
+                "cells": int(cells),
+                "blocks_per_level": {int(k): int(v) for k, v in enumerate(np.bincount(t.level[: t.n_owned])) if v},
+                "l2": "flushed (512 MB write) before every timed step",
+                "parallelism": "replicas" if world > 1 else "single GPU",
+            },
+            "fp64_plain": {"value": value64, "unit": "cell-updates/s", "ms_per_step": res["fp64"]["total_ms"] / args.steps},
+            "speedup_mixed_vs_fp64": value / value64,
+            "l1_err_vs_fp64": l1,
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "gpu_launches": int(res["mixed"]["launches"]),
+            "clocks": res["mixed"]["clocks"],
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

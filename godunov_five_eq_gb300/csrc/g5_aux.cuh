@@ -1,0 +1,257 @@
+// g5_aux.cuh — boundary fill of outside blocks, standalone CFL reduction,
+// refine flags and the device-side dt update of the solver loop.
+#pragma once
+
+#include "g5_common.cuh"
+
+namespace g5
+{
+
+// FillOutsideCellFunctor::operator() (border_conditions/FillOutside.cpp:71-170):
+// one thread per outside cell; the faces are visited in order and the last
+// face that applies wins (as in the reference's face loop).
+template <int DIM, int B>
+__global__ void
+fill_outside_kernel(double * U, DevMesh m, PhysParams P)
+{
+  using H = V<DIM>;
+  constexpr int NC = (DIM == 2) ? B * B : B * B * B;
+  const long    gid = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= (long)m.n_outside * NC)
+    return;
+  const int o = (int)(gid / NC), c = (int)(gid % NC);
+  const int nout = m.n_owned + o;
+  const int nin = m.out_src[o];
+  if (nin < 0 || nin >= m.n_owned)
+    return;
+  const int co[3] = { c % B, (c / B) % B, DIM == 3 ? c / (B * B) : 0 };
+  for (int face = 0; face < 2 * DIM; ++face)
+  {
+    const int dir = face >> 1;
+    if (!(m.out_border[o * 6 + face] && m.out_normal[o * 3 + dir] != 0))
+      continue;
+    const int bc = P.bc[face];
+    int       ci[3] = { co[0], co[1], co[2] };
+    if (bc == 2)
+      ci[dir] = (face & 1) ? B - 1 : 0;
+    else if (bc == 3)
+      ci[dir] = B - 1 - co[dir];
+    else
+      continue;
+    const int cin = ci[0] + B * (ci[1] + B * ci[2]);
+    for (int v = 0; v < H::NV; ++v)
+      U[((size_t)nout * H::NV + v) * NC + c] = U[((size_t)nin * H::NV + v) * NC + cin];
+    if (bc == 3)
+      U[((size_t)nout * H::NV + H::IU + dir) * NC + c] *= -1;
+  }
+}
+
+// ComputeDtFiveEqFunctor (scheme/ComputeDtFiveEqFunctor.cpp:87-134): one CTA
+// per block, block max, one atomic per CTA.
+template <int DIM, int B>
+__global__ void
+inv_dt_kernel(const double * U, DevMesh m, PhysParams P, double * invdt)
+{
+  using H = V<DIM>;
+  constexpr int NC = (DIM == 2) ? B * B : B * B * B;
+  __shared__ double sred[32];
+  for (int n = blockIdx.x; n < m.n_owned; n += gridDim.x)
+  {
+    const double dx = P.level_dx[m.level[n]];
+    double       mx = 0.0;
+    for (int c = threadIdx.x; c < NC; c += blockDim.x)
+    {
+      double u[H::NV], q[H::NQ];
+      for (int v = 0; v < H::NV; ++v)
+        u[v] = U[((size_t)n * H::NV + v) * NC + c];
+      const double cs = prim_fp64<DIM>(u, q, P);
+      const double vx = cs + fabs(q[H::QU]);
+      const double vy = cs + fabs(q[H::QV]);
+      if constexpr (DIM == 2)
+        mx = fmax(mx, vx / dx + vy / dx);
+      else
+        mx = fmax(mx, vx / dx + vy / dx + (cs + fabs(q[H::QW])) / dx);
+    }
+    for (int o = 16; o > 0; o >>= 1)
+      mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0)
+      sred[threadIdx.x >> 5] = mx;
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+      double mm = 0.0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w)
+        mm = fmax(mm, sred[w]);
+      atomic_max_pos(invdt + (m.inst ? m.inst[n] : 0), mm);
+    }
+    __syncthreads();
+  }
+}
+
+// dt = cfl / inv_dt per instance; inv_dt accumulator cleared for the next step
+__global__ void
+dt_update_kernel(double * invdt, double * dt, double * dt_hist, int n_inst, double cfl)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_inst)
+    return;
+  const double d = cfl / invdt[i];
+  dt[i] = d;
+  if (dt_hist)
+    dt_hist[i] = d;
+  invdt[i] = 0.0;
+}
+
+// ComputeRefineFlags (scheme/ComputeRefineFlags.cpp:66-368): value of the
+// same-level face neighbour of a cell (getNeighborDataSameLevel)
+template <int DIM, int B>
+__device__ double
+neighbor_same_level(const double * U, const DevMesh & m, int n, const int * cell, int dir, int side, int var)
+{
+  using H = V<DIM>;
+  constexpr int NC = (DIM == 2) ? B * B : B * B * B;
+  constexpr int NS = (DIM == 2) ? 9 : 27, NCH = (DIM == 2) ? 4 : 8;
+  auto          cidx = [](int x, int y, int z) { return x + B * (y + B * z); };
+  int           g[3] = { cell[0], cell[1], cell[2] };
+  g[dir] += side;
+  if (g[dir] >= 0 && g[dir] < B)
+    return U[((size_t)n * H::NV + var) * NC + cidx(g[0], g[1], g[2])];
+  int d[3] = { 0, 0, 0 }, v[3] = { g[0], g[1], g[2] };
+  d[dir] = side;
+  v[dir] = g[dir] - side * B;
+  const int s = (d[0] + 1) + 3 * (d[1] + 1) + (DIM == 3 ? 9 * (d[2] + 1) : 0);
+  const int rel = m.nbr_rel[n * NS + s];
+  const int * nb = m.nbr + (n * NS + s) * NCH;
+  const double here = U[((size_t)n * H::NV + var) * NC + cidx(cell[0], cell[1], cell[2])];
+  if (rel <= 0)
+  {
+    const int src = nb[0];
+    if (src < 0 || src >= m.n_owned)
+      return here; // outside the domain: value of the current cell
+    if (rel == 0)
+      return U[((size_t)src * H::NV + var) * NC + cidx(v[0], v[1], v[2])];
+    int cc[3] = { 0, 0, 0 };
+    for (int e = 0; e < DIM; ++e)
+      cc[e] = ((m.coord[n * 3 + e] + d[e]) & 1) * (B / 2) + (v[e] >> 1);
+    return U[((size_t)src * H::NV + var) * NC + cidx(cc[0], cc[1], cc[2])];
+  }
+  int f0[3] = { 0, 0, 0 }, ch[3] = { 0, 0, 0 };
+  for (int e = 0; e < DIM; ++e)
+  {
+    const int f = 2 * v[e];
+    ch[e] = f / B;
+    f0[e] = f - ch[e] * B;
+  }
+  const int F = nb[ch[0] + 2 * ch[1] + 4 * ch[2]];
+  if (F < 0 || F >= m.n_owned)
+    return here;
+  double sum = 0.0;
+  for (int oz = 0; oz < (DIM == 3 ? 2 : 1); ++oz)
+    for (int oy = 0; oy < 2; ++oy)
+      for (int ox = 0; ox < 2; ++ox)
+        sum += U[((size_t)F * H::NV + var) * NC + cidx(f0[0] + ox, f0[1] + oy, f0[2] + oz)];
+  return sum / (double)(1 << DIM);
+}
+
+__device__ __forceinline__ double
+normalized_gradient(double v1, double v2)
+{
+  double vmax = fmax(fabs(v1), fabs(v2));
+  if (vmax < 0.001)
+    return 0.0;
+  vmax = fabs(v1 - v2) / vmax;
+  return fmax(fmin(vmax, 1.0), 0.0);
+}
+
+template <int DIM, int B>
+__global__ void
+refine_flags_kernel(const double * U,
+                    DevMesh        m,
+                    int            indicator,
+                    double         eps_r,
+                    double         eps_c,
+                    double         eps_l,
+                    int            lmin,
+                    int            lmax,
+                    int8_t *       flags)
+{
+  using H = V<DIM>;
+  constexpr int NC = (DIM == 2) ? B * B : B * B * B;
+  __shared__ int sflag;
+  for (int n = blockIdx.x; n < m.n_owned; n += gridDim.x)
+  {
+    if (threadIdx.x == 0)
+      sflag = -1;
+    __syncthreads();
+    const int lev = m.level[n];
+    int       bflag = -1;
+    for (int c = threadIdx.x; c < NC; c += blockDim.x)
+    {
+      const int cell[3] = { c % B, (c / B) % B, DIM == 3 ? c / (B * B) : 0 };
+      int       flag = -1;
+      auto      update = [&](double ind) {
+        int f;
+        if (lev < lmax && ind > eps_r)
+          f = 2;
+        else if (lev > lmin && ind < eps_c)
+          f = 0;
+        else
+          f = 1;
+        flag = flag > f ? flag : f;
+      };
+      const int vars[2] = { H::IAD0, H::IAD1 };
+      if (indicator == 2)
+      {
+        for (int t = 0; t < 2; ++t)
+          for (int d = 0; d < DIM; ++d)
+          {
+            const double L = neighbor_same_level<DIM, B>(U, m, n, cell, d, -1, vars[t]);
+            const double R = neighbor_same_level<DIM, B>(U, m, n, cell, d, +1, vars[t]);
+            const double C = U[((size_t)n * H::NV + vars[t]) * NC + c];
+            update(fabs(L - 2 * C + R) / (fabs(R - C) + fabs(C - L) + eps_l * (fabs(L) + 2 * fabs(C) + fabs(R))));
+          }
+      }
+      else
+      {
+        for (int t = 0; t < 2; ++t)
+        {
+          const double C = U[((size_t)n * H::NV + vars[t]) * NC + c];
+          if (indicator == 1)
+          {
+            double num = 0.0, den = 0.0;
+            for (int d = 0; d < DIM; ++d)
+            {
+              const double L = neighbor_same_level<DIM, B>(U, m, n, cell, d, -1, vars[t]);
+              const double R = neighbor_same_level<DIM, B>(U, m, n, cell, d, +1, vars[t]);
+              const double aa = L - 2 * C + R;
+              num = d == 0 ? aa * aa : num + aa * aa;
+              const double tmp = fabs(R - C) + fabs(C - L) + eps_l * (fabs(L) + 2 * fabs(C) + fabs(R));
+              den = d == 0 ? tmp * tmp : den + tmp * tmp;
+            }
+            update(sqrt(num / den));
+          }
+          else
+          {
+            double res = -1.7976931348623157e308;
+            for (int d = 0; d < DIM; ++d)
+            {
+              const double L = neighbor_same_level<DIM, B>(U, m, n, cell, d, -1, vars[t]);
+              const double R = neighbor_same_level<DIM, B>(U, m, n, cell, d, +1, vars[t]);
+              res = fmax(res, normalized_gradient(C, L));
+              res = fmax(res, normalized_gradient(C, R));
+            }
+            update(res);
+          }
+        }
+      }
+      bflag = bflag > flag ? bflag : flag;
+    }
+    atomicMax(&sflag, bflag);
+    __syncthreads();
+    if (threadIdx.x == 0)
+      flags[n] = (int8_t)sflag;
+    __syncthreads();
+  }
+}
+
+} // namespace g5

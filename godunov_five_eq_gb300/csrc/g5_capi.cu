@@ -1,0 +1,627 @@
+// g5_capi.cu — the C ABI (include/g5gpu.h): context, block-table upload,
+// scratch sizing, launches, the graph-replayed solver loop and the autotuner.
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/g5gpu.h"
+#include "g5_launch.h"
+
+struct G5Context
+{
+  G5Params       prm;
+  g5::PhysParams phys;
+  int            dim = 2, b = 16, nv = 8, ns = 9, nch = 4;
+  int            device = 0;
+  bool           has_mesh = false;
+  int            n_owned = 0, n_outside = 0, n_total = 0, n_inst = 1;
+  int            n_defer = 0, n_reflux = 0;
+  // device block table
+  int32_t *d_level = nullptr, *d_coord = nullptr, *d_nbr = nullptr, *d_inst = nullptr;
+  int32_t *d_reflux_slot = nullptr, *d_defer_slot = nullptr, *d_defer_list = nullptr, *d_out_src = nullptr;
+  int8_t * d_nbr_rel = nullptr, *d_out_normal = nullptr, *d_out_border = nullptr;
+  // scratch
+  double *       d_reflux_buf = nullptr, *d_defer_buf = nullptr;
+  double *       d_dt = nullptr, *d_invdt = nullptr;
+  int *          d_step = nullptr;
+  unsigned int * d_status = nullptr;
+  int64_t        bytes = 0;
+  int            ctas_per_sm[2] = { 0, 0 };
+  int            last_launches = 0;
+  // cached one-step graphs of g5_advance
+  struct GraphSlot
+  {
+    cudaGraphExec_t exec = nullptr;
+    const void *    U = nullptr;
+    const void *    U2 = nullptr;
+    const void *    dt_out = nullptr;
+    int             mode = -1;
+    int             launches = 0;
+  };
+  static constexpr int kGraphs = 4;
+  GraphSlot            graphs[kGraphs];
+  int                  next_graph = 0;
+};
+
+namespace
+{
+
+template <typename T>
+int
+dev_alloc(G5Context * c, T ** p, size_t count)
+{
+  *p = nullptr;
+  if (count == 0)
+    return G5_OK;
+  if (cudaMalloc((void **)p, count * sizeof(T)) != cudaSuccess)
+    return G5_ERR_CUDA;
+  c->bytes += (int64_t)(count * sizeof(T));
+  return G5_OK;
+}
+
+template <typename T>
+int
+dev_upload(G5Context * c, T ** p, const T * host, size_t count)
+{
+  int rc = dev_alloc(c, p, count);
+  if (rc || count == 0)
+    return rc;
+  if (cudaMemcpy(*p, host, count * sizeof(T), cudaMemcpyHostToDevice) != cudaSuccess)
+    return G5_ERR_CUDA;
+  return G5_OK;
+}
+
+void
+drop_graphs(G5Context * c)
+{
+  for (auto & g : c->graphs)
+  {
+    if (g.exec)
+      cudaGraphExecDestroy(g.exec);
+    g = G5Context::GraphSlot();
+  }
+}
+
+void
+free_mesh(G5Context * c)
+{
+  void * ptrs[] = { c->d_level,       c->d_coord,       c->d_nbr,        c->d_inst,       c->d_reflux_slot,
+                    c->d_defer_slot,  c->d_defer_list,  c->d_out_src,    c->d_nbr_rel,    c->d_out_normal,
+                    c->d_out_border,  c->d_reflux_buf,  c->d_defer_buf,  c->d_dt,         c->d_invdt,
+                    c->d_step };
+  for (void * p : ptrs)
+    if (p)
+      cudaFree(p);
+  c->d_level = c->d_coord = c->d_nbr = c->d_inst = nullptr;
+  c->d_reflux_slot = c->d_defer_slot = c->d_defer_list = c->d_out_src = nullptr;
+  c->d_nbr_rel = c->d_out_normal = c->d_out_border = nullptr;
+  c->d_reflux_buf = c->d_defer_buf = c->d_dt = c->d_invdt = nullptr;
+  c->d_step = nullptr;
+  drop_graphs(c);
+  c->has_mesh = false;
+  c->bytes = c->d_status ? (int64_t)sizeof(unsigned int) : 0;
+}
+
+g5::DevMesh
+dev_mesh(const G5Context * c)
+{
+  g5::DevMesh m;
+  m.level = c->d_level;
+  m.coord = c->d_coord;
+  m.nbr = c->d_nbr;
+  m.nbr_rel = c->d_nbr_rel;
+  m.inst = c->d_inst;
+  m.reflux_slot = (c->n_defer > 0) ? c->d_reflux_slot : nullptr;
+  m.defer_slot = (c->n_defer > 0) ? c->d_defer_slot : nullptr;
+  m.defer_list = c->d_defer_list;
+  m.out_src = c->d_out_src;
+  m.out_normal = c->d_out_normal;
+  m.out_border = c->d_out_border;
+  m.n_owned = c->n_owned;
+  m.n_outside = c->n_outside;
+  m.n_total = c->n_total;
+  m.n_inst = c->n_inst;
+  m.n_defer = c->n_defer;
+  return m;
+}
+
+int
+do_step(G5Context * c, const double * U, double * U2, const double * d_dt, int mode, double * invdt, cudaStream_t s)
+{
+  if (!c || !c->has_mesh || !U || !U2 || !d_dt)
+    return G5_ERR_ARG;
+  if (mode != G5_MODE_FP64 && mode != G5_MODE_MIXED)
+    return G5_ERR_ARG;
+  if (!g5::step_supported(c->dim, c->b))
+    return G5_ERR_UNSUPPORTED;
+  g5::StepArgs a;
+  a.U = U;
+  a.U2 = U2;
+  a.dt = d_dt;
+  a.reflux_buf = c->d_reflux_buf;
+  a.defer_buf = c->d_defer_buf;
+  a.invdt = invdt;
+  a.status = c->d_status;
+  a.m = dev_mesh(c);
+  a.p = c->phys;
+  int         launches = 0;
+  cudaError_t e = mode == G5_MODE_FP64 ? g5::launch_step_fp64(c->dim, c->b, a, c->ctas_per_sm[0], s, &launches)
+                                       : g5::launch_step_mixed(c->dim, c->b, a, c->ctas_per_sm[1], s, &launches);
+  c->last_launches = launches;
+  return e == cudaSuccess ? G5_OK : G5_ERR_CUDA;
+}
+
+} // namespace
+
+extern "C" const char *
+g5_version(void)
+{
+  return "g5gpu 0.1 (sm_103a)";
+}
+
+extern "C" int
+g5_create(const G5Params * params, G5Context ** out_ctx)
+{
+  if (!params || !out_ctx)
+    return G5_ERR_ARG;
+  *out_ctx = nullptr;
+  if (params->dim != 2 && params->dim != 3)
+    return G5_ERR_ARG;
+  if (params->bsize < 4 || (params->bsize & 1))
+    return G5_ERR_ARG;
+  if (!g5::step_supported(params->dim, params->bsize))
+    return G5_ERR_UNSUPPORTED;
+  if (params->integrator != 0 && params->integrator != 1)
+    return G5_ERR_UNSUPPORTED;
+  if (params->source_term != 0 || params->prolongation != 0)
+    return G5_ERR_UNSUPPORTED;
+  for (int k = 0; k < 2; ++k)
+    if (!(params->gamma[k] > 1.0))
+      return G5_ERR_ARG;
+  G5Context * c = new G5Context;
+  c->prm = *params;
+  c->dim = params->dim;
+  c->b = params->bsize;
+  c->nv = params->dim == 2 ? 8 : 9;
+  c->ns = params->dim == 2 ? 9 : 27;
+  c->nch = params->dim == 2 ? 4 : 8;
+  cudaGetDevice(&c->device);
+  g5::PhysParams & p = c->phys;
+  p.smallr = params->smallr;
+  p.smallc = params->smallc;
+  p.smallp = params->smallc * params->smallc;
+  p.slope_type = params->slope_type;
+  for (int k = 0; k < 2; ++k)
+  {
+    p.gamma[k] = params->gamma[k];
+    p.pinf[k] = params->pinf[k];
+    p.xi[k] = 1.0 / (params->gamma[k] - 1.0);
+    p.gpx[k] = params->gamma[k] * params->pinf[k] * p.xi[k];
+  }
+  p.cfl = params->cfl;
+  p.thinc_beta = params->thinc_beta;
+  p.thinc_eps = params->thinc_eps;
+  p.integrator = params->integrator;
+  p.thinc = params->thinc;
+  for (int f = 0; f < 6; ++f)
+    p.bc[f] = params->bc[f];
+  for (int l = 0; l < 32; ++l)
+    p.level_dx[l] = params->level_dx[l];
+  if (cudaMalloc((void **)&c->d_status, sizeof(unsigned int)) != cudaSuccess ||
+      cudaMemset(c->d_status, 0, sizeof(unsigned int)) != cudaSuccess)
+  {
+    delete c;
+    return G5_ERR_CUDA;
+  }
+  c->bytes = sizeof(unsigned int);
+  *out_ctx = c;
+  return G5_OK;
+}
+
+extern "C" int
+g5_destroy(G5Context * ctx)
+{
+  if (!ctx)
+    return G5_ERR_ARG;
+  free_mesh(ctx);
+  if (ctx->d_status)
+    cudaFree(ctx->d_status);
+  delete ctx;
+  return G5_OK;
+}
+
+extern "C" int
+g5_set_mesh(G5Context * c, const G5Mesh * m)
+{
+  if (!c || !m || m->n_owned < 0 || m->n_outside < 0 || !m->level || !m->coord)
+    return G5_ERR_ARG;
+  if (m->n_owned > 0 && (!m->nbr || !m->nbr_rel))
+    return G5_ERR_ARG;
+  if (m->n_outside > 0 && (!m->out_src || !m->out_normal || !m->out_border))
+    return G5_ERR_ARG;
+  const int n_owned = m->n_owned, n_total = m->n_owned + m->n_outside;
+  const int n_inst = m->n_inst > 0 ? m->n_inst : 1;
+  const int ns = c->ns, nch = c->nch, dim = c->dim;
+  // ---- validate the table (the reference asserts these in StencilHelper / hashmap lookups)
+  for (int n = 0; n < n_total; ++n)
+    if (m->level[n] < 0 || m->level[n] > 31)
+      return G5_ERR_MESH;
+  if (m->inst)
+    for (int n = 0; n < n_total; ++n)
+      if (m->inst[n] < 0 || m->inst[n] >= n_inst)
+        return G5_ERR_MESH;
+  for (int n = 0; n < n_owned; ++n)
+    for (int s = 0; s < ns; ++s)
+    {
+      const int center = dim == 2 ? 4 : 13;
+      if (s == center)
+        continue;
+      const int   rel = m->nbr_rel[(size_t)n * ns + s];
+      const int * nb = m->nbr + ((size_t)n * ns + s) * nch;
+      if (rel < -1 || rel > 1)
+        return G5_ERR_MESH;
+      if (rel <= 0)
+      {
+        if (nb[0] < 0 || nb[0] >= n_total)
+          return G5_ERR_MESH;
+      }
+      else
+      {
+        const int d[3] = { s % 3 - 1, (s / 3) % 3 - 1, s / 9 - 1 };
+        for (int ch = 0; ch < nch; ++ch)
+        {
+          bool needed = true;
+          for (int e = 0; e < dim; ++e)
+          {
+            const int ce = (ch >> e) & 1;
+            if ((d[e] == -1 && ce != 1) || (d[e] == 1 && ce != 0))
+              needed = false;
+          }
+          if (needed && (nb[ch] < 0 || nb[ch] >= n_total))
+            return G5_ERR_MESH;
+          if (!needed && nb[ch] >= n_total)
+            return G5_ERR_MESH;
+        }
+      }
+    }
+  for (int o = 0; o < m->n_outside; ++o)
+    if (m->out_src[o] < 0 || m->out_src[o] >= n_owned)
+      return G5_ERR_MESH;
+
+  // ---- coarse/fine face records
+  const int            nfaces = 2 * dim;
+  std::vector<int32_t> reflux_slot((size_t)n_owned * nfaces, -1), defer_slot((size_t)n_owned * nfaces, -1), defer_list;
+  int                  n_reflux = 0, n_defer = 0;
+  for (int n = 0; n < n_owned; ++n)
+    for (int f = 0; f < nfaces; ++f)
+    {
+      int d[3] = { 0, 0, 0 };
+      d[f >> 1] = (f & 1) ? 1 : -1;
+      const int s = (d[0] + 1) + 3 * (d[1] + 1) + (dim == 3 ? 9 * (d[2] + 1) : 0);
+      const int rel = m->nbr_rel[(size_t)n * ns + s];
+      const int * nb = m->nbr + ((size_t)n * ns + s) * nch;
+      if (rel < 0 && nb[0] < n_owned)
+        reflux_slot[(size_t)n * nfaces + f] = n_reflux++;
+      if (rel > 0)
+      {
+        bool owned = true;
+        for (int ch = 0; ch < nch; ++ch)
+          if (nb[ch] >= n_owned)
+            owned = false;
+        if (owned)
+        {
+          defer_slot[(size_t)n * nfaces + f] = n_defer++;
+          defer_list.push_back(n * 8 + f);
+        }
+      }
+    }
+
+  free_mesh(c);
+  const size_t face_cells = dim == 2 ? (size_t)c->b : (size_t)c->b * c->b;
+  const size_t nf = dim == 2 ? 8 : 9;
+  int          rc = 0;
+  rc |= dev_upload(c, &c->d_level, m->level, (size_t)n_total);
+  rc |= dev_upload(c, &c->d_coord, m->coord, (size_t)n_total * 3);
+  rc |= dev_upload(c, &c->d_nbr, m->nbr, (size_t)n_owned * ns * nch);
+  rc |= dev_upload(c, &c->d_nbr_rel, m->nbr_rel, (size_t)n_owned * ns);
+  if (m->inst)
+    rc |= dev_upload(c, &c->d_inst, m->inst, (size_t)n_total);
+  if (m->n_outside > 0)
+  {
+    rc |= dev_upload(c, &c->d_out_src, m->out_src, (size_t)m->n_outside);
+    rc |= dev_upload(c, &c->d_out_normal, m->out_normal, (size_t)m->n_outside * 3);
+    rc |= dev_upload(c, &c->d_out_border, m->out_border, (size_t)m->n_outside * 6);
+  }
+  if (n_defer > 0)
+  {
+    rc |= dev_upload(c, &c->d_reflux_slot, reflux_slot.data(), reflux_slot.size());
+    rc |= dev_upload(c, &c->d_defer_slot, defer_slot.data(), defer_slot.size());
+    rc |= dev_upload(c, &c->d_defer_list, defer_list.data(), defer_list.size());
+    rc |= dev_alloc(c, &c->d_reflux_buf, (size_t)n_reflux * face_cells * nf);
+    rc |= dev_alloc(c, &c->d_defer_buf, (size_t)n_defer * face_cells * 2 * dim * nf);
+  }
+  rc |= dev_alloc(c, &c->d_dt, (size_t)n_inst);
+  rc |= dev_alloc(c, &c->d_invdt, (size_t)n_inst);
+  rc |= dev_alloc(c, &c->d_step, 1);
+  if (rc)
+  {
+    free_mesh(c);
+    return G5_ERR_CUDA;
+  }
+  c->n_owned = n_owned;
+  c->n_outside = m->n_outside;
+  c->n_total = n_total;
+  c->n_inst = n_inst;
+  c->n_defer = n_defer;
+  c->n_reflux = n_reflux;
+  c->has_mesh = true;
+  return G5_OK;
+}
+
+extern "C" int64_t
+g5_mem_bytes(const G5Context * ctx)
+{
+  return ctx ? ctx->bytes : (int64_t)G5_ERR_ARG;
+}
+
+extern "C" int
+g5_step_dev(G5Context * ctx, const double * d_U, double * d_U2, const double * d_dt, int mode, double * d_inv_dt_out, void * stream)
+{
+  return do_step(ctx, d_U, d_U2, d_dt, mode, d_inv_dt_out, (cudaStream_t)stream);
+}
+
+extern "C" int
+g5_step(G5Context * ctx, const double * d_U, double * d_U2, const double * dt_host, int mode, double * d_inv_dt_out, void * stream)
+{
+  if (!ctx || !ctx->has_mesh || !dt_host)
+    return G5_ERR_ARG;
+  for (int i = 0; i < ctx->n_inst; ++i)
+    if (!(dt_host[i] > 0.0))
+      return G5_ERR_ARG;
+  if (cudaMemcpyAsync(ctx->d_dt, dt_host, sizeof(double) * ctx->n_inst, cudaMemcpyHostToDevice, (cudaStream_t)stream) != cudaSuccess)
+    return G5_ERR_CUDA;
+  return do_step(ctx, d_U, d_U2, ctx->d_dt, mode, d_inv_dt_out, (cudaStream_t)stream);
+}
+
+extern "C" int
+g5_compute_inv_dt(G5Context * ctx, const double * d_U, double * d_inv_dt, void * stream)
+{
+  if (!ctx || !ctx->has_mesh || !d_U || !d_inv_dt)
+    return G5_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (cudaMemsetAsync(d_inv_dt, 0, sizeof(double) * ctx->n_inst, s) != cudaSuccess)
+    return G5_ERR_CUDA;
+  return g5::launch_inv_dt(ctx->dim, ctx->b, d_U, dev_mesh(ctx), ctx->phys, d_inv_dt, s) == cudaSuccess ? G5_OK : G5_ERR_CUDA;
+}
+
+extern "C" int
+g5_fill_outside(G5Context * ctx, double * d_U, void * stream)
+{
+  if (!ctx || !ctx->has_mesh || !d_U)
+    return G5_ERR_ARG;
+  return g5::launch_fill_outside(ctx->dim, ctx->b, d_U, dev_mesh(ctx), ctx->phys, (cudaStream_t)stream) == cudaSuccess ? G5_OK
+                                                                                                                    : G5_ERR_CUDA;
+}
+
+extern "C" int
+g5_refine_flags(G5Context * ctx,
+                const double * d_U,
+                int            indicator,
+                double         eps_refine,
+                double         eps_coarsen,
+                double         eps_lohner,
+                int            level_min,
+                int            level_max,
+                int8_t *       d_flags,
+                void *         stream)
+{
+  if (!ctx || !ctx->has_mesh || !d_U || !d_flags || indicator < 0 || indicator > 2)
+    return G5_ERR_ARG;
+  return g5::launch_refine_flags(ctx->dim, ctx->b, d_U, dev_mesh(ctx), indicator, eps_refine, eps_coarsen, eps_lohner, level_min,
+                                 level_max, d_flags, (cudaStream_t)stream) == cudaSuccess
+           ? G5_OK
+           : G5_ERR_CUDA;
+}
+
+namespace
+{
+// one step of the device-driven solver loop: dt <- cfl / inv_dt(U); U2 <- step(U); fill outside of U2
+int
+loop_step(G5Context * c, const double * U, double * U2, int mode, double * dt_out, cudaStream_t s, int * launches)
+{
+  if (g5::launch_dt_update(c->d_invdt, c->d_dt, dt_out, c->n_inst, c->phys.cfl, s) != cudaSuccess)
+    return G5_ERR_CUDA;
+  ++*launches;
+  int rc = do_step(c, U, U2, c->d_dt, mode, c->d_invdt, s);
+  if (rc)
+    return rc;
+  *launches += c->last_launches;
+  if (c->n_outside > 0)
+  {
+    if (g5::launch_fill_outside(c->dim, c->b, U2, dev_mesh(c), c->phys, s) != cudaSuccess)
+      return G5_ERR_CUDA;
+    ++*launches;
+  }
+  return G5_OK;
+}
+} // namespace
+
+extern "C" int
+g5_begin(G5Context * c, double * d_U, void * stream)
+{
+  if (!c || !c->has_mesh || !d_U)
+    return G5_ERR_ARG;
+  int rc = g5_fill_outside(c, d_U, stream);
+  if (rc)
+    return rc;
+  rc = g5_compute_inv_dt(c, d_U, c->d_invdt, stream);
+  c->last_launches = 2;
+  return rc;
+}
+
+extern "C" int
+g5_advance(G5Context * c, const double * d_U, double * d_U2, int mode, double * d_dt_out, void * stream)
+{
+  if (!c || !c->has_mesh || !d_U || !d_U2 || d_U == d_U2)
+    return G5_ERR_ARG;
+  if (mode != G5_MODE_FP64 && mode != G5_MODE_MIXED)
+    return G5_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  // cached graph of one loop step for (U, U2, mode, dt_out)
+  G5Context::GraphSlot * slot = nullptr;
+  for (auto & g : c->graphs)
+    if (g.exec && g.U == d_U && g.U2 == d_U2 && g.mode == mode && g.dt_out == d_dt_out)
+      slot = &g;
+  if (!slot)
+  {
+    slot = &c->graphs[c->next_graph];
+    c->next_graph = (c->next_graph + 1) % G5Context::kGraphs;
+    if (slot->exec)
+    {
+      cudaGraphExecDestroy(slot->exec);
+      slot->exec = nullptr;
+    }
+    cudaStream_t cap;
+    if (cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking) != cudaSuccess)
+      return G5_ERR_CUDA;
+    int         n = 0;
+    cudaGraph_t g = nullptr;
+    if (cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+    {
+      cudaStreamDestroy(cap);
+      return G5_ERR_CUDA;
+    }
+    int         rc = loop_step(c, d_U, d_U2, mode, d_dt_out, cap, &n);
+    cudaError_t e = cudaStreamEndCapture(cap, &g);
+    cudaStreamDestroy(cap);
+    if (rc || e != cudaSuccess)
+    {
+      if (g)
+        cudaGraphDestroy(g);
+      return rc ? rc : G5_ERR_CUDA;
+    }
+    e = cudaGraphInstantiate(&slot->exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess)
+    {
+      slot->exec = nullptr;
+      return G5_ERR_CUDA;
+    }
+    slot->U = d_U;
+    slot->U2 = d_U2;
+    slot->mode = mode;
+    slot->dt_out = d_dt_out;
+    slot->launches = n;
+  }
+  if (cudaGraphLaunch(slot->exec, s) != cudaSuccess)
+    return G5_ERR_CUDA;
+  c->last_launches = slot->launches;
+  return G5_OK;
+}
+
+extern "C" int
+g5_run(G5Context * c, double * d_U, double * d_U2, int nsteps, int mode, double * d_dt_hist, void * stream)
+{
+  if (!c || !c->has_mesh || !d_U || !d_U2 || nsteps < 0)
+    return G5_ERR_ARG;
+  if (mode != G5_MODE_FP64 && mode != G5_MODE_MIXED)
+    return G5_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  int          rc = g5_begin(c, d_U, stream);
+  if (rc)
+    return rc;
+  int launches = 2;
+  for (int k = 0; k < nsteps; ++k)
+  {
+    double * A = (k & 1) ? d_U2 : d_U;
+    double * B = (k & 1) ? d_U : d_U2;
+    if (d_dt_hist)
+      rc = loop_step(c, A, B, mode, d_dt_hist + (size_t)k * c->n_inst, s, &launches);
+    else
+    {
+      rc = g5_advance(c, A, B, mode, nullptr, stream);
+      launches += c->last_launches;
+    }
+    if (rc)
+      return rc;
+  }
+  if (nsteps & 1)
+  {
+    // the final state is in U2: copy it back so that d_U holds it
+    const size_t bytes = (size_t)c->n_total * c->nv * (c->dim == 2 ? c->b * c->b : c->b * c->b * c->b) * sizeof(double);
+    if (cudaMemcpyAsync(d_U, d_U2, bytes, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+      return G5_ERR_CUDA;
+  }
+  c->last_launches = launches;
+  return G5_OK;
+}
+
+extern "C" int
+g5_status(G5Context * ctx, void * stream)
+{
+  if (!ctx)
+    return G5_ERR_ARG;
+  unsigned int h = 0;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (cudaMemcpyAsync(&h, ctx->d_status, sizeof(h), cudaMemcpyDeviceToHost, s) != cudaSuccess)
+    return G5_ERR_CUDA;
+  if (cudaMemsetAsync(ctx->d_status, 0, sizeof(unsigned int), s) != cudaSuccess)
+    return G5_ERR_CUDA;
+  if (cudaStreamSynchronize(s) != cudaSuccess)
+    return G5_ERR_CUDA;
+  return (int)h;
+}
+
+extern "C" int
+g5_tune(G5Context * c, const double * d_U, double * d_U2, int mode, void * stream)
+{
+  if (!c || !c->has_mesh || !d_U || !d_U2 || (mode != G5_MODE_FP64 && mode != G5_MODE_MIXED))
+    return G5_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  const int    occ = mode == G5_MODE_FP64 ? g5::step_max_ctas_per_sm_fp64(c->dim, c->b) : g5::step_max_ctas_per_sm_mixed(c->dim, c->b);
+  if (occ <= 0)
+    return G5_ERR_UNSUPPORTED;
+  // dt from the state itself
+  int rc = g5_compute_inv_dt(c, d_U, c->d_invdt, stream);
+  if (rc)
+    return rc;
+  if (g5::launch_dt_update(c->d_invdt, c->d_dt, nullptr, c->n_inst, c->phys.cfl, s) != cudaSuccess)
+    return G5_ERR_CUDA;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 1e30f;
+  int   best_k = occ;
+  for (int k = 1; k <= occ; ++k)
+  {
+    c->ctas_per_sm[mode] = k;
+    rc = do_step(c, d_U, d_U2, c->d_dt, mode, nullptr, s); // warm-up
+    if (rc)
+      break;
+    cudaEventRecord(e0, s);
+    for (int r = 0; r < 3; ++r)
+      do_step(c, d_U, d_U2, c->d_dt, mode, nullptr, s);
+    cudaEventRecord(e1, s);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best)
+    {
+      best = ms;
+      best_k = k;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  c->ctas_per_sm[mode] = best_k;
+  drop_graphs(c);
+  return rc ? rc : best_k;
+}
+
+extern "C" int
+g5_last_launch_count(const G5Context * ctx)
+{
+  return ctx ? ctx->last_launches : G5_ERR_ARG;
+}

@@ -1,0 +1,500 @@
+// g5_common.cuh — shared device types and the per-cell physics of the
+// five-equation model (FP64 form and the FP32-bulk form).
+//
+// The FP64 functions evaluate every expression in the same order as the
+// reference (and the translation unit is compiled with --fmad=false), so the
+// FP64 path reproduces the reference method bit for bit on identical inputs.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace g5
+{
+
+// ---------------------------------------------------------------------------
+// parameters and block table passed by value to every kernel
+// ---------------------------------------------------------------------------
+struct PhysParams
+{
+  double smallr, smallc, smallp, slope_type;
+  double gamma[2], pinf[2];
+  double xi[2];  // 1/(gamma_k - 1)
+  double gpx[2]; // gamma_k pinf_k xi_k
+  double cfl, thinc_beta, thinc_eps;
+  int    integrator; // 0 HANCOCK, 1 RK1
+  int    thinc;      // 0 MUSCL, 1 THINC
+  int    bc[6];
+  double level_dx[32];
+};
+
+struct DevMesh
+{
+  const int32_t * level;
+  const int32_t * coord;       // [n_total*3]
+  const int32_t * nbr;         // [n_owned * NS * NC]
+  const int8_t *  nbr_rel;     // [n_owned * NS]
+  const int32_t * inst;        // [n_total]
+  const int32_t * reflux_slot; // [n_owned * 2*dim] slot in reflux_buf, or -1
+  const int32_t * defer_slot;  // [n_owned * 2*dim] slot in defer_buf, or -1
+  const int32_t * defer_list;  // [n_defer_slots] (block*8 + face) of each deferred record
+  const int32_t * out_src;     // [n_outside]
+  const int8_t *  out_normal;  // [n_outside*3]
+  const int8_t *  out_border;  // [n_outside*6]
+  int             n_owned, n_outside, n_total, n_inst;
+  int             n_defer;
+};
+
+struct StepArgs
+{
+  const double * U;
+  double *       U2;
+  const double * dt;         // [n_inst] on the device
+  double *       reflux_buf; // fine-block face fluxes at coarse/fine faces
+  double *       defer_buf;  // own face fluxes of coarse cells next to finer faces
+  double *       invdt;      // [n_inst] (bit-pattern max), may be null
+  unsigned int * status;
+  DevMesh        m;
+  PhysParams     p;
+};
+
+constexpr unsigned STATUS_NONPHYSICAL = 1u;
+constexpr unsigned STATUS_MESH = 2u;
+
+// variable ids (models/FiveEq.h:35-50)
+template <int DIM>
+struct V
+{
+  static constexpr int ID = 0, IE = 1, IP = 1, IU = 2, IV = 3;
+  static constexpr int IW = (DIM == 2) ? 3 : 4;
+  static constexpr int HC = IW + 1;
+  static constexpr int IA0 = HC, IAD0 = HC + 1, IA1 = HC + 2, IAD1 = HC + 3;
+  static constexpr int NV = HC + 4;
+  // primitive components kept in shared memory: r0 r1 p u v (w) alpha0
+  static constexpr int QR0 = 0, QR1 = 1, QP = 2, QU = 3, QV = 4, QW = 5;
+  static constexpr int NR = (DIM == 2) ? 5 : 6; // reconstructed components
+  static constexpr int QA = NR;                 // alpha0
+  static constexpr int NQ = NR + 1;
+  // face record: r0 r1 a0 a1 e u v (w) ustar  (already multiplied by dt/dx)
+  static constexpr int FR0 = 0, FR1 = 1, FA0 = 2, FA1 = 3, FE = 4, FU = 5, FV = 6, FW = 7;
+  static constexpr int FUS = (DIM == 2) ? 7 : 8;
+  static constexpr int NF = FUS + 1;
+};
+
+__device__ __forceinline__ void
+raise_status(unsigned int * st, unsigned bits)
+{
+  atomicOr(st, bits);
+}
+
+// positive doubles order like their bit patterns: max by integer atomic
+__device__ __forceinline__ void
+atomic_max_pos(double * addr, double v)
+{
+  if (!(v > 0.0))
+    return;
+  atomicMax(reinterpret_cast<unsigned long long *>(addr), (unsigned long long)__double_as_longlong(v));
+}
+
+// ---------------------------------------------------------------------------
+// Stiffened-gas mixture EOS (restated, see the oracle for the formulas)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double
+eosS(const PhysParams & P, double a0, double a1)
+{
+  return a0 * P.xi[0] + a1 * P.xi[1];
+}
+__device__ __forceinline__ double
+eosPI(const PhysParams & P, double a0, double a1)
+{
+  return a0 * P.gpx[0] + a1 * P.gpx[1];
+}
+__device__ __forceinline__ double
+sound_speed_d(const PhysParams & P, double rho, double p, double a0, double a1)
+{
+  const double S = eosS(P, a0, a1);
+  const double c2 = (p * (S + 1.0) + eosPI(P, a0, a1)) / (rho * S);
+  return sqrt(fmax(c2, 0.0));
+}
+
+__device__ __forceinline__ float
+sound_speed_f(float xi0, float xi1, float gp0, float gp1, float rho, float p, float a0)
+{
+  const float a1 = 1.0f - a0;
+  const float S = a0 * xi0 + a1 * xi1;
+  const float PI = a0 * gp0 + a1 * gp1;
+  const float c2 = __fdividef(p * (S + 1.0f) + PI, rho * S);
+  return sqrtf(fmaxf(c2, 0.0f));
+}
+
+// ---------------------------------------------------------------------------
+// conservative (FP64) -> primitive, models/utils.h:200-250 (computePrimitives)
+// q[] receives the shared-memory components (r0 r1 p u v (w) alpha0).
+// Returns the mixture sound speed c; ux/uy/uz are the velocities.
+// ---------------------------------------------------------------------------
+template <int DIM>
+__device__ __forceinline__ double
+prim_fp64(const double * u, double * q, const PhysParams & P)
+{
+  using H = V<DIM>;
+  const double d = fmax(u[H::ID], P.smallr);
+  const double ux = u[H::IU] / d;
+  const double uy = u[H::IV] / d;
+  double       ekin;
+  double       uz = 0.0;
+  if constexpr (DIM == 2)
+    ekin = 0.5 * (ux * ux + uy * uy);
+  else
+  {
+    uz = u[H::IW] / d;
+    ekin = 0.5 * (ux * ux + uy * uy + uz * uz);
+  }
+  const double eint = u[H::IE] / d - ekin;
+  const double a0u = u[H::IA0];
+  const double p = (d * eint - eosPI(P, a0u, 1.0 - a0u)) / eosS(P, a0u, 1.0 - a0u);
+  double       a0 = fmax(0.0, fmin(1.0, a0u));
+  double       r0 = u[H::IAD0], r1 = u[H::IAD1];
+  const double eps = 1e-12;
+  if (r0 < eps)
+    r0 = 0.0;
+  if (r1 < eps)
+    r1 = 0.0;
+  if (a0 < eps)
+    a0 = 0.0;
+  if (a0 > 1.0 - eps)
+    a0 = 1.0;
+  q[H::QR0] = r0;
+  q[H::QR1] = r1;
+  q[H::QP] = p;
+  q[H::QU] = ux;
+  q[H::QV] = uy;
+  if constexpr (DIM == 3)
+    q[H::QW] = uz;
+  q[H::QA] = a0;
+  return sound_speed_d(P, d, p, a0, 1.0 - a0);
+}
+
+// FP32-bulk form: FP64 only for the pressure numerator rho e - PI, where the
+// stiffened-gas constant cancels against the internal energy.
+template <int DIM>
+__device__ __forceinline__ void
+prim_mixed(const double * u, float * q, const PhysParams & P)
+{
+  using H = V<DIM>;
+  const float d = fmaxf((float)u[H::ID], (float)P.smallr);
+  const float inv = __frcp_rn(d);
+  const float ux = (float)u[H::IU] * inv;
+  const float uy = (float)u[H::IV] * inv;
+  float       k2 = ux * ux + uy * uy;
+  float       uz = 0.0f;
+  if constexpr (DIM == 3)
+  {
+    uz = (float)u[H::IW] * inv;
+    k2 += uz * uz;
+  }
+  const double a0u = u[H::IA0];
+  const double a1u = 1.0 - a0u;
+  const double num = (u[H::IE] - (double)(0.5f * d * k2)) - (a0u * P.gpx[0] + a1u * P.gpx[1]);
+  const float  S = (float)a0u * (float)P.xi[0] + (float)a1u * (float)P.xi[1];
+  const float  p = __fdividef((float)num, S);
+  float        a0 = fmaxf(0.0f, fminf(1.0f, (float)a0u));
+  float        r0 = (float)u[H::IAD0], r1 = (float)u[H::IAD1];
+  const float  eps = 1e-12f;
+  if (r0 < eps)
+    r0 = 0.0f;
+  if (r1 < eps)
+    r1 = 0.0f;
+  if (a0 < eps)
+    a0 = 0.0f;
+  if (a0 > 1.0f - eps)
+    a0 = 1.0f;
+  q[H::QR0] = r0;
+  q[H::QR1] = r1;
+  q[H::QP] = p;
+  q[H::QU] = ux;
+  q[H::QV] = uy;
+  if constexpr (DIM == 3)
+    q[H::QW] = uz;
+  q[H::QA] = a0;
+}
+
+// scheme/ComputeLimitedSlopesFunctor.cpp:116-137
+template <typename R>
+__device__ __forceinline__ R
+slope_scalar(R q, R qPlus, R qMinus, R slope_type)
+{
+  R dq = R(0);
+  if (slope_type == R(1) || slope_type == R(2))
+  {
+    const R dlft = slope_type * (q - qMinus);
+    const R drgt = slope_type * (qPlus - q);
+    const R dcen = R(0.5) * (qPlus - qMinus);
+    const R dsgn = (dcen >= R(0)) ? R(1) : R(-1);
+    const R slop = fmin(fabs(dlft), fabs(drgt));
+    const R dlim = (dlft * drgt) <= R(0) ? R(0) : slop;
+    dq = dsgn * fmin(dlim, fabs(dcen));
+  }
+  return dq;
+}
+
+// ---------------------------------------------------------------------------
+// tanh: same algorithm as the oracle (Cody-Waite reduced Taylor expm1),
+// FP64, bit-reproducible on IEEE hardware without contraction.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double
+expm1_small_d(double r)
+{
+  const double c[17] = { 1.0,
+                         1.0,
+                         0.5,
+                         0.16666666666666666,
+                         0.041666666666666664,
+                         0.008333333333333333,
+                         0.001388888888888889,
+                         0.0001984126984126984,
+                         2.48015873015873e-05,
+                         2.7557319223985893e-06,
+                         2.755731922398589e-07,
+                         2.505210838544172e-08,
+                         2.08767569878681e-09,
+                         1.6059043836821613e-10,
+                         1.1470745597729725e-11,
+                         7.647163731819816e-13,
+                         4.779477332387385e-14 };
+  double       p = c[16];
+#pragma unroll
+  for (int k = 15; k >= 1; --k)
+    p = p * r + c[k];
+  return p * r;
+}
+
+__device__ __forceinline__ double
+tanh_d(double x)
+{
+  if (x != x)
+    return x;
+  const double ax = fabs(x);
+  double       t;
+  if (ax > 22.0)
+    t = 1.0;
+  else
+  {
+    const double y = 2.0 * ax;
+    double       em;
+    if (y < 0.34657359027997264)
+      em = expm1_small_d(y);
+    else
+    {
+      const double k = floor(y * 1.4426950408889634 + 0.5);
+      const double r = (y - k * 0.6931471824645996) - k * -1.904654299957768e-09;
+      em = ldexp(expm1_small_d(r) + 1.0, (int)k) - 1.0;
+    }
+    t = em / (em + 2.0);
+  }
+  return x < 0.0 ? -t : t;
+}
+
+// ---------------------------------------------------------------------------
+// HLLC, models/RiemannSolvers.h:57-262, FP64 (reference order).
+// ql/qr: components r0 r1 p u v (w) alpha0 (normal velocity in u).
+// out: FR0 FR1 FA0 FA1 FE FU FV (FW) FUS, NOT yet scaled by dt/dx.
+// ---------------------------------------------------------------------------
+template <int DIM>
+__device__ __forceinline__ void
+hllc_fp64(const double * ql, const double * qr, const PhysParams & P, double * f)
+{
+  using H = V<DIM>;
+  const double smallr = P.smallr, smallp = P.smallp, smallc = P.smallc;
+  const double al = ql[H::QA], ar = qr[H::QA];
+  const double Sl = eosS(P, al, 1 - al), PIl = eosPI(P, al, 1 - al);
+  const double Sr = eosS(P, ar, 1 - ar), PIr = eosPI(P, ar, 1 - ar);
+
+  const double rl = fmax(ql[H::QR0] + ql[H::QR1], smallr);
+  double       pl = fmax(ql[H::QP], rl * smallp);
+  const double ul = ql[H::QU];
+  const double eintl = (pl * Sl + PIl) / rl;
+  pl = (rl * eintl - PIl) / Sl;
+  double ecinl = 0.5 * rl * ul * ul;
+  ecinl += 0.5 * rl * ql[H::QV] * ql[H::QV];
+  if constexpr (DIM == 3)
+    ecinl += 0.5 * rl * ql[H::QW] * ql[H::QW];
+  const double cl2 = (pl * (Sl + 1.0) + PIl) / (rl * Sl);
+  const double cl = sqrt(fmax(cl2, 0.0));
+  const double etotl = rl * eintl + ecinl;
+  const double ptotl = pl;
+
+  const double rr = fmax(qr[H::QR0] + qr[H::QR1], smallr);
+  double       pr = fmax(qr[H::QP], rr * smallp);
+  const double ur = qr[H::QU];
+  const double eintr = (pr * Sr + PIr) / rr;
+  pr = (rr * eintr - PIr) / Sr;
+  double ecinr = 0.5 * rr * ur * ur;
+  ecinr += 0.5 * rr * qr[H::QV] * qr[H::QV];
+  if constexpr (DIM == 3)
+    ecinr += 0.5 * rr * qr[H::QW] * qr[H::QW];
+  const double cr2 = (pr * (Sr + 1.0) + PIr) / (rr * Sr);
+  const double cr = sqrt(fmax(cr2, 0.0));
+  const double etotr = rr * eintr + ecinr;
+  const double ptotr = pr;
+
+  const double cfastl = sqrt(fmax(cl * cl, smallc * smallc));
+  const double cfastr = sqrt(fmax(cr * cr, smallc * smallc));
+  const double SL = fmin(ul, ur) - fmax(cfastl, cfastr);
+  const double SR = fmax(ul, ur) + fmax(cfastl, cfastr);
+
+  const double rcl = rl * (ul - SL);
+  const double rcr = rr * (SR - ur);
+  const double us = (rcr * ur + rcl * ul + (ptotl - ptotr)) / (rcr + rcl);
+  const double ptotstar = (rcr * ptotl + rcl * ptotr + rcl * rcr * (ul - ur)) / (rcr + rcl);
+
+  double ro, ro_0, ro_1, uo, ptoto, etoto;
+  if (SL > 0.0)
+  {
+    ro_0 = ql[H::QR0];
+    ro_1 = ql[H::QR1];
+    ro = rl;
+    uo = ul;
+    ptoto = ptotl;
+    etoto = etotl;
+  }
+  else if (us > 0.0)
+  {
+    const double factorL = (SL - ul) / (SL - us);
+    ro_0 = ql[H::QR0] * factorL;
+    ro_1 = ql[H::QR1] * factorL;
+    ro = rl * factorL;
+    uo = us;
+    ptoto = ptotstar;
+    etoto = ((SL - ul) * etotl - ptotl * ul + ptotstar * us) / (SL - us);
+  }
+  else if (SR > 0.0)
+  {
+    const double factorR = (SR - ur) / (SR - us);
+    ro_0 = qr[H::QR0] * factorR;
+    ro_1 = qr[H::QR1] * factorR;
+    ro = rr * factorR;
+    uo = us;
+    ptoto = ptotstar;
+    etoto = ((SR - ur) * etotr - ptotr * ur + ptotstar * us) / (SR - us);
+  }
+  else
+  {
+    ro_0 = qr[H::QR0];
+    ro_1 = qr[H::QR1];
+    ro = rr;
+    uo = ur;
+    ptoto = ptotr;
+    etoto = etotr;
+  }
+  const double fid = (ro_0 + ro_1) * uo;
+  f[H::FR0] = ro_0 * uo;
+  f[H::FR1] = ro_1 * uo;
+  f[H::FU] = ro * uo * uo + ptoto;
+  f[H::FE] = (etoto + ptoto) * uo;
+  f[H::FV] = (fid > 0.0) ? fid * ql[H::QV] : fid * qr[H::QV];
+  if constexpr (DIM == 3)
+    f[H::FW] = (fid > 0.0) ? fid * ql[H::QW] : fid * qr[H::QW];
+  const double phi0 = (fid > 0.0) ? al : ar;
+  const double phi1 = 1.0 - phi0;
+  f[H::FA0] = uo * phi0;
+  f[H::FA1] = uo * phi1;
+  f[H::FUS] = uo;
+}
+
+// HLLC in FP32.  The p -> e -> p round trip of the reference is an identity
+// in exact arithmetic and is dropped here (in FP32 it would cancel the
+// stiffened-gas constant against p S).
+template <int DIM>
+__device__ __forceinline__ void
+hllc_fp32(const float * ql, const float * qr, float xi0, float xi1, float gp0, float gp1, float smallr, float smallp, float smallc, float * f)
+{
+  using H = V<DIM>;
+  const float al = ql[H::QA], ar = qr[H::QA];
+  const float Sl = al * xi0 + (1.0f - al) * xi1, PIl = al * gp0 + (1.0f - al) * gp1;
+  const float Sr = ar * xi0 + (1.0f - ar) * xi1, PIr = ar * gp0 + (1.0f - ar) * gp1;
+
+  const float rl = fmaxf(ql[H::QR0] + ql[H::QR1], smallr);
+  const float pl = fmaxf(ql[H::QP], rl * smallp);
+  const float ul = ql[H::QU];
+  float       k2l = ul * ul + ql[H::QV] * ql[H::QV];
+  if constexpr (DIM == 3)
+    k2l += ql[H::QW] * ql[H::QW];
+  const float rel = pl * Sl + PIl; // rho e
+  const float cl = sqrtf(fmaxf(__fdividef(pl * (Sl + 1.0f) + PIl, rl * Sl), 0.0f));
+  const float etotl = rel + 0.5f * rl * k2l;
+
+  const float rr = fmaxf(qr[H::QR0] + qr[H::QR1], smallr);
+  const float pr = fmaxf(qr[H::QP], rr * smallp);
+  const float ur = qr[H::QU];
+  float       k2r = ur * ur + qr[H::QV] * qr[H::QV];
+  if constexpr (DIM == 3)
+    k2r += qr[H::QW] * qr[H::QW];
+  const float rer = pr * Sr + PIr;
+  const float cr = sqrtf(fmaxf(__fdividef(pr * (Sr + 1.0f) + PIr, rr * Sr), 0.0f));
+  const float etotr = rer + 0.5f * rr * k2r;
+
+  const float cf = fmaxf(fmaxf(cl, smallc), fmaxf(cr, smallc));
+  const float SL = fminf(ul, ur) - cf;
+  const float SR = fmaxf(ul, ur) + cf;
+  const float rcl = rl * (ul - SL);
+  const float rcr = rr * (SR - ur);
+  const float inv = __frcp_rn(rcr + rcl);
+  const float us = (rcr * ur + rcl * ul + (pl - pr)) * inv;
+  const float ps = (rcr * pl + rcl * pr + rcl * rcr * (ul - ur)) * inv;
+
+  float ro_0, ro_1, ro, uo, po, eo;
+  if (SL > 0.0f)
+  {
+    ro_0 = ql[H::QR0];
+    ro_1 = ql[H::QR1];
+    ro = rl;
+    uo = ul;
+    po = pl;
+    eo = etotl;
+  }
+  else if (us > 0.0f)
+  {
+    const float ifl = __frcp_rn(SL - us);
+    const float fl = (SL - ul) * ifl;
+    ro_0 = ql[H::QR0] * fl;
+    ro_1 = ql[H::QR1] * fl;
+    ro = rl * fl;
+    uo = us;
+    po = ps;
+    eo = ((SL - ul) * etotl - pl * ul + ps * us) * ifl;
+  }
+  else if (SR > 0.0f)
+  {
+    const float ifr = __frcp_rn(SR - us);
+    const float fr = (SR - ur) * ifr;
+    ro_0 = qr[H::QR0] * fr;
+    ro_1 = qr[H::QR1] * fr;
+    ro = rr * fr;
+    uo = us;
+    po = ps;
+    eo = ((SR - ur) * etotr - pr * ur + ps * us) * ifr;
+  }
+  else
+  {
+    ro_0 = qr[H::QR0];
+    ro_1 = qr[H::QR1];
+    ro = rr;
+    uo = ur;
+    po = pr;
+    eo = etotr;
+  }
+  const float fid = (ro_0 + ro_1) * uo;
+  f[H::FR0] = ro_0 * uo;
+  f[H::FR1] = ro_1 * uo;
+  f[H::FU] = ro * uo * uo + po;
+  f[H::FE] = (eo + po) * uo;
+  f[H::FV] = (fid > 0.0f) ? fid * ql[H::QV] : fid * qr[H::QV];
+  if constexpr (DIM == 3)
+    f[H::FW] = (fid > 0.0f) ? fid * ql[H::QW] : fid * qr[H::QW];
+  const float phi0 = (fid > 0.0f) ? al : ar;
+  f[H::FA0] = uo * phi0;
+  f[H::FA1] = uo * (1.0f - phi0);
+  f[H::FUS] = uo;
+}
+
+} // namespace g5

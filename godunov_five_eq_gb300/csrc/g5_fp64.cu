@@ -1,0 +1,183 @@
+// g5_fp64.cu — FP64 instantiations.  Built with --fmad=false so that every
+// product and sum is rounded separately, as in the reference's arithmetic.
+#include "g5_aux.cuh"
+#include "g5_launch.h"
+#include "g5_step2d.cuh"
+
+namespace g5
+{
+
+static int g_num_sms = 0;
+
+static int
+num_sms()
+{
+  if (g_num_sms == 0)
+  {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
+    if (g_num_sms <= 0)
+      g_num_sms = 1;
+  }
+  return g_num_sms;
+}
+
+template <int B, bool MIXED>
+static cudaError_t
+launch_step2d(const StepArgs & a, int ctas_per_sm, cudaStream_t s, int * launches)
+{
+  using T = Step2DTraits<B, MIXED>;
+  static bool configured = false;
+  static int  occ = 1;
+  if (!configured)
+  {
+    cudaError_t e = cudaFuncSetAttribute(step2d_kernel<B, MIXED>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::smem_bytes);
+    if (e != cudaSuccess)
+      return e;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, step2d_kernel<B, MIXED>, T::NT, T::smem_bytes);
+    if (occ < 1)
+      occ = 1;
+    configured = true;
+  }
+  const int per_sm = (ctas_per_sm > 0 && ctas_per_sm < occ) ? ctas_per_sm : occ;
+  int       grid = num_sms() * per_sm;
+  if (grid > a.m.n_owned)
+    grid = a.m.n_owned;
+  if (grid < 1)
+    return cudaSuccess;
+  step2d_kernel<B, MIXED><<<grid, T::NT, T::smem_bytes, s>>>(a);
+  ++*launches;
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess)
+    return e;
+  if (a.m.n_defer > 0)
+  {
+    const int n = a.m.n_defer * B;
+    reflux2d_kernel<B, false><<<(n + 127) / 128, 128, 0, s>>>(a);
+    ++*launches;
+    e = cudaGetLastError();
+  }
+  return e;
+}
+
+template <int B, bool MIXED>
+static int
+occupancy2d()
+{
+  using T = Step2DTraits<B, MIXED>;
+  cudaFuncSetAttribute(step2d_kernel<B, MIXED>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::smem_bytes);
+  int occ = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, step2d_kernel<B, MIXED>, T::NT, T::smem_bytes);
+  return occ;
+}
+
+bool
+step_supported(int dim, int b)
+{
+  return dim == 2 && (b == 8 || b == 16);
+}
+
+cudaError_t
+launch_step_fp64(int dim, int b, const StepArgs & a, int ctas_per_sm, cudaStream_t s, int * launches)
+{
+  if (dim == 2 && b == 16)
+    return launch_step2d<16, false>(a, ctas_per_sm, s, launches);
+  if (dim == 2 && b == 8)
+    return launch_step2d<8, false>(a, ctas_per_sm, s, launches);
+  return cudaErrorInvalidValue;
+}
+
+int
+step_max_ctas_per_sm_fp64(int dim, int b)
+{
+  if (dim == 2 && b == 16)
+    return occupancy2d<16, false>();
+  if (dim == 2 && b == 8)
+    return occupancy2d<8, false>();
+  return 0;
+}
+
+template <int DIM, int B>
+static cudaError_t
+fill_outside_t(double * U, const DevMesh & m, const PhysParams & p, cudaStream_t s)
+{
+  constexpr int NC = (DIM == 2) ? B * B : B * B * B;
+  const long    n = (long)m.n_outside * NC;
+  if (n == 0)
+    return cudaSuccess;
+  fill_outside_kernel<DIM, B><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(U, m, p);
+  return cudaGetLastError();
+}
+
+cudaError_t
+launch_fill_outside(int dim, int b, double * U, const DevMesh & m, const PhysParams & p, cudaStream_t s)
+{
+  if (dim == 2 && b == 16)
+    return fill_outside_t<2, 16>(U, m, p, s);
+  if (dim == 2 && b == 8)
+    return fill_outside_t<2, 8>(U, m, p, s);
+  if (dim == 3 && b == 8)
+    return fill_outside_t<3, 8>(U, m, p, s);
+  return cudaErrorInvalidValue;
+}
+
+template <int DIM, int B>
+static cudaError_t
+inv_dt_t(const double * U, const DevMesh & m, const PhysParams & p, double * invdt, cudaStream_t s)
+{
+  if (m.n_owned == 0)
+    return cudaSuccess;
+  int grid = num_sms() * 8;
+  if (grid > m.n_owned)
+    grid = m.n_owned;
+  inv_dt_kernel<DIM, B><<<grid, 256, 0, s>>>(U, m, p, invdt);
+  return cudaGetLastError();
+}
+
+cudaError_t
+launch_inv_dt(int dim, int b, const double * U, const DevMesh & m, const PhysParams & p, double * invdt, cudaStream_t s)
+{
+  if (dim == 2 && b == 16)
+    return inv_dt_t<2, 16>(U, m, p, invdt, s);
+  if (dim == 2 && b == 8)
+    return inv_dt_t<2, 8>(U, m, p, invdt, s);
+  if (dim == 3 && b == 8)
+    return inv_dt_t<3, 8>(U, m, p, invdt, s);
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t
+launch_dt_update(double * invdt, double * dt, double * dt_hist, int n_inst, double cfl, cudaStream_t s)
+{
+  dt_update_kernel<<<(n_inst + 127) / 128, 128, 0, s>>>(invdt, dt, dt_hist, n_inst, cfl);
+  return cudaGetLastError();
+}
+
+template <int DIM, int B>
+static cudaError_t
+flags_t(const double * U, const DevMesh & m, int ind, double er, double ec, double el, int lmin, int lmax, int8_t * flags, cudaStream_t s)
+{
+  if (m.n_owned == 0)
+    return cudaSuccess;
+  int grid = num_sms() * 8;
+  if (grid > m.n_owned)
+    grid = m.n_owned;
+  refine_flags_kernel<DIM, B><<<grid, 256, 0, s>>>(U, m, ind, er, ec, el, lmin, lmax, flags);
+  return cudaGetLastError();
+}
+
+cudaError_t
+launch_refine_flags(int dim, int b, const double * U, const DevMesh & m, int indicator, double er, double ec, double el,
+                    int lmin, int lmax, int8_t * flags, cudaStream_t s)
+{
+  if (dim == 2 && b == 16)
+    return flags_t<2, 16>(U, m, indicator, er, ec, el, lmin, lmax, flags, s);
+  if (dim == 2 && b == 8)
+    return flags_t<2, 8>(U, m, indicator, er, ec, el, lmin, lmax, flags, s);
+  if (dim == 3 && b == 8)
+    return flags_t<3, 8>(U, m, indicator, er, ec, el, lmin, lmax, flags, s);
+  return cudaErrorInvalidValue;
+}
+
+} // namespace g5

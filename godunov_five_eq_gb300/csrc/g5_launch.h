@@ -1,0 +1,28 @@
+// g5_launch.h — launchers exported by the kernel translation units to the
+// C-ABI layer (internal to libg5gpu.so).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "g5_common.cuh"
+
+namespace g5
+{
+
+// fused step (FP64 TU: mixed == false, mixed TU: mixed == true).
+// ctas_per_sm <= 0 selects the occupancy maximum.  Returns the launch error.
+cudaError_t launch_step_fp64(int dim, int b, const StepArgs & a, int ctas_per_sm, cudaStream_t s, int * launches);
+cudaError_t launch_step_mixed(int dim, int b, const StepArgs & a, int ctas_per_sm, cudaStream_t s, int * launches);
+// whether the (dim, b) pair is compiled
+bool step_supported(int dim, int b);
+// occupancy (CTAs per SM) of the fused step kernel
+int step_max_ctas_per_sm_fp64(int dim, int b);
+int step_max_ctas_per_sm_mixed(int dim, int b);
+
+cudaError_t launch_fill_outside(int dim, int b, double * U, const DevMesh & m, const PhysParams & p, cudaStream_t s);
+cudaError_t launch_inv_dt(int dim, int b, const double * U, const DevMesh & m, const PhysParams & p, double * invdt, cudaStream_t s);
+cudaError_t launch_dt_update(double * invdt, double * dt, double * dt_hist, int n_inst, double cfl, cudaStream_t s);
+cudaError_t launch_refine_flags(int dim, int b, const double * U, const DevMesh & m, int indicator, double er, double ec,
+                                double el, int lmin, int lmax, int8_t * flags, cudaStream_t s);
+
+} // namespace g5

@@ -1,0 +1,93 @@
+// g5_mixed.cu — FP32-bulk instantiations (fast FP32 math; FP64 kept for the
+// pressure numerator, the accumulation into U2, the renormalisation and dt).
+#include "g5_launch.h"
+#include "g5_step2d.cuh"
+
+namespace g5
+{
+
+static int
+num_sms_m()
+{
+  static int n = 0;
+  if (n == 0)
+  {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n <= 0)
+      n = 1;
+  }
+  return n;
+}
+
+template <int B>
+static cudaError_t
+launch_step2d_m(const StepArgs & a, int ctas_per_sm, cudaStream_t s, int * launches)
+{
+  using T = Step2DTraits<B, true>;
+  static bool configured = false;
+  static int  occ = 1;
+  if (!configured)
+  {
+    cudaError_t e = cudaFuncSetAttribute(step2d_kernel<B, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::smem_bytes);
+    if (e != cudaSuccess)
+      return e;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, step2d_kernel<B, true>, T::NT, T::smem_bytes);
+    if (occ < 1)
+      occ = 1;
+    configured = true;
+  }
+  const int per_sm = (ctas_per_sm > 0 && ctas_per_sm < occ) ? ctas_per_sm : occ;
+  int       grid = num_sms_m() * per_sm;
+  if (grid > a.m.n_owned)
+    grid = a.m.n_owned;
+  if (grid < 1)
+    return cudaSuccess;
+  step2d_kernel<B, true><<<grid, T::NT, T::smem_bytes, s>>>(a);
+  ++*launches;
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess)
+    return e;
+  if (a.m.n_defer > 0)
+  {
+    const int n = a.m.n_defer * B;
+    reflux2d_kernel<B, true><<<(n + 127) / 128, 128, 0, s>>>(a);
+    ++*launches;
+    e = cudaGetLastError();
+  }
+  return e;
+}
+
+template <int B>
+static int
+occupancy2d_m()
+{
+  using T = Step2DTraits<B, true>;
+  cudaFuncSetAttribute(step2d_kernel<B, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::smem_bytes);
+  int occ = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, step2d_kernel<B, true>, T::NT, T::smem_bytes);
+  return occ;
+}
+
+cudaError_t
+launch_step_mixed(int dim, int b, const StepArgs & a, int ctas_per_sm, cudaStream_t s, int * launches)
+{
+  if (dim == 2 && b == 16)
+    return launch_step2d_m<16>(a, ctas_per_sm, s, launches);
+  if (dim == 2 && b == 8)
+    return launch_step2d_m<8>(a, ctas_per_sm, s, launches);
+  return cudaErrorInvalidValue;
+}
+
+int
+step_max_ctas_per_sm_mixed(int dim, int b)
+{
+  if (dim == 2 && b == 16)
+    return occupancy2d_m<16>();
+  if (dim == 2 && b == 8)
+    return occupancy2d_m<8>();
+  return 0;
+}
+
+} // namespace g5

@@ -1,0 +1,714 @@
+// g5_step2d.cuh — fused 2D block timestep (one CTA per 16x16 or 8x8 block,
+// persistent over the block list).
+//
+// Per block, entirely in shared memory:
+//   1. gather the block and its 2-cell halo from U (same level: copy,
+//      finer neighbour: mean of 4 fine cells, coarser neighbour: the coarse
+//      cell) and convert to primitives                         (a2, a3)
+//   2. per cell of the (b+2)^2 ring: limited slopes, sound speed and the
+//      Hancock half-step source                                  (a5, a6)
+//   3. per face: reconstruct both sides (MUSCL or THINC), HLLC, scale by
+//      dt/dx                                                     (a6-a9)
+//   4. per owned cell: X update + clamps, Y update + clamps, volume-fraction
+//      renormalisation, write U2, CFL reduction of the new state  (a10-a12)
+// Cells next to a finer face are deferred to the reflux kernel; fine blocks
+// next to a coarser face publish their face fluxes for it.
+#pragma once
+
+#include "g5_common.cuh"
+
+namespace g5
+{
+
+template <int B, bool MIXED>
+struct Step2DTraits
+{
+  using R = typename std::conditional<MIXED, float, double>::type;
+  static constexpr int NT = B * B;
+  static constexpr int G = B + 4;  // ghosted extent
+  static constexpr int S = B + 2;  // ring extent
+  static constexpr int NQ = 6;     // r0 r1 p u v a0
+  static constexpr int NREC = 17;  // dqx[5] dqy[5] hS[5] |nx| |ny|
+  static constexpr int NFF = B * (B + 1);
+  static constexpr size_t smem_bytes = sizeof(R) * (size_t)(NQ * G * G + NREC * S * S + 2 * 8 * NFF) + 64;
+};
+
+// halo cell h (0 .. G*G - B*B - 1) -> ghosted coordinates
+template <int B>
+__device__ __forceinline__ void
+halo_coords(int h, int & gx, int & gy)
+{
+  constexpr int G = B + 4;
+  if (h < 2 * G)
+  {
+    gx = h % G - 2;
+    gy = h / G - 2;
+    return;
+  }
+  h -= 2 * G;
+  if (h < 2 * G)
+  {
+    gx = h % G - 2;
+    gy = B + h / G;
+    return;
+  }
+  h -= 2 * G;
+  // side columns: 4 per row, rows 0..B-1
+  const int r = h >> 2, c = h & 3;
+  gy = r;
+  gx = c < 2 ? c - 2 : B + (c - 2);
+}
+
+// load the conservative state seen by ghost cell (gx, gy) of block n.
+// Returns false (and raises the mesh status) on a bad neighbour index.
+template <int B>
+__device__ __forceinline__ bool
+gather_ghost_2d(const StepArgs & a, int n, int gx, int gy, double * u)
+{
+  using H = V<2>;
+  constexpr int NC = B * B;
+  const int     dxs = gx < 0 ? -1 : (gx >= B ? 1 : 0);
+  const int     dys = gy < 0 ? -1 : (gy >= B ? 1 : 0);
+  const int     vx = gx - dxs * B, vy = gy - dys * B;
+  const int     s = (dxs + 1) + 3 * (dys + 1);
+  const int     rel = a.m.nbr_rel[n * 9 + s];
+  const int *   nb = a.m.nbr + (n * 9 + s) * 4;
+  if (rel == 0)
+  {
+    const int src = nb[0];
+    if (src < 0 || src >= a.m.n_total)
+      return false;
+    const double * base = a.U + (size_t)src * H::NV * NC + vx + B * vy;
+#pragma unroll
+    for (int v = 0; v < H::NV; ++v)
+      u[v] = base[v * NC];
+    return true;
+  }
+  if (rel < 0)
+  {
+    const int src = nb[0];
+    if (src < 0 || src >= a.m.n_total)
+      return false;
+    const int cx = ((a.m.coord[n * 3 + 0] + dxs) & 1) * (B / 2) + (vx >> 1);
+    const int cy = ((a.m.coord[n * 3 + 1] + dys) & 1) * (B / 2) + (vy >> 1);
+    const double * base = a.U + (size_t)src * H::NV * NC + cx + B * cy;
+#pragma unroll
+    for (int v = 0; v < H::NV; ++v)
+      u[v] = base[v * NC];
+    return true;
+  }
+  // finer: mean of the 4 fine cells (sum in x-fastest order, then / 4)
+  const int fx = 2 * vx, fy = 2 * vy;
+  const int chx = fx / B, chy = fy / B;
+  const int src = nb[chx + 2 * chy];
+  if (src < 0 || src >= a.m.n_total)
+    return false;
+  const int      lx = fx - chx * B, ly = fy - chy * B;
+  const double * base = a.U + (size_t)src * H::NV * NC + lx + B * ly;
+  const int      vars[6] = { H::IE, H::IU, H::IV, H::IAD0, H::IAD1, H::IA0 };
+#pragma unroll
+  for (int t = 0; t < 6; ++t)
+  {
+    const double * p = base + vars[t] * NC;
+    double         sum = 0.0;
+    sum += p[0];
+    sum += p[1];
+    sum += p[B];
+    sum += p[B + 1];
+    u[vars[t]] = sum / 4.0;
+  }
+  u[H::IA1] = 1.0 - u[H::IA0];
+  u[H::ID] = u[H::IAD0] + u[H::IAD1];
+  return true;
+}
+
+template <int B, bool MIXED>
+__device__ __forceinline__ void
+store_prim(typename Step2DTraits<B, MIXED>::R * sQ, int gidx, const double * u, const PhysParams & P)
+{
+  constexpr int GG = (B + 4) * (B + 4);
+  if constexpr (MIXED)
+  {
+    float q[6];
+    prim_mixed<2>(u, q, P);
+#pragma unroll
+    for (int k = 0; k < 6; ++k)
+      sQ[k * GG + gidx] = q[k];
+  }
+  else
+  {
+    double q[6];
+    prim_fp64<2>(u, q, P);
+#pragma unroll
+    for (int k = 0; k < 6; ++k)
+      sQ[k * GG + gidx] = q[k];
+  }
+}
+
+// Youngs normal (restated: (1,2,1)-weighted central differences), |n_x|, |n_y|
+template <typename R, int G>
+__device__ __forceinline__ void
+youngs_abs_2d(const R * A, int gi, R & nx, R & ny)
+{
+  auto a = [&](int dx, int dy) { return A[gi + dx + G * dy]; };
+  const R gx = (a(1, -1) + R(2) * a(1, 0) + a(1, 1)) - (a(-1, -1) + R(2) * a(-1, 0) + a(-1, 1));
+  const R gy = (a(-1, 1) + R(2) * a(0, 1) + a(1, 1)) - (a(-1, -1) + R(2) * a(0, -1) + a(1, -1));
+  R       nrm = gx * gx + gy * gy;
+  nrm = sqrt(nrm);
+  nx = (nrm > R(0)) ? fabs(-gx / nrm) : R(0);
+  ny = (nrm > R(0)) ? fabs(-gy / nrm) : R(0);
+}
+
+// reconstruct one side of a face from cell (ci, cj) (ghosted-ring coordinates)
+// dir: 0 X, 1 Y; side: +1 -> right face of the cell (qL), -1 -> left face (qR)
+template <int B, bool MIXED>
+__device__ __forceinline__ void
+face_state(const typename Step2DTraits<B, MIXED>::R * sQ,
+           const typename Step2DTraits<B, MIXED>::R * sRec,
+           int                                          ci,
+           int                                          cj,
+           int                                          dir,
+           int                                          side,
+           const PhysParams &                           P,
+           typename Step2DTraits<B, MIXED>::R *         q)
+{
+  using T = Step2DTraits<B, MIXED>;
+  using R = typename T::R;
+  constexpr int G = T::G, S = T::S, GG = G * G, SS = S * S;
+  const int     gi = (ci + 2) + G * (cj + 2);
+  const int     si = (ci + 1) + S * (cj + 1);
+  const R       offx = dir == 0 ? R(0.5) * R(side) : R(0);
+  const R       offy = dir == 1 ? R(0.5) * R(side) : R(0);
+  const bool    hancock = P.integrator == 0;
+  R             qc[5], dqx[5], dqy[5], hs[5];
+#pragma unroll
+  for (int k = 0; k < 5; ++k)
+  {
+    qc[k] = sQ[k * GG + gi];
+    dqx[k] = sRec[k * SS + si];
+    dqy[k] = sRec[(5 + k) * SS + si];
+    hs[k] = sRec[(10 + k) * SS + si];
+  }
+  const R a0 = sQ[5 * GG + gi];
+#pragma unroll
+  for (int k = 0; k < 5; ++k)
+  {
+    if constexpr (MIXED)
+      q[k] = qc[k] + offx * dqx[k] + offy * dqy[k] + (hancock ? hs[k] : R(0));
+    else
+    {
+      q[k] = qc[k] + offx * dqx[k] + offy * dqy[k];
+      if (hancock)
+        q[k] += hs[k];
+    }
+  }
+  q[5] = a0;
+  if (P.thinc)
+  {
+    // THINC (scheme/ComputeFluxesAndStoreTHINCFunctor.cpp:122-283): alpha
+    // and the partial densities from the hyperbolic-tangent profile
+    const int  o = dir == 0 ? 1 : G;
+    const R *  A = sQ + 5 * GG;
+    const R    aP = A[gi + o], aM = A[gi - o];
+    const R    mono = (aP - a0) * (a0 - aM);
+    const bool req = (a0 > R(P.thinc_eps)) && (a0 < R(1) - R(P.thinc_eps)) && mono > R(0);
+    if (req)
+    {
+      const R nd = sRec[(15 + dir) * SS + si];
+      const R beta = R(P.thinc_beta) * nd + R(0.01);
+      const R Aa = (aP + aM) / R(2);
+      const R Bb = (aP - aM) / R(2);
+      R       C, D;
+      if constexpr (MIXED)
+      {
+        C = tanhf(R(0.5) * beta);
+        D = tanhf(R(0.5) * beta * (a0 - Aa) / Bb);
+      }
+      else
+      {
+        C = tanh_d(R(0.5) * beta);
+        D = tanh_d(R(0.5) * beta * (a0 - Aa) / Bb);
+      }
+      const R bs = R(side);
+      const R af = Aa + bs * Bb * (C + bs * D / C) / (R(1) + bs * D);
+      const R r0 = qc[0], r1 = qc[1];
+      R       q0 = r0 + r0 / a0 * (af - a0);
+      R       q1 = r1 + r1 / (R(1) - a0) * (a0 - af);
+      if (hancock)
+      {
+        q0 += hs[0];
+        q1 += hs[1];
+      }
+      q[0] = q0;
+      q[1] = q1;
+      q[5] = af;
+    }
+    // THINC functor: no smallr clamp on the partial densities
+  }
+  else
+  {
+    q[0] = fmax(R(P.smallr), q[0]);
+    q[1] = fmax(R(P.smallr), q[1]);
+  }
+}
+
+template <int B, bool MIXED>
+__global__ void __launch_bounds__(B * B)
+step2d_kernel(StepArgs a)
+{
+  using T = Step2DTraits<B, MIXED>;
+  using R = typename T::R;
+  using H = V<2>;
+  constexpr int NT = T::NT, G = T::G, S = T::S, GG = G * G, SS = S * S, NC = B * B;
+  constexpr int NFF = T::NFF;
+  constexpr int NHALO = GG - NC;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  R *          sQ = reinterpret_cast<R *>(smem_raw);
+  R *          sRec = sQ + T::NQ * GG;
+  R *          sFx = sRec + T::NREC * SS; // [8][NFF]  X faces (B+1) x B
+  R *          sFy = sFx + 8 * NFF;       // [8][NFF]  Y faces B x (B+1)
+  __shared__ double sRed[NT / 32];
+  const int         tid = threadIdx.x;
+  const PhysParams & P = a.p;
+
+  for (int n = blockIdx.x; n < a.m.n_owned; n += gridDim.x)
+  {
+    const int    lev = a.m.level[n];
+    const int    ins = a.m.inst ? a.m.inst[n] : 0;
+    const double dx = P.level_dx[lev];
+    const double dtdx = a.dt[ins] / dx;
+    const R      dtdx_r = R(dtdx);
+
+    // ---------------- phase 1: own cell (coalesced) + halo gather -> primitives
+    const int ci = tid % B, cj = tid / B;
+    double    uin[H::NV];
+    {
+      const double * base = a.U + (size_t)n * H::NV * NC + tid;
+#pragma unroll
+      for (int v = 0; v < H::NV; ++v)
+        uin[v] = base[v * NC];
+      store_prim<B, MIXED>(sQ, (ci + 2) + G * (cj + 2), uin, P);
+    }
+    for (int h = tid; h < NHALO; h += NT)
+    {
+      int gx, gy;
+      halo_coords<B>(h, gx, gy);
+      double u[H::NV];
+      if (!gather_ghost_2d<B>(a, n, gx, gy, u))
+      {
+        raise_status(a.status, STATUS_MESH);
+#pragma unroll
+        for (int v = 0; v < H::NV; ++v)
+          u[v] = uin[v];
+      }
+      store_prim<B, MIXED>(sQ, (gx + 2) + G * (gy + 2), u, P);
+    }
+    __syncthreads();
+
+    // ---------------- phase 2: per ring cell slopes + Hancock source
+    for (int r = tid; r < SS; r += NT)
+    {
+      const int ri = r % S - 1, rj = r / S - 1;
+      const bool corner = (ri < 0 || ri >= B) && (rj < 0 || rj >= B);
+      if (corner)
+        continue;
+      const int gi = (ri + 2) + G * (rj + 2);
+      R         q[5], dqx[5], dqy[5];
+      const R   st = R(P.slope_type);
+#pragma unroll
+      for (int k = 0; k < 5; ++k)
+      {
+        const R * Qk = sQ + k * GG;
+        q[k] = Qk[gi];
+        dqx[k] = slope_scalar<R>(q[k], Qk[gi + 1], Qk[gi - 1], st);
+        dqy[k] = slope_scalar<R>(q[k], Qk[gi + G], Qk[gi - G], st);
+        sRec[k * SS + r] = dqx[k];
+        sRec[(5 + k) * SS + r] = dqy[k];
+      }
+      const R a0 = sQ[5 * GG + gi];
+      if (P.integrator == 0)
+      {
+        // Hancock half-step source (ComputeFluxesAndStoreFunctor.cpp:174-199)
+        const R r0 = q[0], r1 = q[1], p = q[2], u = q[3], v = q[4];
+        const R rr = r0 + r1;
+        R       c;
+        if constexpr (MIXED)
+          c = sound_speed_f((float)P.xi[0], (float)P.xi[1], (float)P.gpx[0], (float)P.gpx[1], rr, p, a0);
+        else
+          c = sound_speed_d(P, rr, p, a0, 1 - a0);
+        const R drx0 = dqx[0], drx1 = dqx[1], dpx = dqx[2], dux = dqx[3], dvx = dqx[4];
+        const R dry0 = dqy[0], dry1 = dqy[1], dpy = dqy[2], duy = dqy[3], dvy = dqy[4];
+        const R dtdy = dtdx_r;
+        const R sr0 = (-u * (drx0 + drx1) - dux * rr) * dtdx_r + (-v * (dry0 + dry1) - dvy * rr) * dtdy;
+        const R sr0_0 = sr0 * a0;
+        const R sr0_1 = sr0 * (R(1) - a0);
+        const R su0 = (-u * dux - dpx / rr) * dtdx_r + (-v * duy) * dtdy;
+        const R sv0 = (-u * dvx) * dtdx_r + (-v * dvy - dpy / rr) * dtdy;
+        const R sp0 = (-u * dpx - dux * rr * c * c) * dtdx_r + (-v * dpy - dvy * rr * c * c) * dtdy;
+        sRec[10 * SS + r] = R(0.5) * sr0_0;
+        sRec[11 * SS + r] = R(0.5) * sr0_1;
+        sRec[12 * SS + r] = R(0.5) * sp0;
+        sRec[13 * SS + r] = R(0.5) * su0;
+        sRec[14 * SS + r] = R(0.5) * sv0;
+      }
+      if (P.thinc)
+      {
+        R nx, ny;
+        youngs_abs_2d<R, G>(sQ + 5 * GG, gi, nx, ny);
+        sRec[15 * SS + r] = nx;
+        sRec[16 * SS + r] = ny;
+      }
+    }
+    __syncthreads();
+
+    // ---------------- phase 3: faces (X then Y) -> HLLC -> shared fluxes
+    for (int f = tid; f < 2 * NFF; f += NT)
+    {
+      const int dir = f >= NFF ? 1 : 0;
+      const int ff = f - dir * NFF;
+      int       li, lj, ri, rj;
+      if (dir == 0)
+      {
+        const int fi = ff % (B + 1), fj = ff / (B + 1);
+        li = fi - 1;
+        lj = fj;
+        ri = fi;
+        rj = fj;
+      }
+      else
+      {
+        const int fi = ff % B, fj = ff / B;
+        li = fi;
+        lj = fj - 1;
+        ri = fi;
+        rj = fj;
+      }
+      R qL[6], qR[6], fl[8];
+      face_state<B, MIXED>(sQ, sRec, li, lj, dir, +1, P, qL);
+      face_state<B, MIXED>(sQ, sRec, ri, rj, dir, -1, P, qR);
+      if (dir == 1)
+      {
+        R t = qL[3];
+        qL[3] = qL[4];
+        qL[4] = t;
+        t = qR[3];
+        qR[3] = qR[4];
+        qR[4] = t;
+      }
+      if constexpr (MIXED)
+        hllc_fp32<2>(qL, qR, (float)P.xi[0], (float)P.xi[1], (float)P.gpx[0], (float)P.gpx[1], (float)P.smallr, (float)P.smallp, (float)P.smallc, fl);
+      else
+        hllc_fp64<2>(qL, qR, P, fl);
+      if (dir == 1)
+      {
+        const R t = fl[H::FU];
+        fl[H::FU] = fl[H::FV];
+        fl[H::FV] = t;
+      }
+      R * dst = dir == 0 ? sFx : sFy;
+#pragma unroll
+      for (int k = 0; k < 8; ++k)
+        dst[k * NFF + ff] = fl[k] * dtdx_r;
+    }
+    __syncthreads();
+
+    // ---------------- publish coarse/fine records (AMR only)
+    if (a.m.reflux_slot)
+    {
+      for (int face = 0; face < 4; ++face)
+      {
+        const int rs = a.m.reflux_slot[n * 4 + face];
+        if (rs >= 0 && tid < B)
+        {
+          // fine block face next to a coarser neighbour: publish its B face fluxes
+          const int dir = face >> 1, side = face & 1;
+          const int idx = dir == 0 ? (side ? B : 0) + (B + 1) * tid : tid + B * (side ? B : 0);
+          const R * src = dir == 0 ? sFx : sFy;
+          double *  dst = a.reflux_buf + ((size_t)rs * B + tid) * 8;
+#pragma unroll
+          for (int k = 0; k < 8; ++k)
+            dst[k] = (double)src[k * NFF + idx];
+        }
+        const int ds = a.m.defer_slot[n * 4 + face];
+        if (ds >= 0 && tid < B)
+        {
+          // coarse cell next to a finer face: save its four own face fluxes
+          const int dir = face >> 1, side = face & 1;
+          const int cx = dir == 0 ? (side ? B - 1 : 0) : tid;
+          const int cy = dir == 0 ? tid : (side ? B - 1 : 0);
+          double *  dst = a.defer_buf + ((size_t)ds * B + tid) * 32;
+          const int fxl = cx + (B + 1) * cy, fyl = cx + B * cy;
+#pragma unroll
+          for (int k = 0; k < 8; ++k)
+          {
+            dst[0 * 8 + k] = (double)sFx[k * NFF + fxl];
+            dst[1 * 8 + k] = (double)sFx[k * NFF + fxl + 1];
+            dst[2 * 8 + k] = (double)sFy[k * NFF + fyl];
+            dst[3 * 8 + k] = (double)sFy[k * NFF + fyl + B];
+          }
+        }
+      }
+    }
+
+    // ---------------- phase 4: update of the owned cell (tid)
+    bool deferred = false;
+    if (a.m.defer_slot)
+    {
+      const int * dsl = a.m.defer_slot + n * 4;
+      deferred = (ci == 0 && dsl[0] >= 0) || (ci == B - 1 && dsl[1] >= 0) || (cj == 0 && dsl[2] >= 0) ||
+                 (cj == B - 1 && dsl[3] >= 0);
+    }
+    double m_inv = 0.0;
+    if (!deferred)
+    {
+      double u2[H::NV];
+#pragma unroll
+      for (int v = 0; v < H::NV; ++v)
+        u2[v] = uin[v];
+      const double a0n = uin[H::IA0], a1n = uin[H::IA1];
+#pragma unroll
+      for (int dir = 0; dir < 2; ++dir)
+      {
+        const R * F = dir == 0 ? sFx : sFy;
+        const int il = dir == 0 ? ci + (B + 1) * cj : ci + B * cj;
+        const int ir = dir == 0 ? il + 1 : il + B;
+        double    acc[7];
+        // left face: + F ; alpha source - u* alpha^n
+#pragma unroll
+        for (int k = 0; k < 7; ++k)
+          acc[k] = 0.0 + (double)F[k * NFF + il];
+        const double usl = (double)F[7 * NFF + il];
+        acc[H::FA0] -= usl * a0n;
+        acc[H::FA1] -= usl * a1n;
+#pragma unroll
+        for (int k = 0; k < 7; ++k)
+          acc[k] = acc[k] - (double)F[k * NFF + ir];
+        const double usr = (double)F[7 * NFF + ir];
+        acc[H::FA0] += usr * a0n;
+        acc[H::FA1] += usr * a1n;
+        // update_U with the per-direction clamps (.h:319-349)
+        const double eps = 1e-12;
+        u2[H::IAD0] += acc[H::FR0];
+        if (u2[H::IAD0] < eps)
+          u2[H::IAD0] = 0.0;
+        u2[H::IAD1] += acc[H::FR1];
+        if (u2[H::IAD1] < eps)
+          u2[H::IAD1] = 0.0;
+        u2[H::IA0] += acc[H::FA0];
+        if (u2[H::IA0] < eps)
+          u2[H::IA0] = 0.0;
+        if (u2[H::IA0] > 1.0 - eps)
+          u2[H::IA0] = 1.0;
+        u2[H::IA1] += acc[H::FA1];
+        if (u2[H::IA1] < eps)
+          u2[H::IA1] = 0.0;
+        if (u2[H::IA1] > 1.0 - eps)
+          u2[H::IA1] = 1.0;
+        u2[H::IE] += acc[H::FE];
+        u2[H::IU] += acc[H::FU];
+        u2[H::IV] += acc[H::FV];
+      }
+      // FixVolumeFractionsNormalization (.cpp:49-72)
+      const double sum_alpha = u2[H::IA0] + u2[H::IA1];
+      const double sum_alpha_rho = u2[H::IAD0] + u2[H::IAD1];
+      const double inv = 1.0 / sum_alpha;
+      u2[H::IA0] *= inv;
+      u2[H::IA1] *= inv;
+      u2[H::ID] = sum_alpha_rho;
+      double * out = a.U2 + (size_t)n * H::NV * NC + tid;
+      bool     finite = true;
+#pragma unroll
+      for (int v = 0; v < H::NV; ++v)
+      {
+        out[v * NC] = u2[v];
+        finite = finite && isfinite(u2[v]);
+      }
+      if (!finite)
+        raise_status(a.status, STATUS_NONPHYSICAL);
+      if (a.invdt)
+      {
+        // ComputeDtFiveEqFunctor::compute_cfl on the new state
+        double       q[6];
+        const double c = prim_fp64<2>(u2, q, P);
+        const double vx = c + fabs(q[H::QU]);
+        const double vy = c + fabs(q[H::QV]);
+        m_inv = fmax(m_inv, vx / dx + vy / dx);
+      }
+    }
+    if (a.invdt)
+    {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1)
+        m_inv = fmax(m_inv, __shfl_xor_sync(0xffffffffu, m_inv, o));
+      if ((tid & 31) == 0)
+        sRed[tid >> 5] = m_inv;
+      __syncthreads();
+      if (tid == 0)
+      {
+        double mm = 0.0;
+        for (int w = 0; w < NT / 32; ++w)
+          mm = fmax(mm, sRed[w]);
+        atomic_max_pos(a.invdt + ins, mm);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// reflux: coarse cells next to finer faces (one thread per deferred record
+// entry).  Replays update_U with the fine face sums of
+// get_flux_from_fine_neighbor (ReadFluxesAndConservativeUpdateFunctor.h:256-307).
+// ---------------------------------------------------------------------------
+// MIXED only keeps the two instantiations (FMA-free and fast-math units) apart
+template <int B, bool MIXED>
+__global__ void
+reflux2d_kernel(StepArgs a)
+{
+  using H = V<2>;
+  constexpr int NC = B * B;
+  const int     gid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= a.m.n_defer * B)
+    return;
+  const int rec = gid / B, pos = gid % B;
+  const int code = a.m.defer_list[rec];
+  const int n = code >> 3, face = code & 7;
+  const int dirf = face >> 1, sidef = face & 1;
+  const int ci = dirf == 0 ? (sidef ? B - 1 : 0) : pos;
+  const int cj = dirf == 0 ? pos : (sidef ? B - 1 : 0);
+  const int * dsl = a.m.defer_slot + n * 4;
+  // a cell next to two finer faces is handled by the lower face index
+  for (int f2 = 0; f2 < face; ++f2)
+  {
+    if (dsl[f2] < 0)
+      continue;
+    const int d2 = f2 >> 1, s2 = f2 & 1;
+    const int c2 = d2 == 0 ? ci : cj;
+    if (c2 == (s2 ? B - 1 : 0))
+      return;
+  }
+  const double * own = a.defer_buf + ((size_t)dsl[face] * B + pos) * 32;
+  const int      cell = ci + B * cj;
+  const double * ub = a.U + (size_t)n * H::NV * NC + cell;
+  double         uin[H::NV], u2[H::NV];
+#pragma unroll
+  for (int v = 0; v < H::NV; ++v)
+    u2[v] = uin[v] = ub[v * NC];
+  const int    ins = a.m.inst ? a.m.inst[n] : 0;
+  const double dx = a.p.level_dx[a.m.level[n]];
+  const double a0n = uin[H::IA0], a1n = uin[H::IA1];
+  for (int dir = 0; dir < 2; ++dir)
+  {
+    const int cd = dir == 0 ? ci : cj;
+    const int ct = dir == 0 ? cj : ci; // transverse coordinate
+    double    acc[7];
+    for (int k = 0; k < 7; ++k)
+      acc[k] = 0.0;
+    for (int side = 0; side < 2; ++side)
+    {
+      const int  fface = 2 * dir + side;
+      const bool fine = (side == 0 ? cd == 0 : cd == B - 1) && dsl[fface] >= 0;
+      double     fv[8];
+      if (fine)
+      {
+        // fine neighbour across face `fface`: children touching the block
+        const int dxs = dir == 0 ? (side ? 1 : -1) : 0;
+        const int dys = dir == 1 ? (side ? 1 : -1) : 0;
+        const int s = (dxs + 1) + 3 * (dys + 1);
+        const int f = 2 * ct;
+        const int cht = f / B, fl = f - cht * B;
+        const int chd = side ? 0 : 1;
+        const int child = dir == 0 ? chd + 2 * cht : cht + 2 * chd;
+        const int F = a.m.nbr[(n * 9 + s) * 4 + child];
+        const int rs = (F >= 0 && F < a.m.n_owned) ? a.m.reflux_slot[F * 4 + (fface ^ 1)] : -1;
+        if (rs < 0)
+        {
+          raise_status(a.status, STATUS_MESH);
+          return;
+        }
+        const double * r0 = a.reflux_buf + ((size_t)rs * B + fl) * 8;
+        const double * r1 = r0 + 8;
+        for (int k = 0; k < 8; ++k)
+        {
+          double sum = 0.0;
+          sum += r0[k];
+          sum += r1[k];
+          fv[k] = sum;
+        }
+        for (int k = 0; k < 7; ++k)
+          acc[k] = side == 0 ? acc[k] + fv[k] / 4.0 : acc[k] - fv[k] / 4.0;
+        const double us = fv[7];
+        if (side == 0)
+        {
+          acc[H::FA0] -= us * a0n / 4.0;
+          acc[H::FA1] -= us * a1n / 4.0;
+        }
+        else
+        {
+          acc[H::FA0] += us * a0n / 4.0;
+          acc[H::FA1] += us * a1n / 4.0;
+        }
+      }
+      else
+      {
+        const double * fr = own + (2 * dir + side) * 8;
+        for (int k = 0; k < 7; ++k)
+          acc[k] = side == 0 ? acc[k] + fr[k] : acc[k] - fr[k];
+        const double us = fr[7];
+        if (side == 0)
+        {
+          acc[H::FA0] -= us * a0n;
+          acc[H::FA1] -= us * a1n;
+        }
+        else
+        {
+          acc[H::FA0] += us * a0n;
+          acc[H::FA1] += us * a1n;
+        }
+      }
+    }
+    const double eps = 1e-12;
+    u2[H::IAD0] += acc[H::FR0];
+    if (u2[H::IAD0] < eps)
+      u2[H::IAD0] = 0.0;
+    u2[H::IAD1] += acc[H::FR1];
+    if (u2[H::IAD1] < eps)
+      u2[H::IAD1] = 0.0;
+    u2[H::IA0] += acc[H::FA0];
+    if (u2[H::IA0] < eps)
+      u2[H::IA0] = 0.0;
+    if (u2[H::IA0] > 1.0 - eps)
+      u2[H::IA0] = 1.0;
+    u2[H::IA1] += acc[H::FA1];
+    if (u2[H::IA1] < eps)
+      u2[H::IA1] = 0.0;
+    if (u2[H::IA1] > 1.0 - eps)
+      u2[H::IA1] = 1.0;
+    u2[H::IE] += acc[H::FE];
+    u2[H::IU] += acc[H::FU];
+    u2[H::IV] += acc[H::FV];
+  }
+  const double sum_alpha = u2[H::IA0] + u2[H::IA1];
+  const double sum_alpha_rho = u2[H::IAD0] + u2[H::IAD1];
+  const double inv = 1.0 / sum_alpha;
+  u2[H::IA0] *= inv;
+  u2[H::IA1] *= inv;
+  u2[H::ID] = sum_alpha_rho;
+  double * out = a.U2 + (size_t)n * H::NV * NC + cell;
+  bool     finite = true;
+  for (int v = 0; v < H::NV; ++v)
+  {
+    out[v * NC] = u2[v];
+    finite = finite && isfinite(u2[v]);
+  }
+  if (!finite)
+    raise_status(a.status, STATUS_NONPHYSICAL);
+  if (a.invdt)
+  {
+    double       q[6];
+    const double c = prim_fp64<2>(u2, q, a.p);
+    atomic_max_pos(a.invdt + ins, (c + fabs(q[V<2>::QU])) / dx + (c + fabs(q[V<2>::QV])) / dx);
+  }
+}
+
+} // namespace g5

@@ -1,0 +1,373 @@
+"""Host-side mirror of the reference's GodunovImplemBase over the C ABI.
+
+``GodunovImplemGB300`` keeps the reference's member names and argument
+meaning (scheme/GodunovImplemBase.h:59-198, scheme/GodunovImplemV0.h:42-214):
+
+* ``resize_auxiliary_data(table)``   -> g5_set_mesh
+* ``total_mem_size_in_bytes()``      -> g5_mem_bytes
+* ``do_time_step(U, U2, dt)``        -> g5_step          (U2 <- step(U))
+* ``do_time_step(U, U2, t, dt)``     -> same (t is unused, as in V0 for
+  every problem but circle_advection)
+* ``compute_dt_local(U)``            -> g5_compute_inv_dt, dt = cfl / invDt
+  (SolverGodunovFiveEq.cpp:367-390)
+* ``fill_outside_quadrants(U)``      -> g5_fill_outside
+  (SolverGodunovFiveEq.cpp:977-1019)
+
+Device arrays are torch CUDA tensors of dtype float64 and shape
+``[n_blocks, nv, bsize^dim]`` (torch provides device memory and streams
+only).  The product path always runs the CUDA library: if it cannot be
+loaded, construction raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+G5_MODE_FP64 = 0
+G5_MODE_MIXED = 1
+MODES = {"fp64": G5_MODE_FP64, "mixed": G5_MODE_MIXED}
+
+ERRORS = {
+    -1: "G5_ERR_ARG",
+    -2: "G5_ERR_CUDA",
+    -3: "G5_ERR_NONPHYSICAL",
+    -4: "G5_ERR_TIMEOUT",
+    -5: "G5_ERR_MESH",
+    -6: "G5_ERR_UNSUPPORTED",
+}
+
+
+class G5Error(RuntimeError):
+    def __init__(self, code, what=""):
+        super().__init__(f"{what}: {ERRORS.get(code, code)}")
+        self.code = code
+
+
+class G5Params(ctypes.Structure):
+    _fields_ = [
+        ("dim", ctypes.c_int32),
+        ("bsize", ctypes.c_int32),
+        ("integrator", ctypes.c_int32),
+        ("thinc", ctypes.c_int32),
+        ("source_term", ctypes.c_int32),
+        ("prolongation", ctypes.c_int32),
+        ("bc", ctypes.c_int32 * 6),
+        ("gamma", ctypes.c_double * 2),
+        ("pinf", ctypes.c_double * 2),
+        ("smallr", ctypes.c_double),
+        ("smallc", ctypes.c_double),
+        ("slope_type", ctypes.c_double),
+        ("cfl", ctypes.c_double),
+        ("thinc_beta", ctypes.c_double),
+        ("thinc_eps", ctypes.c_double),
+        ("level_dx", ctypes.c_double * 32),
+    ]
+
+
+class G5Mesh(ctypes.Structure):
+    _fields_ = [
+        ("n_owned", ctypes.c_int32),
+        ("n_outside", ctypes.c_int32),
+        ("n_inst", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+        ("level", ctypes.c_void_p),
+        ("coord", ctypes.c_void_p),
+        ("nbr", ctypes.c_void_p),
+        ("nbr_rel", ctypes.c_void_p),
+        ("out_src", ctypes.c_void_p),
+        ("out_normal", ctypes.c_void_p),
+        ("out_border", ctypes.c_void_p),
+        ("inst", ctypes.c_void_p),
+    ]
+
+
+EXPORTS = [
+    "g5_version",
+    "g5_create",
+    "g5_destroy",
+    "g5_set_mesh",
+    "g5_mem_bytes",
+    "g5_step",
+    "g5_step_dev",
+    "g5_compute_inv_dt",
+    "g5_fill_outside",
+    "g5_begin",
+    "g5_advance",
+    "g5_run",
+    "g5_refine_flags",
+    "g5_status",
+    "g5_tune",
+    "g5_last_launch_count",
+]
+
+_lib = None
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load_library(build_if_missing: bool = True):
+    """Load libg5gpu.so (building it in-tree if needed)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = library_path()
+    if not os.path.exists(path) or not _build.up_to_date():
+        if not build_if_missing:
+            raise RuntimeError(f"CUDA library missing: {path}")
+        _build.build()
+    L = ctypes.CDLL(path)
+    vp = ctypes.c_void_p
+    L.g5_version.restype = ctypes.c_char_p
+    L.g5_create.argtypes = [ctypes.POINTER(G5Params), ctypes.POINTER(vp)]
+    L.g5_destroy.argtypes = [vp]
+    L.g5_set_mesh.argtypes = [vp, ctypes.POINTER(G5Mesh)]
+    L.g5_mem_bytes.restype = ctypes.c_int64
+    L.g5_mem_bytes.argtypes = [vp]
+    L.g5_step.argtypes = [vp, vp, vp, vp, ctypes.c_int, vp, vp]
+    L.g5_step_dev.argtypes = [vp, vp, vp, vp, ctypes.c_int, vp, vp]
+    L.g5_compute_inv_dt.argtypes = [vp, vp, vp, vp]
+    L.g5_fill_outside.argtypes = [vp, vp, vp]
+    L.g5_run.argtypes = [vp, vp, vp, ctypes.c_int, ctypes.c_int, vp, vp]
+    L.g5_begin.argtypes = [vp, vp, vp]
+    L.g5_advance.argtypes = [vp, vp, vp, ctypes.c_int, vp, vp]
+    L.g5_refine_flags.argtypes = [vp, vp, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int, vp, vp]
+    L.g5_status.argtypes = [vp, vp]
+    L.g5_tune.argtypes = [vp, vp, vp, ctypes.c_int, vp]
+    L.g5_last_launch_count.argtypes = [vp]
+    _lib = L
+    return L
+
+
+def make_params(p) -> G5Params:
+    o = G5Params()
+    o.dim = p.dim
+    o.bsize = p.bsize
+    o.integrator = p.integrator
+    o.thinc = p.thinc
+    o.source_term = p.source_term
+    o.prolongation = p.prolongation
+    for i in range(6):
+        o.bc[i] = int(p.bc[i])
+    for k in range(2):
+        o.gamma[k] = p.gamma[k]
+        o.pinf[k] = p.pinf[k]
+    o.smallr = p.smallr
+    o.smallc = p.smallc
+    o.slope_type = p.slope_type
+    o.cfl = p.cfl
+    o.thinc_beta = p.thinc_beta
+    o.thinc_eps = p.thinc_eps
+    for i in range(32):
+        o.level_dx[i] = float(p.level_dx[i])
+    return o
+
+
+def _dptr(t) -> int:
+    import torch
+
+    if not isinstance(t, torch.Tensor) or not t.is_cuda or t.dtype != torch.float64 or not t.is_contiguous():
+        raise TypeError("expected a contiguous float64 CUDA tensor")
+    return t.data_ptr()
+
+
+def _stream(stream):
+    import torch
+
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+class GodunovImplemGB300:
+    """GB300 implementation of the reference's GodunovImplemBase (implementation_version 3)."""
+
+    implementation_version = 3
+
+    def __init__(self, params, table=None):
+        self.lib = load_library()
+        self.params = params
+        self._prm = make_params(params)
+        ctx = ctypes.c_void_p()
+        rc = self.lib.g5_create(ctypes.byref(self._prm), ctypes.byref(ctx))
+        if rc != 0:
+            raise G5Error(rc, "g5_create")
+        self.ctx = ctx
+        self.table = None
+        if table is not None:
+            self.resize_auxiliary_data(table)
+
+    def close(self):
+        if getattr(self, "ctx", None):
+            self.lib.g5_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # --------------------------------------------------------------- the API
+    def resize_auxiliary_data(self, table):
+        keep = dict(
+            level=np.ascontiguousarray(table.level, np.int32),
+            coord=np.ascontiguousarray(table.coord, np.int32),
+            nbr=np.ascontiguousarray(table.nbr, np.int32),
+            nbr_rel=np.ascontiguousarray(table.nbr_rel, np.int8),
+            out_src=np.ascontiguousarray(table.out_src, np.int32),
+            out_normal=np.ascontiguousarray(table.out_normal, np.int8),
+            out_border=np.ascontiguousarray(table.out_border, np.int8),
+            inst=np.ascontiguousarray(table.inst, np.int32),
+        )
+        m = G5Mesh()
+        m.n_owned = table.n_owned
+        m.n_outside = table.n_outside
+        m.n_inst = table.n_inst
+        for k, v in keep.items():
+            setattr(m, k, v.ctypes.data_as(ctypes.c_void_p) if v.size else None)
+        rc = self.lib.g5_set_mesh(self.ctx, ctypes.byref(m))
+        if rc != 0:
+            raise G5Error(rc, "g5_set_mesh")
+        self.table = table
+
+    def total_mem_size_in_bytes(self) -> int:
+        return int(self.lib.g5_mem_bytes(self.ctx))
+
+    def do_time_step(self, U, U2, *args, mode="fp64", inv_dt_out=None, stream=None):
+        """do_time_step(U, U2, dt) or do_time_step(U, U2, t, dt); dt scalar or per instance."""
+        dt = args[-1]
+        dt = np.ascontiguousarray(np.broadcast_to(np.asarray(dt, np.float64), (self.table.n_inst,)))
+        rc = self.lib.g5_step(
+            self.ctx,
+            ctypes.c_void_p(_dptr(U)),
+            ctypes.c_void_p(_dptr(U2)),
+            dt.ctypes.data_as(ctypes.c_void_p),
+            MODES[mode],
+            ctypes.c_void_p(_dptr(inv_dt_out)) if inv_dt_out is not None else None,
+            _stream(stream),
+        )
+        if rc != 0:
+            raise G5Error(rc, "g5_step")
+
+    def do_time_step_dev(self, U, U2, dt_dev, mode="fp64", inv_dt_out=None, stream=None):
+        rc = self.lib.g5_step_dev(
+            self.ctx,
+            ctypes.c_void_p(_dptr(U)),
+            ctypes.c_void_p(_dptr(U2)),
+            ctypes.c_void_p(_dptr(dt_dev)),
+            MODES[mode],
+            ctypes.c_void_p(_dptr(inv_dt_out)) if inv_dt_out is not None else None,
+            _stream(stream),
+        )
+        if rc != 0:
+            raise G5Error(rc, "g5_step_dev")
+
+    def compute_inv_dt(self, U, out=None, stream=None):
+        import torch
+
+        if out is None:
+            out = torch.zeros(self.table.n_inst, dtype=torch.float64, device=U.device)
+        rc = self.lib.g5_compute_inv_dt(self.ctx, ctypes.c_void_p(_dptr(U)), ctypes.c_void_p(_dptr(out)), _stream(stream))
+        if rc != 0:
+            raise G5Error(rc, "g5_compute_inv_dt")
+        return out
+
+    def compute_dt_local(self, U, stream=None):
+        return self.params.cfl / self.compute_inv_dt(U, stream=stream)
+
+    def fill_outside_quadrants(self, U, stream=None):
+        rc = self.lib.g5_fill_outside(self.ctx, ctypes.c_void_p(_dptr(U)), _stream(stream))
+        if rc != 0:
+            raise G5Error(rc, "g5_fill_outside")
+
+    def run(self, U, U2, nsteps, mode="fp64", dt_hist=None, stream=None):
+        """Solver loop: nsteps x {dt = cfl/invDt; step; fill outside}; final state in U."""
+        rc = self.lib.g5_run(
+            self.ctx,
+            ctypes.c_void_p(_dptr(U)),
+            ctypes.c_void_p(_dptr(U2)),
+            int(nsteps),
+            MODES[mode],
+            ctypes.c_void_p(_dptr(dt_hist)) if dt_hist is not None else None,
+            _stream(stream),
+        )
+        if rc != 0:
+            raise G5Error(rc, "g5_run")
+
+    def begin(self, U, stream=None):
+        """g5_begin: fill outside blocks of U and set the CFL accumulator to inv_dt(U)."""
+        rc = self.lib.g5_begin(self.ctx, ctypes.c_void_p(_dptr(U)), _stream(stream))
+        if rc != 0:
+            raise G5Error(rc, "g5_begin")
+
+    def advance(self, U, U2, mode="fp64", dt_out=None, stream=None):
+        """g5_advance: one solver step U -> U2 with the device-resident dt (graph replay)."""
+        rc = self.lib.g5_advance(
+            self.ctx,
+            ctypes.c_void_p(_dptr(U)),
+            ctypes.c_void_p(_dptr(U2)),
+            MODES[mode],
+            ctypes.c_void_p(_dptr(dt_out)) if dt_out is not None else None,
+            _stream(stream),
+        )
+        if rc != 0:
+            raise G5Error(rc, "g5_advance")
+
+    def refine_flags(self, U, indicator=0, eps_refine=0.1, eps_coarsen=0.0125, eps_lohner=0.02, level_min=0, level_max=30, stream=None):
+        import torch
+
+        flags = torch.empty(self.table.n_owned, dtype=torch.int8, device=U.device)
+        rc = self.lib.g5_refine_flags(
+            self.ctx,
+            ctypes.c_void_p(_dptr(U)),
+            int(indicator),
+            float(eps_refine),
+            float(eps_coarsen),
+            float(eps_lohner),
+            int(level_min),
+            int(level_max),
+            ctypes.c_void_p(flags.data_ptr()),
+            _stream(stream),
+        )
+        if rc != 0:
+            raise G5Error(rc, "g5_refine_flags")
+        return flags
+
+    def status(self, stream=None) -> int:
+        rc = self.lib.g5_status(self.ctx, _stream(stream))
+        if rc < 0:
+            raise G5Error(rc, "g5_status")
+        return rc
+
+    def tune(self, U, U2, mode="fp64", stream=None) -> int:
+        rc = self.lib.g5_tune(self.ctx, ctypes.c_void_p(_dptr(U)), ctypes.c_void_p(_dptr(U2)), MODES[mode], _stream(stream))
+        if rc < 0:
+            raise G5Error(rc, "g5_tune")
+        return rc
+
+    def last_launch_count(self) -> int:
+        return int(self.lib.g5_last_launch_count(self.ctx))
+
+
+def gpu_flag_fn(indicator=0, eps_refine=0.1, eps_coarsen=0.0125, eps_lohner=0.02):
+    """Refine-flag callback (runs g5_refine_flags on the GPU) for
+    configs.refine_from_initial_condition."""
+
+    def fn(table, params, U, level_min, level_max):
+        import torch
+
+        impl = GodunovImplemGB300(params, table)
+        d = torch.from_numpy(U).cuda()
+        impl.fill_outside_quadrants(d)
+        f = impl.refine_flags(d, indicator, eps_refine, eps_coarsen, eps_lohner, level_min, level_max)
+        torch.cuda.synchronize()
+        out = f.cpu().numpy()
+        impl.close()
+        return out
+
+    return fn

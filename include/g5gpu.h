@@ -1,0 +1,199 @@
+/*
+ * g5gpu.h — C ABI of the GB300 (sm_103a) five-equation block timestep.
+ *
+ * This is the drop-in boundary for the reference's GodunovImplemBase
+ * (scheme/GodunovImplemBase.h:59-198): a solver that owns U and U2 on the
+ * device calls g5_step where it called GodunovImplemBase::do_time_step, and
+ * g5_compute_inv_dt where it called ComputeDtFiveEqFunctor::apply.  Plain
+ * pointers and sizes only; all device pointers are caller-owned except the
+ * scratch the context allocates in g5_set_mesh and frees in g5_destroy.
+ *
+ * Data layout (identical to the reference's DataArrayBlock, cell index
+ * fastest, then variable, then block):
+ *   U[n_blocks][nv][bsize^dim], FP64, nv = 8 (2D) or 9 (3D),
+ *   variable ids ID=0 IE=1 IU=2 IV=3 (IW=4) IA0 IAD0 IA1 IAD1
+ *   (models/FiveEq.h:35-50); owned blocks first, then outside blocks.
+ *
+ * Every call returns 0 on success or a negative G5_ERR_* code.  Nothing
+ * traps or asserts on the device: device-side problems raise bits in a
+ * status word read by g5_status.  Calls are asynchronous on the stream
+ * given; g5_step, g5_step_dev, g5_fill_outside and g5_compute_inv_dt
+ * neither allocate nor synchronise, so they may be captured in a CUDA graph.
+ */
+#ifndef G5GPU_H_
+#define G5GPU_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* error codes */
+#define G5_OK 0
+#define G5_ERR_ARG (-1)         /* invalid argument */
+#define G5_ERR_CUDA (-2)        /* a CUDA runtime call failed */
+#define G5_ERR_NONPHYSICAL (-3) /* device flag: non-finite state or empty volume fractions */
+#define G5_ERR_TIMEOUT (-4)     /* device flag: a bounded device wait gave up */
+#define G5_ERR_MESH (-5)        /* invalid block table (or device flag: index out of range) */
+#define G5_ERR_UNSUPPORTED (-6) /* (dim, bsize, option) combination not compiled */
+
+/* status bits returned by g5_status */
+#define G5_STATUS_NONPHYSICAL 1u
+#define G5_STATUS_MESH 2u
+#define G5_STATUS_TIMEOUT 4u
+
+/* precision modes of g5_step (arithmetic of the flux computation) */
+#define G5_MODE_FP64 0  /* the reference's method, all FP64 */
+#define G5_MODE_MIXED 1 /* FP32 bulk (slopes, predictor, HLLC), FP64 pressure recovery, accumulation, renormalisation, dt */
+
+/* boundary condition codes (border_conditions/FillOutside.h:51-55) */
+#define G5_BC_NONE 0
+#define G5_BC_PERIODIC 1
+#define G5_BC_ZERO_GRADIENT 2
+#define G5_BC_WALL 3
+
+/*
+ * Scheme parameters: HydroSettings (models/HydroSettings.h:30-54), the EOS of
+ * the two materials (stiffened gas; gamma, pinf), THINCParams, the time
+ * integrator, the volume-fraction source term type, border conditions and the
+ * cell length of every AMR level (compute_cell_length(level, bx) *
+ * scaling_factor, scheme/ComputeFluxesAndStoreFunctor.cpp:359).
+ */
+typedef struct G5Params
+{
+  int32_t dim;          /* 2 or 3 */
+  int32_t bsize;        /* cells per block edge: 2D 8 or 16, 3D 8 */
+  int32_t integrator;   /* 0 HANCOCK, 1 RK1 */
+  int32_t thinc;        /* 0 MUSCL, 1 THINC interface reconstruction */
+  int32_t source_term;  /* 0 ALLAIRE_KOKH (only value implemented on the GPU) */
+  int32_t prolongation; /* 0 SIMPLE_COPY (only value implemented) */
+  int32_t bc[6];        /* xmin xmax ymin ymax zmin zmax */
+  double  gamma[2];
+  double  pinf[2];
+  double  smallr;
+  double  smallc;
+  double  slope_type; /* 1 minmod, 2 MC */
+  double  cfl;
+  double  thinc_beta;
+  double  thinc_eps;
+  double  level_dx[32];
+} G5Params;
+
+/*
+ * Block table (host pointers; copied to the device by g5_set_mesh).  It
+ * replaces the reference's orchard keys + hashmap + StencilHelper +
+ * conformal status for one step (resize_auxiliary_data,
+ * scheme/GodunovImplemV0.cpp:37-61).  Slot s of a block is the same-level
+ * neighbour at offset (dx,dy,dz) in {-1,0,1}^dim, s = (dx+1) + 3(dy+1) + 9(dz+1).
+ */
+typedef struct G5Mesh
+{
+  int32_t         n_owned;    /* owned leaf blocks */
+  int32_t         n_outside;  /* outside blocks (boundary conditions), stored after the owned ones */
+  int32_t         n_inst;     /* independent instances batched in the table (>= 1) */
+  int32_t         reserved;
+  const int32_t * level;      /* [n_owned + n_outside] AMR level */
+  const int32_t * coord;      /* [(n_owned + n_outside) * 3] block coordinates at its level */
+  const int32_t * nbr;        /* [n_owned * 3^dim * 2^dim] neighbour blocks per slot (children for finer slots) */
+  const int8_t *  nbr_rel;    /* [n_owned * 3^dim] -1 coarser, 0 same level, +1 finer */
+  const int32_t * out_src;    /* [n_outside] inside block copied by each outside block */
+  const int8_t *  out_normal; /* [n_outside * 3] outside normal of each outside block */
+  const int8_t *  out_border; /* [n_outside * 6] inside block touches domain face f */
+  const int32_t * inst;       /* [n_owned + n_outside] instance of each block, NULL = all 0 */
+} G5Mesh;
+
+typedef struct G5Context G5Context;
+
+/* version string of the library */
+const char * g5_version(void);
+
+/* Create a context on the current CUDA device.  Mirrors the
+ * GodunovImplemBase constructor (scheme/GodunovImplemBase.h:71-89). */
+int g5_create(const G5Params * params, G5Context ** out_ctx);
+
+/* Destroy a context and free its device memory. */
+int g5_destroy(G5Context * ctx);
+
+/* Upload a block table and size the scratch memory: mirrors
+ * GodunovImplemV0::resize_auxiliary_data (scheme/GodunovImplemV0.cpp:37-61).
+ * Synchronous (allocates); call it outside stream capture. */
+int g5_set_mesh(G5Context * ctx, const G5Mesh * mesh);
+
+/* Device bytes held by the context: GodunovImplemBase::total_mem_size_in_bytes
+ * (scheme/GodunovImplemBase.h:98-99). */
+int64_t g5_mem_bytes(const G5Context * ctx);
+
+/* One time step U -> U2 of every owned block, with dt per instance given on
+ * the host (dt_host[n_inst]).  GodunovImplemBase::do_time_step(U, U2, dt)
+ * (scheme/GodunovImplemBase.h:102-103, scheme/GodunovImplemV0.cpp:85-151).
+ * U's outside blocks must hold the boundary values (g5_fill_outside).
+ * The owned blocks of U2 are written (U2's outside blocks are untouched);
+ * U2 need not be initialised.  mode = G5_MODE_FP64 or G5_MODE_MIXED.
+ * inv_dt_out (device, [n_inst], may be NULL) receives, fused in the same
+ * kernels, max over owned cells of sum_d (c+|u_d|)/dx of the NEW state U2,
+ * i.e. the input of the next step's dt (ComputeDtFiveEqFunctor::compute_cfl,
+ * scheme/ComputeDtFiveEqFunctor.cpp:87-134); it must be zeroed by the caller
+ * (or use g5_step_dev, which manages it). */
+int g5_step(G5Context * ctx, const double * d_U, double * d_U2, const double * dt_host, int mode, double * d_inv_dt_out, void * stream);
+
+/* Same as g5_step with dt read from device memory (d_dt[n_inst]). */
+int g5_step_dev(G5Context * ctx, const double * d_U, double * d_U2, const double * d_dt, int mode, double * d_inv_dt_out, void * stream);
+
+/* ComputeDtFiveEqFunctor::apply (scheme/ComputeDtFiveEqFunctor.h:113-121):
+ * d_inv_dt[n_inst] <- max over owned cells of sum_d (c+|u_d|)/dx. */
+int g5_compute_inv_dt(G5Context * ctx, const double * d_U, double * d_inv_dt, void * stream);
+
+/* FillOutsideCellFunctor::apply (border_conditions/FillOutside.cpp:44-65):
+ * fill the outside blocks of U from the inside blocks. */
+int g5_fill_outside(G5Context * ctx, double * d_U, void * stream);
+
+/* Solver loop of SolverGodunovFiveEq::next_iteration_impl for HANCOCK/RK1
+ * (SolverGodunovFiveEq.cpp:394-526), split in two calls so that a caller can
+ * interleave its own work between steps:
+ *   g5_begin(U):        fill the outside blocks of U and set the context's
+ *                       CFL accumulator to inv_dt(U) (compute_dt_local);
+ *   g5_advance(U, U2):  dt = cfl / inv_dt (kept on the device), U2 = step(U),
+ *                       fill the outside blocks of U2, inv_dt(U2) fused in
+ *                       the step.  The caller then swaps U and U2.
+ * g5_advance replays a CUDA graph cached per (U, U2, mode).  d_dt_out
+ * (device, [n_inst], may be NULL) receives the dt used. */
+int g5_begin(G5Context * ctx, double * d_U, void * stream);
+int g5_advance(G5Context * ctx, const double * d_U, double * d_U2, int mode, double * d_dt_out, void * stream);
+
+/* nsteps of the loop above (g5_begin then g5_advance with U/U2 swapped each
+ * step); on exit the final state is in d_U (d_U2 is scratch of the same
+ * size).  d_dt_hist (device, [nsteps * n_inst], may be NULL) receives every dt. */
+int g5_run(G5Context * ctx, double * d_U, double * d_U2, int nsteps, int mode, double * d_dt_hist, void * stream);
+
+/* ComputeRefineFlags::run (scheme/ComputeRefineFlags.cpp:18-65): per owned
+ * block, max over cells of the indicator flag (-1 init, 0 coarsen, 1 nothing,
+ * 2 refine).  indicator: 0 SIMPLE_GRADIENT, 1 LOHNER_UNSPLIT, 2 LOHNER_SPLIT. */
+int g5_refine_flags(G5Context * ctx,
+                    const double * d_U,
+                    int            indicator,
+                    double         eps_refine,
+                    double         eps_coarsen,
+                    double         eps_lohner,
+                    int            level_min,
+                    int            level_max,
+                    int8_t *       d_flags,
+                    void *         stream);
+
+/* Read and clear the device status word (synchronises the stream).
+ * Returns the G5_STATUS_* bits (>= 0) or a negative error. */
+int g5_status(G5Context * ctx, void * stream);
+
+/* Autotune the launch shape (CTAs per SM of the persistent step kernel) for
+ * the current mesh: times each candidate on d_U -> d_U2 and keeps the best.
+ * Returns the chosen CTAs per SM (> 0) or a negative error. */
+int g5_tune(G5Context * ctx, const double * d_U, double * d_U2, int mode, void * stream);
+
+/* Number of kernel launches issued by the last g5_step / g5_advance / g5_run call. */
+int g5_last_launch_count(const G5Context * ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* G5GPU_H_ */
