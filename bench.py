@@ -43,7 +43,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "cell-updates/s, 1 GB300: mixed vs FP64 plain at L1 err<=1e-5 vs FP64; %HBM peak"
 BYTES_PER_CELL_2D = 2 * 8 * 8  # read U + write U2, 8 FP64 variables
-L1_STEPS = {"shock_bubble": 500, "gas_water": 200, "droplets": 100, "shock_bubble_r22_thinc": 500}
+L1_STEPS = {"shock_bubble": 500, "gas_water": 200, "droplets": 100, "droplets32": 100, "shock_bubble_r22_thinc": 500}
 
 
 def parse():
@@ -55,6 +55,7 @@ def parse():
     ap.add_argument("--workload", choices=list(L1_STEPS), default="shock_bubble")
     ap.add_argument("--no-l1", action="store_true", help="skip the 500-step accuracy run")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--profile", action="store_true", help="one FP64 and one mixed step kernel launch, for ncu")
     return ap.parse_args()
 
 
@@ -70,6 +71,10 @@ def build_workload(name, flag_fn):
     elif name == "gas_water":
         mesh, t, p, U = configs.gas_water_shock_tube()
         desc = "gas_water_shock_tube_2d_512x32_16x16"
+    elif name == "droplets32":
+        _, t, p, U, _ = configs.droplet_instances(n_inst=32)
+        U = np.ascontiguousarray(U)
+        desc = "droplet_advection_2d_32_instances_16x16"
     else:
         _, t, p, U, _ = configs.droplet_instances()
         U = np.ascontiguousarray(U)
@@ -225,6 +230,19 @@ def run_reference(args):
     return 0
 
 
+def _load(impl, A, B, mode, seconds):
+    """Untimed solver steps for about `seconds` (keeps the GPU under the timed load)."""
+    import torch
+
+    t0 = time.perf_counter()
+    while time.perf_counter() - t0 < seconds:
+        for _ in range(20):
+            impl.advance(A, B, mode)
+            A, B = B, A
+        torch.cuda.synchronize()
+    return A, B
+
+
 def time_steps(impl, A, B, mode, steps, flush, stream):
     """K solver steps, each timed alone after an L2 flush; returns (total ms, launches, A, B)."""
     import torch
@@ -261,10 +279,32 @@ def time_kernel(impl, A, B, d_dt, mode, steps, flush, stream):
     return float(np.mean(ts))
 
 
+def run_profile_case(args):
+    """The step kernel launched once in FP64 and once in mixed mode (for ncu)."""
+    import torch
+
+    from godunov_five_eq_gb300 import GodunovImplemGB300, gpu_flag_fn
+
+    desc, t, p, U = build_workload(args.workload, gpu_flag_fn())
+    impl = GodunovImplemGB300(p, t)
+    A = torch.from_numpy(U.copy()).cuda()
+    B = torch.zeros_like(A)
+    impl.fill_outside_quadrants(A)
+    dt = impl.compute_dt_local(A)
+    impl.do_time_step_dev(A, B, dt, mode="fp64")
+    impl.do_time_step_dev(A, B, dt, mode="mixed")
+    torch.cuda.synchronize()
+    st = impl.status()
+    print(json.dumps({"profile_case": desc, "cells": int(t.n_owned * t.ncell), "status": st}))
+    return 0 if st == 0 else 1
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.profile:
+        return run_profile_case(args)
     import torch
     import torch.distributed as dist
 
@@ -294,8 +334,13 @@ def main():
             dist.barrier()
         sampler = ClockSampler(local) if mode == "mixed" else None
         if sampler:
+            # nvidia-smi samples every 200 ms: the same load runs for ~0.5 s
+            # before and after the timed steps so that the samples see it
             sampler.start()
+            A, B = _load(impl, A, B, mode, 0.5)
         total_ms, launches, A, B = time_steps(impl, A, B, mode, args.steps, flush, stream)
+        if sampler:
+            A, B = _load(impl, A, B, mode, 0.4)
         clocks = sampler.stop() if sampler else None
         if world > 1:
             tt = torch.tensor([total_ms], device="cuda", dtype=torch.float64)

@@ -174,50 +174,6 @@ prim_fp64(const double * u, double * q, const PhysParams & P)
   return sound_speed_d(P, d, p, a0, 1.0 - a0);
 }
 
-// FP32-bulk form: FP64 only for the pressure numerator rho e - PI, where the
-// stiffened-gas constant cancels against the internal energy.
-template <int DIM>
-__device__ __forceinline__ void
-prim_mixed(const double * u, float * q, const PhysParams & P)
-{
-  using H = V<DIM>;
-  const float d = fmaxf((float)u[H::ID], (float)P.smallr);
-  const float inv = __frcp_rn(d);
-  const float ux = (float)u[H::IU] * inv;
-  const float uy = (float)u[H::IV] * inv;
-  float       k2 = ux * ux + uy * uy;
-  float       uz = 0.0f;
-  if constexpr (DIM == 3)
-  {
-    uz = (float)u[H::IW] * inv;
-    k2 += uz * uz;
-  }
-  const double a0u = u[H::IA0];
-  const double a1u = 1.0 - a0u;
-  const double num = (u[H::IE] - (double)(0.5f * d * k2)) - (a0u * P.gpx[0] + a1u * P.gpx[1]);
-  const float  S = (float)a0u * (float)P.xi[0] + (float)a1u * (float)P.xi[1];
-  const float  p = __fdividef((float)num, S);
-  float        a0 = fmaxf(0.0f, fminf(1.0f, (float)a0u));
-  float        r0 = (float)u[H::IAD0], r1 = (float)u[H::IAD1];
-  const float  eps = 1e-12f;
-  if (r0 < eps)
-    r0 = 0.0f;
-  if (r1 < eps)
-    r1 = 0.0f;
-  if (a0 < eps)
-    a0 = 0.0f;
-  if (a0 > 1.0f - eps)
-    a0 = 1.0f;
-  q[H::QR0] = r0;
-  q[H::QR1] = r1;
-  q[H::QP] = p;
-  q[H::QU] = ux;
-  q[H::QV] = uy;
-  if constexpr (DIM == 3)
-    q[H::QW] = uz;
-  q[H::QA] = a0;
-}
-
 // scheme/ComputeLimitedSlopesFunctor.cpp:116-137
 template <typename R>
 __device__ __forceinline__ R
@@ -495,6 +451,136 @@ hllc_fp32(const float * ql, const float * qr, float xi0, float xi1, float gp0, f
   f[H::FA0] = uo * phi0;
   f[H::FA1] = uo * (1.0f - phi0);
   f[H::FUS] = uo;
+}
+
+
+// ---------------------------------------------------------------------------
+// helpers of the FP32-bulk path.  On GB300 the FP64 pipe issues 1.6
+// instructions/clk/SM against 115 for FP32, and float -> double conversion
+// runs on the FP64 pipe, so the mixed path keeps FP64 to the adds into the
+// stored state, the renormalisation and the stiffened-gas pressure
+// numerator, and does everything else on the FP32 and integer pipes.
+// ---------------------------------------------------------------------------
+
+// exact float -> double on the integer pipe (float denormals read as zero,
+// as the fast-math build flushes them anyway)
+__device__ __forceinline__ double
+f2d_exact(float f)
+{
+  const unsigned b = __float_as_uint(f);
+  const unsigned e = (b >> 23) & 0xFFu;
+  const unsigned sgn = b & 0x80000000u;
+  const unsigned m = b & 0x7FFFFFu;
+  unsigned       hi = sgn | ((e + 896u) << 20) | (m >> 3);
+  unsigned       lo = m << 29;
+  if (e == 0u)
+  {
+    hi = sgn;
+    lo = 0u;
+  }
+  if (e == 0xFFu)
+    hi = sgn | 0x7FF00000u | (m >> 3);
+  return __hiloint2double((int)hi, (int)lo);
+}
+
+// error-free difference of two floats: a - b == hi + lo exactly (Knuth's TwoSum)
+__device__ __forceinline__ void
+two_diff(float a, float b, float & hi, float & lo)
+{
+  hi = __fsub_rn(a, b);
+  const float bb = __fsub_rn(a, hi);
+  lo = __fadd_rn(__fsub_rn(a, __fadd_rn(hi, bb)), __fsub_rn(bb, b));
+}
+
+// error-free sum of two floats: a + b == hi + lo exactly
+__device__ __forceinline__ void
+two_sum(float a, float b, float & hi, float & lo)
+{
+  hi = __fadd_rn(a, b);
+  const float bb = __fsub_rn(hi, a);
+  lo = __fadd_rn(__fsub_rn(a, __fsub_rn(hi, bb)), __fsub_rn(b, bb));
+}
+
+// ordered comparisons of doubles against positive constants on the integer
+// pipe (IEEE doubles order like sign-magnitude integers; NaN never clamps to 0)
+__device__ __forceinline__ bool
+dlt_pos(double x, double c)
+{
+  return __double_as_longlong(x) < __double_as_longlong(c);
+}
+__device__ __forceinline__ bool
+dgt_pos(double x, double c)
+{
+  const long long b = __double_as_longlong(x);
+  return b > __double_as_longlong(c) && b < 0x7FF0000000000001LL;
+}
+__device__ __forceinline__ bool
+finite_bits(double x)
+{
+  return (__double2hiint(x) & 0x7FF00000) != 0x7FF00000;
+}
+
+// mixture pressure from a conservative state: FP32 except the numerator
+// rho e - PI when a stiffened-gas constant makes it cancel (FP64 then).
+// Returns p; also the FP32 density and velocities.
+template <int DIM>
+__device__ __forceinline__ float
+pressure_mixed(const double * u, const PhysParams & P, bool stiff, float & d, float & ux, float & uy, float & uz, float & a0f)
+{
+  using H = V<DIM>;
+  d = fmaxf((float)u[H::ID], (float)P.smallr);
+  const float inv = __frcp_rn(d);
+  ux = (float)u[H::IU] * inv;
+  uy = (float)u[H::IV] * inv;
+  float k2 = ux * ux + uy * uy;
+  uz = 0.0f;
+  if constexpr (DIM == 3)
+  {
+    uz = (float)u[H::IW] * inv;
+    k2 += uz * uz;
+  }
+  const double a0u = u[H::IA0];
+  a0f = (float)a0u;
+  const float K = 0.5f * d * k2;
+  float       num;
+  if (stiff)
+  {
+    const double PI = fma(a0u, P.gpx[0] - P.gpx[1], P.gpx[1]);
+    num = (float)((u[H::IE] - PI) - f2d_exact(K));
+  }
+  else
+    num = (float)u[H::IE] - K;
+  const float S = fmaf(a0f, (float)(P.xi[0] - P.xi[1]), (float)P.xi[1]);
+  return __fdividef(num, S);
+}
+
+// FP32-bulk conservative -> primitive (computePrimitives, models/utils.h:200-250)
+template <int DIM>
+__device__ __forceinline__ void
+prim_mixed(const double * u, float * q, const PhysParams & P, bool stiff)
+{
+  using H = V<DIM>;
+  float       d, ux, uy, uz, a0f;
+  const float p = pressure_mixed<DIM>(u, P, stiff, d, ux, uy, uz, a0f);
+  float       a0 = fmaxf(0.0f, fminf(1.0f, a0f));
+  float       r0 = (float)u[H::IAD0], r1 = (float)u[H::IAD1];
+  const float eps = 1e-12f;
+  if (r0 < eps)
+    r0 = 0.0f;
+  if (r1 < eps)
+    r1 = 0.0f;
+  if (a0 < eps)
+    a0 = 0.0f;
+  if (a0 > 1.0f - eps)
+    a0 = 1.0f;
+  q[H::QR0] = r0;
+  q[H::QR1] = r1;
+  q[H::QP] = p;
+  q[H::QU] = ux;
+  q[H::QV] = uy;
+  if constexpr (DIM == 3)
+    q[H::QW] = uz;
+  q[H::QA] = a0;
 }
 
 } // namespace g5

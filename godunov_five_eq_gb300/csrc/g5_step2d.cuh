@@ -124,13 +124,13 @@ gather_ghost_2d(const StepArgs & a, int n, int gx, int gy, double * u)
 
 template <int B, bool MIXED>
 __device__ __forceinline__ void
-store_prim(typename Step2DTraits<B, MIXED>::R * sQ, int gidx, const double * u, const PhysParams & P)
+store_prim(typename Step2DTraits<B, MIXED>::R * sQ, int gidx, const double * u, const PhysParams & P, bool stiff)
 {
   constexpr int GG = (B + 4) * (B + 4);
   if constexpr (MIXED)
   {
     float q[6];
-    prim_mixed<2>(u, q, P);
+    prim_mixed<2>(u, q, P, stiff);
 #pragma unroll
     for (int k = 0; k < 6; ++k)
       sQ[k * GG + gidx] = q[k];
@@ -252,6 +252,160 @@ face_state(const typename Step2DTraits<B, MIXED>::R * sQ,
   }
 }
 
+// ReadFluxesAndConservativeUpdateFunctor (X then Y, update_U with the
+// per-direction clamps, .cpp:115-305, .h:319-349), FixVolumeFractionsNormalization
+// (.cpp:49-72) and the CFL rate of the new state (ComputeDtFiveEqFunctor.cpp:87-134),
+// FP64 in the reference's operation order.  Returns the cell's CFL rate (or 0).
+template <int B>
+__device__ __forceinline__ double
+update_fp64(const double * uin, double * u2, const double * sFx, const double * sFy, int ci, int cj, double dx, const PhysParams & P, bool want_dt)
+{
+  using H = V<2>;
+  constexpr int NFF = B * (B + 1);
+#pragma unroll
+  for (int v = 0; v < H::NV; ++v)
+    u2[v] = uin[v];
+  const double a0n = uin[H::IA0], a1n = uin[H::IA1];
+#pragma unroll
+  for (int dir = 0; dir < 2; ++dir)
+  {
+    const double * F = dir == 0 ? sFx : sFy;
+    const int      il = dir == 0 ? ci + (B + 1) * cj : ci + B * cj;
+    const int      ir = dir == 0 ? il + 1 : il + B;
+    double         acc[7];
+#pragma unroll
+    for (int k = 0; k < 7; ++k)
+      acc[k] = 0.0 + F[k * NFF + il];
+    const double usl = F[7 * NFF + il];
+    acc[H::FA0] -= usl * a0n;
+    acc[H::FA1] -= usl * a1n;
+#pragma unroll
+    for (int k = 0; k < 7; ++k)
+      acc[k] = acc[k] - F[k * NFF + ir];
+    const double usr = F[7 * NFF + ir];
+    acc[H::FA0] += usr * a0n;
+    acc[H::FA1] += usr * a1n;
+    const double eps = 1e-12;
+    u2[H::IAD0] += acc[H::FR0];
+    if (u2[H::IAD0] < eps)
+      u2[H::IAD0] = 0.0;
+    u2[H::IAD1] += acc[H::FR1];
+    if (u2[H::IAD1] < eps)
+      u2[H::IAD1] = 0.0;
+    u2[H::IA0] += acc[H::FA0];
+    if (u2[H::IA0] < eps)
+      u2[H::IA0] = 0.0;
+    if (u2[H::IA0] > 1.0 - eps)
+      u2[H::IA0] = 1.0;
+    u2[H::IA1] += acc[H::FA1];
+    if (u2[H::IA1] < eps)
+      u2[H::IA1] = 0.0;
+    if (u2[H::IA1] > 1.0 - eps)
+      u2[H::IA1] = 1.0;
+    u2[H::IE] += acc[H::FE];
+    u2[H::IU] += acc[H::FU];
+    u2[H::IV] += acc[H::FV];
+  }
+  const double sum_alpha = u2[H::IA0] + u2[H::IA1];
+  const double sum_alpha_rho = u2[H::IAD0] + u2[H::IAD1];
+  const double inv = 1.0 / sum_alpha;
+  u2[H::IA0] *= inv;
+  u2[H::IA1] *= inv;
+  u2[H::ID] = sum_alpha_rho;
+  if (!want_dt)
+    return 0.0;
+  double       q[6];
+  const double c = prim_fp64<2>(u2, q, P);
+  return (c + fabs(q[H::QU])) / dx + (c + fabs(q[H::QV])) / dx;
+}
+
+// The same update in the FP32-bulk form.  FP64 is used only for the adds
+// into the stored state: the partial densities receive both face fluxes of
+// each direction exactly (error-free float difference, two FP64 adds), so
+// per-material mass is conserved to FP64 round-off; energy and momentum
+// accumulate both directions as an exact float-float sum; the clamps run on
+// the integer pipe; the renormalisation divides by 1 + d as a multiply by
+// (1 - d) when |d| < 1e-8 (exact to FP64 rounding).
+template <int B>
+__device__ __forceinline__ float
+update_mixed(const double * uin, double * u2, const float * sFx, const float * sFy, int ci, int cj, float dx, const PhysParams & P, bool stiff, bool want_dt)
+{
+  using H = V<2>;
+  constexpr int NFF = B * (B + 1);
+#pragma unroll
+  for (int v = 0; v < H::NV; ++v)
+    u2[v] = uin[v];
+  const float a0f = (float)uin[H::IA0], a1f = (float)uin[H::IA1];
+  float       eh[3] = { 0.f, 0.f, 0.f }, el[3] = { 0.f, 0.f, 0.f };
+  const double eps = 1e-12, one_m_eps = 1.0 - 1e-12;
+#pragma unroll
+  for (int dir = 0; dir < 2; ++dir)
+  {
+    const float * F = dir == 0 ? sFx : sFy;
+    const int     il = dir == 0 ? ci + (B + 1) * cj : ci + B * cj;
+    const int     ir = dir == 0 ? il + 1 : il + B;
+    float         h, l;
+    two_diff(F[H::FR0 * NFF + il], F[H::FR0 * NFF + ir], h, l);
+    u2[H::IAD0] = (u2[H::IAD0] + f2d_exact(h)) + f2d_exact(l);
+    if (dlt_pos(u2[H::IAD0], eps))
+      u2[H::IAD0] = 0.0;
+    two_diff(F[H::FR1 * NFF + il], F[H::FR1 * NFF + ir], h, l);
+    u2[H::IAD1] = (u2[H::IAD1] + f2d_exact(h)) + f2d_exact(l);
+    if (dlt_pos(u2[H::IAD1], eps))
+      u2[H::IAD1] = 0.0;
+    const float usl = F[H::FUS * NFF + il], usr = F[H::FUS * NFF + ir];
+    const float dA0 = ((F[H::FA0 * NFF + il] - usl * a0f) - F[H::FA0 * NFF + ir]) + usr * a0f;
+    const float dA1 = ((F[H::FA1 * NFF + il] - usl * a1f) - F[H::FA1 * NFF + ir]) + usr * a1f;
+    u2[H::IA0] += f2d_exact(dA0);
+    if (dlt_pos(u2[H::IA0], eps))
+      u2[H::IA0] = 0.0;
+    if (dgt_pos(u2[H::IA0], one_m_eps))
+      u2[H::IA0] = 1.0;
+    u2[H::IA1] += f2d_exact(dA1);
+    if (dlt_pos(u2[H::IA1], eps))
+      u2[H::IA1] = 0.0;
+    if (dgt_pos(u2[H::IA1], one_m_eps))
+      u2[H::IA1] = 1.0;
+    const int ke[3] = { H::FE, H::FU, H::FV };
+#pragma unroll
+    for (int e = 0; e < 3; ++e)
+    {
+      two_diff(F[ke[e] * NFF + il], F[ke[e] * NFF + ir], h, l);
+      float t;
+      two_sum(eh[e], h, eh[e], t);
+      el[e] += t + l;
+    }
+  }
+  u2[H::IE] = (u2[H::IE] + f2d_exact(eh[0])) + f2d_exact(el[0]);
+  u2[H::IU] = (u2[H::IU] + f2d_exact(eh[1])) + f2d_exact(el[1]);
+  u2[H::IV] = (u2[H::IV] + f2d_exact(eh[2])) + f2d_exact(el[2]);
+  // renormalisation
+  const double s = u2[H::IA0] + u2[H::IA1];
+  const double d = s - 1.0;
+  if (d != 0.0)
+  {
+    if ((__double_as_longlong(d) & 0x7FFFFFFFFFFFFFFFLL) < __double_as_longlong(1e-8))
+    {
+      u2[H::IA0] = fma(-u2[H::IA0], d, u2[H::IA0]);
+      u2[H::IA1] = fma(-u2[H::IA1], d, u2[H::IA1]);
+    }
+    else
+    {
+      const double inv = 1.0 / s;
+      u2[H::IA0] *= inv;
+      u2[H::IA1] *= inv;
+    }
+  }
+  u2[H::ID] = u2[H::IAD0] + u2[H::IAD1];
+  if (!want_dt)
+    return 0.0f;
+  float       df, ux, uy, uz, a0;
+  const float p = pressure_mixed<2>(u2, P, stiff, df, ux, uy, uz, a0);
+  const float a0s = fmaxf(0.0f, fminf(1.0f, a0));
+  const float c = sound_speed_f((float)P.xi[0], (float)P.xi[1], (float)P.gpx[0], (float)P.gpx[1], df, p, a0s);
+  return ((c + fabsf(ux)) + (c + fabsf(uy))) * __frcp_rn(dx);
+}
+
 template <int B, bool MIXED>
 __global__ void __launch_bounds__(B * B)
 step2d_kernel(StepArgs a)
@@ -267,17 +421,23 @@ step2d_kernel(StepArgs a)
   R *          sRec = sQ + T::NQ * GG;
   R *          sFx = sRec + T::NREC * SS; // [8][NFF]  X faces (B+1) x B
   R *          sFy = sFx + 8 * NFF;       // [8][NFF]  Y faces B x (B+1)
-  __shared__ double sRed[NT / 32];
+  using DtT = typename std::conditional<MIXED, float, double>::type;
+  __shared__ DtT sRed[NT / 32];
   const int         tid = threadIdx.x;
   const PhysParams & P = a.p;
+  // a stiffened-gas constant makes the pressure numerator cancel: FP64 there
+  const bool stiff = P.gpx[0] != 0.0 || P.gpx[1] != 0.0;
 
   for (int n = blockIdx.x; n < a.m.n_owned; n += gridDim.x)
   {
     const int    lev = a.m.level[n];
     const int    ins = a.m.inst ? a.m.inst[n] : 0;
     const double dx = P.level_dx[lev];
-    const double dtdx = a.dt[ins] / dx;
-    const R      dtdx_r = R(dtdx);
+    R            dtdx_r;
+    if constexpr (MIXED)
+      dtdx_r = (float)a.dt[ins] * __frcp_rn((float)dx);
+    else
+      dtdx_r = a.dt[ins] / dx;
 
     // ---------------- phase 1: own cell (coalesced) + halo gather -> primitives
     const int ci = tid % B, cj = tid / B;
@@ -287,7 +447,7 @@ step2d_kernel(StepArgs a)
 #pragma unroll
       for (int v = 0; v < H::NV; ++v)
         uin[v] = base[v * NC];
-      store_prim<B, MIXED>(sQ, (ci + 2) + G * (cj + 2), uin, P);
+      store_prim<B, MIXED>(sQ, (ci + 2) + G * (cj + 2), uin, P, stiff);
     }
     for (int h = tid; h < NHALO; h += NT)
     {
@@ -301,7 +461,7 @@ step2d_kernel(StepArgs a)
         for (int v = 0; v < H::NV; ++v)
           u[v] = uin[v];
       }
-      store_prim<B, MIXED>(sQ, (gx + 2) + G * (gy + 2), u, P);
+      store_prim<B, MIXED>(sQ, (gx + 2) + G * (gy + 2), u, P, stiff);
     }
     __syncthreads();
 
@@ -458,82 +618,24 @@ step2d_kernel(StepArgs a)
       deferred = (ci == 0 && dsl[0] >= 0) || (ci == B - 1 && dsl[1] >= 0) || (cj == 0 && dsl[2] >= 0) ||
                  (cj == B - 1 && dsl[3] >= 0);
     }
-    double m_inv = 0.0;
+    DtT m_inv = DtT(0);
     if (!deferred)
     {
       double u2[H::NV];
-#pragma unroll
-      for (int v = 0; v < H::NV; ++v)
-        u2[v] = uin[v];
-      const double a0n = uin[H::IA0], a1n = uin[H::IA1];
-#pragma unroll
-      for (int dir = 0; dir < 2; ++dir)
-      {
-        const R * F = dir == 0 ? sFx : sFy;
-        const int il = dir == 0 ? ci + (B + 1) * cj : ci + B * cj;
-        const int ir = dir == 0 ? il + 1 : il + B;
-        double    acc[7];
-        // left face: + F ; alpha source - u* alpha^n
-#pragma unroll
-        for (int k = 0; k < 7; ++k)
-          acc[k] = 0.0 + (double)F[k * NFF + il];
-        const double usl = (double)F[7 * NFF + il];
-        acc[H::FA0] -= usl * a0n;
-        acc[H::FA1] -= usl * a1n;
-#pragma unroll
-        for (int k = 0; k < 7; ++k)
-          acc[k] = acc[k] - (double)F[k * NFF + ir];
-        const double usr = (double)F[7 * NFF + ir];
-        acc[H::FA0] += usr * a0n;
-        acc[H::FA1] += usr * a1n;
-        // update_U with the per-direction clamps (.h:319-349)
-        const double eps = 1e-12;
-        u2[H::IAD0] += acc[H::FR0];
-        if (u2[H::IAD0] < eps)
-          u2[H::IAD0] = 0.0;
-        u2[H::IAD1] += acc[H::FR1];
-        if (u2[H::IAD1] < eps)
-          u2[H::IAD1] = 0.0;
-        u2[H::IA0] += acc[H::FA0];
-        if (u2[H::IA0] < eps)
-          u2[H::IA0] = 0.0;
-        if (u2[H::IA0] > 1.0 - eps)
-          u2[H::IA0] = 1.0;
-        u2[H::IA1] += acc[H::FA1];
-        if (u2[H::IA1] < eps)
-          u2[H::IA1] = 0.0;
-        if (u2[H::IA1] > 1.0 - eps)
-          u2[H::IA1] = 1.0;
-        u2[H::IE] += acc[H::FE];
-        u2[H::IU] += acc[H::FU];
-        u2[H::IV] += acc[H::FV];
-      }
-      // FixVolumeFractionsNormalization (.cpp:49-72)
-      const double sum_alpha = u2[H::IA0] + u2[H::IA1];
-      const double sum_alpha_rho = u2[H::IAD0] + u2[H::IAD1];
-      const double inv = 1.0 / sum_alpha;
-      u2[H::IA0] *= inv;
-      u2[H::IA1] *= inv;
-      u2[H::ID] = sum_alpha_rho;
+      if constexpr (MIXED)
+        m_inv = update_mixed<B>(uin, u2, sFx, sFy, ci, cj, (float)dx, P, stiff, a.invdt != nullptr);
+      else
+        m_inv = update_fp64<B>(uin, u2, sFx, sFy, ci, cj, dx, P, a.invdt != nullptr);
       double * out = a.U2 + (size_t)n * H::NV * NC + tid;
       bool     finite = true;
 #pragma unroll
       for (int v = 0; v < H::NV; ++v)
       {
         out[v * NC] = u2[v];
-        finite = finite && isfinite(u2[v]);
+        finite = finite && finite_bits(u2[v]);
       }
       if (!finite)
         raise_status(a.status, STATUS_NONPHYSICAL);
-      if (a.invdt)
-      {
-        // ComputeDtFiveEqFunctor::compute_cfl on the new state
-        double       q[6];
-        const double c = prim_fp64<2>(u2, q, P);
-        const double vx = c + fabs(q[H::QU]);
-        const double vy = c + fabs(q[H::QV]);
-        m_inv = fmax(m_inv, vx / dx + vy / dx);
-      }
     }
     if (a.invdt)
     {
@@ -545,10 +647,10 @@ step2d_kernel(StepArgs a)
       __syncthreads();
       if (tid == 0)
       {
-        double mm = 0.0;
+        DtT mm = DtT(0);
         for (int w = 0; w < NT / 32; ++w)
           mm = fmax(mm, sRed[w]);
-        atomic_max_pos(a.invdt + ins, mm);
+        atomic_max_pos(a.invdt + ins, (double)mm);
       }
     }
     __syncthreads();
