@@ -209,6 +209,19 @@ g5_create(const G5Params * params, G5Context ** out_ctx)
     p.bc[f] = params->bc[f];
   for (int l = 0; l < 32; ++l)
     p.level_dx[l] = params->level_dx[l];
+  p.f_smallr = (float)p.smallr;
+  p.f_smallc = (float)p.smallc;
+  p.f_smallp = (float)p.smallp;
+  p.f_slope_type = (float)p.slope_type;
+  p.f_thinc_beta = (float)p.thinc_beta;
+  p.f_thinc_eps = (float)p.thinc_eps;
+  for (int k = 0; k < 2; ++k)
+  {
+    p.f_xi[k] = (float)p.xi[k];
+    p.f_gpx[k] = (float)p.gpx[k];
+  }
+  p.f_dxi = (float)(p.xi[0] - p.xi[1]);
+  p.dgpx = p.gpx[0] - p.gpx[1];
   if (cudaMalloc((void **)&c->d_status, sizeof(unsigned int)) != cudaSuccess ||
       cudaMemset(c->d_status, 0, sizeof(unsigned int)) != cudaSuccess)
   {

@@ -26,6 +26,10 @@ struct PhysParams
   int    thinc;      // 0 MUSCL, 1 THINC
   int    bc[6];
   double level_dx[32];
+  // FP32 copies for the FP32-bulk path (converted once on the host)
+  float f_smallr, f_smallc, f_smallp, f_slope_type, f_thinc_beta, f_thinc_eps;
+  float f_xi[2], f_gpx[2], f_dxi; // f_dxi = xi0 - xi1
+  double dgpx;                    // gpx0 - gpx1
 };
 
 struct DevMesh
@@ -462,6 +466,20 @@ hllc_fp32(const float * ql, const float * qr, float xi0, float xi1, float gp0, f
 // numerator, and does everything else on the FP32 and integer pipes.
 // ---------------------------------------------------------------------------
 
+// double -> float on the integer pipe: round half away from zero on the
+// magnitude bits, flush below FLT_MIN (values of the state stay far from
+// FLT_MAX).  The hardware conversion issues on the FP64 pipe.
+__device__ __forceinline__ float
+d2f_fast(double x)
+{
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x) + (1ull << 28);
+  const unsigned           hi = (unsigned)(b >> 32);
+  unsigned                 f = ((unsigned)(b >> 29) - (384u << 23)) & 0x7FFFFFFFu;
+  if ((hi & 0x7FFFFFFFu) < (897u << 20))
+    f = 0u;
+  return __uint_as_float(f | (hi & 0x80000000u));
+}
+
 // exact float -> double on the integer pipe (float denormals read as zero,
 // as the fast-math build flushes them anyway)
 __device__ __forceinline__ double
@@ -528,32 +546,31 @@ __device__ __forceinline__ float
 pressure_mixed(const double * u, const PhysParams & P, bool stiff, float & d, float & ux, float & uy, float & uz, float & a0f)
 {
   using H = V<DIM>;
-  d = fmaxf((float)u[H::ID], (float)P.smallr);
+  d = fmaxf(d2f_fast(u[H::ID]), P.f_smallr);
   const float inv = __frcp_rn(d);
-  ux = (float)u[H::IU] * inv;
-  uy = (float)u[H::IV] * inv;
+  ux = d2f_fast(u[H::IU]) * inv;
+  uy = d2f_fast(u[H::IV]) * inv;
   float k2 = ux * ux + uy * uy;
   uz = 0.0f;
   if constexpr (DIM == 3)
   {
-    uz = (float)u[H::IW] * inv;
+    uz = d2f_fast(u[H::IW]) * inv;
     k2 += uz * uz;
   }
   const double a0u = u[H::IA0];
-  a0f = (float)a0u;
+  a0f = d2f_fast(a0u);
   const float K = 0.5f * d * k2;
   float       num;
   if (stiff)
   {
-    const double PI = fma(a0u, P.gpx[0] - P.gpx[1], P.gpx[1]);
-    num = (float)((u[H::IE] - PI) - f2d_exact(K));
+    const double PI = fma(a0u, P.dgpx, P.gpx[1]);
+    num = d2f_fast((u[H::IE] - PI) - f2d_exact(K));
   }
   else
-    num = (float)u[H::IE] - K;
-  const float S = fmaf(a0f, (float)(P.xi[0] - P.xi[1]), (float)P.xi[1]);
+    num = d2f_fast(u[H::IE]) - K;
+  const float S = fmaf(a0f, P.f_dxi, P.f_xi[1]);
   return __fdividef(num, S);
 }
-
 // FP32-bulk conservative -> primitive (computePrimitives, models/utils.h:200-250)
 template <int DIM>
 __device__ __forceinline__ void
@@ -563,7 +580,7 @@ prim_mixed(const double * u, float * q, const PhysParams & P, bool stiff)
   float       d, ux, uy, uz, a0f;
   const float p = pressure_mixed<DIM>(u, P, stiff, d, ux, uy, uz, a0f);
   float       a0 = fmaxf(0.0f, fminf(1.0f, a0f));
-  float       r0 = (float)u[H::IAD0], r1 = (float)u[H::IAD1];
+  float       r0 = d2f_fast(u[H::IAD0]), r1 = d2f_fast(u[H::IAD1]);
   const float eps = 1e-12f;
   if (r0 < eps)
     r0 = 0.0f;

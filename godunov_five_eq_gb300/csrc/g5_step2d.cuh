@@ -180,7 +180,20 @@ face_state(const typename Step2DTraits<B, MIXED>::R * sQ,
   const R       offx = dir == 0 ? R(0.5) * R(side) : R(0);
   const R       offy = dir == 1 ? R(0.5) * R(side) : R(0);
   const bool    hancock = P.integrator == 0;
-  R             qc[5], dqx[5], dqy[5], hs[5];
+  R             thinc_eps, thinc_beta, smallr;
+  if constexpr (MIXED)
+  {
+    thinc_eps = P.f_thinc_eps;
+    thinc_beta = P.f_thinc_beta;
+    smallr = P.f_smallr;
+  }
+  else
+  {
+    thinc_eps = P.thinc_eps;
+    thinc_beta = P.thinc_beta;
+    smallr = P.smallr;
+  }
+  R qc[5], dqx[5], dqy[5], hs[5];
 #pragma unroll
   for (int k = 0; k < 5; ++k)
   {
@@ -211,11 +224,11 @@ face_state(const typename Step2DTraits<B, MIXED>::R * sQ,
     const R *  A = sQ + 5 * GG;
     const R    aP = A[gi + o], aM = A[gi - o];
     const R    mono = (aP - a0) * (a0 - aM);
-    const bool req = (a0 > R(P.thinc_eps)) && (a0 < R(1) - R(P.thinc_eps)) && mono > R(0);
+    const bool req = (a0 > thinc_eps) && (a0 < R(1) - thinc_eps) && mono > R(0);
     if (req)
     {
       const R nd = sRec[(15 + dir) * SS + si];
-      const R beta = R(P.thinc_beta) * nd + R(0.01);
+      const R beta = thinc_beta * nd + R(0.01);
       const R Aa = (aP + aM) / R(2);
       const R Bb = (aP - aM) / R(2);
       R       C, D;
@@ -247,8 +260,8 @@ face_state(const typename Step2DTraits<B, MIXED>::R * sQ,
   }
   else
   {
-    q[0] = fmax(R(P.smallr), q[0]);
-    q[1] = fmax(R(P.smallr), q[1]);
+    q[0] = fmax(smallr, q[0]);
+    q[1] = fmax(smallr, q[1]);
   }
 }
 
@@ -335,7 +348,7 @@ update_mixed(const double * uin, double * u2, const float * sFx, const float * s
 #pragma unroll
   for (int v = 0; v < H::NV; ++v)
     u2[v] = uin[v];
-  const float a0f = (float)uin[H::IA0], a1f = (float)uin[H::IA1];
+  const float a0f = d2f_fast(uin[H::IA0]), a1f = d2f_fast(uin[H::IA1]);
   float       eh[3] = { 0.f, 0.f, 0.f }, el[3] = { 0.f, 0.f, 0.f };
   const double eps = 1e-12, one_m_eps = 1.0 - 1e-12;
 #pragma unroll
@@ -402,7 +415,7 @@ update_mixed(const double * uin, double * u2, const float * sFx, const float * s
   float       df, ux, uy, uz, a0;
   const float p = pressure_mixed<2>(u2, P, stiff, df, ux, uy, uz, a0);
   const float a0s = fmaxf(0.0f, fminf(1.0f, a0));
-  const float c = sound_speed_f((float)P.xi[0], (float)P.xi[1], (float)P.gpx[0], (float)P.gpx[1], df, p, a0s);
+  const float c = sound_speed_f(P.f_xi[0], P.f_xi[1], P.f_gpx[0], P.f_gpx[1], df, p, a0s);
   return ((c + fabsf(ux)) + (c + fabsf(uy))) * __frcp_rn(dx);
 }
 
@@ -435,7 +448,7 @@ step2d_kernel(StepArgs a)
     const double dx = P.level_dx[lev];
     R            dtdx_r;
     if constexpr (MIXED)
-      dtdx_r = (float)a.dt[ins] * __frcp_rn((float)dx);
+      dtdx_r = d2f_fast(a.dt[ins]) * __frcp_rn(d2f_fast(dx));
     else
       dtdx_r = a.dt[ins] / dx;
 
@@ -474,7 +487,11 @@ step2d_kernel(StepArgs a)
         continue;
       const int gi = (ri + 2) + G * (rj + 2);
       R         q[5], dqx[5], dqy[5];
-      const R   st = R(P.slope_type);
+      R st;
+      if constexpr (MIXED)
+        st = P.f_slope_type;
+      else
+        st = P.slope_type;
 #pragma unroll
       for (int k = 0; k < 5; ++k)
       {
@@ -493,7 +510,7 @@ step2d_kernel(StepArgs a)
         const R rr = r0 + r1;
         R       c;
         if constexpr (MIXED)
-          c = sound_speed_f((float)P.xi[0], (float)P.xi[1], (float)P.gpx[0], (float)P.gpx[1], rr, p, a0);
+          c = sound_speed_f(P.f_xi[0], P.f_xi[1], P.f_gpx[0], P.f_gpx[1], rr, p, a0);
         else
           c = sound_speed_d(P, rr, p, a0, 1 - a0);
         const R drx0 = dqx[0], drx1 = dqx[1], dpx = dqx[2], dux = dqx[3], dvx = dqx[4];
@@ -556,7 +573,7 @@ step2d_kernel(StepArgs a)
         qR[4] = t;
       }
       if constexpr (MIXED)
-        hllc_fp32<2>(qL, qR, (float)P.xi[0], (float)P.xi[1], (float)P.gpx[0], (float)P.gpx[1], (float)P.smallr, (float)P.smallp, (float)P.smallc, fl);
+        hllc_fp32<2>(qL, qR, P.f_xi[0], P.f_xi[1], P.f_gpx[0], P.f_gpx[1], P.f_smallr, P.f_smallp, P.f_smallc, fl);
       else
         hllc_fp64<2>(qL, qR, P, fl);
       if (dir == 1)
@@ -623,7 +640,7 @@ step2d_kernel(StepArgs a)
     {
       double u2[H::NV];
       if constexpr (MIXED)
-        m_inv = update_mixed<B>(uin, u2, sFx, sFy, ci, cj, (float)dx, P, stiff, a.invdt != nullptr);
+        m_inv = update_mixed<B>(uin, u2, sFx, sFy, ci, cj, d2f_fast(dx), P, stiff, a.invdt != nullptr);
       else
         m_inv = update_fp64<B>(uin, u2, sFx, sFy, ci, cj, dx, P, a.invdt != nullptr);
       double * out = a.U2 + (size_t)n * H::NV * NC + tid;
