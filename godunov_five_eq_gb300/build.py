@@ -1,9 +1,10 @@
 """In-tree build of libg5gpu.so (sm_103a) with nvcc.
 
-Three translation units compiled in parallel:
+Four translation units compiled in parallel:
   g5_fp64.cu   FP64 kernels, --fmad=false (bit-reproducible reference arithmetic)
   g5_mixed.cu  FP32-bulk kernels, --use_fast_math
   g5_capi.cu   the C ABI (include/g5gpu.h)
+  g5_static.cu the allocation-free g5_step_static and its fixed scratch array
 """
 from __future__ import annotations
 
@@ -22,6 +23,7 @@ UNITS = {
     "g5_fp64.cu": ["--fmad=false"],
     "g5_mixed.cu": ["--use_fast_math"],
     "g5_capi.cu": [],
+    "g5_static.cu": [],
 }
 
 

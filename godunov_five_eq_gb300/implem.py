@@ -102,6 +102,7 @@ EXPORTS = [
     "g5_status",
     "g5_tune",
     "g5_last_launch_count",
+    "g5_step_static",
 ]
 
 _lib = None
@@ -140,6 +141,7 @@ def load_library(build_if_missing: bool = True):
     L.g5_status.argtypes = [vp, vp]
     L.g5_tune.argtypes = [vp, vp, vp, ctypes.c_int, vp]
     L.g5_last_launch_count.argtypes = [vp]
+    L.g5_step_static.argtypes = [ctypes.POINTER(G5Params), ctypes.POINTER(G5Mesh), vp, vp, vp, ctypes.c_int, vp, vp, vp]
     _lib = L
     return L
 

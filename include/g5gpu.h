@@ -192,6 +192,42 @@ int g5_tune(G5Context * ctx, const double * d_U, double * d_U2, int mode, void *
 /* Number of kernel launches issued by the last g5_step / g5_advance / g5_run call. */
 int g5_last_launch_count(const G5Context * ctx);
 
+/* Size of the fixed device scratch array used by g5_step_static (16 MiB). */
+#define G5_STATIC_SCRATCH_BYTES (16u << 20)
+
+/* No counterpart in the reference: an allocation-free variant of g5_step.
+ *
+ * For callers that must not allocate device memory while they advance the
+ * solution, e.g. a solver whose device memory belongs to its framework's
+ * pool allocator, or a plugin whose host process accounts for every device
+ * allocation.  It needs no context: the block table is taken from host memory
+ * (the G5Mesh pointers are HOST pointers, as for g5_set_mesh), and dt, the
+ * block table, the coarse/fine face records and the status word are staged
+ * in one file-scope device array of G5_STATIC_SCRATCH_BYTES that every GPU
+ * loading the library keeps until the process exits.  No cudaMalloc, cudaFree
+ * or other allocating routine is called.
+ *
+ * Same step and arguments meaning as g5_step; d_status_out (device, may be
+ * NULL) receives the G5_STATUS_* bits raised by the kernels (the caller zeroes
+ * it).  Returns G5_ERR_ARG when the mesh needs more than
+ * G5_STATIC_SCRATCH_BYTES of scratch.
+ *
+ * The first call on a device looks up the array's device address with that
+ * device current (cudaGetSymbolAddress); make that first call before any
+ * stream capture.  All calls share the one array and the last call's contents
+ * stay in it: calls whose work overlaps on the GPU (several streams, or
+ * several host threads on one device) race and must be serialised by the
+ * caller. */
+int g5_step_static(const G5Params * params,
+                   const G5Mesh *   mesh,
+                   const double *   d_U,
+                   double *         d_U2,
+                   const double *   dt_host,
+                   int              mode,
+                   double *         d_inv_dt_out,
+                   unsigned int *   d_status_out,
+                   void *           stream);
+
 #ifdef __cplusplus
 }
 #endif
