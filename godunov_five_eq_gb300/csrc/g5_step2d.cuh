@@ -348,53 +348,99 @@ update_mixed(const double * uin, double * u2, const float * sFx, const float * s
 #pragma unroll
   for (int v = 0; v < H::NV; ++v)
     u2[v] = uin[v];
-  const float a0f = d2f_fast(uin[H::IA0]), a1f = d2f_fast(uin[H::IA1]);
-  float       eh[3] = { 0.f, 0.f, 0.f }, el[3] = { 0.f, 0.f, 0.f };
+  const float  a0f = d2f_fast(uin[H::IA0]), a1f = d2f_fast(uin[H::IA1]);
   const double eps = 1e-12, one_m_eps = 1.0 - 1e-12;
+  const int    ilx = ci + (B + 1) * cj, irx = ilx + 1;
+  const int    ily = ci + B * cj, iry = ily + B;
+  // error-free per-direction increments of the conserved quantities:
+  // d[dir] = F_left - F_right = h + l exactly
+  float h[2][5], l[2][5];
+  const int ks[5] = { H::FR0, H::FR1, H::FE, H::FU, H::FV };
 #pragma unroll
-  for (int dir = 0; dir < 2; ++dir)
+  for (int k = 0; k < 5; ++k)
   {
-    const float * F = dir == 0 ? sFx : sFy;
-    const int     il = dir == 0 ? ci + (B + 1) * cj : ci + B * cj;
-    const int     ir = dir == 0 ? il + 1 : il + B;
-    float         h, l;
-    two_diff(F[H::FR0 * NFF + il], F[H::FR0 * NFF + ir], h, l);
-    u2[H::IAD0] = (u2[H::IAD0] + f2d_exact(h)) + f2d_exact(l);
-    if (dlt_pos(u2[H::IAD0], eps))
-      u2[H::IAD0] = 0.0;
-    two_diff(F[H::FR1 * NFF + il], F[H::FR1 * NFF + ir], h, l);
-    u2[H::IAD1] = (u2[H::IAD1] + f2d_exact(h)) + f2d_exact(l);
-    if (dlt_pos(u2[H::IAD1], eps))
-      u2[H::IAD1] = 0.0;
-    const float usl = F[H::FUS * NFF + il], usr = F[H::FUS * NFF + ir];
-    const float dA0 = ((F[H::FA0 * NFF + il] - usl * a0f) - F[H::FA0 * NFF + ir]) + usr * a0f;
-    const float dA1 = ((F[H::FA1 * NFF + il] - usl * a1f) - F[H::FA1 * NFF + ir]) + usr * a1f;
-    u2[H::IA0] += f2d_exact(dA0);
-    if (dlt_pos(u2[H::IA0], eps))
-      u2[H::IA0] = 0.0;
-    if (dgt_pos(u2[H::IA0], one_m_eps))
-      u2[H::IA0] = 1.0;
-    u2[H::IA1] += f2d_exact(dA1);
-    if (dlt_pos(u2[H::IA1], eps))
-      u2[H::IA1] = 0.0;
-    if (dgt_pos(u2[H::IA1], one_m_eps))
-      u2[H::IA1] = 1.0;
-    const int ke[3] = { H::FE, H::FU, H::FV };
+    two_diff(sFx[ks[k] * NFF + ilx], sFx[ks[k] * NFF + irx], h[0][k], l[0][k]);
+    two_diff(sFy[ks[k] * NFF + ily], sFy[ks[k] * NFF + iry], h[1][k], l[1][k]);
+  }
+  float dA[2][2];
+  {
+    const float uslx = sFx[H::FUS * NFF + ilx], usrx = sFx[H::FUS * NFF + irx];
+    const float usly = sFy[H::FUS * NFF + ily], usry = sFy[H::FUS * NFF + iry];
+    dA[0][0] = ((sFx[H::FA0 * NFF + ilx] - uslx * a0f) - sFx[H::FA0 * NFF + irx]) + usrx * a0f;
+    dA[0][1] = ((sFx[H::FA1 * NFF + ilx] - uslx * a1f) - sFx[H::FA1 * NFF + irx]) + usrx * a1f;
+    dA[1][0] = ((sFy[H::FA0 * NFF + ily] - usly * a0f) - sFy[H::FA0 * NFF + iry]) + usry * a0f;
+    dA[1][1] = ((sFy[H::FA1 * NFF + ily] - usly * a1f) - sFy[H::FA1 * NFF + iry]) + usry * a1f;
+  }
+  // partial densities: clamp after X cannot trigger when the state dominates
+  // the X decrease (checked in FP32 with a factor-2 margin); then both
+  // directions are summed exactly in float-float and added with two FP64
+  // adds, otherwise the X and Y increments are applied one after the other.
 #pragma unroll
-    for (int e = 0; e < 3; ++e)
+  for (int k = 0; k < 2; ++k)
+  {
+    const int   iv = k == 0 ? H::IAD0 : H::IAD1;
+    const float uf = d2f_fast(u2[iv]);
+    if (uf > 2.0f * fabsf(h[0][k]) + 2e-12f)
     {
-      two_diff(F[ke[e] * NFF + il], F[ke[e] * NFF + ir], h, l);
-      float t;
-      two_sum(eh[e], h, eh[e], t);
-      el[e] += t + l;
+      float s, t;
+      two_sum(h[0][k], h[1][k], s, t);
+      t += l[0][k] + l[1][k];
+      u2[iv] = (u2[iv] + f2d_exact(s)) + f2d_exact(t);
+      if (dlt_pos(u2[iv], eps))
+        u2[iv] = 0.0;
+    }
+    else
+    {
+#pragma unroll
+      for (int dir = 0; dir < 2; ++dir)
+      {
+        u2[iv] = (u2[iv] + f2d_exact(h[dir][k])) + f2d_exact(l[dir][k]);
+        if (dlt_pos(u2[iv], eps))
+          u2[iv] = 0.0;
+      }
     }
   }
-  u2[H::IE] = (u2[H::IE] + f2d_exact(eh[0])) + f2d_exact(el[0]);
-  u2[H::IU] = (u2[H::IU] + f2d_exact(eh[1])) + f2d_exact(el[1]);
-  u2[H::IV] = (u2[H::IV] + f2d_exact(eh[2])) + f2d_exact(el[2]);
+  // volume fractions: the same test against both clamp bounds
+#pragma unroll
+  for (int k = 0; k < 2; ++k)
+  {
+    const int   iv = k == 0 ? H::IA0 : H::IA1;
+    const float af = k == 0 ? a0f : a1f;
+    const float m = 2.0f * fabsf(dA[0][k]) + 2e-12f;
+    if (af > m && af + m < 1.0f)
+    {
+      u2[iv] += f2d_exact(dA[0][k] + dA[1][k]);
+      if (dlt_pos(u2[iv], eps))
+        u2[iv] = 0.0;
+      if (dgt_pos(u2[iv], one_m_eps))
+        u2[iv] = 1.0;
+    }
+    else
+    {
+#pragma unroll
+      for (int dir = 0; dir < 2; ++dir)
+      {
+        u2[iv] += f2d_exact(dA[dir][k]);
+        if (dlt_pos(u2[iv], eps))
+          u2[iv] = 0.0;
+        if (dgt_pos(u2[iv], one_m_eps))
+          u2[iv] = 1.0;
+      }
+    }
+  }
+  // energy and momentum: no clamps, one exact float-float sum of both directions
+  const int ive[3] = { H::IE, H::IU, H::IV };
+#pragma unroll
+  for (int e = 0; e < 3; ++e)
+  {
+    float s, t;
+    two_sum(h[0][2 + e], h[1][2 + e], s, t);
+    t += l[0][2 + e] + l[1][2 + e];
+    u2[ive[e]] = (u2[ive[e]] + f2d_exact(s)) + f2d_exact(t);
+  }
   // renormalisation
-  const double s = u2[H::IA0] + u2[H::IA1];
-  const double d = s - 1.0;
+  const double sa = u2[H::IA0] + u2[H::IA1];
+  const double d = sa - 1.0;
   if (d != 0.0)
   {
     if ((__double_as_longlong(d) & 0x7FFFFFFFFFFFFFFFLL) < __double_as_longlong(1e-8))
@@ -404,7 +450,7 @@ update_mixed(const double * uin, double * u2, const float * sFx, const float * s
     }
     else
     {
-      const double inv = 1.0 / s;
+      const double inv = 1.0 / sa;
       u2[H::IA0] *= inv;
       u2[H::IA1] *= inv;
     }
@@ -419,8 +465,10 @@ update_mixed(const double * uin, double * u2, const float * sFx, const float * s
   return ((c + fabsf(ux)) + (c + fabsf(uy))) * __frcp_rn(dx);
 }
 
+// 4 CTAs per SM in the FP32-bulk form (64 registers), so that CTAs in the
+// FP64-heavy update overlap with CTAs in the FP32 face phase
 template <int B, bool MIXED>
-__global__ void __launch_bounds__(B * B)
+__global__ void __launch_bounds__(B * B, MIXED ? (B == 16 ? 4 : 8) : 1)
 step2d_kernel(StepArgs a)
 {
   using T = Step2DTraits<B, MIXED>;

@@ -1,0 +1,10 @@
+#pragma once
+#include <kalypsso/utils/config/ConfigMap.h>
+namespace kalypsso { namespace core { namespace eos {
+template <typename device_t>
+class StiffenedGasMixture
+{
+public:
+  StiffenedGasMixture(ConfigMap const &) {}
+};
+} } }
