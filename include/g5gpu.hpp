@@ -1,0 +1,238 @@
+// g5gpu.hpp — C++17 host mirror of the reference's GodunovImplemBase over the
+// C ABI of include/g5gpu.h (header-only; link libg5gpu.so and cudart).
+//
+// godunov_five_eq::GodunovImplemGB300<dim> keeps the member names and the
+// argument meaning of the reference's GodunovImplemBase
+// (scheme/GodunovImplemBase.h:59-198) and GodunovImplemV0
+// (scheme/GodunovImplemV0.h:42-214):
+//   resize_auxiliary_data(mesh)        <- block table of the new mesh
+//   total_mem_size_in_bytes()
+//   do_time_step(U, U2, dt)            U2 <- one step of U (device arrays)
+//   do_time_step(U, U2, t, dt)         same (t unused, as in V0)
+// plus the pieces of SolverGodunovFiveEq the step depends on:
+//   compute_dt_local(U)                ComputeDtFiveEqFunctor + cfl / invDt
+//   fill_outside_quadrants(U)          FillOutsideCellFunctor
+// Errors from the C ABI are thrown as g5::Error (the reference aborts).
+#pragma once
+
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "g5gpu.h"
+
+namespace g5
+{
+
+class Error : public std::runtime_error
+{
+public:
+  Error(int code, const std::string & what)
+    : std::runtime_error(what + ": g5 error " + std::to_string(code))
+    , code_(code)
+  {}
+  int code() const { return code_; }
+
+private:
+  int code_;
+};
+
+inline void
+check(int rc, const char * what)
+{
+  if (rc < 0)
+    throw Error(rc, what);
+}
+
+// Stand-in for the reference's DataArrayBlock<dim, real_t, device_t>: a device
+// array [n_blocks][nv][bsize^dim] of FP64 owned by the caller.
+struct BlockArray
+{
+  double * data = nullptr;
+  int      n_blocks = 0;
+};
+
+// Host copy of a block table (the arrays G5Mesh points to).
+struct BlockTable
+{
+  int                  n_owned = 0, n_outside = 0, n_inst = 1;
+  std::vector<int32_t> level, coord, nbr, out_src, inst;
+  std::vector<int8_t>  nbr_rel, out_normal, out_border;
+
+  G5Mesh view() const
+  {
+    G5Mesh m{};
+    m.n_owned = n_owned;
+    m.n_outside = n_outside;
+    m.n_inst = n_inst;
+    m.level = level.data();
+    m.coord = coord.data();
+    m.nbr = nbr.data();
+    m.nbr_rel = nbr_rel.data();
+    m.out_src = out_src.empty() ? nullptr : out_src.data();
+    m.out_normal = out_normal.empty() ? nullptr : out_normal.data();
+    m.out_border = out_border.empty() ? nullptr : out_border.data();
+    m.inst = inst.empty() ? nullptr : inst.data();
+    return m;
+  }
+};
+
+// Uniform single-level block table on an nx x ny brick of blocks (2D), with
+// the outside blocks of the non-periodic directions (one twin per border block
+// and outside normal, as the reference's outside quadrants).  Blocks are
+// ordered row by row.
+inline BlockTable
+uniform_block_table_2d(int nx, int ny, bool periodic_x, bool periodic_y, int level)
+{
+  BlockTable t;
+  t.n_owned = nx * ny;
+  auto id = [&](int i, int j) { return i + nx * j; };
+  std::vector<int> okey; // outside blocks keyed by (i, j) position
+  std::vector<int> oi, oj;
+  auto find_out = [&](int i, int j) {
+    for (size_t k = 0; k < oi.size(); ++k)
+      if (oi[k] == i && oj[k] == j)
+        return (int)k;
+    return -1;
+  };
+  for (int j = 0; j < ny; ++j)
+    for (int i = 0; i < nx; ++i)
+    {
+      t.level.push_back(level);
+      t.coord.insert(t.coord.end(), { i, j, 0 });
+    }
+  for (int j = 0; j < ny; ++j)
+    for (int i = 0; i < nx; ++i)
+    {
+      const int tx[3] = { 0, i == 0 && !periodic_x ? -1 : 0, i == nx - 1 && !periodic_x ? 1 : 0 };
+      const int ty[3] = { 0, j == 0 && !periodic_y ? -1 : 0, j == ny - 1 && !periodic_y ? 1 : 0 };
+      for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b)
+        {
+          const int nxo = tx[a], nyo = ty[b];
+          if ((a > 0 && nxo == 0) || (b > 0 && nyo == 0) || (nxo == 0 && nyo == 0))
+            continue;
+          oi.push_back(i + nxo);
+          oj.push_back(j + nyo);
+          t.out_src.push_back(id(i, j));
+          t.out_normal.insert(t.out_normal.end(), { (int8_t)nxo, (int8_t)nyo, 0 });
+          t.out_border.insert(t.out_border.end(),
+                              { (int8_t)(i == 0), (int8_t)(i == nx - 1), (int8_t)(j == 0), (int8_t)(j == ny - 1), 0, 0 });
+          t.level.push_back(level);
+          t.coord.insert(t.coord.end(), { i + nxo, j + nyo, 0 });
+        }
+    }
+  t.n_outside = (int)oi.size();
+  t.nbr.assign((size_t)t.n_owned * 9 * 4, -1);
+  t.nbr_rel.assign((size_t)t.n_owned * 9, 0);
+  for (int j = 0; j < ny; ++j)
+    for (int i = 0; i < nx; ++i)
+      for (int dy = -1; dy <= 1; ++dy)
+        for (int dx = -1; dx <= 1; ++dx)
+        {
+          if (!dx && !dy)
+            continue;
+          int       ii = i + dx, jj = j + dy;
+          const int s = (dx + 1) + 3 * (dy + 1);
+          if (periodic_x)
+            ii = (ii + nx) % nx;
+          if (periodic_y)
+            jj = (jj + ny) % ny;
+          int n;
+          if (ii >= 0 && ii < nx && jj >= 0 && jj < ny)
+            n = id(ii, jj);
+          else
+            n = t.n_owned + find_out(ii, jj);
+          t.nbr[((size_t)id(i, j) * 9 + s) * 4] = n;
+        }
+  (void)okey;
+  return t;
+}
+
+} // namespace g5
+
+namespace godunov_five_eq
+{
+
+// GB300 implementation of GodunovImplemBase (implementation_version 3).
+template <size_t dim>
+class GodunovImplemGB300
+{
+public:
+  static constexpr int implementation_version = 3;
+
+  GodunovImplemGB300(const G5Params & params, int mode = G5_MODE_FP64, cudaStream_t stream = nullptr)
+    : m_params(params)
+    , m_mode(mode)
+    , m_stream(stream)
+  {
+    if (params.dim != (int)dim)
+      throw g5::Error(G5_ERR_ARG, "GodunovImplemGB300: dim mismatch");
+    g5::check(g5_create(&params, &m_ctx), "g5_create");
+  }
+  ~GodunovImplemGB300()
+  {
+    if (m_ctx)
+      g5_destroy(m_ctx);
+  }
+  GodunovImplemGB300(const GodunovImplemGB300 &) = delete;
+  GodunovImplemGB300 & operator=(const GodunovImplemGB300 &) = delete;
+
+  //! resize only auxiliary data array (GodunovImplemV0.cpp:37-61)
+  void resize_auxiliary_data(const g5::BlockTable & table)
+  {
+    m_table = table;
+    const G5Mesh m = m_table.view();
+    g5::check(g5_set_mesh(m_ctx, &m), "g5_set_mesh");
+  }
+
+  //! memory footprint monitoring
+  uint64_t total_mem_size_in_bytes() const { return (uint64_t)g5_mem_bytes(m_ctx); }
+
+  //! Perform actual time integration: U2 <- step(U) (GodunovImplemV0.cpp:85-151)
+  void do_time_step(const g5::BlockArray & U, const g5::BlockArray & U2, double dt)
+  {
+    std::vector<double> dts(m_table.n_inst, dt);
+    g5::check(g5_step(m_ctx, U.data, U2.data, dts.data(), m_mode, nullptr, m_stream), "g5_step");
+  }
+
+  //! Perform actual time integration (t is unused, as in GodunovImplemV0)
+  void do_time_step(const g5::BlockArray & U, const g5::BlockArray & U2, double /*t*/, double dt) { do_time_step(U, U2, dt); }
+
+  //! SolverGodunovFiveEq::compute_dt_local: dt = cfl / max over cells of sum (c+|u_d|)/dx
+  double compute_dt_local(const g5::BlockArray & U)
+  {
+    double * d_inv = nullptr;
+    if (cudaMalloc(&d_inv, sizeof(double) * m_table.n_inst) != cudaSuccess)
+      throw g5::Error(G5_ERR_CUDA, "cudaMalloc");
+    int                 rc = g5_compute_inv_dt(m_ctx, U.data, d_inv, m_stream);
+    std::vector<double> inv(m_table.n_inst);
+    if (rc == 0 && cudaMemcpyAsync(inv.data(), d_inv, sizeof(double) * inv.size(), cudaMemcpyDeviceToHost, m_stream) != cudaSuccess)
+      rc = G5_ERR_CUDA;
+    if (rc == 0 && cudaStreamSynchronize(m_stream) != cudaSuccess)
+      rc = G5_ERR_CUDA;
+    cudaFree(d_inv);
+    g5::check(rc, "g5_compute_inv_dt");
+    return m_params.cfl / inv[0];
+  }
+
+  //! SolverGodunovFiveEq::fill_outside_quadrants
+  void fill_outside_quadrants(const g5::BlockArray & U) { g5::check(g5_fill_outside(m_ctx, U.data, m_stream), "g5_fill_outside"); }
+
+  //! device status word (G5_STATUS_* bits), cleared by the read
+  int status() { return g5_status(m_ctx, m_stream); }
+
+  G5Context * context() const { return m_ctx; }
+
+private:
+  G5Params       m_params;
+  int            m_mode;
+  cudaStream_t   m_stream;
+  G5Context *    m_ctx = nullptr;
+  g5::BlockTable m_table;
+};
+
+} // namespace godunov_five_eq
