@@ -3,6 +3,7 @@
 #include "g5_aux.cuh"
 #include "g5_launch.h"
 #include "g5_step2d.cuh"
+#include "g5_step3d.cuh"
 
 namespace g5
 {
@@ -72,10 +73,59 @@ occupancy2d()
   return occ;
 }
 
+template <bool MIXED>
+static cudaError_t
+launch_step3d(const StepArgs & a, int ctas_per_sm, cudaStream_t s, int * launches)
+{
+  using T = Step3DTraits<MIXED>;
+  static bool configured = false;
+  static int  occ = 1;
+  if (!configured)
+  {
+    cudaError_t e = cudaFuncSetAttribute(step3d_kernel<MIXED>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::smem_bytes);
+    if (e != cudaSuccess)
+      return e;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, step3d_kernel<MIXED>, T::NT, T::smem_bytes);
+    if (occ < 1)
+      occ = 1;
+    configured = true;
+  }
+  const int per_sm = (ctas_per_sm > 0 && ctas_per_sm < occ) ? ctas_per_sm : occ;
+  int       grid = num_sms() * per_sm;
+  if (grid > a.m.n_owned)
+    grid = a.m.n_owned;
+  if (grid < 1)
+    return cudaSuccess;
+  step3d_kernel<MIXED><<<grid, T::NT, T::smem_bytes, s>>>(a);
+  ++*launches;
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess)
+    return e;
+  if (a.m.n_defer > 0)
+  {
+    const int n = a.m.n_defer * 64;
+    reflux3d_kernel<MIXED><<<(n + 127) / 128, 128, 0, s>>>(a);
+    ++*launches;
+    e = cudaGetLastError();
+  }
+  return e;
+}
+
+template <bool MIXED>
+static int
+occupancy3d()
+{
+  using T = Step3DTraits<MIXED>;
+  cudaFuncSetAttribute(step3d_kernel<MIXED>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::smem_bytes);
+  int occ = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, step3d_kernel<MIXED>, T::NT, T::smem_bytes);
+  return occ;
+}
+
 bool
 step_supported(int dim, int b)
 {
-  return dim == 2 && (b == 8 || b == 16);
+  return (dim == 2 && (b == 8 || b == 16)) || (dim == 3 && b == 8);
 }
 
 cudaError_t
@@ -85,6 +135,8 @@ launch_step_fp64(int dim, int b, const StepArgs & a, int ctas_per_sm, cudaStream
     return launch_step2d<16, false>(a, ctas_per_sm, s, launches);
   if (dim == 2 && b == 8)
     return launch_step2d<8, false>(a, ctas_per_sm, s, launches);
+  if (dim == 3 && b == 8)
+    return launch_step3d<false>(a, ctas_per_sm, s, launches);
   return cudaErrorInvalidValue;
 }
 
@@ -95,6 +147,8 @@ step_max_ctas_per_sm_fp64(int dim, int b)
     return occupancy2d<16, false>();
   if (dim == 2 && b == 8)
     return occupancy2d<8, false>();
+  if (dim == 3 && b == 8)
+    return occupancy3d<false>();
   return 0;
 }
 

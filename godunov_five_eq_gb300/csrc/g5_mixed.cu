@@ -2,6 +2,7 @@
 // pressure numerator, the accumulation into U2, the renormalisation and dt).
 #include "g5_launch.h"
 #include "g5_step2d.cuh"
+#include "g5_step3d.cuh"
 
 namespace g5
 {
@@ -70,9 +71,48 @@ occupancy2d_m()
   return occ;
 }
 
+static cudaError_t
+launch_step3d_m(const StepArgs & a, int ctas_per_sm, cudaStream_t s, int * launches)
+{
+  using T = Step3DTraits<true>;
+  static bool configured = false;
+  static int  occ = 1;
+  if (!configured)
+  {
+    cudaError_t e = cudaFuncSetAttribute(step3d_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::smem_bytes);
+    if (e != cudaSuccess)
+      return e;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, step3d_kernel<true>, T::NT, T::smem_bytes);
+    if (occ < 1)
+      occ = 1;
+    configured = true;
+  }
+  const int per_sm = (ctas_per_sm > 0 && ctas_per_sm < occ) ? ctas_per_sm : occ;
+  int       grid = num_sms_m() * per_sm;
+  if (grid > a.m.n_owned)
+    grid = a.m.n_owned;
+  if (grid < 1)
+    return cudaSuccess;
+  step3d_kernel<true><<<grid, T::NT, T::smem_bytes, s>>>(a);
+  ++*launches;
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess)
+    return e;
+  if (a.m.n_defer > 0)
+  {
+    const int n = a.m.n_defer * 64;
+    reflux3d_kernel<true><<<(n + 127) / 128, 128, 0, s>>>(a);
+    ++*launches;
+    e = cudaGetLastError();
+  }
+  return e;
+}
+
 cudaError_t
 launch_step_mixed(int dim, int b, const StepArgs & a, int ctas_per_sm, cudaStream_t s, int * launches)
 {
+  if (dim == 3 && b == 8)
+    return launch_step3d_m(a, ctas_per_sm, s, launches);
   if (dim == 2 && b == 16)
     return launch_step2d_m<16>(a, ctas_per_sm, s, launches);
   if (dim == 2 && b == 8)
@@ -87,6 +127,14 @@ step_max_ctas_per_sm_mixed(int dim, int b)
     return occupancy2d_m<16>();
   if (dim == 2 && b == 8)
     return occupancy2d_m<8>();
+  if (dim == 3 && b == 8)
+  {
+    using T = Step3DTraits<true>;
+    cudaFuncSetAttribute(step3d_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::smem_bytes);
+    int occ = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, step3d_kernel<true>, T::NT, T::smem_bytes);
+    return occ;
+  }
   return 0;
 }
 

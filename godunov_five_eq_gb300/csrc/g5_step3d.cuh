@@ -1,0 +1,856 @@
+// g5_step3d.cuh — fused 3D block timestep (one CTA of 512 threads per 8^3
+// block, persistent over the block list).
+//
+// Shared memory holds the 12^3 ghosted primitives, the Hancock half-step
+// source (and the THINC |normal|) of the 10^3 ring, and the face fluxes of
+// ONE direction.  The update runs direction by direction (X, Y, Z: the
+// reference's order, GodunovImplemV0.cpp:121-139, with update_U's clamps after
+// each direction), the running state of each owned cell in registers.
+// Cells next to a finer face are deferred to reflux3d_kernel; fine blocks
+// next to a coarser face publish their face fluxes for it.
+#pragma once
+
+#include <type_traits>
+
+#include "g5_common.cuh"
+
+namespace g5
+{
+
+template <bool MIXED>
+struct Step3DTraits
+{
+  using R = typename std::conditional<MIXED, float, double>::type;
+  static constexpr int B = 8;
+  static constexpr int NT = 512;
+  static constexpr int G = B + 4, GG = G * G, GGG = G * G * G; // ghosted extent
+  static constexpr int S = B + 2, SS = S * S, SSS = S * S * S; // ring extent
+  static constexpr int NQ = 7;                                  // r0 r1 p u v w a0
+  static constexpr int NHS = 6;                                 // Hancock source r0 r1 p u v w
+  static constexpr int NN = 3;                                  // THINC |n_d|
+  static constexpr int NFF = (B + 1) * B * B;                   // faces of one direction
+  static constexpr int NF = 9;                                  // r0 r1 a0 a1 e u v w ustar
+  static constexpr size_t smem_bytes = sizeof(R) * (size_t)(NQ * GGG + NHS * SSS + NN * SSS + NF * NFF) + 64;
+};
+
+__device__ __forceinline__ bool
+neg_zero(double x)
+{
+  return __double_as_longlong(x) == (long long)0x8000000000000000ULL;
+}
+__device__ __forceinline__ bool
+neg_zero(float x)
+{
+  return __float_as_uint(x) == 0x80000000u;
+}
+
+// conservative state seen by ghost cell g of block n (3D); false on a bad index
+__device__ __forceinline__ bool
+gather_ghost_3d(const StepArgs & a, int n, const int * g, double * u)
+{
+  using H = V<3>;
+  constexpr int B = 8, NC = 512;
+  int           d[3], v[3];
+#pragma unroll
+  for (int e = 0; e < 3; ++e)
+  {
+    d[e] = g[e] < 0 ? -1 : (g[e] >= B ? 1 : 0);
+    v[e] = g[e] - d[e] * B;
+  }
+  const int   s = (d[0] + 1) + 3 * (d[1] + 1) + 9 * (d[2] + 1);
+  const int   rel = a.m.nbr_rel[n * 27 + s];
+  const int * nb = a.m.nbr + (n * 27 + s) * 8;
+  if (rel <= 0)
+  {
+    const int src = nb[0];
+    if (src < 0 || src >= a.m.n_total)
+      return false;
+    int c[3];
+#pragma unroll
+    for (int e = 0; e < 3; ++e)
+      c[e] = rel == 0 ? v[e] : ((a.m.coord[n * 3 + e] + d[e]) & 1) * (B / 2) + (v[e] >> 1);
+    const double * base = a.U + (size_t)src * H::NV * NC + c[0] + B * (c[1] + B * c[2]);
+#pragma unroll
+    for (int k = 0; k < H::NV; ++k)
+      u[k] = base[k * NC];
+    return true;
+  }
+  int ch[3], f0[3];
+#pragma unroll
+  for (int e = 0; e < 3; ++e)
+  {
+    const int f = 2 * v[e];
+    ch[e] = f / B;
+    f0[e] = f - ch[e] * B;
+  }
+  const int src = nb[ch[0] + 2 * ch[1] + 4 * ch[2]];
+  if (src < 0 || src >= a.m.n_total)
+    return false;
+  const double * base = a.U + (size_t)src * H::NV * NC + f0[0] + B * (f0[1] + B * f0[2]);
+  const int      vars[7] = { H::IE, H::IU, H::IV, H::IW, H::IAD0, H::IAD1, H::IA0 };
+#pragma unroll
+  for (int t = 0; t < 7; ++t)
+  {
+    const double * p = base + vars[t] * NC;
+    double         sum = 0.0;
+#pragma unroll
+    for (int oz = 0; oz < 2; ++oz)
+#pragma unroll
+      for (int oy = 0; oy < 2; ++oy)
+#pragma unroll
+        for (int ox = 0; ox < 2; ++ox)
+          sum += p[ox + B * (oy + B * oz)];
+    u[vars[t]] = sum / 8.0;
+  }
+  u[H::IA1] = 1.0 - u[H::IA0];
+  u[H::ID] = u[H::IAD0] + u[H::IAD1];
+  return true;
+}
+
+template <bool MIXED>
+__device__ __forceinline__ void
+store_prim3(typename Step3DTraits<MIXED>::R * sQ, int gidx, const double * u, const PhysParams & P, bool stiff)
+{
+  constexpr int GGG = Step3DTraits<MIXED>::GGG;
+  if constexpr (MIXED)
+  {
+    float q[7];
+    prim_mixed<3>(u, q, P, stiff);
+#pragma unroll
+    for (int k = 0; k < 7; ++k)
+      sQ[k * GGG + gidx] = q[k];
+  }
+  else
+  {
+    double q[7];
+    prim_fp64<3>(u, q, P);
+#pragma unroll
+    for (int k = 0; k < 7; ++k)
+      sQ[k * GGG + gidx] = q[k];
+  }
+}
+
+// limited slope of component k at ghosted index gi along the stride o
+template <typename R>
+__device__ __forceinline__ R
+slope_at(const R * Qk, int gi, int o, R st)
+{
+  return slope_scalar<R>(Qk[gi], Qk[gi + o], Qk[gi - o], st);
+}
+
+// reconstructed state of cell (ci,cj,ck) at its face in direction dir
+// (side +1: right face, side -1: left face); q[7] = r0 r1 p u v w a0
+template <bool MIXED>
+__device__ __forceinline__ void
+face_state3(const typename Step3DTraits<MIXED>::R * sQ,
+            const typename Step3DTraits<MIXED>::R * sHS,
+            const typename Step3DTraits<MIXED>::R * sN,
+            int                                     ci,
+            int                                     cj,
+            int                                     ck,
+            int                                     dir,
+            int                                     side,
+            const PhysParams &                      P,
+            typename Step3DTraits<MIXED>::R *       q)
+{
+  using T = Step3DTraits<MIXED>;
+  using R = typename T::R;
+  constexpr int G = T::G, GG = T::GG, GGG = T::GGG, S = T::S, SS = T::SS, SSS = T::SSS;
+  const int     gi = (ci + 2) + G * (cj + 2) + GG * (ck + 2);
+  const int     si = (ci + 1) + S * (cj + 1) + SS * (ck + 1);
+  const int     strides[3] = { 1, G, GG };
+  const int     o = strides[dir];
+  R             st, smallr, thinc_eps, thinc_beta;
+  if constexpr (MIXED)
+  {
+    st = P.f_slope_type;
+    smallr = P.f_smallr;
+    thinc_eps = P.f_thinc_eps;
+    thinc_beta = P.f_thinc_beta;
+  }
+  else
+  {
+    st = P.slope_type;
+    smallr = P.smallr;
+    thinc_eps = P.thinc_eps;
+    thinc_beta = P.thinc_beta;
+  }
+  const bool hancock = P.integrator == 0;
+  const R    off = R(0.5) * R(side);
+#pragma unroll
+  for (int k = 0; k < 6; ++k)
+  {
+    const R * Qk = sQ + k * GGG;
+    const R   qc = Qk[gi];
+    const R   dq = slope_at<R>(Qk, gi, o, st);
+    R         t = qc + off * dq;
+    if constexpr (!MIXED)
+    {
+      // the reference adds the zero-offset terms of the other directions,
+      // ((q + o_x dq_x) + o_y dq_y) + o_z dq_z; they can only change the sign
+      // of a zero, so they are evaluated only when a negative zero occurs
+      if (neg_zero(qc) || neg_zero(t))
+      {
+        R dd[3];
+#pragma unroll
+        for (int e = 0; e < 3; ++e)
+          dd[e] = slope_at<R>(Qk, gi, strides[e], st);
+        const R o0 = dir == 0 ? off : R(0), o1 = dir == 1 ? off : R(0), o2 = dir == 2 ? off : R(0);
+        t = qc + o0 * dd[0] + o1 * dd[1] + o2 * dd[2];
+      }
+    }
+    q[k] = t;
+    if (hancock)
+      q[k] += sHS[k * SSS + si];
+  }
+  const R a0 = sQ[6 * GGG + gi];
+  q[6] = a0;
+  if (P.thinc)
+  {
+    const R *  A = sQ + 6 * GGG;
+    const R    aP = A[gi + o], aM = A[gi - o];
+    const R    mono = (aP - a0) * (a0 - aM);
+    const bool req = (a0 > thinc_eps) && (a0 < R(1) - thinc_eps) && mono > R(0);
+    if (req)
+    {
+      const R nd = sN[dir * SSS + si];
+      const R beta = thinc_beta * nd + R(0.01);
+      const R Aa = (aP + aM) / R(2);
+      const R Bb = (aP - aM) / R(2);
+      R       C, D;
+      if constexpr (MIXED)
+      {
+        C = tanhf(R(0.5) * beta);
+        D = tanhf(R(0.5) * beta * (a0 - Aa) / Bb);
+      }
+      else
+      {
+        C = tanh_d(R(0.5) * beta);
+        D = tanh_d(R(0.5) * beta * (a0 - Aa) / Bb);
+      }
+      const R bs = R(side);
+      const R af = Aa + bs * Bb * (C + bs * D / C) / (R(1) + bs * D);
+      const R r0 = sQ[0 * GGG + gi], r1 = sQ[1 * GGG + gi];
+      R       q0 = r0 + r0 / a0 * (af - a0);
+      R       q1 = r1 + r1 / (R(1) - a0) * (a0 - af);
+      if (hancock)
+      {
+        q0 += sHS[0 * SSS + si];
+        q1 += sHS[1 * SSS + si];
+      }
+      q[0] = q0;
+      q[1] = q1;
+      q[6] = af;
+    }
+  }
+  else
+  {
+    q[0] = fmax(smallr, q[0]);
+    q[1] = fmax(smallr, q[1]);
+  }
+}
+
+// one direction of update_U (FP64, reference order); returns nothing, u2 updated
+__device__ __forceinline__ void
+apply_dir_fp64(double * u2, const double * acc)
+{
+  using H = V<3>;
+  const double eps = 1e-12;
+  u2[H::IAD0] += acc[H::FR0];
+  if (u2[H::IAD0] < eps)
+    u2[H::IAD0] = 0.0;
+  u2[H::IAD1] += acc[H::FR1];
+  if (u2[H::IAD1] < eps)
+    u2[H::IAD1] = 0.0;
+  u2[H::IA0] += acc[H::FA0];
+  if (u2[H::IA0] < eps)
+    u2[H::IA0] = 0.0;
+  if (u2[H::IA0] > 1.0 - eps)
+    u2[H::IA0] = 1.0;
+  u2[H::IA1] += acc[H::FA1];
+  if (u2[H::IA1] < eps)
+    u2[H::IA1] = 0.0;
+  if (u2[H::IA1] > 1.0 - eps)
+    u2[H::IA1] = 1.0;
+  u2[H::IE] += acc[H::FE];
+  u2[H::IU] += acc[H::FU];
+  u2[H::IV] += acc[H::FV];
+  u2[H::IW] += acc[H::FW];
+}
+
+template <bool MIXED>
+__global__ void __launch_bounds__(512, MIXED ? 2 : 1)
+step3d_kernel(StepArgs a)
+{
+  using T = Step3DTraits<MIXED>;
+  using R = typename T::R;
+  using H = V<3>;
+  constexpr int B = T::B, NT = T::NT, G = T::G, GG = T::GG, GGG = T::GGG, S = T::S, SS = T::SS, SSS = T::SSS, NC = 512;
+  constexpr int NFF = T::NFF;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  R *          sQ = reinterpret_cast<R *>(smem_raw);
+  R *          sHS = sQ + T::NQ * GGG;
+  R *          sN = sHS + T::NHS * SSS;
+  R *          sF = sN + T::NN * SSS; // [9][NFF] faces of the current direction
+  using DtT = typename std::conditional<MIXED, float, double>::type;
+  __shared__ DtT     sRed[NT / 32];
+  const int          tid = threadIdx.x;
+  const PhysParams & P = a.p;
+  const bool         stiff = P.gpx[0] != 0.0 || P.gpx[1] != 0.0;
+  const int          ci = tid % B, cj = (tid / B) % B, ck = tid / (B * B);
+
+  for (int n = blockIdx.x; n < a.m.n_owned; n += gridDim.x)
+  {
+    const int    ins = a.m.inst ? a.m.inst[n] : 0;
+    const double dx = P.level_dx[a.m.level[n]];
+    R            dtdx_r;
+    if constexpr (MIXED)
+      dtdx_r = d2f_fast(a.dt[ins]) * __frcp_rn(d2f_fast(dx));
+    else
+      dtdx_r = a.dt[ins] / dx;
+
+    // ---------------- phase 1: own cell (coalesced) + halo -> primitives
+    double uin[H::NV];
+    {
+      const double * base = a.U + (size_t)n * H::NV * NC + tid;
+#pragma unroll
+      for (int v = 0; v < H::NV; ++v)
+        uin[v] = base[v * NC];
+      store_prim3<MIXED>(sQ, (ci + 2) + G * (cj + 2) + GG * (ck + 2), uin, P, stiff);
+    }
+    for (int h = tid; h < GGG; h += NT)
+    {
+      const int g[3] = { h % G - 2, (h / G) % G - 2, h / GG - 2 };
+      if (g[0] >= 0 && g[0] < B && g[1] >= 0 && g[1] < B && g[2] >= 0 && g[2] < B)
+        continue;
+      double u[H::NV];
+      if (!gather_ghost_3d(a, n, g, u))
+      {
+        raise_status(a.status, STATUS_MESH);
+#pragma unroll
+        for (int v = 0; v < H::NV; ++v)
+          u[v] = uin[v];
+      }
+      store_prim3<MIXED>(sQ, h, u, P, stiff);
+    }
+    __syncthreads();
+
+    // ---------------- phase 2: ring cells: Hancock source (and THINC |n|)
+    for (int r = tid; r < SSS; r += NT)
+    {
+      const int ri = r % S - 1, rj = (r / S) % S - 1, rk = r / SS - 1;
+      const int outside = (ri < 0 || ri >= B) + (rj < 0 || rj >= B) + (rk < 0 || rk >= B);
+      if (outside > 1)
+        continue; // edges and corners of the ring are never a face neighbour
+      const int gi = (ri + 2) + G * (rj + 2) + GG * (rk + 2);
+      if (P.integrator == 0)
+      {
+        R st;
+        if constexpr (MIXED)
+          st = P.f_slope_type;
+        else
+          st = P.slope_type;
+        R dq[3][6], q[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k)
+        {
+          const R * Qk = sQ + k * GGG;
+          q[k] = Qk[gi];
+          dq[0][k] = slope_at<R>(Qk, gi, 1, st);
+          dq[1][k] = slope_at<R>(Qk, gi, G, st);
+          dq[2][k] = slope_at<R>(Qk, gi, GG, st);
+        }
+        const R a0 = sQ[6 * GGG + gi];
+        const R r0 = q[0], r1 = q[1], p = q[2], u = q[3], v = q[4], w = q[5];
+        const R rr = r0 + r1;
+        R       c;
+        if constexpr (MIXED)
+          c = sound_speed_f(P.f_xi[0], P.f_xi[1], P.f_gpx[0], P.f_gpx[1], rr, p, a0);
+        else
+          c = sound_speed_d(P, rr, p, a0, 1 - a0);
+        const R drx0 = dq[0][0], drx1 = dq[0][1], dpx = dq[0][2], dux = dq[0][3], dvx = dq[0][4], dwx = dq[0][5];
+        const R dry0 = dq[1][0], dry1 = dq[1][1], dpy = dq[1][2], duy = dq[1][3], dvy = dq[1][4], dwy = dq[1][5];
+        const R drz0 = dq[2][0], drz1 = dq[2][1], dpz = dq[2][2], duz = dq[2][3], dvz = dq[2][4], dwz = dq[2][5];
+        const R dtdx = dtdx_r, dtdy = dtdx_r, dtdz = dtdx_r;
+        // ComputeFluxesAndStoreFunctor.cpp:273-306
+        const R sr0 = (-u * (drx0 + drx1) - dux * rr) * dtdx + (-v * (dry0 + dry1) - dvy * rr) * dtdy +
+                      (-w * (drz0 + drz1) - dwz * rr) * dtdz;
+        const R sr0_0 = sr0 * a0;
+        const R sr0_1 = sr0 * (R(1) - a0);
+        const R su0 = (-u * dux - dpx / rr) * dtdx + (-v * duy) * dtdy + (-w * duz) * dtdz;
+        const R sv0 = (-u * dvx) * dtdx + (-v * dvy - dpy / rr) * dtdy + (-w * dvz) * dtdz;
+        const R sw0 = (-u * dwx) * dtdx + (-v * dwy) * dtdy + (-w * dwz - dpz / rr) * dtdz;
+        const R sp0 = (-u * dpx - dux * rr * c * c) * dtdx + (-v * dpy - dvy * rr * c * c) * dtdy +
+                      (-w * dpz - dwz * rr * c * c) * dtdz;
+        sHS[0 * SSS + r] = R(0.5) * sr0_0;
+        sHS[1 * SSS + r] = R(0.5) * sr0_1;
+        sHS[2 * SSS + r] = R(0.5) * sp0;
+        sHS[3 * SSS + r] = R(0.5) * su0;
+        sHS[4 * SSS + r] = R(0.5) * sv0;
+        sHS[5 * SSS + r] = R(0.5) * sw0;
+      }
+      if (P.thinc)
+      {
+        // Youngs normal, (1,2,1)x(1,2,1) weights, unit cell
+        const R * A = sQ + 6 * GGG;
+        const R   w[3] = { R(1), R(2), R(1) };
+        R         g0 = R(0), g1 = R(0), g2 = R(0);
+        for (int cc = -1; cc <= 1; ++cc)
+          for (int bb = -1; bb <= 1; ++bb)
+          {
+            const R ww = w[bb + 1] * w[cc + 1];
+            g0 += ww * (A[gi + 1 + G * bb + GG * cc] - A[gi - 1 + G * bb + GG * cc]);
+            g1 += ww * (A[gi + bb + G + GG * cc] - A[gi + bb - G + GG * cc]);
+            g2 += ww * (A[gi + bb + G * cc + GG] - A[gi + bb + G * cc - GG]);
+          }
+        R nrm = g0 * g0 + g1 * g1;
+        nrm += g2 * g2;
+        nrm = sqrt(nrm);
+        sN[0 * SSS + r] = (nrm > R(0)) ? fabs(-g0 / nrm) : R(0);
+        sN[1 * SSS + r] = (nrm > R(0)) ? fabs(-g1 / nrm) : R(0);
+        sN[2 * SSS + r] = (nrm > R(0)) ? fabs(-g2 / nrm) : R(0);
+      }
+    }
+    __syncthreads();
+
+    // deferred cells (next to a finer face) are finished by reflux3d_kernel
+    const int * dsl = a.m.defer_slot ? a.m.defer_slot + n * 6 : nullptr;
+    bool        deferred = false;
+    if (dsl)
+    {
+      const int cc[3] = { ci, cj, ck };
+#pragma unroll
+      for (int f = 0; f < 6; ++f)
+        deferred = deferred || (dsl[f] >= 0 && cc[f >> 1] == ((f & 1) ? B - 1 : 0));
+    }
+
+    // running state of the owned cell
+    double u2[H::NV];
+#pragma unroll
+    for (int v = 0; v < H::NV; ++v)
+      u2[v] = uin[v];
+    // mixed form: per-direction increments of the clamped quantities (exact
+    // float pairs) and running float-float sums of energy and momentum
+    float hh[3][2], ll[3][2], dA[3][2];
+    float es[4] = { 0.f, 0.f, 0.f, 0.f }, et[4] = { 0.f, 0.f, 0.f, 0.f };
+
+    for (int dir = 0; dir < 3; ++dir)
+    {
+      // ---------------- phase 3: faces of this direction
+      for (int f = tid; f < NFF; f += NT)
+      {
+        int fi, fj, fk;
+        if (dir == 0)
+        {
+          fi = f % (B + 1);
+          fj = (f / (B + 1)) % B;
+          fk = f / ((B + 1) * B);
+        }
+        else if (dir == 1)
+        {
+          fi = f % B;
+          fj = (f / B) % (B + 1);
+          fk = f / (B * (B + 1));
+        }
+        else
+        {
+          fi = f % B;
+          fj = (f / B) % B;
+          fk = f / (B * B);
+        }
+        R qL[7], qR[7], fl[9];
+        face_state3<MIXED>(sQ, sHS, sN, fi - (dir == 0), fj - (dir == 1), fk - (dir == 2), dir, +1, P, qL);
+        face_state3<MIXED>(sQ, sHS, sN, fi, fj, fk, dir, -1, P, qR);
+        const int iw = dir == 1 ? 4 : 5; // component swapped with u
+        if (dir > 0)
+        {
+          R t = qL[3];
+          qL[3] = qL[iw];
+          qL[iw] = t;
+          t = qR[3];
+          qR[3] = qR[iw];
+          qR[iw] = t;
+        }
+        if constexpr (MIXED)
+          hllc_fp32<3>(qL, qR, P.f_xi[0], P.f_xi[1], P.f_gpx[0], P.f_gpx[1], P.f_smallr, P.f_smallp, P.f_smallc, fl);
+        else
+          hllc_fp64<3>(qL, qR, P, fl);
+        if (dir > 0)
+        {
+          const int fw = dir == 1 ? H::FV : H::FW;
+          const R   t = fl[H::FU];
+          fl[H::FU] = fl[fw];
+          fl[fw] = t;
+        }
+#pragma unroll
+        for (int k = 0; k < 9; ++k)
+          sF[k * NFF + f] = fl[k] * dtdx_r;
+      }
+      __syncthreads();
+
+      // face index of the owned cell's left/right face in this direction
+      const int ext0 = B + (dir == 0), ext1 = B + (dir == 1);
+      const int il = ci + ext0 * (cj + ext1 * ck);
+      const int step = dir == 0 ? 1 : (dir == 1 ? ext0 : ext0 * ext1);
+      const int ir = il + step;
+
+      // ---------------- publish coarse/fine records of this direction (AMR only)
+      if (a.m.reflux_slot)
+      {
+        for (int side = 0; side < 2; ++side)
+        {
+          const int face = 2 * dir + side;
+          const int rs = a.m.reflux_slot[n * 6 + face];
+          const int ds = a.m.defer_slot[n * 6 + face];
+          // positions along the face: the two transverse coordinates (first, second)
+          if (rs >= 0 && tid < B * B)
+          {
+            const int t1 = tid % B, t2 = tid / B;
+            int       c3[3];
+            c3[dir] = side ? B : 0;
+            c3[dir == 0 ? 1 : 0] = t1;
+            c3[dir == 2 ? 1 : 2] = t2;
+            const int fidx = c3[0] + ext0 * (c3[1] + ext1 * c3[2]);
+            double *  dst = a.reflux_buf + ((size_t)rs * B * B + tid) * 9;
+#pragma unroll
+            for (int k = 0; k < 9; ++k)
+              dst[k] = (double)sF[k * NFF + fidx];
+          }
+          (void)ds;
+        }
+        // own face fluxes of deferred cells, this direction (left then right)
+        if (deferred)
+        {
+          const int cc[3] = { ci, cj, ck };
+          for (int f = 0; f < 6; ++f)
+          {
+            if (dsl[f] < 0 || cc[f >> 1] != ((f & 1) ? B - 1 : 0))
+              continue;
+            const int d2 = f >> 1;
+            const int t1 = cc[d2 == 0 ? 1 : 0], t2 = cc[d2 == 2 ? 1 : 2];
+            double *  dst = a.defer_buf + (((size_t)dsl[f] * B * B + t1 + B * t2) * 6 + 2 * dir) * 9;
+#pragma unroll
+            for (int k = 0; k < 9; ++k)
+            {
+              dst[k] = (double)sF[k * NFF + il];
+              dst[9 + k] = (double)sF[k * NFF + ir];
+            }
+          }
+        }
+      }
+
+      // ---------------- phase 4: this direction's update of the owned cell
+      if constexpr (!MIXED)
+      {
+        const double a0n = uin[H::IA0], a1n = uin[H::IA1];
+        double       acc[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+          acc[k] = 0.0 + sF[k * NFF + il];
+        const double usl = sF[H::FUS * NFF + il];
+        acc[H::FA0] -= usl * a0n;
+        acc[H::FA1] -= usl * a1n;
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+          acc[k] = acc[k] - sF[k * NFF + ir];
+        const double usr = sF[H::FUS * NFF + ir];
+        acc[H::FA0] += usr * a0n;
+        acc[H::FA1] += usr * a1n;
+        apply_dir_fp64(u2, acc);
+      }
+      else
+      {
+        const float a0f = d2f_fast(uin[H::IA0]), a1f = d2f_fast(uin[H::IA1]);
+        two_diff(sF[H::FR0 * NFF + il], sF[H::FR0 * NFF + ir], hh[dir][0], ll[dir][0]);
+        two_diff(sF[H::FR1 * NFF + il], sF[H::FR1 * NFF + ir], hh[dir][1], ll[dir][1]);
+        const int ke[4] = { H::FE, H::FU, H::FV, H::FW };
+#pragma unroll
+        for (int e = 0; e < 4; ++e)
+        {
+          float h, l, t;
+          two_diff(sF[ke[e] * NFF + il], sF[ke[e] * NFF + ir], h, l);
+          two_sum(es[e], h, es[e], t);
+          et[e] += t + l;
+        }
+        const float usl = sF[H::FUS * NFF + il], usr = sF[H::FUS * NFF + ir];
+        dA[dir][0] = ((sF[H::FA0 * NFF + il] - usl * a0f) - sF[H::FA0 * NFF + ir]) + usr * a0f;
+        dA[dir][1] = ((sF[H::FA1 * NFF + il] - usl * a1f) - sF[H::FA1 * NFF + ir]) + usr * a1f;
+      }
+      __syncthreads();
+    }
+
+    if constexpr (MIXED)
+    {
+      // partial densities and volume fractions: the three directions combined
+      // when no per-direction clamp can trigger (FP32 test with margin),
+      // otherwise applied direction by direction; energy and momentum in one
+      // exact float-float sum
+      const double eps = 1e-12, one_m_eps = 1.0 - 1e-12;
+#pragma unroll
+      for (int k = 0; k < 2; ++k)
+      {
+        const int   iv = k == 0 ? H::IAD0 : H::IAD1;
+        const float uf = d2f_fast(u2[iv]);
+        if (uf > 2.0f * (fabsf(hh[0][k]) + fabsf(hh[1][k])) + 2e-12f)
+        {
+          float s, t, s2, t2;
+          two_sum(hh[0][k], hh[1][k], s, t);
+          two_sum(s, hh[2][k], s2, t2);
+          t2 += t + ll[0][k] + ll[1][k] + ll[2][k];
+          u2[iv] = (u2[iv] + f2d_exact(s2)) + f2d_exact(t2);
+          if (dlt_pos(u2[iv], eps))
+            u2[iv] = 0.0;
+        }
+        else
+        {
+#pragma unroll
+          for (int d = 0; d < 3; ++d)
+          {
+            u2[iv] = (u2[iv] + f2d_exact(hh[d][k])) + f2d_exact(ll[d][k]);
+            if (dlt_pos(u2[iv], eps))
+              u2[iv] = 0.0;
+          }
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < 2; ++k)
+      {
+        const int   iv = k == 0 ? H::IA0 : H::IA1;
+        const float af = d2f_fast(uin[iv]);
+        const float m = 2.0f * (fabsf(dA[0][k]) + fabsf(dA[1][k])) + 2e-12f;
+        if (af > m && af + m < 1.0f)
+        {
+          u2[iv] += f2d_exact((dA[0][k] + dA[1][k]) + dA[2][k]);
+          if (dlt_pos(u2[iv], eps))
+            u2[iv] = 0.0;
+          if (dgt_pos(u2[iv], one_m_eps))
+            u2[iv] = 1.0;
+        }
+        else
+        {
+#pragma unroll
+          for (int d = 0; d < 3; ++d)
+          {
+            u2[iv] += f2d_exact(dA[d][k]);
+            if (dlt_pos(u2[iv], eps))
+              u2[iv] = 0.0;
+            if (dgt_pos(u2[iv], one_m_eps))
+              u2[iv] = 1.0;
+          }
+        }
+      }
+      const int ive[4] = { H::IE, H::IU, H::IV, H::IW };
+#pragma unroll
+      for (int e = 0; e < 4; ++e)
+        u2[ive[e]] = (u2[ive[e]] + f2d_exact(es[e])) + f2d_exact(et[e]);
+      const double sa = u2[H::IA0] + u2[H::IA1];
+      const double d = sa - 1.0;
+      if (d != 0.0)
+      {
+        if ((__double_as_longlong(d) & 0x7FFFFFFFFFFFFFFFLL) < __double_as_longlong(1e-8))
+        {
+          u2[H::IA0] = fma(-u2[H::IA0], d, u2[H::IA0]);
+          u2[H::IA1] = fma(-u2[H::IA1], d, u2[H::IA1]);
+        }
+        else
+        {
+          const double inv = 1.0 / sa;
+          u2[H::IA0] *= inv;
+          u2[H::IA1] *= inv;
+        }
+      }
+      u2[H::ID] = u2[H::IAD0] + u2[H::IAD1];
+    }
+    else
+    {
+      // FixVolumeFractionsNormalization (.cpp:49-72)
+      const double sum_alpha = u2[H::IA0] + u2[H::IA1];
+      const double sum_alpha_rho = u2[H::IAD0] + u2[H::IAD1];
+      const double inv = 1.0 / sum_alpha;
+      u2[H::IA0] *= inv;
+      u2[H::IA1] *= inv;
+      u2[H::ID] = sum_alpha_rho;
+    }
+
+    DtT m_inv = DtT(0);
+    if (!deferred)
+    {
+      double * out = a.U2 + (size_t)n * H::NV * NC + tid;
+      bool     finite = true;
+#pragma unroll
+      for (int v = 0; v < H::NV; ++v)
+      {
+        out[v * NC] = u2[v];
+        finite = finite && finite_bits(u2[v]);
+      }
+      if (!finite)
+        raise_status(a.status, STATUS_NONPHYSICAL);
+      if (a.invdt)
+      {
+        if constexpr (MIXED)
+        {
+          float       df, ux, uy, uz, a0;
+          const float p = pressure_mixed<3>(u2, P, stiff, df, ux, uy, uz, a0);
+          const float c = sound_speed_f(P.f_xi[0], P.f_xi[1], P.f_gpx[0], P.f_gpx[1], df, p, fmaxf(0.0f, fminf(1.0f, a0)));
+          m_inv = (((c + fabsf(ux)) + (c + fabsf(uy))) + (c + fabsf(uz))) * __frcp_rn(d2f_fast(dx));
+        }
+        else
+        {
+          double       q[7];
+          const double c = prim_fp64<3>(u2, q, P);
+          m_inv = (c + fabs(q[H::QU])) / dx + (c + fabs(q[H::QV])) / dx + (c + fabs(q[H::QW])) / dx;
+        }
+      }
+    }
+    if (a.invdt)
+    {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1)
+        m_inv = fmax(m_inv, __shfl_xor_sync(0xffffffffu, m_inv, o));
+      if ((tid & 31) == 0)
+        sRed[tid >> 5] = m_inv;
+      __syncthreads();
+      if (tid == 0)
+      {
+        DtT mm = DtT(0);
+        for (int w = 0; w < NT / 32; ++w)
+          mm = fmax(mm, sRed[w]);
+        atomic_max_pos(a.invdt + ins, (double)mm);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// reflux: coarse cells next to finer faces, one thread per (record, cell of
+// the face).  Replays update_U direction by direction with the fine face sums
+// (2x2 fine faces, / 8) of get_flux_from_fine_neighbor.
+template <bool MIXED>
+__global__ void
+reflux3d_kernel(StepArgs a)
+{
+  using H = V<3>;
+  constexpr int B = 8, NC = 512;
+  const int     gid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= a.m.n_defer * B * B)
+    return;
+  const int rec = gid / (B * B), pos = gid % (B * B);
+  const int code = a.m.defer_list[rec];
+  const int n = code >> 3, face = code & 7;
+  const int dirf = face >> 1, sidef = face & 1;
+  int       cc[3];
+  cc[dirf] = sidef ? B - 1 : 0;
+  cc[dirf == 0 ? 1 : 0] = pos % B;
+  cc[dirf == 2 ? 1 : 2] = pos / B;
+  const int * dsl = a.m.defer_slot + n * 6;
+  for (int f2 = 0; f2 < face; ++f2)
+    if (dsl[f2] >= 0 && cc[f2 >> 1] == ((f2 & 1) ? B - 1 : 0))
+      return; // handled by the lower face index
+  const double * own = a.defer_buf + ((size_t)dsl[face] * B * B + pos) * 54;
+  const int      cell = cc[0] + B * (cc[1] + B * cc[2]);
+  const double * ub = a.U + (size_t)n * H::NV * NC + cell;
+  double         uin[H::NV], u2[H::NV];
+  for (int v = 0; v < H::NV; ++v)
+    u2[v] = uin[v] = ub[v * NC];
+  const int    ins = a.m.inst ? a.m.inst[n] : 0;
+  const double dx = a.p.level_dx[a.m.level[n]];
+  const double a0n = uin[H::IA0], a1n = uin[H::IA1];
+  for (int dir = 0; dir < 3; ++dir)
+  {
+    const int e1 = dir == 0 ? 1 : 0, e2 = dir == 2 ? 1 : 2;
+    double    acc[8];
+    for (int k = 0; k < 8; ++k)
+      acc[k] = 0.0;
+    for (int side = 0; side < 2; ++side)
+    {
+      const int  fface = 2 * dir + side;
+      const bool fine = cc[dir] == (side ? B - 1 : 0) && dsl[fface] >= 0;
+      if (fine)
+      {
+        int d3[3] = { 0, 0, 0 };
+        d3[dir] = side ? 1 : -1;
+        const int s = (d3[0] + 1) + 3 * (d3[1] + 1) + 9 * (d3[2] + 1);
+        int       ch[3], fl[3];
+        ch[dir] = side ? 0 : 1;
+        fl[dir] = 0;
+        for (int e = 0; e < 3; ++e)
+          if (e != dir)
+          {
+            const int f = 2 * cc[e];
+            ch[e] = f / B;
+            fl[e] = f - ch[e] * B;
+          }
+        const int F = a.m.nbr[(n * 27 + s) * 8 + ch[0] + 2 * ch[1] + 4 * ch[2]];
+        const int rs = (F >= 0 && F < a.m.n_owned) ? a.m.reflux_slot[F * 6 + (fface ^ 1)] : -1;
+        if (rs < 0)
+        {
+          raise_status(a.status, STATUS_MESH);
+          return;
+        }
+        double fv[9];
+        for (int k = 0; k < 9; ++k)
+        {
+          double sum = 0.0;
+          for (int o2 = 0; o2 < 2; ++o2)
+            for (int o1 = 0; o1 < 2; ++o1)
+              sum += a.reflux_buf[((size_t)rs * B * B + (fl[e1] + o1) + B * (fl[e2] + o2)) * 9 + k];
+          fv[k] = sum;
+        }
+        for (int k = 0; k < 8; ++k)
+          acc[k] = side == 0 ? acc[k] + fv[k] / 8.0 : acc[k] - fv[k] / 8.0;
+        const double us = fv[8];
+        if (side == 0)
+        {
+          acc[H::FA0] -= us * a0n / 8.0;
+          acc[H::FA1] -= us * a1n / 8.0;
+        }
+        else
+        {
+          acc[H::FA0] += us * a0n / 8.0;
+          acc[H::FA1] += us * a1n / 8.0;
+        }
+      }
+      else
+      {
+        const double * fr = own + (2 * dir + side) * 9;
+        for (int k = 0; k < 8; ++k)
+          acc[k] = side == 0 ? acc[k] + fr[k] : acc[k] - fr[k];
+        const double us = fr[8];
+        if (side == 0)
+        {
+          acc[H::FA0] -= us * a0n;
+          acc[H::FA1] -= us * a1n;
+        }
+        else
+        {
+          acc[H::FA0] += us * a0n;
+          acc[H::FA1] += us * a1n;
+        }
+      }
+    }
+    apply_dir_fp64(u2, acc);
+  }
+  const double sum_alpha = u2[H::IA0] + u2[H::IA1];
+  const double sum_alpha_rho = u2[H::IAD0] + u2[H::IAD1];
+  const double inv = 1.0 / sum_alpha;
+  u2[H::IA0] *= inv;
+  u2[H::IA1] *= inv;
+  u2[H::ID] = sum_alpha_rho;
+  double * out = a.U2 + (size_t)n * H::NV * NC + cell;
+  bool     finite = true;
+  for (int v = 0; v < H::NV; ++v)
+  {
+    out[v * NC] = u2[v];
+    finite = finite && finite_bits(u2[v]);
+  }
+  if (!finite)
+    raise_status(a.status, STATUS_NONPHYSICAL);
+  if (a.invdt)
+  {
+    double       q[7];
+    const double c = prim_fp64<3>(u2, q, a.p);
+    atomic_max_pos(a.invdt + ins, (c + fabs(q[H::QU])) / dx + (c + fabs(q[H::QV])) / dx + (c + fabs(q[H::QW])) / dx);
+  }
+}
+
+} // namespace g5
