@@ -43,7 +43,8 @@ sys.path.insert(0, ROOT)
 
 METRIC = "cell-updates/s, 1 GB300: mixed vs FP64 plain at L1 err<=1e-5 vs FP64; %HBM peak"
 BYTES_PER_CELL_2D = 2 * 8 * 8  # read U + write U2, 8 FP64 variables
-L1_STEPS = {"shock_bubble": 500, "gas_water": 200, "droplets": 100, "droplets32": 100, "shock_bubble_r22_thinc": 500}
+BYTES_PER_CELL_3D = 2 * 9 * 8  # read U + write U2, 9 FP64 variables
+L1_STEPS = {"shock_bubble": 500, "gas_water": 200, "droplets": 100, "droplets32": 100, "shock_bubble_r22_thinc": 500, "triple_point_3d": 300, "triple_point_3d_small": 50}
 
 
 def parse():
@@ -56,6 +57,7 @@ def parse():
     ap.add_argument("--no-l1", action="store_true", help="skip the 500-step accuracy run")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--profile", action="store_true", help="one FP64 and one mixed step kernel launch, for ncu")
+    ap.add_argument("--no-clocks", action="store_true", help="skip the nvidia-smi clock sampling (and its bracketing load)")
     return ap.parse_args()
 
 
@@ -68,6 +70,12 @@ def build_workload(name, flag_fn):
     elif name == "shock_bubble_r22_thinc":
         mesh, t, p, U = configs.shock_bubble("r22", thinc=True, flag_fn=flag_fn)
         desc = "shock_bubble_air_r22_thinc_2d_amr_levels4-6_16x16"
+    elif name == "triple_point_3d":
+        mesh, t, p, U = configs.triple_point_3d(flag_fn=flag_fn)
+        desc = "triple_point_3d_thinc_amr_levels0-3_8x8x8"
+    elif name == "triple_point_3d_small":
+        mesh, t, p, U = configs.triple_point_3d(level_min=0, level_max=2, flag_fn=flag_fn)
+        desc = "triple_point_3d_thinc_amr_levels0-2_8x8x8"
     elif name == "gas_water":
         mesh, t, p, U = configs.gas_water_shock_tube()
         desc = "gas_water_shock_tube_2d_512x32_16x16"
@@ -332,7 +340,7 @@ def main():
         torch.cuda.synchronize()
         if world > 1:
             dist.barrier()
-        sampler = ClockSampler(local) if mode == "mixed" else None
+        sampler = ClockSampler(local) if (mode == "mixed" and not args.no_clocks) else None
         if sampler:
             # nvidia-smi samples every 200 ms: the same load runs for ~0.5 s
             # before and after the timed steps so that the samples see it
@@ -400,7 +408,8 @@ def main():
     }
     peak, peak_kind = measured_peaks()
     kern_s = res["mixed"]["kern_ms"] * 1e-3
-    achieved = cells * BYTES_PER_CELL_2D / kern_s / 1e9
+    bpc = BYTES_PER_CELL_2D if t.dim == 2 else BYTES_PER_CELL_3D
+    achieved = cells * bpc / kern_s / 1e9
     roofline = {
         "bound": "hbm",
         "achieved": achieved,
@@ -409,11 +418,11 @@ def main():
         "frac": achieved / peak,
         "traffic": ncu_traffic(args.workload, "mixed"),
         "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback 6.8 TB/s",
-        "kernel": "step2d_kernel<16,mixed> (+reflux2d)",
+        "kernel": "step2d_kernel<16,mixed> (+reflux2d)" if t.dim == 2 else "step3d_kernel<mixed> (+reflux3d)",
         "kernel_ms": res["mixed"]["kern_ms"],
-        "algorithmic_bytes_per_launch": cells * BYTES_PER_CELL_2D,
+        "algorithmic_bytes_per_launch": cells * bpc,
         "fp64_kernel_ms": res["fp64"]["kern_ms"],
-        "fp64_frac": cells * BYTES_PER_CELL_2D / (res["fp64"]["kern_ms"] * 1e-3) / 1e9 / peak,
+        "fp64_frac": cells * bpc / (res["fp64"]["kern_ms"] * 1e-3) / 1e9 / peak,
     }
     cpu = None
     if rank == 0 and not args.no_cpu:
