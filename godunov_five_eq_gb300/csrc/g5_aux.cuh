@@ -2,6 +2,8 @@
 // refine flags and the device-side dt update of the solver loop.
 #pragma once
 
+#include <type_traits>
+
 #include "g5_common.cuh"
 
 namespace g5
@@ -88,8 +90,74 @@ inv_dt_kernel(const double * U, DevMesh m, PhysParams P, double * invdt)
   }
 }
 
-// dt = cfl / inv_dt per instance; inv_dt accumulator cleared for the next step
+// RK2_SSP final stage (SolverGodunovFiveEq.cpp:519-520, the external
+// LinearCombination with the SSP coefficients): U2 = 0.5 U + 0.5 U2 on the
+// owned blocks, fused with the CFL rate of the result (one CTA per block).
+template <int DIM, int B, bool MIXED>
 __global__ void
+rk2_combine_kernel(const double * U, double * U2, DevMesh m, PhysParams P, double * invdt)
+{
+  using H = V<DIM>;
+  constexpr int NC = (DIM == 2) ? B * B : B * B * B;
+  using DtT = typename std::conditional<MIXED, float, double>::type;
+  __shared__ DtT sred[32];
+  const bool     stiff = P.gpx[0] != 0.0 || P.gpx[1] != 0.0;
+  for (int n = blockIdx.x; n < m.n_owned; n += gridDim.x)
+  {
+    const double dx = P.level_dx[m.level[n]];
+    DtT          mx = DtT(0);
+    for (int c = threadIdx.x; c < NC; c += blockDim.x)
+    {
+      double u[H::NV];
+      for (int v = 0; v < H::NV; ++v)
+      {
+        const size_t i = ((size_t)n * H::NV + v) * NC + c;
+        u[v] = 0.5 * U[i] + 0.5 * U2[i];
+        U2[i] = u[v];
+      }
+      if constexpr (MIXED)
+      {
+        float       d, ux, uy, uz, a0;
+        const float p = pressure_mixed<DIM>(u, P, stiff, d, ux, uy, uz, a0);
+        const float cs = sound_speed_f(P.f_xi[0], P.f_xi[1], P.f_gpx[0], P.f_gpx[1], d, p, fmaxf(0.0f, fminf(1.0f, a0)));
+        float       r = (cs + fabsf(ux)) + (cs + fabsf(uy));
+        if constexpr (DIM == 3)
+          r += cs + fabsf(uz);
+        mx = fmaxf(mx, r * __frcp_rn(d2f_fast(dx)));
+      }
+      else
+      {
+        double       q[H::NQ];
+        const double cs = prim_fp64<DIM>(u, q, P);
+        const double vx = cs + fabs(q[H::QU]);
+        const double vy = cs + fabs(q[H::QV]);
+        if constexpr (DIM == 2)
+          mx = fmax(mx, vx / dx + vy / dx);
+        else
+          mx = fmax(mx, vx / dx + vy / dx + (cs + fabs(q[H::QW])) / dx);
+      }
+    }
+    if (invdt)
+    {
+      for (int o = 16; o > 0; o >>= 1)
+        mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+      if ((threadIdx.x & 31) == 0)
+        sred[threadIdx.x >> 5] = mx;
+      __syncthreads();
+      if (threadIdx.x == 0)
+      {
+        DtT mm = DtT(0);
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w)
+          mm = fmax(mm, sred[w]);
+        atomic_max_pos(invdt + (m.inst ? m.inst[n] : 0), (double)mm);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// dt = cfl / inv_dt per instance; inv_dt accumulator cleared for the next step
+static __global__ void
 dt_update_kernel(double * invdt, double * dt, double * dt_hist, int n_inst, double cfl)
 {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;

@@ -25,6 +25,7 @@ struct G5Context
   // scratch
   double *       d_reflux_buf = nullptr, *d_defer_buf = nullptr;
   double *       d_dt = nullptr, *d_invdt = nullptr;
+  double *       d_urk = nullptr; // RK2_SSP intermediate stage (SolverGodunovFiveEq.h:349-358 m_U_RK)
   int *          d_step = nullptr;
   unsigned int * d_status = nullptr;
   int64_t        bytes = 0;
@@ -90,7 +91,7 @@ free_mesh(G5Context * c)
   void * ptrs[] = { c->d_level,       c->d_coord,       c->d_nbr,        c->d_inst,       c->d_reflux_slot,
                     c->d_defer_slot,  c->d_defer_list,  c->d_out_src,    c->d_nbr_rel,    c->d_out_normal,
                     c->d_out_border,  c->d_reflux_buf,  c->d_defer_buf,  c->d_dt,         c->d_invdt,
-                    c->d_step };
+                    c->d_step,        c->d_urk };
   for (void * p : ptrs)
     if (p)
       cudaFree(p);
@@ -99,6 +100,7 @@ free_mesh(G5Context * c)
   c->d_nbr_rel = c->d_out_normal = c->d_out_border = nullptr;
   c->d_reflux_buf = c->d_defer_buf = c->d_dt = c->d_invdt = nullptr;
   c->d_step = nullptr;
+  c->d_urk = nullptr;
   drop_graphs(c);
   c->has_mesh = false;
   c->bytes = c->d_status ? (int64_t)sizeof(unsigned int) : 0;
@@ -173,7 +175,7 @@ g5_create(const G5Params * params, G5Context ** out_ctx)
     return G5_ERR_ARG;
   if (!g5::step_supported(params->dim, params->bsize))
     return G5_ERR_UNSUPPORTED;
-  if (params->integrator != 0 && params->integrator != 1)
+  if (params->integrator < 0 || params->integrator > 2)
     return G5_ERR_UNSUPPORTED;
   if (params->source_term != 0 || params->prolongation != 0)
     return G5_ERR_UNSUPPORTED;
@@ -358,6 +360,8 @@ g5_set_mesh(G5Context * c, const G5Mesh * m)
   rc |= dev_alloc(c, &c->d_dt, (size_t)n_inst);
   rc |= dev_alloc(c, &c->d_invdt, (size_t)n_inst);
   rc |= dev_alloc(c, &c->d_step, 1);
+  if (c->prm.integrator == 2)
+    rc |= dev_alloc(c, &c->d_urk, (size_t)n_total * c->nv * (dim == 2 ? c->b * c->b : c->b * c->b * c->b));
   if (rc)
   {
     free_mesh(c);
@@ -447,6 +451,35 @@ loop_step(G5Context * c, const double * U, double * U2, int mode, double * dt_ou
   if (g5::launch_dt_update(c->d_invdt, c->d_dt, dt_out, c->n_inst, c->phys.cfl, s) != cudaSuccess)
     return G5_ERR_CUDA;
   ++*launches;
+  if (c->prm.integrator == 2)
+  {
+    // RK2_SSP (SolverGodunovFiveEq.cpp:496-524): U_RK = step(U); fill;
+    // U2 = step(U_RK); U2 = 0.5 U + 0.5 U2 (with the CFL rate of the result)
+    int rc = do_step(c, U, c->d_urk, c->d_dt, mode, nullptr, s);
+    if (rc)
+      return rc;
+    *launches += c->last_launches;
+    if (c->n_outside > 0)
+    {
+      if (g5::launch_fill_outside(c->dim, c->b, c->d_urk, dev_mesh(c), c->phys, s) != cudaSuccess)
+        return G5_ERR_CUDA;
+      ++*launches;
+    }
+    rc = do_step(c, c->d_urk, U2, c->d_dt, mode, nullptr, s);
+    if (rc)
+      return rc;
+    *launches += c->last_launches;
+    if (g5::launch_rk2_combine(c->dim, c->b, mode == G5_MODE_MIXED, U, U2, dev_mesh(c), c->phys, c->d_invdt, s) != cudaSuccess)
+      return G5_ERR_CUDA;
+    ++*launches;
+    if (c->n_outside > 0)
+    {
+      if (g5::launch_fill_outside(c->dim, c->b, U2, dev_mesh(c), c->phys, s) != cudaSuccess)
+        return G5_ERR_CUDA;
+      ++*launches;
+    }
+    return G5_OK;
+  }
   int rc = do_step(c, U, U2, c->d_dt, mode, c->d_invdt, s);
   if (rc)
     return rc;

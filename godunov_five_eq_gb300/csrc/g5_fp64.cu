@@ -201,6 +201,34 @@ launch_inv_dt(int dim, int b, const double * U, const DevMesh & m, const PhysPar
   return cudaErrorInvalidValue;
 }
 
+template <int DIM, int B>
+static cudaError_t
+rk2_t(const double * U, double * U2, const DevMesh & m, const PhysParams & p, double * invdt, cudaStream_t s)
+{
+  if (m.n_owned == 0)
+    return cudaSuccess;
+  int grid = num_sms() * 8;
+  if (grid > m.n_owned)
+    grid = m.n_owned;
+  rk2_combine_kernel<DIM, B, false><<<grid, 256, 0, s>>>(U, U2, m, p, invdt);
+  return cudaGetLastError();
+}
+
+cudaError_t
+launch_rk2_combine(int dim, int b, bool mixed, const double * U, double * U2, const DevMesh & m, const PhysParams & p, double * invdt,
+                   cudaStream_t s)
+{
+  if (mixed)
+    return launch_rk2_combine_mixed(dim, b, U, U2, m, p, invdt, s);
+  if (dim == 2 && b == 16)
+    return rk2_t<2, 16>(U, U2, m, p, invdt, s);
+  if (dim == 2 && b == 8)
+    return rk2_t<2, 8>(U, U2, m, p, invdt, s);
+  if (dim == 3 && b == 8)
+    return rk2_t<3, 8>(U, U2, m, p, invdt, s);
+  return cudaErrorInvalidValue;
+}
+
 cudaError_t
 launch_dt_update(double * invdt, double * dt, double * dt_hist, int n_inst, double cfl, cudaStream_t s)
 {

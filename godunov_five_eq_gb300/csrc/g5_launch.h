@@ -21,6 +21,10 @@ int step_max_ctas_per_sm_mixed(int dim, int b);
 
 cudaError_t launch_fill_outside(int dim, int b, double * U, const DevMesh & m, const PhysParams & p, cudaStream_t s);
 cudaError_t launch_inv_dt(int dim, int b, const double * U, const DevMesh & m, const PhysParams & p, double * invdt, cudaStream_t s);
+cudaError_t launch_rk2_combine(int dim, int b, bool mixed, const double * U, double * U2, const DevMesh & m, const PhysParams & p,
+                               double * invdt, cudaStream_t s);
+cudaError_t launch_rk2_combine_mixed(int dim, int b, const double * U, double * U2, const DevMesh & m, const PhysParams & p,
+                                     double * invdt, cudaStream_t s);
 cudaError_t launch_dt_update(double * invdt, double * dt, double * dt_hist, int n_inst, double cfl, cudaStream_t s);
 cudaError_t launch_refine_flags(int dim, int b, const double * U, const DevMesh & m, int indicator, double er, double ec,
                                 double el, int lmin, int lmax, int8_t * flags, cudaStream_t s);

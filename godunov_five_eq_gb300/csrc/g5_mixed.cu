@@ -1,5 +1,6 @@
 // g5_mixed.cu — FP32-bulk instantiations (fast FP32 math; FP64 kept for the
 // pressure numerator, the accumulation into U2, the renormalisation and dt).
+#include "g5_aux.cuh"
 #include "g5_launch.h"
 #include "g5_step2d.cuh"
 #include "g5_step3d.cuh"
@@ -106,6 +107,32 @@ launch_step3d_m(const StepArgs & a, int ctas_per_sm, cudaStream_t s, int * launc
     e = cudaGetLastError();
   }
   return e;
+}
+
+template <int DIM, int B>
+static cudaError_t
+rk2_m(const double * U, double * U2, const DevMesh & m, const PhysParams & p, double * invdt, cudaStream_t s)
+{
+  if (m.n_owned == 0)
+    return cudaSuccess;
+  int grid = num_sms_m() * 8;
+  if (grid > m.n_owned)
+    grid = m.n_owned;
+  rk2_combine_kernel<DIM, B, true><<<grid, 256, 0, s>>>(U, U2, m, p, invdt);
+  return cudaGetLastError();
+}
+
+cudaError_t
+launch_rk2_combine_mixed(int dim, int b, const double * U, double * U2, const DevMesh & m, const PhysParams & p, double * invdt,
+                         cudaStream_t s)
+{
+  if (dim == 2 && b == 16)
+    return rk2_m<2, 16>(U, U2, m, p, invdt, s);
+  if (dim == 2 && b == 8)
+    return rk2_m<2, 8>(U, U2, m, p, invdt, s);
+  if (dim == 3 && b == 8)
+    return rk2_m<3, 8>(U, U2, m, p, invdt, s);
+  return cudaErrorInvalidValue;
 }
 
 cudaError_t

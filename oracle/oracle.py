@@ -186,14 +186,27 @@ class Oracle:
         return flags
 
     def run(self, U: np.ndarray, nsteps: int, fill_first: bool = True):
-        """Solver loop of SolverGodunovFiveEq (HANCOCK/RK1): fill outside, dt, step."""
+        """Solver loop of SolverGodunovFiveEq::godunov_unsplit (SolverGodunovFiveEq.cpp:480-526).
+
+        HANCOCK / RK1: fill outside, dt, one step.  RK2_SSP (integrator 2): two
+        steps without the Hancock predictor and U^{n+1} = 0.5 U^n + 0.5 U2 on
+        the owned blocks (the external LinearCombination with the standard
+        SSP-RK2 coefficients; its stage-1 combination is the identity)."""
         U = U.copy()
+        n = self.table.n_owned
         dts = []
         for _ in range(nsteps):
             self.fill_outside(U)
             dt = self.dt(U)
             dts.append(dt)
-            U = self.step(U, dt)
+            if self.params.integrator == 2:
+                R = self.step(U, dt)
+                self.fill_outside(R)
+                U2 = self.step(R, dt)
+                U2[:n] = 0.5 * U[:n] + 0.5 * U2[:n]
+                U = U2
+            else:
+                U = self.step(U, dt)
         self.fill_outside(U)
         return U, np.array(dts)
 

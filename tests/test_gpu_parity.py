@@ -169,3 +169,29 @@ def test_bad_mesh_rejected():
     t.nbr[0, 0, 0] = t.n_total + 5
     with pytest.raises(G5Error):
         GodunovImplemGB300(p, t)
+
+
+@pytest.mark.parametrize("thinc", [0, 1])
+def test_rk2_ssp_run_fp64_exact_and_mixed(thinc):
+    """RK2_SSP solver loop (two stages + 0.5 U + 0.5 U2) against the oracle's loop."""
+    mesh, t = amr_mesh(dim=2, b=8, nref=4, seed=2, periodic=False)
+    p = water_air_params(t, bc=(2, 2, 3, 3, 1, 1), thinc=thinc, integrator=2)
+    U = smooth_state(mesh, t, p, seed=1)
+    nsteps = 5
+    o = Oracle(t, p)
+    ref, dts = o.run(U, nsteps)
+    impl = GodunovImplemGB300(p, t)
+    hist = torch.zeros(nsteps, dtype=torch.float64, device="cuda")
+    d_U = torch.from_numpy(U.copy()).cuda()
+    d_U2 = torch.zeros_like(d_U)
+    impl.run(d_U, d_U2, nsteps, mode="fp64", dt_hist=hist)
+    torch.cuda.synchronize()
+    assert np.array_equal(hist.cpu().numpy(), dts.reshape(-1))
+    assert np.array_equal(d_U.cpu().numpy()[: t.n_owned], ref[: t.n_owned])
+    d_U = torch.from_numpy(U.copy()).cuda()
+    impl.run(d_U, d_U2, nsteps, mode="mixed")
+    torch.cuda.synchronize()
+    from godunov_five_eq_gb300.metrics import l1_relative
+
+    assert l1_relative(t, d_U.cpu().numpy(), ref).max() <= L1_TOL_MIXED
+    assert impl.status() == 0
