@@ -153,13 +153,27 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def ncu_traffic(workload, mode):
-    """Per-launch DRAM bytes of the step kernel from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", f"ncu_step2d_{workload}.md")
+# committed ncu summary of each workload's step kernel, and the cells of the captured case
+PROFILE_OF = {
+    "shock_bubble": ("ncu_step2d_shock_bubble.md", 431104),
+    "droplets32": ("ncu_step2d_droplets32.md", 2244608),
+    "droplets": ("ncu_step2d_droplets32.md", 2244608),
+    "triple_point_3d": ("ncu_step3d_triple_point.md", 1720320),
+    "triple_point_3d_small": ("ncu_step3d_triple_point.md", 1720320),
+}
+
+
+def ncu_traffic(workload, mode, cells):
+    """Per-launch DRAM bytes of the step kernel from the committed ncu summary,
+    scaled by cells when the capture was a smaller case of the same kernel."""
+    if workload not in PROFILE_OF:
+        return None
+    name, captured = PROFILE_OF[workload]
+    path = os.path.join(ROOT, "profiles", name)
     if not os.path.exists(path):
         return None
     m = re.search(rf"traffic_bytes_per_launch_{mode}:\s*([0-9.eE+]+)", open(path).read())
-    return float(m.group(1)) if m else None
+    return float(m.group(1)) * cells / captured if m else None
 
 
 def cpu_baseline(t, p, U, max_seconds=20.0):
@@ -416,7 +430,7 @@ def main():
         "peak": peak,
         "unit": "GB/s",
         "frac": achieved / peak,
-        "traffic": ncu_traffic(args.workload, "mixed"),
+        "traffic": ncu_traffic(args.workload, "mixed", cells),
         "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback 6.8 TB/s",
         "kernel": "step2d_kernel<16,mixed> (+reflux2d)" if t.dim == 2 else "step3d_kernel<mixed> (+reflux3d)",
         "kernel_ms": res["mixed"]["kern_ms"],

@@ -177,7 +177,7 @@ g5_create(const G5Params * params, G5Context ** out_ctx)
     return G5_ERR_UNSUPPORTED;
   if (params->integrator < 0 || params->integrator > 2)
     return G5_ERR_UNSUPPORTED;
-  if (params->source_term != 0 || params->prolongation != 0)
+  if ((params->source_term != 0 && params->source_term != 1) || params->prolongation != 0)
     return G5_ERR_UNSUPPORTED;
   for (int k = 0; k < 2; ++k)
     if (!(params->gamma[k] > 1.0))
@@ -207,6 +207,7 @@ g5_create(const G5Params * params, G5Context ** out_ctx)
   p.thinc_eps = params->thinc_eps;
   p.integrator = params->integrator;
   p.thinc = params->thinc;
+  p.source_term = params->source_term;
   for (int f = 0; f < 6; ++f)
     p.bc[f] = params->bc[f];
   for (int l = 0; l < 32; ++l)

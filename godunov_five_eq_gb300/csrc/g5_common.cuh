@@ -22,8 +22,9 @@ struct PhysParams
   double xi[2];  // 1/(gamma_k - 1)
   double gpx[2]; // gamma_k pinf_k xi_k
   double cfl, thinc_beta, thinc_eps;
-  int    integrator; // 0 HANCOCK, 1 RK1
-  int    thinc;      // 0 MUSCL, 1 THINC
+  int    integrator;  // 0 HANCOCK, 1 RK1, 2 RK2_SSP
+  int    thinc;       // 0 MUSCL, 1 THINC
+  int    source_term; // 0 ALLAIRE_KOKH, 1 MILLER_PUCKETT
   int    bc[6];
   double level_dx[32];
   // FP32 copies for the FP32-bulk path (converted once on the host)
@@ -176,6 +177,42 @@ prim_fp64(const double * u, double * q, const PhysParams & P)
     q[H::QW] = uz;
   q[H::QA] = a0;
   return sound_speed_d(P, d, p, a0, 1.0 - a0);
+}
+
+// Volume-fraction source-term factors st_k of get_source_term_factor
+// (ReadFluxesAndConservativeUpdateFunctor.h:412-443): 1 for ALLAIRE_KOKH;
+// MILLER_PUCKETT: 1 - Kbar / K_k with K_k = gamma_k (p + pinf_k) and
+// 1/Kbar = a0/K0 + a1/K1 (stiffened gas, restated), p from
+// compute_mixture_pressure (models/utils.h:160-185).  FP64, reference order.
+template <int DIM>
+__device__ __forceinline__ void
+source_factors_fp64(const double * u, const PhysParams & P, double & st0, double & st1)
+{
+  using H = V<DIM>;
+  if (P.source_term != 1)
+  {
+    st0 = st1 = 1.0;
+    return;
+  }
+  const double d = fmax(u[H::IAD0] + u[H::IAD1], P.smallr);
+  const double dd = fmax(u[H::ID], P.smallr);
+  const double ux = u[H::IU] / dd, uy = u[H::IV] / dd;
+  double       ekin;
+  if constexpr (DIM == 2)
+    ekin = 0.5 * (ux * ux + uy * uy);
+  else
+  {
+    const double uz = u[H::IW] / dd;
+    ekin = 0.5 * (ux * ux + uy * uy + uz * uz);
+  }
+  const double eint = u[H::IE] / d - ekin;
+  const double a0 = u[H::IA0];
+  const double p = (d * eint - eosPI(P, a0, 1 - a0)) / eosS(P, a0, 1 - a0);
+  const double K0 = P.gamma[0] * (p + P.pinf[0]);
+  const double K1 = P.gamma[1] * (p + P.pinf[1]);
+  const double kbar = 1.0 / (u[H::IA0] / K0 + u[H::IA1] / K1);
+  st0 = 1.0 - kbar / K0;
+  st1 = 1.0 - kbar / K1;
 }
 
 // scheme/ComputeLimitedSlopesFunctor.cpp:116-137
@@ -571,6 +608,26 @@ pressure_mixed(const double * u, const PhysParams & P, bool stiff, float & d, fl
   const float S = fmaf(a0f, P.f_dxi, P.f_xi[1]);
   return __fdividef(num, S);
 }
+// FP32 form of the source-term factors (see source_factors_fp64)
+template <int DIM>
+__device__ __forceinline__ void
+source_factors_mixed(const double * u, const PhysParams & P, bool stiff, float & st0, float & st1)
+{
+  using H = V<DIM>;
+  if (P.source_term != 1)
+  {
+    st0 = st1 = 1.0f;
+    return;
+  }
+  float       d, ux, uy, uz, a0f;
+  const float p = pressure_mixed<DIM>(u, P, stiff, d, ux, uy, uz, a0f);
+  const float K0 = (float)P.gamma[0] * (p + (float)P.pinf[0]);
+  const float K1 = (float)P.gamma[1] * (p + (float)P.pinf[1]);
+  const float kbar = __frcp_rn(a0f * __frcp_rn(K0) + d2f_fast(u[H::IA1]) * __frcp_rn(K1));
+  st0 = 1.0f - kbar * __frcp_rn(K0);
+  st1 = 1.0f - kbar * __frcp_rn(K1);
+}
+
 // FP32-bulk conservative -> primitive (computePrimitives, models/utils.h:200-250)
 template <int DIM>
 __device__ __forceinline__ void

@@ -55,7 +55,7 @@ launch_step2d(const StepArgs & a, int ctas_per_sm, cudaStream_t s, int * launche
   if (a.m.n_defer > 0)
   {
     const int n = a.m.n_defer * B;
-    reflux2d_kernel<B, false><<<(n + 127) / 128, 128, 0, s>>>(a);
+    reflux2d_kernel<B, false><<<(n + 31) / 32, 32, 0, s>>>(a);
     ++*launches;
     e = cudaGetLastError();
   }
@@ -104,7 +104,7 @@ launch_step3d(const StepArgs & a, int ctas_per_sm, cudaStream_t s, int * launche
   if (a.m.n_defer > 0)
   {
     const int n = a.m.n_defer * 64;
-    reflux3d_kernel<MIXED><<<(n + 127) / 128, 128, 0, s>>>(a);
+    reflux3d_kernel<MIXED><<<(n + 31) / 32, 32, 0, s>>>(a);
     ++*launches;
     e = cudaGetLastError();
   }

@@ -54,7 +54,7 @@ launch_step2d_m(const StepArgs & a, int ctas_per_sm, cudaStream_t s, int * launc
   if (a.m.n_defer > 0)
   {
     const int n = a.m.n_defer * B;
-    reflux2d_kernel<B, true><<<(n + 127) / 128, 128, 0, s>>>(a);
+    reflux2d_kernel<B, true><<<(n + 31) / 32, 32, 0, s>>>(a);
     ++*launches;
     e = cudaGetLastError();
   }
@@ -102,7 +102,7 @@ launch_step3d_m(const StepArgs & a, int ctas_per_sm, cudaStream_t s, int * launc
   if (a.m.n_defer > 0)
   {
     const int n = a.m.n_defer * 64;
-    reflux3d_kernel<true><<<(n + 127) / 128, 128, 0, s>>>(a);
+    reflux3d_kernel<true><<<(n + 31) / 32, 32, 0, s>>>(a);
     ++*launches;
     e = cudaGetLastError();
   }

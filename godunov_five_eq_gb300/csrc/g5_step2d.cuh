@@ -279,6 +279,8 @@ update_fp64(const double * uin, double * u2, const double * sFx, const double * 
   for (int v = 0; v < H::NV; ++v)
     u2[v] = uin[v];
   const double a0n = uin[H::IA0], a1n = uin[H::IA1];
+  double       st0, st1;
+  source_factors_fp64<2>(uin, P, st0, st1);
 #pragma unroll
   for (int dir = 0; dir < 2; ++dir)
   {
@@ -290,14 +292,14 @@ update_fp64(const double * uin, double * u2, const double * sFx, const double * 
     for (int k = 0; k < 7; ++k)
       acc[k] = 0.0 + F[k * NFF + il];
     const double usl = F[7 * NFF + il];
-    acc[H::FA0] -= usl * a0n;
-    acc[H::FA1] -= usl * a1n;
+    acc[H::FA0] -= st0 * usl * a0n;
+    acc[H::FA1] -= st1 * usl * a1n;
 #pragma unroll
     for (int k = 0; k < 7; ++k)
       acc[k] = acc[k] - F[k * NFF + ir];
     const double usr = F[7 * NFF + ir];
-    acc[H::FA0] += usr * a0n;
-    acc[H::FA1] += usr * a1n;
+    acc[H::FA0] += st0 * usr * a0n;
+    acc[H::FA1] += st1 * usr * a1n;
     const double eps = 1e-12;
     u2[H::IAD0] += acc[H::FR0];
     if (u2[H::IAD0] < eps)
@@ -348,7 +350,13 @@ update_mixed(const double * uin, double * u2, const float * sFx, const float * s
 #pragma unroll
   for (int v = 0; v < H::NV; ++v)
     u2[v] = uin[v];
-  const float  a0f = d2f_fast(uin[H::IA0]), a1f = d2f_fast(uin[H::IA1]);
+  float        a0f = d2f_fast(uin[H::IA0]), a1f = d2f_fast(uin[H::IA1]);
+  {
+    float st0, st1;
+    source_factors_mixed<2>(uin, P, stiff, st0, st1);
+    a0f *= st0;
+    a1f *= st1;
+  }
   const double eps = 1e-12, one_m_eps = 1.0 - 1e-12;
   const int    ilx = ci + (B + 1) * cj, irx = ilx + 1;
   const int    ily = ci + B * cj, iry = ily + B;
@@ -405,7 +413,7 @@ update_mixed(const double * uin, double * u2, const float * sFx, const float * s
   for (int k = 0; k < 2; ++k)
   {
     const int   iv = k == 0 ? H::IA0 : H::IA1;
-    const float af = k == 0 ? a0f : a1f;
+    const float af = d2f_fast(uin[iv]);
     const float m = 2.0f * fabsf(dA[0][k]) + 2e-12f;
     if (af > m && af + m < 1.0f)
     {
@@ -764,6 +772,8 @@ reflux2d_kernel(StepArgs a)
   const int    ins = a.m.inst ? a.m.inst[n] : 0;
   const double dx = a.p.level_dx[a.m.level[n]];
   const double a0n = uin[H::IA0], a1n = uin[H::IA1];
+  double       st0, st1;
+  source_factors_fp64<2>(uin, a.p, st0, st1);
   for (int dir = 0; dir < 2; ++dir)
   {
     const int cd = dir == 0 ? ci : cj;
@@ -807,13 +817,13 @@ reflux2d_kernel(StepArgs a)
         const double us = fv[7];
         if (side == 0)
         {
-          acc[H::FA0] -= us * a0n / 4.0;
-          acc[H::FA1] -= us * a1n / 4.0;
+          acc[H::FA0] -= st0 * us * a0n / 4.0;
+          acc[H::FA1] -= st1 * us * a1n / 4.0;
         }
         else
         {
-          acc[H::FA0] += us * a0n / 4.0;
-          acc[H::FA1] += us * a1n / 4.0;
+          acc[H::FA0] += st0 * us * a0n / 4.0;
+          acc[H::FA1] += st1 * us * a1n / 4.0;
         }
       }
       else
@@ -824,13 +834,13 @@ reflux2d_kernel(StepArgs a)
         const double us = fr[7];
         if (side == 0)
         {
-          acc[H::FA0] -= us * a0n;
-          acc[H::FA1] -= us * a1n;
+          acc[H::FA0] -= st0 * us * a0n;
+          acc[H::FA1] -= st1 * us * a1n;
         }
         else
         {
-          acc[H::FA0] += us * a0n;
-          acc[H::FA1] += us * a1n;
+          acc[H::FA0] += st0 * us * a0n;
+          acc[H::FA1] += st1 * us * a1n;
         }
       }
     }
@@ -872,9 +882,20 @@ reflux2d_kernel(StepArgs a)
     raise_status(a.status, STATUS_NONPHYSICAL);
   if (a.invdt)
   {
-    double       q[6];
-    const double c = prim_fp64<2>(u2, q, a.p);
-    atomic_max_pos(a.invdt + ins, (c + fabs(q[V<2>::QU])) / dx + (c + fabs(q[V<2>::QV])) / dx);
+    if constexpr (MIXED)
+    {
+      float       df, ux, uy, uz, a0;
+      const bool  stiff = a.p.gpx[0] != 0.0 || a.p.gpx[1] != 0.0;
+      const float p = pressure_mixed<2>(u2, a.p, stiff, df, ux, uy, uz, a0);
+      const float c = sound_speed_f(a.p.f_xi[0], a.p.f_xi[1], a.p.f_gpx[0], a.p.f_gpx[1], df, p, fmaxf(0.0f, fminf(1.0f, a0)));
+      atomic_max_pos(a.invdt + ins, (double)(((c + fabsf(ux)) + (c + fabsf(uy))) * __frcp_rn(d2f_fast(dx))));
+    }
+    else
+    {
+      double       q[6];
+      const double c = prim_fp64<2>(u2, q, a.p);
+      atomic_max_pos(a.invdt + ins, (c + fabs(q[V<2>::QU])) / dx + (c + fabs(q[V<2>::QV])) / dx);
+    }
   }
 }
 

@@ -424,6 +424,13 @@ step3d_kernel(StepArgs a)
         deferred = deferred || (dsl[f] >= 0 && cc[f >> 1] == ((f & 1) ? B - 1 : 0));
     }
 
+    // volume-fraction source-term factors of the owned cell
+    double st0 = 1.0, st1 = 1.0;
+    float  fst0 = 1.0f, fst1 = 1.0f;
+    if constexpr (MIXED)
+      source_factors_mixed<3>(uin, P, stiff, fst0, fst1);
+    else
+      source_factors_fp64<3>(uin, P, st0, st1);
     // running state of the owned cell
     double u2[H::NV];
 #pragma unroll
@@ -548,19 +555,19 @@ step3d_kernel(StepArgs a)
         for (int k = 0; k < 8; ++k)
           acc[k] = 0.0 + sF[k * NFF + il];
         const double usl = sF[H::FUS * NFF + il];
-        acc[H::FA0] -= usl * a0n;
-        acc[H::FA1] -= usl * a1n;
+        acc[H::FA0] -= st0 * usl * a0n;
+        acc[H::FA1] -= st1 * usl * a1n;
 #pragma unroll
         for (int k = 0; k < 8; ++k)
           acc[k] = acc[k] - sF[k * NFF + ir];
         const double usr = sF[H::FUS * NFF + ir];
-        acc[H::FA0] += usr * a0n;
-        acc[H::FA1] += usr * a1n;
+        acc[H::FA0] += st0 * usr * a0n;
+        acc[H::FA1] += st1 * usr * a1n;
         apply_dir_fp64(u2, acc);
       }
       else
       {
-        const float a0f = d2f_fast(uin[H::IA0]), a1f = d2f_fast(uin[H::IA1]);
+        const float a0f = d2f_fast(uin[H::IA0]) * fst0, a1f = d2f_fast(uin[H::IA1]) * fst1;
         two_diff(sF[H::FR0 * NFF + il], sF[H::FR0 * NFF + ir], hh[dir][0], ll[dir][0]);
         two_diff(sF[H::FR1 * NFF + il], sF[H::FR1 * NFF + ir], hh[dir][1], ll[dir][1]);
         const int ke[4] = { H::FE, H::FU, H::FV, H::FW };
@@ -755,6 +762,8 @@ reflux3d_kernel(StepArgs a)
   const int    ins = a.m.inst ? a.m.inst[n] : 0;
   const double dx = a.p.level_dx[a.m.level[n]];
   const double a0n = uin[H::IA0], a1n = uin[H::IA1];
+  double       st0, st1;
+  source_factors_fp64<3>(uin, a.p, st0, st1);
   for (int dir = 0; dir < 3; ++dir)
   {
     const int e1 = dir == 0 ? 1 : 0, e2 = dir == 2 ? 1 : 2;
@@ -801,13 +810,13 @@ reflux3d_kernel(StepArgs a)
         const double us = fv[8];
         if (side == 0)
         {
-          acc[H::FA0] -= us * a0n / 8.0;
-          acc[H::FA1] -= us * a1n / 8.0;
+          acc[H::FA0] -= st0 * us * a0n / 8.0;
+          acc[H::FA1] -= st1 * us * a1n / 8.0;
         }
         else
         {
-          acc[H::FA0] += us * a0n / 8.0;
-          acc[H::FA1] += us * a1n / 8.0;
+          acc[H::FA0] += st0 * us * a0n / 8.0;
+          acc[H::FA1] += st1 * us * a1n / 8.0;
         }
       }
       else
@@ -818,13 +827,13 @@ reflux3d_kernel(StepArgs a)
         const double us = fr[8];
         if (side == 0)
         {
-          acc[H::FA0] -= us * a0n;
-          acc[H::FA1] -= us * a1n;
+          acc[H::FA0] -= st0 * us * a0n;
+          acc[H::FA1] -= st1 * us * a1n;
         }
         else
         {
-          acc[H::FA0] += us * a0n;
-          acc[H::FA1] += us * a1n;
+          acc[H::FA0] += st0 * us * a0n;
+          acc[H::FA1] += st1 * us * a1n;
         }
       }
     }
@@ -847,9 +856,20 @@ reflux3d_kernel(StepArgs a)
     raise_status(a.status, STATUS_NONPHYSICAL);
   if (a.invdt)
   {
-    double       q[7];
-    const double c = prim_fp64<3>(u2, q, a.p);
-    atomic_max_pos(a.invdt + ins, (c + fabs(q[H::QU])) / dx + (c + fabs(q[H::QV])) / dx + (c + fabs(q[H::QW])) / dx);
+    if constexpr (MIXED)
+    {
+      float       df, ux, uy, uz, a0;
+      const bool  stiff = a.p.gpx[0] != 0.0 || a.p.gpx[1] != 0.0;
+      const float p = pressure_mixed<3>(u2, a.p, stiff, df, ux, uy, uz, a0);
+      const float c = sound_speed_f(a.p.f_xi[0], a.p.f_xi[1], a.p.f_gpx[0], a.p.f_gpx[1], df, p, fmaxf(0.0f, fminf(1.0f, a0)));
+      atomic_max_pos(a.invdt + ins, (double)((((c + fabsf(ux)) + (c + fabsf(uy))) + (c + fabsf(uz))) * __frcp_rn(d2f_fast(dx))));
+    }
+    else
+    {
+      double       q[7];
+      const double c = prim_fp64<3>(u2, q, a.p);
+      atomic_max_pos(a.invdt + ins, (c + fabs(q[H::QU])) / dx + (c + fabs(q[H::QV])) / dx + (c + fabs(q[H::QW])) / dx);
+    }
   }
 }
 

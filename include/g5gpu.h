@@ -66,7 +66,7 @@ typedef struct G5Params
   int32_t bsize;        /* cells per block edge: 2D 8 or 16, 3D 8 */
   int32_t integrator;   /* 0 HANCOCK, 1 RK1, 2 RK2_SSP (two stages in g5_advance / g5_run) */
   int32_t thinc;        /* 0 MUSCL, 1 THINC interface reconstruction */
-  int32_t source_term;  /* 0 ALLAIRE_KOKH (only value implemented on the GPU) */
+  int32_t source_term;  /* 0 ALLAIRE_KOKH, 1 MILLER_PUCKETT */
   int32_t prolongation; /* 0 SIMPLE_COPY (only value implemented) */
   int32_t bc[6];        /* xmin xmax ymin ymax zmin zmax */
   double  gamma[2];

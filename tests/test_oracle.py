@@ -22,10 +22,10 @@ def _totals(table, U, names):
 
 
 @pytest.mark.parametrize("dim", [2, 3])
-@pytest.mark.parametrize("thinc", [0, 1])
-def test_uniform_state_preserved(dim, thinc):
+@pytest.mark.parametrize("thinc,source_term", [(0, 0), (1, 0), (0, 1)])
+def test_uniform_state_preserved(dim, thinc, source_term):
     mesh, t = amr_mesh(dim=dim, b=4 if dim == 3 else 8, nref=2)
-    p = water_air_params(t, dim=dim, b=t.bsize, thinc=thinc)
+    p = water_air_params(t, dim=dim, b=t.bsize, thinc=thinc, source_term=source_term)
     vel = (10.0, -3.0) if dim == 2 else (10.0, -3.0, 2.0)
     U = np.zeros((t.n_total, t.nv, t.ncell))
     U[: t.n_owned] = np.moveaxis(configs.prim_to_cons(dim, p, np.full((t.n_owned, t.ncell), 0.3), 300.0, 0.7, 1e5, vel), 0, 1)
