@@ -474,9 +474,10 @@ update_mixed(const double * uin, double * u2, const float * sFx, const float * s
 }
 
 // 4 CTAs per SM in the FP32-bulk form (64 registers), so that CTAs in the
-// FP64-heavy update overlap with CTAs in the FP32 face phase
+// FP64-heavy update overlap with CTAs in the FP32 face phase; 2 CTAs per SM
+// (128 registers) in the FP64 form
 template <int B, bool MIXED>
-__global__ void __launch_bounds__(B * B, MIXED ? (B == 16 ? 4 : 8) : 1)
+__global__ void __launch_bounds__(B * B, MIXED ? (B == 16 ? 4 : 8) : (B == 16 ? 2 : 8))
 step2d_kernel(StepArgs a)
 {
   using T = Step2DTraits<B, MIXED>;
