@@ -17,8 +17,9 @@
  * Every call returns 0 on success or a negative G5_ERR_* code.  Nothing
  * traps or asserts on the device: device-side problems raise bits in a
  * status word read by g5_status.  Calls are asynchronous on the stream
- * given; g5_step, g5_step_dev, g5_fill_outside and g5_compute_inv_dt
- * neither allocate nor synchronise, so they may be captured in a CUDA graph.
+ * given; g5_step_dev, g5_fill_outside, g5_compute_inv_dt and g5_advance
+ * neither allocate nor synchronise, so they may be captured in a CUDA graph
+ * (g5_step copies dt from host memory first: capture g5_step_dev instead).
  */
 #ifndef G5GPU_H_
 #define G5GPU_H_
