@@ -151,16 +151,20 @@ def _shock_bubble_prim(params, xc, dxf, bubble_gamma_rho, mach=1.22):
     return a0, ar0, ar1, p, u
 
 
-def shock_bubble(bubble="helium", thinc=False, level_min=4, level_max=6, bsize=16, flag_fn=None, slope_type=1.0):
+def shock_bubble(bubble="helium", thinc=False, level_min=4, level_max=6, bsize=16, flag_fn=None, slope_type=1.0, initial_level=None):
     """Mach 1.22 shock in air hitting a helium (or R22) bubble; domain [0,4]x[0,1].
 
     The mesh is refined from ``level_min`` by the refine flags evaluated on the
     initial condition (``flag_fn(table, params, U, level_min, level_max) -> int8
     flags``; SIMPLE_GRADIENT on alpha_rho_k, eps_refine 0.1, eps_coarsen
     0.0125), level by level, with 2:1 balance; the mesh then stays fixed.
+    ``initial_level`` (optional) first refines the whole domain uniformly to
+    that level (a mesh that a dynamic AMR cycle then coarsens and refines).
     """
     gb = {"helium": (1.648, 0.138), "r22": (1.249, 3.1538)}[bubble]
     mesh = BlockMesh(2, bsize, (4, 1), (False, False), level_min, level_max, scaling=1.0)
+    for _ in range(level_min, initial_level if initial_level is not None else level_min):
+        mesh.refine(list(mesh.leaves))
     params = HydroParams(
         dim=2,
         bsize=bsize,

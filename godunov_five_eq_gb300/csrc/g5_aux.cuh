@@ -322,4 +322,85 @@ refine_flags_kernel(const double * U,
   }
 }
 
+// ---------------------------------------------------------------------------
+// block remap after a mesh adaptation (SolverGodunovFiveEq::
+// map_userdata_after_adapt, SolverGodunovFiveEq.cpp:1137-1169): one CTA per new
+// owned block.  kind 0 copies an old block, kind 1 is the SIMPLE_COPY
+// prolongation of one child of an old block (every fine cell takes the parent
+// cell containing its centre), kind 2 the restriction of 2^dim old children
+// (get_conservative_vars_restriction, ConvertToPrimitivesVariablesFunctor.cpp:
+// 208-246: mean of the fine cells for IE IU IV (IW) IAD0 IAD1 IA0, summed in
+// z, y, x order, IA1 = 1 - IA0, ID = IAD0 + IAD1).  The host validated kind and
+// src, so every index read here is in range.
+// ---------------------------------------------------------------------------
+template <int DIM, int B>
+__global__ void __launch_bounds__(256)
+remap_kernel(const double * __restrict__ Uold, double * __restrict__ Unew, const int8_t * __restrict__ kind,
+             const int32_t * __restrict__ src, int n_new)
+{
+  using H = V<DIM>;
+  constexpr int NC = DIM == 2 ? B * B : B * B * B;
+  constexpr int NCH = 1 << DIM;
+  for (int j = blockIdx.x; j < n_new; j += gridDim.x)
+  {
+    const int       k = kind[j];
+    const int32_t * s = src + (size_t)j * NCH;
+    double *        out = Unew + (size_t)j * H::NV * NC;
+    if (k == 0)
+    {
+      const double2 * in2 = reinterpret_cast<const double2 *>(Uold + (size_t)s[0] * H::NV * NC);
+      double2 *       out2 = reinterpret_cast<double2 *>(out);
+      for (int t = threadIdx.x; t < H::NV * NC / 2; t += blockDim.x)
+        out2[t] = in2[t];
+      continue;
+    }
+    for (int c = threadIdx.x; c < NC; c += blockDim.x)
+    {
+      const int cc[3] = { c % B, (c / B) % B, DIM == 3 ? c / (B * B) : 0 };
+      if (k == 1)
+      {
+        const int      ch = s[1];
+        const int      px = (ch & 1) * (B / 2) + (cc[0] >> 1);
+        const int      py = ((ch >> 1) & 1) * (B / 2) + (cc[1] >> 1);
+        const int      pz = DIM == 3 ? ((ch >> 2) & 1) * (B / 2) + (cc[2] >> 1) : 0;
+        const double * in = Uold + (size_t)s[0] * H::NV * NC + px + B * (py + B * pz);
+#pragma unroll
+        for (int v = 0; v < H::NV; ++v)
+          out[v * NC + c] = in[v * NC];
+      }
+      else
+      {
+        int ch[3] = { 0, 0, 0 }, f0[3] = { 0, 0, 0 };
+#pragma unroll
+        for (int e = 0; e < DIM; ++e)
+        {
+          const int f = 2 * cc[e];
+          ch[e] = f / B;
+          f0[e] = f - ch[e] * B;
+        }
+        const double * in = Uold + (size_t)s[ch[0] + 2 * ch[1] + 4 * ch[2]] * H::NV * NC;
+        const int      vars[7] = { H::IE, H::IU, H::IV, H::IW, H::IAD0, H::IAD1, H::IA0 };
+#pragma unroll
+        for (int t = 0; t < 7; ++t)
+        {
+          if (DIM == 2 && t == 3)
+            continue;
+          const int v = vars[t];
+          double    sum = 0.0;
+#pragma unroll
+          for (int oz = 0; oz < (DIM == 3 ? 2 : 1); ++oz)
+#pragma unroll
+            for (int oy = 0; oy < 2; ++oy)
+#pragma unroll
+              for (int ox = 0; ox < 2; ++ox)
+                sum += in[v * NC + (f0[0] + ox) + B * ((f0[1] + oy) + B * (DIM == 3 ? f0[2] + oz : 0))];
+          out[v * NC + c] = sum / (double)(1 << DIM);
+        }
+        out[H::IA1 * NC + c] = 1.0 - out[H::IA0 * NC + c];
+        out[H::ID * NC + c] = out[H::IAD0 * NC + c] + out[H::IAD1 * NC + c];
+      }
+    }
+  }
+}
+
 } // namespace g5

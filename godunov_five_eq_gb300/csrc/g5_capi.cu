@@ -443,6 +443,50 @@ g5_refine_flags(G5Context * ctx,
            : G5_ERR_CUDA;
 }
 
+extern "C" int
+g5_remap(G5Context * ctx, const G5Remap * r, const double * d_Uold, double * d_Unew, void * stream)
+{
+  if (!ctx || !r || r->n_new < 0 || r->n_old < 0 || (r->n_new > 0 && (!r->kind || !r->src || !d_Uold || !d_Unew)))
+    return G5_ERR_ARG;
+  if (r->n_new == 0)
+    return G5_OK;
+  const int nch = ctx->nch;
+  // every index the kernel reads is checked here
+  for (int j = 0; j < r->n_new; ++j)
+  {
+    const int32_t * s = r->src + (size_t)j * nch;
+    const int       k = r->kind[j];
+    if (k < 0 || k > 2)
+      return G5_ERR_MESH;
+    const int nread = k == 2 ? nch : 1;
+    for (int t = 0; t < nread; ++t)
+      if (s[t] < 0 || s[t] >= r->n_old)
+        return G5_ERR_MESH;
+    if (k == 1 && (s[1] < 0 || s[1] >= nch))
+      return G5_ERR_MESH;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  int8_t *     d_kind = nullptr;
+  int32_t *    d_src = nullptr;
+  const size_t nk = (size_t)r->n_new, ns = (size_t)r->n_new * nch * sizeof(int32_t);
+  if (cudaMallocAsync((void **)&d_kind, nk, st) != cudaSuccess)
+    return G5_ERR_CUDA;
+  if (cudaMallocAsync((void **)&d_src, ns, st) != cudaSuccess)
+  {
+    cudaFreeAsync(d_kind, st);
+    return G5_ERR_CUDA;
+  }
+  int rc = G5_OK;
+  if (cudaMemcpyAsync(d_kind, r->kind, nk, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+      cudaMemcpyAsync(d_src, r->src, ns, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+      g5::launch_remap(ctx->dim, ctx->b, d_Uold, d_Unew, d_kind, d_src, r->n_new, st) != cudaSuccess)
+    rc = G5_ERR_CUDA;
+  cudaFreeAsync(d_kind, st);
+  cudaFreeAsync(d_src, st);
+  ctx->last_launches = 1;
+  return rc;
+}
+
 namespace
 {
 // one step of the device-driven solver loop: dt <- cfl / inv_dt(U); U2 <- step(U); fill outside of U2

@@ -262,4 +262,29 @@ launch_refine_flags(int dim, int b, const double * U, const DevMesh & m, int ind
   return cudaErrorInvalidValue;
 }
 
+template <int DIM, int B>
+static cudaError_t
+remap_t(const double * Uold, double * Unew, const int8_t * kind, const int32_t * src, int n_new, cudaStream_t s)
+{
+  if (n_new == 0)
+    return cudaSuccess;
+  int grid = num_sms() * 8;
+  if (grid > n_new)
+    grid = n_new;
+  remap_kernel<DIM, B><<<grid, 256, 0, s>>>(Uold, Unew, kind, src, n_new);
+  return cudaGetLastError();
+}
+
+cudaError_t
+launch_remap(int dim, int b, const double * Uold, double * Unew, const int8_t * kind, const int32_t * src, int n_new, cudaStream_t s)
+{
+  if (dim == 2 && b == 16)
+    return remap_t<2, 16>(Uold, Unew, kind, src, n_new, s);
+  if (dim == 2 && b == 8)
+    return remap_t<2, 8>(Uold, Unew, kind, src, n_new, s);
+  if (dim == 3 && b == 8)
+    return remap_t<3, 8>(Uold, Unew, kind, src, n_new, s);
+  return cudaErrorInvalidValue;
+}
+
 } // namespace g5

@@ -28,5 +28,8 @@ cudaError_t launch_rk2_combine_mixed(int dim, int b, const double * U, double * 
 cudaError_t launch_dt_update(double * invdt, double * dt, double * dt_hist, int n_inst, double cfl, cudaStream_t s);
 cudaError_t launch_refine_flags(int dim, int b, const double * U, const DevMesh & m, int indicator, double er, double ec,
                                 double el, int lmin, int lmax, int8_t * flags, cudaStream_t s);
+// block remap after a mesh adaptation (kind/src validated by the caller)
+cudaError_t launch_remap(int dim, int b, const double * Uold, double * Unew, const int8_t * kind, const int32_t * src, int n_new,
+                         cudaStream_t s);
 
 } // namespace g5

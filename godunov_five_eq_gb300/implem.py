@@ -85,6 +85,15 @@ class G5Mesh(ctypes.Structure):
     ]
 
 
+class G5Remap(ctypes.Structure):
+    _fields_ = [
+        ("n_old", ctypes.c_int32),
+        ("n_new", ctypes.c_int32),
+        ("kind", ctypes.c_void_p),
+        ("src", ctypes.c_void_p),
+    ]
+
+
 EXPORTS = [
     "g5_version",
     "g5_create",
@@ -103,6 +112,7 @@ EXPORTS = [
     "g5_tune",
     "g5_last_launch_count",
     "g5_step_static",
+    "g5_remap",
 ]
 
 _lib = None
@@ -141,6 +151,7 @@ def load_library(build_if_missing: bool = True):
     L.g5_status.argtypes = [vp, vp]
     L.g5_tune.argtypes = [vp, vp, vp, ctypes.c_int, vp]
     L.g5_last_launch_count.argtypes = [vp]
+    L.g5_remap.argtypes = [vp, ctypes.POINTER(G5Remap), vp, vp, vp]
     L.g5_step_static.argtypes = [ctypes.POINTER(G5Params), ctypes.POINTER(G5Mesh), vp, vp, vp, ctypes.c_int, vp, vp, vp]
     _lib = L
     return L
@@ -339,6 +350,34 @@ class GodunovImplemGB300:
         if rc != 0:
             raise G5Error(rc, "g5_refine_flags")
         return flags
+
+    def remap(self, rt, U_old, U_new, stream=None):
+        """g5_remap: owned blocks of U_new (the adapted mesh) from U_old, by the
+        old -> new map `rt` (mesh.RemapTable) of one adaptation."""
+        kind = np.ascontiguousarray(rt.kind, np.int8)
+        src = np.ascontiguousarray(rt.src, np.int32)
+        r = G5Remap(int(rt.n_old), int(rt.n_new), kind.ctypes.data, src.ctypes.data)
+        rc = self.lib.g5_remap(self.ctx, ctypes.byref(r), ctypes.c_void_p(_dptr(U_old)), ctypes.c_void_p(_dptr(U_new)), _stream(stream))
+        if rc != 0:
+            raise G5Error(rc, "g5_remap")
+
+    def do_amr_cycle(self, mesh, U, indicator=0, eps_refine=0.1, eps_coarsen=0.0125, eps_lohner=0.02, stream=None):
+        """SolverGodunovFiveEq::do_amr_cycle (SolverGodunovFiveEq.cpp:258-314) on
+        one GPU: boundary fill and refine flags of U on the device, forest
+        adaptation on the host (`mesh.adapt`), remap of U to the new mesh on
+        the device, block table upload (resize_auxiliary_data) and boundary
+        fill of the new state.  Returns (new U, its block table, the remap)."""
+        import torch
+
+        self.fill_outside_quadrants(U, stream=stream)
+        flags = self.refine_flags(U, indicator, eps_refine, eps_coarsen, eps_lohner, mesh.level_min, mesh.level_max, stream=stream)
+        rt = mesh.adapt(flags.cpu().numpy())
+        table = mesh.build()
+        U_new = torch.empty((table.n_total, table.nv, table.ncell), dtype=torch.float64, device=U.device)
+        self.remap(rt, U, U_new, stream=stream)
+        self.resize_auxiliary_data(table)
+        self.fill_outside_quadrants(U_new, stream=stream)
+        return U_new, table, rt
 
     def status(self, stream=None) -> int:
         rc = self.lib.g5_status(self.ctx, _stream(stream))

@@ -82,6 +82,32 @@ class BlockTable:
         return self.n_owned * self.ncell
 
 
+REMAP_COPY, REMAP_REFINED, REMAP_COARSENED = 0, 1, 2
+
+
+@dataclass
+class RemapTable:
+    """Old -> new owned-block map of one mesh adaptation.
+
+    kind[j] = REMAP_COPY: new block j is old block src[j, 0];
+    REMAP_REFINED: new block j is child src[j, 1] (x + 2y + 4z) of old block
+    src[j, 0]; REMAP_COARSENED: new block j is the parent of the old blocks
+    src[j, 0 .. 2^dim - 1] (child order x + 2y + 4z)."""
+
+    dim: int
+    bsize: int
+    n_old: int
+    kind: np.ndarray  # int8 [n_new]
+    src: np.ndarray  # int32 [n_new, 2^dim]
+
+    @property
+    def n_new(self) -> int:
+        return int(self.kind.shape[0])
+
+    def counts(self) -> dict:
+        return {name: int((self.kind == v).sum()) for name, v in (("copied", 0), ("refined", 1), ("coarsened", 2))}
+
+
 class BlockMesh:
     """A balanced block-AMR forest on a brick of trees."""
 
@@ -180,6 +206,115 @@ class BlockMesh:
             if not marked:
                 return total
             total += self.refine(marked)
+
+    # ------------------------------------------------------------ adaptation
+    def _coarsening_breaks_balance(self, parent) -> bool:
+        """True when a leaf finer than parent level + 1 touches `parent`
+        (faces, edges or corners): some same-level position next to one of
+        its children is not covered by a leaf of that level or coarser."""
+        L = parent[0] + 1
+        lo = [2 * parent[1 + e] for e in range(self.dim)]
+        offsets = itertools.product(*[range(lo[e] - 1, lo[e] + 3) for e in range(self.dim)])
+        for c in offsets:
+            if all(lo[e] <= c[e] < lo[e] + 2 for e in range(self.dim)):
+                continue
+            cw, outside = self.wrap(L, c)
+            if any(outside):
+                continue
+            if self._covering_leaf(L, cw) is None:
+                return True
+        return False
+
+    def adapt(self, flags) -> "RemapTable":
+        """Apply per-block refine flags and return the old -> new block map.
+
+        `flags` holds one ComputeRefineFlags code per owned block of the
+        current table (ordered_leaves order): 2 refine, 0 coarsen, other
+        values keep the block (scheme/ComputeRefineFlags.cpp:250-368).  The
+        forest adaptation itself is p4est's (the reference's
+        AMRManager::rebuild_from_context, SolverGodunovFiveEq.cpp:258-314);
+        restated here as: refine every flagged block below level_max,
+        restore 2:1 balance by refining, then coarsen each complete family
+        of leaves above level_min whose 2^dim members are all flagged 0 and
+        were not refined, unless the coarse block would touch a leaf two
+        levels finer (such families are kept until none is left).  Every
+        new block therefore comes from one old block (kept or refined once)
+        or from the 2^dim old children of a family."""
+        old = self.ordered_leaves()
+        flags = np.asarray(flags).reshape(-1)
+        if flags.shape[0] != len(old):
+            raise ValueError(f"expected {len(old)} flags, got {flags.shape[0]}")
+        old_index = {k: i for i, k in enumerate(old)}
+        refined_from: dict = {}
+
+        def refine_one(k):
+            if k in refined_from:
+                raise RuntimeError("a block would be refined twice in one adaptation")
+            self.leaves.remove(k)
+            for ch in self.children(k):
+                self.leaves.add(ch)
+                refined_from[ch] = k
+
+        for k, f in zip(old, flags):
+            if f == 2 and k[0] < self.level_max:
+                refine_one(k)
+        # 2:1 balance by refinement (the same sweep as balance())
+        offsets = [o for o in itertools.product((-1, 0, 1), repeat=self.dim) if any(o)]
+        while True:
+            marked = set()
+            for key in self.leaves:
+                L = key[0]
+                if L - self.level_min < 2:
+                    continue
+                for o in offsets:
+                    c = tuple(key[1 + e] + o[e] for e in range(self.dim))
+                    cw, outside = self.wrap(L, c)
+                    if any(outside):
+                        continue
+                    leaf = self._covering_leaf(L, cw)
+                    if leaf is not None and leaf[0] < L - 1:
+                        marked.add(leaf)
+            if not marked:
+                break
+            for k in marked:
+                if k[0] < self.level_max:
+                    refine_one(k)
+        # coarsening of complete families
+        parents = set()
+        for k, f in zip(old, flags):
+            if f == 0 and k[0] > self.level_min:
+                parents.add((k[0] - 1,) + tuple(c >> 1 for c in k[1 : 1 + self.dim]) + (0,) * (3 - self.dim))
+        families = {}
+        for P in parents:
+            kids = self.children(P)
+            if all(ch in self.leaves and ch in old_index and flags[old_index[ch]] == 0 for ch in kids):
+                families[P] = kids
+        for P, kids in families.items():
+            self.leaves.difference_update(kids)
+            self.leaves.add(P)
+        while True:
+            undo = [P for P in families if self._coarsening_breaks_balance(P)]
+            if not undo:
+                break
+            for P in undo:
+                self.leaves.remove(P)
+                self.leaves.update(families.pop(P))
+        new = self.ordered_leaves()
+        nc = 2**self.dim
+        kind = np.zeros(len(new), np.int8)
+        src = np.full((len(new), nc), -1, np.int32)
+        for j, k in enumerate(new):
+            if k in old_index:
+                src[j, 0] = old_index[k]
+            elif k in refined_from:
+                P = refined_from[k]
+                kind[j] = REMAP_REFINED
+                src[j, 0] = old_index[P]
+                src[j, 1] = sum(((k[1 + e] & 1) << e) for e in range(self.dim))
+            else:
+                kind[j] = REMAP_COARSENED
+                src[j, :] = [old_index[ch] for ch in families[k]]
+        return RemapTable(dim=self.dim, bsize=self.bsize, n_old=len(old), kind=kind, src=src)
 
     # ------------------------------------------------------------------ tables
     def ordered_leaves(self):

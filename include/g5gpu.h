@@ -181,6 +181,35 @@ int g5_refine_flags(G5Context * ctx,
                     int8_t *       d_flags,
                     void *         stream);
 
+/* Block map of one mesh adaptation (host arrays), for g5_remap.  New owned
+ * block j (order of the new mesh's U) comes from the old owned blocks:
+ *   kind[j] = G5_REMAP_COPY:      old block src[j*2^dim];
+ *   kind[j] = G5_REMAP_REFINED:   child src[j*2^dim + 1] (x + 2y + 4z) of old
+ *                                 block src[j*2^dim];
+ *   kind[j] = G5_REMAP_COARSENED: parent of old blocks src[j*2^dim + c],
+ *                                 c = x + 2y + 4z the child position. */
+#define G5_REMAP_COPY 0
+#define G5_REMAP_REFINED 1
+#define G5_REMAP_COARSENED 2
+typedef struct G5Remap
+{
+  int32_t         n_old; /* owned blocks of the old mesh */
+  int32_t         n_new; /* owned blocks of the new mesh */
+  const int8_t *  kind;  /* [n_new] */
+  const int32_t * src;   /* [n_new * 2^dim] */
+} G5Remap;
+
+/* UserDataRemapper::remap_block_data as called by
+ * SolverGodunovFiveEq::map_userdata_after_adapt (SolverGodunovFiveEq.cpp:
+ * 1137-1169): the owned blocks of d_Unew from those of d_Uold.  Refined blocks
+ * take the SIMPLE_COPY prolongation of their parent, coarsened blocks the
+ * restriction of get_conservative_vars_restriction (mean of the 2^dim fine
+ * cells; IA1 = 1 - IA0, ID = IAD0 + IAD1).  Outside blocks of d_Unew are not
+ * written (g5_set_mesh with the new table, then g5_fill_outside).  The map is
+ * validated on the host (G5_ERR_MESH) and copied to stream-ordered device
+ * memory (cudaMallocAsync/cudaFreeAsync on `stream`): not capturable. */
+int g5_remap(G5Context * ctx, const G5Remap * remap, const double * d_Uold, double * d_Unew, void * stream);
+
 /* Read and clear the device status word (synchronises the stream).
  * Returns the G5_STATUS_* bits (>= 0) or a negative error. */
 int g5_status(G5Context * ctx, void * stream);

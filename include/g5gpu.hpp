@@ -222,6 +222,13 @@ public:
   //! SolverGodunovFiveEq::fill_outside_quadrants
   void fill_outside_quadrants(const g5::BlockArray & U) { g5::check(g5_fill_outside(m_ctx, U.data, m_stream), "g5_fill_outside"); }
 
+  //! SolverGodunovFiveEq::map_userdata_after_adapt (SolverGodunovFiveEq.cpp:1137-1169):
+  //! owned blocks of U_new from U_old by the old -> new block map of one adaptation
+  void remap_block_data(const G5Remap & remap, const g5::BlockArray & U_old, const g5::BlockArray & U_new)
+  {
+    g5::check(g5_remap(m_ctx, &remap, U_old.data, U_new.data, m_stream), "g5_remap");
+  }
+
   //! device status word (G5_STATUS_* bits), cleared by the read
   int status() { return g5_status(m_ctx, m_stream); }
 

@@ -1468,3 +1468,87 @@ g5o_mixture_sound_speed(const G5OParams * prm, double rho, double p, double a0)
   const Settings s = make_settings(prm);
   return mixture_sound_speed(s, rho, p, a0, 1.0 - a0);
 }
+
+/* ---------------------------------------------------------------------------
+ * Block remap after a mesh adaptation (UserDataRemapper::remap_block_data,
+ * called from SolverGodunovFiveEq::map_userdata_after_adapt,
+ * SolverGodunovFiveEq.cpp:1137-1169; the remapper is external to the
+ * reference and restated here with the reference's own ghost-cell rules):
+ *   kept block      -> copy;
+ *   refined block   -> SIMPLE_COPY prolongation: each fine cell takes the
+ *                      parent cell containing its centre (all variables);
+ *   coarsened block -> restriction of get_conservative_vars_restriction
+ *                      (scheme/ConvertToPrimitivesVariablesFunctor.cpp:208-246):
+ *                      mean of the 2^dim fine cells for IE IU IV (IW) IAD0
+ *                      IAD1 IA0 (sum in z, y, x order, then / 2^dim),
+ *                      IA1 = 1 - IA0, ID = IAD0 + IAD1.
+ * ------------------------------------------------------------------------- */
+template <int DIM>
+static int
+do_remap(int b, int n_new, const int8_t * kind, const int32_t * src, const double * Uold, double * Unew)
+{
+  using H = Ids<DIM>;
+  const Geo<DIM> geo(b);
+  const int      nc = geo.ncell();
+  const int      nch = 1 << DIM;
+#pragma omp parallel for schedule(static)
+  for (int j = 0; j < n_new; ++j)
+  {
+    const int32_t * s = src + (size_t)j * nch;
+    double *        out = Unew + (size_t)j * H::NV * nc;
+    for (int kk = 0; kk < (DIM == 3 ? b : 1); ++kk)
+      for (int jj = 0; jj < b; ++jj)
+        for (int ii = 0; ii < b; ++ii)
+        {
+          const int c = geo.cell(ii, jj, kk);
+          const int cc[3] = { ii, jj, kk };
+          if (kind[j] == 0)
+          {
+            for (int v = 0; v < H::NV; ++v)
+              out[v * nc + c] = Uold[((size_t)s[0] * H::NV + v) * nc + c];
+          }
+          else if (kind[j] == 1)
+          {
+            int pc[3] = { 0, 0, 0 };
+            for (int e = 0; e < DIM; ++e)
+              pc[e] = ((s[1] >> e) & 1) * (b / 2) + (cc[e] >> 1);
+            const int cp = geo.cell(pc[0], pc[1], pc[2]);
+            for (int v = 0; v < H::NV; ++v)
+              out[v * nc + c] = Uold[((size_t)s[0] * H::NV + v) * nc + cp];
+          }
+          else
+          {
+            int f0[3] = { 0, 0, 0 }, ch[3] = { 0, 0, 0 };
+            for (int e = 0; e < DIM; ++e)
+            {
+              const int f = 2 * cc[e];
+              ch[e] = f / b;
+              f0[e] = f - ch[e] * b;
+            }
+            const int F = s[ch[0] + 2 * ch[1] + 4 * ch[2]];
+            const int vars[7] = { H::IE, H::IU, H::IV, H::IW, H::IAD0, H::IAD1, H::IA0 };
+            for (int t = 0; t < 7; ++t)
+            {
+              if (DIM == 2 && t == 3)
+                continue;
+              const int v = vars[t];
+              double    sum = 0.0;
+              for (int oz = 0; oz < (DIM == 3 ? 2 : 1); ++oz)
+                for (int oy = 0; oy < 2; ++oy)
+                  for (int ox = 0; ox < 2; ++ox)
+                    sum += Uold[((size_t)F * H::NV + v) * nc + geo.cell(f0[0] + ox, f0[1] + oy, DIM == 3 ? f0[2] + oz : 0)];
+              out[v * nc + c] = sum / (double)(1 << DIM);
+            }
+            out[H::IA1 * nc + c] = 1.0 - out[H::IA0 * nc + c];
+            out[H::ID * nc + c] = out[H::IAD0 * nc + c] + out[H::IAD1 * nc + c];
+          }
+        }
+  }
+  return 0;
+}
+
+extern "C" int
+g5o_remap(const G5OParams * prm, int n_new, const int8_t * kind, const int32_t * src, const double * Uold, double * Unew)
+{
+  return prm->dim == 2 ? do_remap<2>(prm->b, n_new, kind, src, Uold, Unew) : do_remap<3>(prm->b, n_new, kind, src, Uold, Unew);
+}

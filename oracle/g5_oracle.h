@@ -84,6 +84,12 @@ int    g5o_refine_flags(void * ctx,
                         int            level_max,
                         int8_t *       flags);
 
+/* block remap after a mesh adaptation: new owned block j from the old owned
+ * blocks (kind 0 copy of src[j*2^dim]; 1 SIMPLE_COPY prolongation of child
+ * src[j*2^dim+1] of old block src[j*2^dim]; 2 restriction of the old children
+ * src[j*2^dim .. +2^dim-1]).  returns 0 */
+int    g5o_remap(const G5OParams * prm, int n_new, const int8_t * kind, const int32_t * src, const double * Uold, double * Unew);
+
 /* point functions (used by the golden-vector pins) */
 double g5o_compute_primitives(const G5OParams * prm, const double * u, double * q);
 void   g5o_riemann_hllc(const G5OParams * prm, const double * qL, const double * qR, double * out);

@@ -88,6 +88,7 @@ def lib():
         L.g5o_mixture_pressure.argtypes = [ctypes.POINTER(G5OParams), ctypes.c_double, ctypes.c_double, ctypes.c_double]
         L.g5o_mixture_sound_speed.restype = ctypes.c_double
         L.g5o_mixture_sound_speed.argtypes = [ctypes.POINTER(G5OParams), ctypes.c_double, ctypes.c_double, ctypes.c_double]
+        L.g5o_remap.argtypes = [ctypes.POINTER(G5OParams), ctypes.c_int, vp, vp, vp, vp]
         _lib = L
     return _lib
 
@@ -209,6 +210,21 @@ class Oracle:
                 U = self.step(U, dt)
         self.fill_outside(U)
         return U, np.array(dts)
+
+
+def remap(params, rt, U_old: np.ndarray, n_total_new: int) -> np.ndarray:
+    """Owned blocks of the adapted mesh from the old state (outside blocks left
+    zero: fill them with Oracle.fill_outside on the new mesh)."""
+    nv = 8 if rt.dim == 2 else 9
+    nc = rt.bsize**rt.dim
+    U_old = np.ascontiguousarray(U_old, np.float64)
+    assert U_old.shape[0] >= rt.n_old
+    U_new = np.zeros((n_total_new, nv, nc))
+    kind = np.ascontiguousarray(rt.kind, np.int8)
+    src = np.ascontiguousarray(rt.src, np.int32)
+    prm = make_params(params)
+    lib().g5o_remap(ctypes.byref(prm), rt.n_new, _ptr(kind), _ptr(src), _ptr(U_old), _ptr(U_new))
+    return U_new
 
 
 def oracle_flag_fn(indicator=0, eps_refine=0.1, eps_coarsen=0.0125, eps_lohner=0.02):
