@@ -44,6 +44,51 @@ struct G5Context
   static constexpr int kGraphs = 4;
   GraphSlot            graphs[kGraphs];
   int                  next_graph = 0;
+  // g5_step_host: U and U2 in host memory, copies pipelined with the step.
+  // The owned blocks are cut into K copy chunks; launch k steps the blocks
+  // whose own and neighbour data have arrived once chunk k is in, then the
+  // coarse/fine records whose blocks are all stepped; U2 chunks are copied
+  // back as soon as their last block is final.
+  struct HostPipe
+  {
+    int                  K = 0;
+    std::vector<int>     lo;       // [K+1] owned-block bounds of the copy chunks
+    std::vector<int>     work_off; // [K+1] launch k steps d_work[work_off[k] .. work_off[k+1])
+    std::vector<int>     rec_off;  // [K+1] launch k refluxes d_recs[rec_off[k] .. rec_off[k+1])
+    std::vector<int>     out_off;  // [K+1] after launch k copy back chunks out_list[out_off[k] .. out_off[k+1])
+    std::vector<int>     out_list;
+    int32_t *            d_work = nullptr;
+    int32_t *            d_recs = nullptr;
+    double *             d_U = nullptr;  // staging of U, n_total blocks (first g5_step_host call)
+    double *             d_U2 = nullptr; // staging of U2, n_owned blocks
+    static constexpr int kComputeStreams = 8;
+    cudaStream_t         s_in = nullptr, s_out = nullptr, s_c[kComputeStreams] = {};
+    cudaEvent_t          ev_start = nullptr, ev_out = nullptr, ev_dt_read = nullptr;
+    std::vector<cudaEvent_t> ev_in, ev_step, ev_comp;
+    double *             h_dt_stage = nullptr;  // pinned copy of dt_host read by the (captured) step
+    double *             h_inv_stage = nullptr; // pinned landing of the CFL rate
+    int                  n_stage = 0;
+    bool                 dt_pending = false; // a launched step may still read h_dt_stage
+    struct InvCopy
+    {
+      double *       dst = nullptr;
+      const double * src = nullptr;
+      size_t         bytes = 0;
+    };
+    struct Graph
+    {
+      cudaGraphExec_t exec = nullptr;
+      const void *    hU = nullptr;
+      const void *    hU2 = nullptr;
+      const void *    inv = nullptr;
+      int             mode = -1;
+      int             launches = 0;
+      InvCopy         inv_copy;
+    };
+    static constexpr int kGraphs = 4;
+    Graph                graphs[kGraphs];
+    int                  next_graph = 0;
+  } pipe;
 };
 
 namespace
@@ -101,6 +146,18 @@ free_mesh(G5Context * c)
   c->d_reflux_buf = c->d_defer_buf = c->d_dt = c->d_invdt = nullptr;
   c->d_step = nullptr;
   c->d_urk = nullptr;
+  for (void * p : { (void *)c->pipe.d_work, (void *)c->pipe.d_recs, (void *)c->pipe.d_U, (void *)c->pipe.d_U2 })
+    if (p)
+      cudaFree(p);
+  c->pipe.d_work = c->pipe.d_recs = nullptr;
+  c->pipe.d_U = c->pipe.d_U2 = nullptr;
+  c->pipe.K = 0;
+  for (auto & g : c->pipe.graphs)
+  {
+    if (g.exec)
+      cudaGraphExecDestroy(g.exec);
+    g = G5Context::HostPipe::Graph();
+  }
   drop_graphs(c);
   c->has_mesh = false;
   c->bytes = c->d_status ? (int64_t)sizeof(unsigned int) : 0;
@@ -153,6 +210,90 @@ do_step(G5Context * c, const double * U, double * U2, const double * d_dt, int m
                                        : g5::launch_step_mixed(c->dim, c->b, a, c->ctas_per_sm[1], s, &launches);
   c->last_launches = launches;
   return e == cudaSuccess ? G5_OK : G5_ERR_CUDA;
+}
+
+// Plan of g5_step_host for the table being uploaded (host arrays of g5_set_mesh).
+int
+plan_host_pipe(G5Context * c, const G5Mesh * m, const std::vector<int32_t> & defer_slot, const std::vector<int32_t> & defer_list)
+{
+  G5Context::HostPipe & hp = c->pipe;
+  const int             n_owned = m->n_owned, ns = c->ns, nch = c->nch, nfaces = 2 * c->dim;
+  const int             center = c->dim == 2 ? 4 : 13;
+  int                   K = n_owned / 64;
+  K = K < 1 ? 1 : (K > 8 ? 8 : K);
+  hp.K = K;
+  hp.lo.assign(K + 1, 0);
+  for (int k = 0; k <= K; ++k)
+    hp.lo[k] = (int)((int64_t)n_owned * k / K);
+  std::vector<int> chunk(n_owned);
+  for (int k = 0; k < K; ++k)
+    for (int n = hp.lo[k]; n < hp.lo[k + 1]; ++n)
+      chunk[n] = k;
+  // outside blocks travel with chunk 0
+  auto arrival = [&](int b) { return b >= n_owned ? 0 : chunk[b]; };
+  std::vector<int> ready(n_owned);
+  for (int n = 0; n < n_owned; ++n)
+  {
+    int r = chunk[n];
+    for (int s = 0; s < ns; ++s)
+    {
+      if (s == center)
+        continue;
+      const int32_t * nb = m->nbr + ((size_t)n * ns + s) * nch;
+      for (int ch = 0; ch < nch; ++ch)
+        if (nb[ch] >= 0)
+          r = r > arrival(nb[ch]) ? r : arrival(nb[ch]);
+    }
+    ready[n] = r;
+  }
+  // a block with coarse/fine records is final once its finer face neighbours are stepped
+  std::vector<int> final_(ready);
+  for (int n = 0; n < n_owned; ++n)
+    for (int f = 0; f < nfaces; ++f)
+    {
+      if (defer_slot.empty() || defer_slot[(size_t)n * nfaces + f] < 0)
+        continue;
+      int d[3] = { 0, 0, 0 };
+      d[f >> 1] = (f & 1) ? 1 : -1;
+      const int       s = (d[0] + 1) + 3 * (d[1] + 1) + (c->dim == 3 ? 9 * (d[2] + 1) : 0);
+      const int32_t * nb = m->nbr + ((size_t)n * ns + s) * nch;
+      for (int ch = 0; ch < nch; ++ch)
+        if (nb[ch] >= 0 && nb[ch] < n_owned)
+          final_[n] = final_[n] > ready[nb[ch]] ? final_[n] : ready[nb[ch]];
+    }
+  std::vector<int32_t> work, recs;
+  hp.work_off.assign(K + 1, 0);
+  hp.rec_off.assign(K + 1, 0);
+  for (int k = 0; k < K; ++k)
+  {
+    hp.work_off[k] = (int)work.size();
+    for (int n = 0; n < n_owned; ++n)
+      if (ready[n] == k)
+        work.push_back(n);
+    hp.rec_off[k] = (int)recs.size();
+    for (int32_t code : defer_list)
+      if (final_[code >> 3] == k)
+        recs.push_back(code);
+  }
+  hp.work_off[K] = (int)work.size();
+  hp.rec_off[K] = (int)recs.size();
+  hp.out_off.assign(K + 1, 0);
+  hp.out_list.clear();
+  std::vector<int> out_ready(K, 0);
+  for (int n = 0; n < n_owned; ++n)
+    out_ready[chunk[n]] = out_ready[chunk[n]] > final_[n] ? out_ready[chunk[n]] : final_[n];
+  for (int k = 0; k < K; ++k)
+  {
+    hp.out_off[k] = (int)hp.out_list.size();
+    for (int d = 0; d < K; ++d)
+      if (out_ready[d] == k)
+        hp.out_list.push_back(d);
+  }
+  hp.out_off[K] = (int)hp.out_list.size();
+  int rc = dev_upload(c, &hp.d_work, work.data(), work.size());
+  if (!recs.empty())
+    rc |= dev_upload(c, &hp.d_recs, recs.data(), recs.size());
+  return rc;
 }
 
 } // namespace
@@ -244,6 +385,30 @@ g5_destroy(G5Context * ctx)
   free_mesh(ctx);
   if (ctx->d_status)
     cudaFree(ctx->d_status);
+  G5Context::HostPipe & hp = ctx->pipe;
+  for (cudaEvent_t e : hp.ev_in)
+    cudaEventDestroy(e);
+  for (cudaEvent_t e : hp.ev_comp)
+    cudaEventDestroy(e);
+  for (cudaEvent_t e : hp.ev_step)
+    cudaEventDestroy(e);
+  for (cudaStream_t q : hp.s_c)
+    if (q)
+      cudaStreamDestroy(q);
+  if (hp.ev_start)
+    cudaEventDestroy(hp.ev_start);
+  if (hp.ev_out)
+    cudaEventDestroy(hp.ev_out);
+  if (hp.ev_dt_read)
+    cudaEventDestroy(hp.ev_dt_read);
+  if (hp.h_dt_stage)
+    cudaFreeHost(hp.h_dt_stage);
+  if (hp.h_inv_stage)
+    cudaFreeHost(hp.h_inv_stage);
+  if (hp.s_in)
+    cudaStreamDestroy(hp.s_in);
+  if (hp.s_out)
+    cudaStreamDestroy(hp.s_out);
   delete ctx;
   return G5_OK;
 }
@@ -374,6 +539,11 @@ g5_set_mesh(G5Context * c, const G5Mesh * m)
   c->n_inst = n_inst;
   c->n_defer = n_defer;
   c->n_reflux = n_reflux;
+  if (plan_host_pipe(c, m, defer_slot, defer_list))
+  {
+    free_mesh(c);
+    return G5_ERR_CUDA;
+  }
   c->has_mesh = true;
   return G5_OK;
 }
@@ -401,6 +571,256 @@ g5_step(G5Context * ctx, const double * d_U, double * d_U2, const double * dt_ho
   if (cudaMemcpyAsync(ctx->d_dt, dt_host, sizeof(double) * ctx->n_inst, cudaMemcpyHostToDevice, (cudaStream_t)stream) != cudaSuccess)
     return G5_ERR_CUDA;
   return do_step(ctx, d_U, d_U2, ctx->d_dt, mode, d_inv_dt_out, (cudaStream_t)stream);
+}
+
+namespace
+{
+void CUDART_CB
+copy_inv_to_caller(void * arg)
+{
+  const G5Context::HostPipe::InvCopy * ic = static_cast<const G5Context::HostPipe::InvCopy *>(arg);
+  std::memcpy(ic->dst, ic->src, ic->bytes);
+}
+
+// Enqueue one pipelined host-buffer step on s (captured into a graph or run
+// directly).  U2 goes straight to host memory when d_U2_host (the device view
+// of the caller's pinned U2) is given, otherwise through the device staging
+// array and chunked copies on s_out.
+bool
+enqueue_host_step(G5Context * c, const double * h_U, double * h_U2, double * d_U2_host, int mode, bool want_inv,
+                  const G5Context::HostPipe::InvCopy * inv, bool capturing, cudaStream_t s, int * launches)
+{
+  G5Context::HostPipe & hp = c->pipe;
+  const int             K = hp.K;
+  const size_t          blk = (size_t)c->nv * (c->dim == 2 ? c->b * c->b : c->b * c->b * c->b);
+  const size_t          bb = blk * sizeof(double);
+  const bool            staged_out = d_U2_host == nullptr;
+  bool ok = cudaMemcpyAsync(c->d_dt, hp.h_dt_stage, sizeof(double) * c->n_inst, cudaMemcpyHostToDevice, s) == cudaSuccess;
+  ok = ok && cudaEventRecordWithFlags(hp.ev_dt_read, s, capturing ? cudaEventRecordExternal : cudaEventRecordDefault) == cudaSuccess;
+  if (want_inv)
+    ok = ok && cudaMemsetAsync(c->d_invdt, 0, sizeof(double) * c->n_inst, s) == cudaSuccess;
+  // the copy streams start after the work already queued on s
+  ok = ok && cudaEventRecord(hp.ev_start, s) == cudaSuccess && cudaStreamWaitEvent(hp.s_in, hp.ev_start, 0) == cudaSuccess;
+  if (staged_out)
+    ok = ok && cudaStreamWaitEvent(hp.s_out, hp.ev_start, 0) == cudaSuccess;
+  for (int k = 0; ok && k < K; ++k)
+  {
+    if (k == 0 && c->n_outside > 0)
+      ok = cudaMemcpyAsync(hp.d_U + (size_t)c->n_owned * blk, h_U + (size_t)c->n_owned * blk, (size_t)c->n_outside * bb,
+                           cudaMemcpyHostToDevice, hp.s_in) == cudaSuccess;
+    const size_t n0 = (size_t)hp.lo[k], n1 = (size_t)hp.lo[k + 1];
+    if (ok && n1 > n0)
+      ok = cudaMemcpyAsync(hp.d_U + n0 * blk, h_U + n0 * blk, (n1 - n0) * bb, cudaMemcpyHostToDevice, hp.s_in) == cudaSuccess;
+    ok = ok && cudaEventRecord(hp.ev_in[k], hp.s_in) == cudaSuccess;
+  }
+  // chunk launches on kComputeStreams streams, so that the (latency-bound)
+  // launches of consecutive chunks run side by side; the coarse/fine records
+  // of chunk k wait for the step launches of chunks 0..k
+  const int P = G5Context::HostPipe::kComputeStreams;
+  for (int q = 0; ok && q < P && q < K; ++q) // (a captured stream without work could not be joined)
+    ok = cudaStreamWaitEvent(hp.s_c[q], hp.ev_start, 0) == cudaSuccess;
+  for (int k = 0; ok && k < K; ++k)
+  {
+    cudaStream_t q = hp.s_c[k % P];
+    ok = cudaStreamWaitEvent(q, hp.ev_in[k], 0) == cudaSuccess;
+    g5::StepArgs a;
+    a.U = hp.d_U;
+    a.U2 = staged_out ? hp.d_U2 : d_U2_host;
+    a.dt = c->d_dt;
+    a.reflux_buf = c->d_reflux_buf;
+    a.defer_buf = c->d_defer_buf;
+    a.invdt = want_inv ? c->d_invdt : nullptr;
+    a.status = c->d_status;
+    a.work = hp.d_work + hp.work_off[k];
+    a.n_work = hp.work_off[k + 1] - hp.work_off[k];
+    a.m = dev_mesh(c);
+    a.m.defer_list = nullptr;
+    a.m.n_defer = 0;
+    a.p = c->phys;
+    auto launch = [&](const g5::StepArgs & args) {
+      const cudaError_t e = mode == G5_MODE_FP64 ? g5::launch_step_fp64(c->dim, c->b, args, c->ctas_per_sm[0], q, launches)
+                                                 : g5::launch_step_mixed(c->dim, c->b, args, c->ctas_per_sm[1], q, launches);
+      return e == cudaSuccess;
+    };
+    if (ok && a.n_work > 0)
+      ok = launch(a);
+    ok = ok && cudaEventRecord(hp.ev_step[k], q) == cudaSuccess;
+    const int n_rec = hp.rec_off[k + 1] - hp.rec_off[k];
+    if (ok && n_rec > 0)
+    {
+      for (int j = 0; ok && j < k; ++j)
+        if (j % P != k % P)
+          ok = cudaStreamWaitEvent(q, hp.ev_step[j], 0) == cudaSuccess;
+      a.work = hp.d_work; // non-null with n_work == 0: the launcher runs the record pass only
+      a.n_work = 0;
+      a.m.defer_list = hp.d_recs + hp.rec_off[k];
+      a.m.n_defer = n_rec;
+      ok = ok && launch(a);
+    }
+    ok = ok && cudaEventRecord(hp.ev_comp[k], q) == cudaSuccess;
+    if (!staged_out)
+      continue;
+    // s_out walks k in order, so it has waited for every launch 0..k
+    ok = ok && cudaStreamWaitEvent(hp.s_out, hp.ev_comp[k], 0) == cudaSuccess;
+    for (int t = hp.out_off[k]; ok && t < hp.out_off[k + 1]; ++t)
+    {
+      const int    d = hp.out_list[t];
+      const size_t n0 = (size_t)hp.lo[d], n1 = (size_t)hp.lo[d + 1];
+      if (n1 > n0)
+        ok = cudaMemcpyAsync(h_U2 + n0 * blk, hp.d_U2 + n0 * blk, (n1 - n0) * bb, cudaMemcpyDeviceToHost, hp.s_out) == cudaSuccess;
+    }
+  }
+  // join everything back into s
+  for (int k = 0; ok && k < K; ++k)
+    ok = cudaStreamWaitEvent(s, hp.ev_comp[k], 0) == cudaSuccess;
+  if (staged_out)
+    ok = ok && cudaEventRecord(hp.ev_out, hp.s_out) == cudaSuccess && cudaStreamWaitEvent(s, hp.ev_out, 0) == cudaSuccess;
+  if (ok && inv)
+    ok = cudaMemcpyAsync(hp.h_inv_stage, c->d_invdt, sizeof(double) * c->n_inst, cudaMemcpyDeviceToHost, s) == cudaSuccess &&
+         cudaLaunchHostFunc(s, copy_inv_to_caller, (void *)inv) == cudaSuccess;
+  return ok;
+}
+} // namespace
+
+extern "C" int
+g5_step_host(G5Context * c, const double * h_U, double * h_U2, const double * dt_host, int mode, double * h_inv_dt_out, void * stream)
+{
+  if (!c || !c->has_mesh || !h_U || !h_U2 || !dt_host)
+    return G5_ERR_ARG;
+  if (mode != G5_MODE_FP64 && mode != G5_MODE_MIXED)
+    return G5_ERR_ARG;
+  for (int i = 0; i < c->n_inst; ++i)
+    if (!(dt_host[i] > 0.0))
+      return G5_ERR_ARG;
+  G5Context::HostPipe & hp = c->pipe;
+  const int             K = hp.K;
+  const size_t          blk = (size_t)c->nv * (c->dim == 2 ? c->b * c->b : c->b * c->b * c->b);
+  if (!hp.s_in)
+  {
+    if (cudaStreamCreateWithFlags(&hp.s_in, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&hp.s_out, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&hp.ev_start, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&hp.ev_out, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&hp.ev_dt_read, cudaEventDisableTiming) != cudaSuccess)
+      return G5_ERR_CUDA;
+    for (cudaStream_t & q : hp.s_c)
+      if (cudaStreamCreateWithFlags(&q, cudaStreamNonBlocking) != cudaSuccess)
+        return G5_ERR_CUDA;
+  }
+  while ((int)hp.ev_in.size() < K)
+  {
+    cudaEvent_t a = nullptr, b = nullptr, e = nullptr;
+    if (cudaEventCreateWithFlags(&a, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
+      return G5_ERR_CUDA;
+    hp.ev_in.push_back(a);
+    hp.ev_comp.push_back(b);
+    hp.ev_step.push_back(e);
+  }
+  if (hp.dt_pending)
+  {
+    // the previous call's step must have read the staged dt before it is overwritten
+    if (cudaEventSynchronize(hp.ev_dt_read) != cudaSuccess)
+      return G5_ERR_CUDA;
+    hp.dt_pending = false;
+  }
+  if (hp.n_stage < c->n_inst)
+  {
+    if (hp.h_dt_stage)
+      cudaFreeHost(hp.h_dt_stage);
+    if (hp.h_inv_stage)
+      cudaFreeHost(hp.h_inv_stage);
+    hp.h_dt_stage = hp.h_inv_stage = nullptr;
+    hp.n_stage = 0;
+    if (cudaMallocHost((void **)&hp.h_dt_stage, sizeof(double) * c->n_inst) != cudaSuccess ||
+        cudaMallocHost((void **)&hp.h_inv_stage, sizeof(double) * c->n_inst) != cudaSuccess)
+      return G5_ERR_CUDA;
+    hp.n_stage = c->n_inst;
+  }
+  if (!hp.d_U)
+  {
+    if (dev_alloc(c, &hp.d_U, (size_t)c->n_total * blk) || dev_alloc(c, &hp.d_U2, (size_t)(c->n_owned > 0 ? c->n_owned : 1) * blk))
+      return G5_ERR_CUDA;
+  }
+  std::memcpy(hp.h_dt_stage, dt_host, sizeof(double) * c->n_inst);
+  // pinned caller buffers: the step writes U2 straight into host memory and the
+  // whole step is replayed from a graph; pageable buffers go through staging
+  double * d_U2_host = nullptr;
+  if (cudaHostGetDevicePointer((void **)&d_U2_host, h_U2, 0) != cudaSuccess)
+  {
+    cudaGetLastError();
+    d_U2_host = nullptr;
+  }
+  cudaPointerAttributes attr;
+  const bool            pinned_in = cudaPointerGetAttributes(&attr, h_U) == cudaSuccess && attr.type == cudaMemoryTypeHost;
+  cudaGetLastError();
+  cudaStream_t s = (cudaStream_t)stream;
+  int          launches = 0;
+  if (!pinned_in || !d_U2_host)
+  {
+    // pageable caller buffers: copies through the staging arrays, and the CFL
+    // rate read back synchronously
+    bool ok = enqueue_host_step(c, h_U, h_U2, nullptr, mode, h_inv_dt_out != nullptr, nullptr, false, s, &launches);
+    hp.dt_pending = true;
+    if (ok && h_inv_dt_out)
+      ok = cudaMemcpyAsync(hp.h_inv_stage, c->d_invdt, sizeof(double) * c->n_inst, cudaMemcpyDeviceToHost, s) == cudaSuccess &&
+           cudaStreamSynchronize(s) == cudaSuccess;
+    if (ok && h_inv_dt_out)
+      std::memcpy(h_inv_dt_out, hp.h_inv_stage, sizeof(double) * c->n_inst);
+    c->last_launches = launches;
+    return ok ? G5_OK : G5_ERR_CUDA;
+  }
+  G5Context::HostPipe::Graph * slot = nullptr;
+  for (auto & g : hp.graphs)
+    if (g.exec && g.hU == h_U && g.hU2 == h_U2 && g.mode == mode && g.inv == h_inv_dt_out)
+      slot = &g;
+  if (!slot)
+  {
+    slot = &hp.graphs[hp.next_graph];
+    hp.next_graph = (hp.next_graph + 1) % G5Context::HostPipe::kGraphs;
+    if (slot->exec)
+      cudaGraphExecDestroy(slot->exec);
+    *slot = G5Context::HostPipe::Graph();
+    slot->inv_copy = { h_inv_dt_out, hp.h_inv_stage, sizeof(double) * c->n_inst };
+    cudaStream_t cap;
+    if (cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking) != cudaSuccess)
+      return G5_ERR_CUDA;
+    cudaGraph_t g = nullptr;
+    if (cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+    {
+      cudaStreamDestroy(cap);
+      return G5_ERR_CUDA;
+    }
+    int         n = 0;
+    const bool  ok = enqueue_host_step(c, h_U, h_U2, d_U2_host, mode, h_inv_dt_out != nullptr, h_inv_dt_out ? &slot->inv_copy : nullptr,
+                                       true, cap, &n);
+    cudaError_t e = cudaStreamEndCapture(cap, &g);
+    cudaStreamDestroy(cap);
+    if (!ok || e != cudaSuccess)
+    {
+      if (g)
+        cudaGraphDestroy(g);
+      return G5_ERR_CUDA;
+    }
+    e = cudaGraphInstantiate(&slot->exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess)
+    {
+      slot->exec = nullptr;
+      return G5_ERR_CUDA;
+    }
+    slot->hU = h_U;
+    slot->hU2 = h_U2;
+    slot->inv = h_inv_dt_out;
+    slot->mode = mode;
+    slot->launches = n;
+  }
+  if (cudaGraphLaunch(slot->exec, s) != cudaSuccess)
+    return G5_ERR_CUDA;
+  hp.dt_pending = true;
+  c->last_launches = slot->launches;
+  return G5_OK;
 }
 
 extern "C" int

@@ -59,9 +59,18 @@ struct StepArgs
   double *       defer_buf;  // own face fluxes of coarse cells next to finer faces
   double *       invdt;      // [n_inst] (bit-pattern max), may be null
   unsigned int * status;
+  const int32_t * work = nullptr; // owned blocks to step (null: all n_owned blocks in order)
+  int             n_work = 0;     // entries of work
   DevMesh        m;
   PhysParams     p;
 };
+
+// number of blocks a step launch walks
+__host__ __device__ inline int
+step_count(const StepArgs & a)
+{
+  return a.work ? a.n_work : a.m.n_owned;
+}
 
 constexpr unsigned STATUS_NONPHYSICAL = 1u;
 constexpr unsigned STATUS_MESH = 2u;

@@ -42,15 +42,17 @@ launch_step2d_m(const StepArgs & a, int ctas_per_sm, cudaStream_t s, int * launc
   }
   const int per_sm = (ctas_per_sm > 0 && ctas_per_sm < occ) ? ctas_per_sm : occ;
   int       grid = num_sms_m() * per_sm;
-  if (grid > a.m.n_owned)
-    grid = a.m.n_owned;
-  if (grid < 1)
-    return cudaSuccess;
-  step2d_kernel<B, true><<<grid, T::NT, T::smem_bytes, s>>>(a);
-  ++*launches;
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess)
-    return e;
+  if (grid > step_count(a))
+    grid = step_count(a);
+  cudaError_t e = cudaSuccess;
+  if (grid >= 1)
+  {
+    step2d_kernel<B, true><<<grid, T::NT, T::smem_bytes, s>>>(a);
+    ++*launches;
+    e = cudaGetLastError();
+    if (e != cudaSuccess)
+      return e;
+  }
   if (a.m.n_defer > 0)
   {
     const int n = a.m.n_defer * B;
@@ -90,15 +92,17 @@ launch_step3d_m(const StepArgs & a, int ctas_per_sm, cudaStream_t s, int * launc
   }
   const int per_sm = (ctas_per_sm > 0 && ctas_per_sm < occ) ? ctas_per_sm : occ;
   int       grid = num_sms_m() * per_sm;
-  if (grid > a.m.n_owned)
-    grid = a.m.n_owned;
-  if (grid < 1)
-    return cudaSuccess;
-  step3d_kernel<true><<<grid, T::NT, T::smem_bytes, s>>>(a);
-  ++*launches;
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess)
-    return e;
+  if (grid > step_count(a))
+    grid = step_count(a);
+  cudaError_t e = cudaSuccess;
+  if (grid >= 1)
+  {
+    step3d_kernel<true><<<grid, T::NT, T::smem_bytes, s>>>(a);
+    ++*launches;
+    e = cudaGetLastError();
+    if (e != cudaSuccess)
+      return e;
+  }
   if (a.m.n_defer > 0)
   {
     const int n = a.m.n_defer * 64;

@@ -498,8 +498,10 @@ step2d_kernel(StepArgs a)
   // a stiffened-gas constant makes the pressure numerator cancel: FP64 there
   const bool stiff = P.gpx[0] != 0.0 || P.gpx[1] != 0.0;
 
-  for (int n = blockIdx.x; n < a.m.n_owned; n += gridDim.x)
+  const int nwalk = step_count(a);
+  for (int iw = blockIdx.x; iw < nwalk; iw += gridDim.x)
   {
+    const int    n = a.work ? a.work[iw] : iw;
     const int    lev = a.m.level[n];
     const int    ins = a.m.inst ? a.m.inst[n] : 0;
     const double dx = P.level_dx[lev];

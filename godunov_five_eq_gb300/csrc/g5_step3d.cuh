@@ -299,8 +299,10 @@ step3d_kernel(StepArgs a)
   const bool         stiff = P.gpx[0] != 0.0 || P.gpx[1] != 0.0;
   const int          ci = tid % B, cj = (tid / B) % B, ck = tid / (B * B);
 
-  for (int n = blockIdx.x; n < a.m.n_owned; n += gridDim.x)
+  const int nwalk = step_count(a);
+  for (int iw = blockIdx.x; iw < nwalk; iw += gridDim.x)
   {
+    const int    n = a.work ? a.work[iw] : iw;
     const int    ins = a.m.inst ? a.m.inst[n] : 0;
     const double dx = P.level_dx[a.m.level[n]];
     R            dtdx_r;

@@ -102,6 +102,7 @@ EXPORTS = [
     "g5_mem_bytes",
     "g5_step",
     "g5_step_dev",
+    "g5_step_host",
     "g5_compute_inv_dt",
     "g5_fill_outside",
     "g5_begin",
@@ -142,6 +143,7 @@ def load_library(build_if_missing: bool = True):
     L.g5_mem_bytes.argtypes = [vp]
     L.g5_step.argtypes = [vp, vp, vp, vp, ctypes.c_int, vp, vp]
     L.g5_step_dev.argtypes = [vp, vp, vp, vp, ctypes.c_int, vp, vp]
+    L.g5_step_host.argtypes = [vp, vp, vp, vp, ctypes.c_int, vp, vp]
     L.g5_compute_inv_dt.argtypes = [vp, vp, vp, vp]
     L.g5_fill_outside.argtypes = [vp, vp, vp]
     L.g5_run.argtypes = [vp, vp, vp, ctypes.c_int, ctypes.c_int, vp, vp]
@@ -179,6 +181,12 @@ def make_params(p) -> G5Params:
     for i in range(32):
         o.level_dx[i] = float(p.level_dx[i])
     return o
+
+
+def _torch():
+    import torch
+
+    return torch
 
 
 def _dptr(t) -> int:
@@ -279,6 +287,31 @@ class GodunovImplemGB300:
         )
         if rc != 0:
             raise G5Error(rc, "g5_step_dev")
+
+    def do_time_step_host(self, U_host, U2_host, dt, mode="fp64", inv_dt_out=None, stream=None):
+        """g5_step_host: U and U2 are CPU tensors (pinned for overlap); the copies
+        run chunk by chunk, overlapped with the step.  Asynchronous on `stream`."""
+        for T in (U_host, U2_host):
+            if T.is_cuda or not T.is_contiguous() or T.dtype != _torch().float64:
+                raise ValueError("U_host/U2_host must be contiguous float64 CPU tensors")
+        dt = np.ascontiguousarray(np.broadcast_to(np.asarray(dt, np.float64), (self.table.n_inst,)))
+        self._dt_keep = dt
+        inv = None
+        if inv_dt_out is not None:
+            if inv_dt_out.is_cuda or inv_dt_out.dtype != _torch().float64:
+                raise ValueError("inv_dt_out must be a float64 CPU tensor")
+            inv = ctypes.c_void_p(inv_dt_out.data_ptr())
+        rc = self.lib.g5_step_host(
+            self.ctx,
+            ctypes.c_void_p(U_host.data_ptr()),
+            ctypes.c_void_p(U2_host.data_ptr()),
+            dt.ctypes.data_as(ctypes.c_void_p),
+            MODES[mode],
+            inv,
+            _stream(stream),
+        )
+        if rc != 0:
+            raise G5Error(rc, "g5_step_host")
 
     def compute_inv_dt(self, U, out=None, stream=None):
         import torch

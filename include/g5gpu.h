@@ -141,6 +141,19 @@ int g5_step(G5Context * ctx, const double * d_U, double * d_U2, const double * d
 /* Same as g5_step with dt read from device memory (d_dt[n_inst]). */
 int g5_step_dev(G5Context * ctx, const double * d_U, double * d_U2, const double * d_dt, int mode, double * d_inv_dt_out, void * stream);
 
+/* GodunovImplemBase::do_time_step for a caller whose U and U2 live in host
+ * memory (pinned, for the copies to overlap): h_U[n_owned + n_outside blocks]
+ * (outside blocks filled) is copied to a device staging array and h_U2's
+ * owned blocks are copied back, in chunks of consecutive blocks on two
+ * internal streams, overlapped with the step: a chunk of blocks is stepped as
+ * soon as its own and its neighbours' data are on the device, and copied back
+ * as soon as its blocks are final (coarse/fine refluxing included).  Same
+ * results as g5_step.  h_inv_dt_out (host, [n_inst], may be NULL) receives the
+ * CFL rate of the new state.  Asynchronous on `stream`: synchronise it before
+ * reading h_U2.  The first call allocates the staging arrays (2 x the state);
+ * g5_set_mesh frees them. */
+int g5_step_host(G5Context * ctx, const double * h_U, double * h_U2, const double * dt_host, int mode, double * h_inv_dt_out, void * stream);
+
 /* ComputeDtFiveEqFunctor::apply (scheme/ComputeDtFiveEqFunctor.h:113-121):
  * d_inv_dt[n_inst] <- max over owned cells of sum_d (c+|u_d|)/dx. */
 int g5_compute_inv_dt(G5Context * ctx, const double * d_U, double * d_inv_dt, void * stream);
