@@ -110,6 +110,23 @@ atomic_max_pos(double * addr, double v)
   atomicMax(reinterpret_cast<unsigned long long *>(addr), (unsigned long long)__double_as_longlong(v));
 }
 
+// The same for one value per thread of a warp, threads of different
+// instances apart: one atomic per instance present in the converged lanes
+// (the max of positive doubles is the max of their bit patterns, taken as
+// high word then low word).  Thousands of per-thread atomics on one address
+// would serialise.
+__device__ __forceinline__ void
+atomic_max_pos_warp(double * base, int ins, double v)
+{
+  const unsigned           active = __activemask();
+  const unsigned           grp = __match_any_sync(active, ins);
+  const unsigned long long b = (v > 0.0) ? (unsigned long long)__double_as_longlong(v) : 0ull;
+  const unsigned           hi = __reduce_max_sync(grp, (unsigned)(b >> 32));
+  const unsigned           lo = __reduce_max_sync(grp, (unsigned)(b >> 32) == hi ? (unsigned)b : 0u);
+  if ((int)(threadIdx.x & 31u) == __ffs(grp) - 1 && (hi | lo) != 0u)
+    atomicMax(reinterpret_cast<unsigned long long *>(base + ins), ((unsigned long long)hi << 32) | lo);
+}
+
 // ---------------------------------------------------------------------------
 // Stiffened-gas mixture EOS (restated, see the oracle for the formulas)
 // ---------------------------------------------------------------------------
@@ -545,6 +562,54 @@ f2d_exact(float f)
   if (e == 0xFFu)
     hi = sgn | 0x7FF00000u | (m >> 3);
   return __hiloint2double((int)hi, (int)lo);
+}
+
+// L2 prefetch of a contiguous range (cp.async.bulk.prefetch: 16-byte aligned
+// address, size a multiple of 16; anything else is skipped) and of one line
+__device__ __forceinline__ void
+prefetch_l2_range(const void * p, unsigned bytes)
+{
+  if ((((unsigned long long)p | bytes) & 15u) == 0)
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(__cvta_generic_to_global(p)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void
+prefetch_l2_line(const void * p)
+{
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(__cvta_generic_to_global(p)));
+}
+
+// The double nearest below (in magnitude) s + t for a renormalised float pair
+// (|t| <= ulp(s)), built on the integer pipe: the 24-bit mantissa of t is added
+// into the 53-bit mantissa of s; bits of t below that window are dropped (an
+// error under 2^-53 |s|).  Pairs that are not renormalised, zero, subnormal or
+// non-finite parts take the FP64 path.
+__device__ __forceinline__ double
+ff_to_d(float s, float t)
+{
+  const unsigned sb = __float_as_uint(s), tb = __float_as_uint(t);
+  const int      es = (int)((sb >> 23) & 0xFFu), et = (int)((tb >> 23) & 0xFFu);
+  if (et == 0)
+    return f2d_exact(s);
+  const int sh = 29 + et - es; // position of t's mantissa within s's 53-bit window
+  if (es == 0 || es == 0xFF || et == 0xFF || sh > 5)
+    return f2d_exact(s) + f2d_exact(t);
+  unsigned long long M = (unsigned long long)((sb & 0x7FFFFFu) | 0x800000u) << 29;
+  const unsigned     mt = (tb & 0x7FFFFFu) | 0x800000u;
+  const unsigned     T = sh >= 0 ? (mt << sh) : (sh > -24 ? (mt >> -sh) : 0u);
+  M = ((sb ^ tb) & 0x80000000u) ? M - T : M + T;
+  unsigned long long e = (unsigned long long)(es + 896); // 1023 - 127
+  if (M >> 53)
+  {
+    M >>= 1;
+    ++e;
+  }
+  else if (!(M >> 52))
+  {
+    M <<= 1;
+    --e;
+  }
+  return __longlong_as_double((long long)(((unsigned long long)(sb & 0x80000000u) << 32) | (e << 52) | (M & 0xFFFFFFFFFFFFFull)));
 }
 
 // error-free difference of two floats: a - b == hi + lo exactly (Knuth's TwoSum)

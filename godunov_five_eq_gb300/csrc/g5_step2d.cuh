@@ -61,9 +61,12 @@ halo_coords(int h, int & gx, int & gy)
 
 // load the conservative state seen by ghost cell (gx, gy) of block n.
 // Returns false (and raises the mesh status) on a bad neighbour index.
+// (cx0, cy0): the block's coordinates.  The slot's relation and its four
+// neighbour entries are read in one wave (a 16-byte row), not one after the
+// other: the gather is latency-bound.
 template <int B>
 __device__ __forceinline__ bool
-gather_ghost_2d(const StepArgs & a, int n, int gx, int gy, double * u)
+gather_ghost_2d(const StepArgs & a, int n, int cx0, int cy0, int gx, int gy, double * u)
 {
   using H = V<2>;
   constexpr int NC = B * B;
@@ -72,7 +75,8 @@ gather_ghost_2d(const StepArgs & a, int n, int gx, int gy, double * u)
   const int     vx = gx - dxs * B, vy = gy - dys * B;
   const int     s = (dxs + 1) + 3 * (dys + 1);
   const int     rel = a.m.nbr_rel[n * 9 + s];
-  const int *   nb = a.m.nbr + (n * 9 + s) * 4;
+  const int4    nb4 = *reinterpret_cast<const int4 *>(a.m.nbr + (n * 9 + s) * 4);
+  const int     nb[4] = { nb4.x, nb4.y, nb4.z, nb4.w };
   if (rel == 0)
   {
     const int src = nb[0];
@@ -89,8 +93,8 @@ gather_ghost_2d(const StepArgs & a, int n, int gx, int gy, double * u)
     const int src = nb[0];
     if (src < 0 || src >= a.m.n_total)
       return false;
-    const int cx = ((a.m.coord[n * 3 + 0] + dxs) & 1) * (B / 2) + (vx >> 1);
-    const int cy = ((a.m.coord[n * 3 + 1] + dys) & 1) * (B / 2) + (vy >> 1);
+    const int cx = ((cx0 + dxs) & 1) * (B / 2) + (vx >> 1);
+    const int cy = ((cy0 + dys) & 1) * (B / 2) + (vy >> 1);
     const double * base = a.U + (size_t)src * H::NV * NC + cx + B * cy;
 #pragma unroll
     for (int v = 0; v < H::NV; ++v)
@@ -335,54 +339,26 @@ update_fp64(const double * uin, double * u2, const double * sFx, const double * 
 }
 
 // The same update in the FP32-bulk form.  FP64 is used only for the adds
-// into the stored state: the partial densities receive both face fluxes of
-// each direction exactly (error-free float difference, two FP64 adds), so
-// per-material mass is conserved to FP64 round-off; energy and momentum
-// accumulate both directions as an exact float-float sum; the clamps run on
-// the integer pipe; the renormalisation divides by 1 + d as a multiply by
-// (1 - d) when |d| < 1e-8 (exact to FP64 rounding).
-template <int B>
+// into the stored state: the face fluxes of both directions are summed as a
+// float-float pair (error-free differences and sums), turned into a double on
+// the integer pipe (ff_to_d, exact but for bits below 2^-53 of the sum) and
+// added with one FP64 add, so per-material mass is conserved to FP64
+// round-off; the clamps run on the integer pipe; the renormalisation divides
+// by 1 + d as a multiply by (1 - d) when |d| < 1e-8 (exact to FP64 rounding).
+//
+// apply_mixed_2d takes the per-direction increments: h + l (float pairs) of
+// r0 r1 e u v and dA (floats, source term included) of alpha0 alpha1; u2 holds
+// the old state on entry.  Returns the CFL rate of the new state (or 0).
 __device__ __forceinline__ float
-update_mixed(const double * uin, double * u2, const float * sFx, const float * sFy, int ci, int cj, float dx, const PhysParams & P, bool stiff, bool want_dt)
+apply_mixed_2d(const double * uin, double * u2, const float (&h)[2][5], const float (&l)[2][5], const float (&dA)[2][2], float dx,
+               const PhysParams & P, bool stiff, bool want_dt)
 {
   using H = V<2>;
-  constexpr int NFF = B * (B + 1);
-#pragma unroll
-  for (int v = 0; v < H::NV; ++v)
-    u2[v] = uin[v];
-  float        a0f = d2f_fast(uin[H::IA0]), a1f = d2f_fast(uin[H::IA1]);
-  {
-    float st0, st1;
-    source_factors_mixed<2>(uin, P, stiff, st0, st1);
-    a0f *= st0;
-    a1f *= st1;
-  }
   const double eps = 1e-12, one_m_eps = 1.0 - 1e-12;
-  const int    ilx = ci + (B + 1) * cj, irx = ilx + 1;
-  const int    ily = ci + B * cj, iry = ily + B;
-  // error-free per-direction increments of the conserved quantities:
-  // d[dir] = F_left - F_right = h + l exactly
-  float h[2][5], l[2][5];
-  const int ks[5] = { H::FR0, H::FR1, H::FE, H::FU, H::FV };
-#pragma unroll
-  for (int k = 0; k < 5; ++k)
-  {
-    two_diff(sFx[ks[k] * NFF + ilx], sFx[ks[k] * NFF + irx], h[0][k], l[0][k]);
-    two_diff(sFy[ks[k] * NFF + ily], sFy[ks[k] * NFF + iry], h[1][k], l[1][k]);
-  }
-  float dA[2][2];
-  {
-    const float uslx = sFx[H::FUS * NFF + ilx], usrx = sFx[H::FUS * NFF + irx];
-    const float usly = sFy[H::FUS * NFF + ily], usry = sFy[H::FUS * NFF + iry];
-    dA[0][0] = ((sFx[H::FA0 * NFF + ilx] - uslx * a0f) - sFx[H::FA0 * NFF + irx]) + usrx * a0f;
-    dA[0][1] = ((sFx[H::FA1 * NFF + ilx] - uslx * a1f) - sFx[H::FA1 * NFF + irx]) + usrx * a1f;
-    dA[1][0] = ((sFy[H::FA0 * NFF + ily] - usly * a0f) - sFy[H::FA0 * NFF + iry]) + usry * a0f;
-    dA[1][1] = ((sFy[H::FA1 * NFF + ily] - usly * a1f) - sFy[H::FA1 * NFF + iry]) + usry * a1f;
-  }
   // partial densities: clamp after X cannot trigger when the state dominates
   // the X decrease (checked in FP32 with a factor-2 margin); then both
-  // directions are summed exactly in float-float and added with two FP64
-  // adds, otherwise the X and Y increments are applied one after the other.
+  // directions are summed in float-float and added with one FP64 add,
+  // otherwise the X and Y increments are applied one after the other.
 #pragma unroll
   for (int k = 0; k < 2; ++k)
   {
@@ -392,8 +368,8 @@ update_mixed(const double * uin, double * u2, const float * sFx, const float * s
     {
       float s, t;
       two_sum(h[0][k], h[1][k], s, t);
-      t += l[0][k] + l[1][k];
-      u2[iv] = (u2[iv] + f2d_exact(s)) + f2d_exact(t);
+      two_sum(s, t + (l[0][k] + l[1][k]), s, t);
+      u2[iv] += ff_to_d(s, t);
       if (dlt_pos(u2[iv], eps))
         u2[iv] = 0.0;
     }
@@ -436,15 +412,15 @@ update_mixed(const double * uin, double * u2, const float * sFx, const float * s
       }
     }
   }
-  // energy and momentum: no clamps, one exact float-float sum of both directions
+  // energy and momentum: no clamps, one float-float sum of both directions
   const int ive[3] = { H::IE, H::IU, H::IV };
 #pragma unroll
   for (int e = 0; e < 3; ++e)
   {
     float s, t;
     two_sum(h[0][2 + e], h[1][2 + e], s, t);
-    t += l[0][2 + e] + l[1][2 + e];
-    u2[ive[e]] = (u2[ive[e]] + f2d_exact(s)) + f2d_exact(t);
+    two_sum(s, t + (l[0][2 + e] + l[1][2 + e]), s, t);
+    u2[ive[e]] += ff_to_d(s, t);
   }
   // renormalisation
   const double sa = u2[H::IA0] + u2[H::IA1];
@@ -472,6 +448,47 @@ update_mixed(const double * uin, double * u2, const float * sFx, const float * s
   const float c = sound_speed_f(P.f_xi[0], P.f_xi[1], P.f_gpx[0], P.f_gpx[1], df, p, a0s);
   return ((c + fabsf(ux)) + (c + fabsf(uy))) * __frcp_rn(dx);
 }
+
+template <int B>
+__device__ __forceinline__ float
+update_mixed(const double * uin, double * u2, const float * sFx, const float * sFy, int ci, int cj, float dx, const PhysParams & P, bool stiff, bool want_dt)
+{
+  using H = V<2>;
+  constexpr int NFF = B * (B + 1);
+#pragma unroll
+  for (int v = 0; v < H::NV; ++v)
+    u2[v] = uin[v];
+  float        a0f = d2f_fast(uin[H::IA0]), a1f = d2f_fast(uin[H::IA1]);
+  {
+    float st0, st1;
+    source_factors_mixed<2>(uin, P, stiff, st0, st1);
+    a0f *= st0;
+    a1f *= st1;
+  }
+  const int    ilx = ci + (B + 1) * cj, irx = ilx + 1;
+  const int    ily = ci + B * cj, iry = ily + B;
+  // error-free per-direction increments of the conserved quantities:
+  // d[dir] = F_left - F_right = h + l exactly
+  float h[2][5], l[2][5];
+  const int ks[5] = { H::FR0, H::FR1, H::FE, H::FU, H::FV };
+#pragma unroll
+  for (int k = 0; k < 5; ++k)
+  {
+    two_diff(sFx[ks[k] * NFF + ilx], sFx[ks[k] * NFF + irx], h[0][k], l[0][k]);
+    two_diff(sFy[ks[k] * NFF + ily], sFy[ks[k] * NFF + iry], h[1][k], l[1][k]);
+  }
+  float dA[2][2];
+  {
+    const float uslx = sFx[H::FUS * NFF + ilx], usrx = sFx[H::FUS * NFF + irx];
+    const float usly = sFy[H::FUS * NFF + ily], usry = sFy[H::FUS * NFF + iry];
+    dA[0][0] = ((sFx[H::FA0 * NFF + ilx] - uslx * a0f) - sFx[H::FA0 * NFF + irx]) + usrx * a0f;
+    dA[0][1] = ((sFx[H::FA1 * NFF + ilx] - uslx * a1f) - sFx[H::FA1 * NFF + irx]) + usrx * a1f;
+    dA[1][0] = ((sFy[H::FA0 * NFF + ily] - usly * a0f) - sFy[H::FA0 * NFF + iry]) + usry * a0f;
+    dA[1][1] = ((sFy[H::FA1 * NFF + ily] - usly * a1f) - sFy[H::FA1 * NFF + iry]) + usry * a1f;
+  }
+  return apply_mixed_2d(uin, u2, h, l, dA, dx, P, stiff, want_dt);
+}
+
 
 // 4 CTAs per SM in the FP32-bulk form (64 registers), so that CTAs in the
 // FP64-heavy update overlap with CTAs in the FP32 face phase; 2 CTAs per SM
@@ -503,6 +520,7 @@ step2d_kernel(StepArgs a)
   {
     const int    n = a.work ? a.work[iw] : iw;
     const int    lev = a.m.level[n];
+    const int    cx0 = a.m.coord[n * 3 + 0], cy0 = a.m.coord[n * 3 + 1];
     const int    ins = a.m.inst ? a.m.inst[n] : 0;
     const double dx = P.level_dx[lev];
     R            dtdx_r;
@@ -526,7 +544,7 @@ step2d_kernel(StepArgs a)
       int gx, gy;
       halo_coords<B>(h, gx, gy);
       double u[H::NV];
-      if (!gather_ghost_2d<B>(a, n, gx, gy, u))
+      if (!gather_ghost_2d<B>(a, n, cx0, cy0, gx, gy, u))
       {
         raise_status(a.status, STATUS_MESH);
 #pragma unroll
@@ -536,6 +554,18 @@ step2d_kernel(StepArgs a)
       store_prim<B, MIXED>(sQ, (gx + 2) + G * (gy + 2), u, P, stiff);
     }
     __syncthreads();
+    // the next block of this CTA: its own cells and table rows into L2 while
+    // this block computes (its gather then hits L2 instead of HBM)
+    if (tid < 3 && iw + (int)gridDim.x < nwalk)
+    {
+      const int nn = a.work ? a.work[iw + gridDim.x] : iw + (int)gridDim.x;
+      if (tid == 0)
+        prefetch_l2_range(a.U + (size_t)nn * H::NV * NC, (unsigned)(H::NV * NC * sizeof(double)));
+      else if (tid == 1)
+        prefetch_l2_line(a.m.nbr + (size_t)nn * 36);
+      else
+        prefetch_l2_line(a.m.nbr_rel + (size_t)nn * 9);
+    }
 
     // ---------------- phase 2: per ring cell slopes + Hancock source
     for (int r = tid; r < SS; r += NT)
@@ -738,7 +768,11 @@ step2d_kernel(StepArgs a)
 // entry).  Replays update_U with the fine face sums of
 // get_flux_from_fine_neighbor (ReadFluxesAndConservativeUpdateFunctor.h:256-307).
 // ---------------------------------------------------------------------------
-// MIXED only keeps the two instantiations (FMA-free and fast-math units) apart
+// MIXED selects the FP32-bulk form of the mixed mode (float-pair increments
+// applied by apply_mixed_2d); the FP64 form replays the reference arithmetic.
+// All loads of a cell are issued in four waves (record, slots and own state,
+// fine-face indices, face fluxes) rather than one dependent chain per face:
+// a thread of this pass is latency-bound, and each L2 round trip counts.
 template <int B, bool MIXED>
 __global__ void
 reflux2d_kernel(StepArgs a)
@@ -754,150 +788,239 @@ reflux2d_kernel(StepArgs a)
   const int dirf = face >> 1, sidef = face & 1;
   const int ci = dirf == 0 ? (sidef ? B - 1 : 0) : pos;
   const int cj = dirf == 0 ? pos : (sidef ? B - 1 : 0);
-  const int * dsl = a.m.defer_slot + n * 4;
-  // a cell next to two finer faces is handled by the lower face index
-  for (int f2 = 0; f2 < face; ++f2)
-  {
-    if (dsl[f2] < 0)
-      continue;
-    const int d2 = f2 >> 1, s2 = f2 & 1;
-    const int c2 = d2 == 0 ? ci : cj;
-    if (c2 == (s2 ? B - 1 : 0))
-      return;
-  }
-  const double * own = a.defer_buf + ((size_t)dsl[face] * B + pos) * 32;
-  const int      cell = ci + B * cj;
-  const double * ub = a.U + (size_t)n * H::NV * NC + cell;
-  double         uin[H::NV], u2[H::NV];
+  const int cell = ci + B * cj;
+  // wave 2: the block's record slots, the cell's old state, the fine-face
+  // neighbour of every face (indices within the block's table rows)
+  int dsl[4], Fn[4];
+  double uin[H::NV], u2[H::NV];
 #pragma unroll
-  for (int v = 0; v < H::NV; ++v)
-    u2[v] = uin[v] = ub[v * NC];
+  for (int f = 0; f < 4; ++f)
+  {
+    dsl[f] = a.m.defer_slot[n * 4 + f];
+    const int dir = f >> 1, side = f & 1;
+    const int ct = dir == 0 ? cj : ci;
+    const int s = dir == 0 ? (side ? 5 : 3) : (side ? 7 : 1);
+    const int cht = (2 * ct) / B;
+    const int chd = side ? 0 : 1;
+    Fn[f] = a.m.nbr[(n * 9 + s) * 4 + (dir == 0 ? chd + 2 * cht : cht + 2 * chd)];
+  }
+  {
+    const double * ub = a.U + (size_t)n * H::NV * NC + cell;
+#pragma unroll
+    for (int v = 0; v < H::NV; ++v)
+      u2[v] = uin[v] = ub[v * NC];
+  }
   const int    ins = a.m.inst ? a.m.inst[n] : 0;
   const double dx = a.p.level_dx[a.m.level[n]];
-  const double a0n = uin[H::IA0], a1n = uin[H::IA1];
-  double       st0, st1;
-  source_factors_fp64<2>(uin, a.p, st0, st1);
-  for (int dir = 0; dir < 2; ++dir)
+  // a cell next to two finer faces is handled by the lower face index
+#pragma unroll
+  for (int f2 = 0; f2 < 4; ++f2)
+    if (f2 < face && dsl[f2] >= 0 && (f2 >> 1 == 0 ? ci : cj) == ((f2 & 1) ? B - 1 : 0))
+      return;
+  // wave 3: reflux slots of the fine faces this cell touches
+  bool fine[4];
+  int  rs[4];
+#pragma unroll
+  for (int f = 0; f < 4; ++f)
   {
-    const int cd = dir == 0 ? ci : cj;
-    const int ct = dir == 0 ? cj : ci; // transverse coordinate
-    double    acc[7];
-    for (int k = 0; k < 7; ++k)
-      acc[k] = 0.0;
-    for (int side = 0; side < 2; ++side)
+    const int cd = (f >> 1) == 0 ? ci : cj;
+    fine[f] = cd == ((f & 1) ? B - 1 : 0) && dsl[f] >= 0;
+    rs[f] = (fine[f] && Fn[f] >= 0 && Fn[f] < a.m.n_owned) ? a.m.reflux_slot[Fn[f] * 4 + (f ^ 1)] : -1;
+  }
+#pragma unroll
+  for (int f = 0; f < 4; ++f)
+    if (fine[f] && rs[f] < 0)
     {
-      const int  fface = 2 * dir + side;
-      const bool fine = (side == 0 ? cd == 0 : cd == B - 1) && dsl[fface] >= 0;
-      double     fv[8];
-      if (fine)
+      raise_status(a.status, STATUS_MESH);
+      return;
+    }
+  // wave 4: the face fluxes: own faces from the record, fine faces from the
+  // two fine faces' published fluxes
+  const double * own = a.defer_buf + ((size_t)dsl[face] * B + pos) * 32;
+  double         F0[4][8], F1[4][8];
+#pragma unroll
+  for (int f = 0; f < 4; ++f)
+  {
+    const int      ct = (f >> 1) == 0 ? cj : ci;
+    const int      fl = 2 * ct - ((2 * ct) / B) * B;
+    const double * p0 = fine[f] ? a.reflux_buf + ((size_t)rs[f] * B + fl) * 8 : own + f * 8;
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+    {
+      F0[f][k] = p0[k];
+      F1[f][k] = fine[f] ? p0[8 + k] : 0.0;
+    }
+  }
+  if constexpr (MIXED)
+  {
+    // FP32-bulk form: per-direction increments as float pairs (a fine face
+    // side is the exact float-float sum of its two fine faces, / 4), applied
+    // as in the step kernel
+    const bool stiff = a.p.gpx[0] != 0.0 || a.p.gpx[1] != 0.0;
+    float      a0f = d2f_fast(uin[H::IA0]), a1f = d2f_fast(uin[H::IA1]);
+    {
+      float st0f, st1f;
+      source_factors_mixed<2>(uin, a.p, stiff, st0f, st1f);
+      a0f *= st0f;
+      a1f *= st1f;
+    }
+    float     h[2][5], l[2][5], dA[2][2];
+    const int ks[5] = { H::FR0, H::FR1, H::FE, H::FU, H::FV };
+#pragma unroll
+    for (int dir = 0; dir < 2; ++dir)
+    {
+      float Fh[2][8], Fl[2][8];
+#pragma unroll
+      for (int side = 0; side < 2; ++side)
       {
-        // fine neighbour across face `fface`: children touching the block
-        const int dxs = dir == 0 ? (side ? 1 : -1) : 0;
-        const int dys = dir == 1 ? (side ? 1 : -1) : 0;
-        const int s = (dxs + 1) + 3 * (dys + 1);
-        const int f = 2 * ct;
-        const int cht = f / B, fl = f - cht * B;
-        const int chd = side ? 0 : 1;
-        const int child = dir == 0 ? chd + 2 * cht : cht + 2 * chd;
-        const int F = a.m.nbr[(n * 9 + s) * 4 + child];
-        const int rs = (F >= 0 && F < a.m.n_owned) ? a.m.reflux_slot[F * 4 + (fface ^ 1)] : -1;
-        if (rs < 0)
-        {
-          raise_status(a.status, STATUS_MESH);
-          return;
-        }
-        const double * r0 = a.reflux_buf + ((size_t)rs * B + fl) * 8;
-        const double * r1 = r0 + 8;
+        const int f = 2 * dir + side;
+#pragma unroll
         for (int k = 0; k < 8; ++k)
         {
-          double sum = 0.0;
-          sum += r0[k];
-          sum += r1[k];
-          fv[k] = sum;
-        }
-        for (int k = 0; k < 7; ++k)
-          acc[k] = side == 0 ? acc[k] + fv[k] / 4.0 : acc[k] - fv[k] / 4.0;
-        const double us = fv[7];
-        if (side == 0)
-        {
-          acc[H::FA0] -= st0 * us * a0n / 4.0;
-          acc[H::FA1] -= st1 * us * a1n / 4.0;
-        }
-        else
-        {
-          acc[H::FA0] += st0 * us * a0n / 4.0;
-          acc[H::FA1] += st1 * us * a1n / 4.0;
+          if (fine[f])
+          {
+            float sh, sl;
+            two_sum(d2f_fast(F0[f][k]), d2f_fast(F1[f][k]), sh, sl);
+            Fh[side][k] = 0.25f * sh;
+            Fl[side][k] = 0.25f * sl;
+          }
+          else
+          {
+            Fh[side][k] = d2f_fast(F0[f][k]);
+            Fl[side][k] = 0.0f;
+          }
         }
       }
-      else
+#pragma unroll
+      for (int k = 0; k < 5; ++k)
       {
-        const double * fr = own + (2 * dir + side) * 8;
-        for (int k = 0; k < 7; ++k)
-          acc[k] = side == 0 ? acc[k] + fr[k] : acc[k] - fr[k];
-        const double us = fr[7];
-        if (side == 0)
+        float hh, ll;
+        two_diff(Fh[0][ks[k]], Fh[1][ks[k]], hh, ll);
+        h[dir][k] = hh;
+        l[dir][k] = ll + (Fl[0][ks[k]] - Fl[1][ks[k]]);
+      }
+      const float usl = Fh[0][H::FUS] + Fl[0][H::FUS], usr = Fh[1][H::FUS] + Fl[1][H::FUS];
+      dA[dir][0] = (((Fh[0][H::FA0] + Fl[0][H::FA0]) - usl * a0f) - (Fh[1][H::FA0] + Fl[1][H::FA0])) + usr * a0f;
+      dA[dir][1] = (((Fh[0][H::FA1] + Fl[0][H::FA1]) - usl * a1f) - (Fh[1][H::FA1] + Fl[1][H::FA1])) + usr * a1f;
+    }
+    const float m_inv = apply_mixed_2d(uin, u2, h, l, dA, d2f_fast(dx), a.p, stiff, a.invdt != nullptr);
+    double *    out = a.U2 + (size_t)n * H::NV * NC + cell;
+    bool        finite = true;
+#pragma unroll
+    for (int v = 0; v < H::NV; ++v)
+    {
+      out[v * NC] = u2[v];
+      finite = finite && finite_bits(u2[v]);
+    }
+    if (!finite)
+      raise_status(a.status, STATUS_NONPHYSICAL);
+    if (a.invdt)
+      atomic_max_pos_warp(a.invdt, ins, (double)m_inv);
+  }
+  else
+  {
+    // update_U with the fine face sums of get_flux_from_fine_neighbor
+    // (ReadFluxesAndConservativeUpdateFunctor.h:256-307), X then Y
+    const double a0n = uin[H::IA0], a1n = uin[H::IA1];
+    double       st0, st1;
+    source_factors_fp64<2>(uin, a.p, st0, st1);
+#pragma unroll
+    for (int dir = 0; dir < 2; ++dir)
+    {
+      double acc[7];
+#pragma unroll
+      for (int k = 0; k < 7; ++k)
+        acc[k] = 0.0;
+#pragma unroll
+      for (int side = 0; side < 2; ++side)
+      {
+        const int f = 2 * dir + side;
+        if (fine[f])
         {
-          acc[H::FA0] -= st0 * us * a0n;
-          acc[H::FA1] -= st1 * us * a1n;
+          double fv[8];
+#pragma unroll
+          for (int k = 0; k < 8; ++k)
+          {
+            double sum = 0.0;
+            sum += F0[f][k];
+            sum += F1[f][k];
+            fv[k] = sum;
+          }
+#pragma unroll
+          for (int k = 0; k < 7; ++k)
+            acc[k] = side == 0 ? acc[k] + fv[k] / 4.0 : acc[k] - fv[k] / 4.0;
+          const double us = fv[7];
+          if (side == 0)
+          {
+            acc[H::FA0] -= st0 * us * a0n / 4.0;
+            acc[H::FA1] -= st1 * us * a1n / 4.0;
+          }
+          else
+          {
+            acc[H::FA0] += st0 * us * a0n / 4.0;
+            acc[H::FA1] += st1 * us * a1n / 4.0;
+          }
         }
         else
         {
-          acc[H::FA0] += st0 * us * a0n;
-          acc[H::FA1] += st1 * us * a1n;
+#pragma unroll
+          for (int k = 0; k < 7; ++k)
+            acc[k] = side == 0 ? acc[k] + F0[f][k] : acc[k] - F0[f][k];
+          const double us = F0[f][7];
+          if (side == 0)
+          {
+            acc[H::FA0] -= st0 * us * a0n;
+            acc[H::FA1] -= st1 * us * a1n;
+          }
+          else
+          {
+            acc[H::FA0] += st0 * us * a0n;
+            acc[H::FA1] += st1 * us * a1n;
+          }
         }
       }
+      const double eps = 1e-12;
+      u2[H::IAD0] += acc[H::FR0];
+      if (u2[H::IAD0] < eps)
+        u2[H::IAD0] = 0.0;
+      u2[H::IAD1] += acc[H::FR1];
+      if (u2[H::IAD1] < eps)
+        u2[H::IAD1] = 0.0;
+      u2[H::IA0] += acc[H::FA0];
+      if (u2[H::IA0] < eps)
+        u2[H::IA0] = 0.0;
+      if (u2[H::IA0] > 1.0 - eps)
+        u2[H::IA0] = 1.0;
+      u2[H::IA1] += acc[H::FA1];
+      if (u2[H::IA1] < eps)
+        u2[H::IA1] = 0.0;
+      if (u2[H::IA1] > 1.0 - eps)
+        u2[H::IA1] = 1.0;
+      u2[H::IE] += acc[H::FE];
+      u2[H::IU] += acc[H::FU];
+      u2[H::IV] += acc[H::FV];
     }
-    const double eps = 1e-12;
-    u2[H::IAD0] += acc[H::FR0];
-    if (u2[H::IAD0] < eps)
-      u2[H::IAD0] = 0.0;
-    u2[H::IAD1] += acc[H::FR1];
-    if (u2[H::IAD1] < eps)
-      u2[H::IAD1] = 0.0;
-    u2[H::IA0] += acc[H::FA0];
-    if (u2[H::IA0] < eps)
-      u2[H::IA0] = 0.0;
-    if (u2[H::IA0] > 1.0 - eps)
-      u2[H::IA0] = 1.0;
-    u2[H::IA1] += acc[H::FA1];
-    if (u2[H::IA1] < eps)
-      u2[H::IA1] = 0.0;
-    if (u2[H::IA1] > 1.0 - eps)
-      u2[H::IA1] = 1.0;
-    u2[H::IE] += acc[H::FE];
-    u2[H::IU] += acc[H::FU];
-    u2[H::IV] += acc[H::FV];
-  }
-  const double sum_alpha = u2[H::IA0] + u2[H::IA1];
-  const double sum_alpha_rho = u2[H::IAD0] + u2[H::IAD1];
-  const double inv = 1.0 / sum_alpha;
-  u2[H::IA0] *= inv;
-  u2[H::IA1] *= inv;
-  u2[H::ID] = sum_alpha_rho;
-  double * out = a.U2 + (size_t)n * H::NV * NC + cell;
-  bool     finite = true;
-  for (int v = 0; v < H::NV; ++v)
-  {
-    out[v * NC] = u2[v];
-    finite = finite && isfinite(u2[v]);
-  }
-  if (!finite)
-    raise_status(a.status, STATUS_NONPHYSICAL);
-  if (a.invdt)
-  {
-    if constexpr (MIXED)
+    const double sum_alpha = u2[H::IA0] + u2[H::IA1];
+    const double sum_alpha_rho = u2[H::IAD0] + u2[H::IAD1];
+    const double inv = 1.0 / sum_alpha;
+    u2[H::IA0] *= inv;
+    u2[H::IA1] *= inv;
+    u2[H::ID] = sum_alpha_rho;
+    double * out = a.U2 + (size_t)n * H::NV * NC + cell;
+    bool     finite = true;
+#pragma unroll
+    for (int v = 0; v < H::NV; ++v)
     {
-      float       df, ux, uy, uz, a0;
-      const bool  stiff = a.p.gpx[0] != 0.0 || a.p.gpx[1] != 0.0;
-      const float p = pressure_mixed<2>(u2, a.p, stiff, df, ux, uy, uz, a0);
-      const float c = sound_speed_f(a.p.f_xi[0], a.p.f_xi[1], a.p.f_gpx[0], a.p.f_gpx[1], df, p, fmaxf(0.0f, fminf(1.0f, a0)));
-      atomic_max_pos(a.invdt + ins, (double)(((c + fabsf(ux)) + (c + fabsf(uy))) * __frcp_rn(d2f_fast(dx))));
+      out[v * NC] = u2[v];
+      finite = finite && isfinite(u2[v]);
     }
-    else
+    if (!finite)
+      raise_status(a.status, STATUS_NONPHYSICAL);
+    if (a.invdt)
     {
       double       q[6];
       const double c = prim_fp64<2>(u2, q, a.p);
-      atomic_max_pos(a.invdt + ins, (c + fabs(q[V<2>::QU])) / dx + (c + fabs(q[V<2>::QV])) / dx);
+      atomic_max_pos_warp(a.invdt, ins, (c + fabs(q[V<2>::QU])) / dx + (c + fabs(q[V<2>::QV])) / dx);
     }
   }
 }

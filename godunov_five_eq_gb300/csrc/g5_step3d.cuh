@@ -46,7 +46,7 @@ neg_zero(float x)
 
 // conservative state seen by ghost cell g of block n (3D); false on a bad index
 __device__ __forceinline__ bool
-gather_ghost_3d(const StepArgs & a, int n, const int * g, double * u)
+gather_ghost_3d(const StepArgs & a, int n, const int * c0, const int * g, double * u)
 {
   using H = V<3>;
   constexpr int B = 8, NC = 512;
@@ -58,8 +58,11 @@ gather_ghost_3d(const StepArgs & a, int n, const int * g, double * u)
     v[e] = g[e] - d[e] * B;
   }
   const int   s = (d[0] + 1) + 3 * (d[1] + 1) + 9 * (d[2] + 1);
+  // relation and the 8 neighbour entries in one wave (two 16-byte loads)
   const int   rel = a.m.nbr_rel[n * 27 + s];
-  const int * nb = a.m.nbr + (n * 27 + s) * 8;
+  const int4  nb_lo = *reinterpret_cast<const int4 *>(a.m.nbr + (n * 27 + s) * 8);
+  const int4  nb_hi = *reinterpret_cast<const int4 *>(a.m.nbr + (n * 27 + s) * 8 + 4);
+  const int   nb[8] = { nb_lo.x, nb_lo.y, nb_lo.z, nb_lo.w, nb_hi.x, nb_hi.y, nb_hi.z, nb_hi.w };
   if (rel <= 0)
   {
     const int src = nb[0];
@@ -68,7 +71,7 @@ gather_ghost_3d(const StepArgs & a, int n, const int * g, double * u)
     int c[3];
 #pragma unroll
     for (int e = 0; e < 3; ++e)
-      c[e] = rel == 0 ? v[e] : ((a.m.coord[n * 3 + e] + d[e]) & 1) * (B / 2) + (v[e] >> 1);
+      c[e] = rel == 0 ? v[e] : ((c0[e] + d[e]) & 1) * (B / 2) + (v[e] >> 1);
     const double * base = a.U + (size_t)src * H::NV * NC + c[0] + B * (c[1] + B * c[2]);
 #pragma unroll
     for (int k = 0; k < H::NV; ++k)
@@ -305,6 +308,7 @@ step3d_kernel(StepArgs a)
     const int    n = a.work ? a.work[iw] : iw;
     const int    ins = a.m.inst ? a.m.inst[n] : 0;
     const double dx = P.level_dx[a.m.level[n]];
+    const int    c0[3] = { a.m.coord[n * 3 + 0], a.m.coord[n * 3 + 1], a.m.coord[n * 3 + 2] };
     R            dtdx_r;
     if constexpr (MIXED)
       dtdx_r = d2f_fast(a.dt[ins]) * __frcp_rn(d2f_fast(dx));
@@ -326,7 +330,7 @@ step3d_kernel(StepArgs a)
       if (g[0] >= 0 && g[0] < B && g[1] >= 0 && g[1] < B && g[2] >= 0 && g[2] < B)
         continue;
       double u[H::NV];
-      if (!gather_ghost_3d(a, n, g, u))
+      if (!gather_ghost_3d(a, n, c0, g, u))
       {
         raise_status(a.status, STATUS_MESH);
 #pragma unroll
@@ -336,6 +340,17 @@ step3d_kernel(StepArgs a)
       store_prim3<MIXED>(sQ, h, u, P, stiff);
     }
     __syncthreads();
+    // the next block of this CTA: its own cells and table rows into L2
+    if (tid < 3 && iw + (int)gridDim.x < nwalk)
+    {
+      const int nn = a.work ? a.work[iw + gridDim.x] : iw + (int)gridDim.x;
+      if (tid == 0)
+        prefetch_l2_range(a.U + (size_t)nn * H::NV * NC, (unsigned)(H::NV * NC * sizeof(double)));
+      else if (tid == 1)
+        prefetch_l2_line(a.m.nbr + (size_t)nn * 27 * 8);
+      else
+        prefetch_l2_line(a.m.nbr_rel + (size_t)nn * 27);
+    }
 
     // ---------------- phase 2: ring cells: Hancock source (and THINC |n|)
     for (int r = tid; r < SSS; r += NT)
@@ -605,8 +620,8 @@ step3d_kernel(StepArgs a)
           float s, t, s2, t2;
           two_sum(hh[0][k], hh[1][k], s, t);
           two_sum(s, hh[2][k], s2, t2);
-          t2 += t + ll[0][k] + ll[1][k] + ll[2][k];
-          u2[iv] = (u2[iv] + f2d_exact(s2)) + f2d_exact(t2);
+          two_sum(s2, t2 + (t + ll[0][k] + ll[1][k] + ll[2][k]), s2, t2);
+          u2[iv] += ff_to_d(s2, t2);
           if (dlt_pos(u2[iv], eps))
             u2[iv] = 0.0;
         }
@@ -651,7 +666,11 @@ step3d_kernel(StepArgs a)
       const int ive[4] = { H::IE, H::IU, H::IV, H::IW };
 #pragma unroll
       for (int e = 0; e < 4; ++e)
-        u2[ive[e]] = (u2[ive[e]] + f2d_exact(es[e])) + f2d_exact(et[e]);
+      {
+        float s, t;
+        two_sum(es[e], et[e], s, t);
+        u2[ive[e]] += ff_to_d(s, t);
+      }
       const double sa = u2[H::IA0] + u2[H::IA1];
       const double d = sa - 1.0;
       if (d != 0.0)
@@ -864,13 +883,13 @@ reflux3d_kernel(StepArgs a)
       const bool  stiff = a.p.gpx[0] != 0.0 || a.p.gpx[1] != 0.0;
       const float p = pressure_mixed<3>(u2, a.p, stiff, df, ux, uy, uz, a0);
       const float c = sound_speed_f(a.p.f_xi[0], a.p.f_xi[1], a.p.f_gpx[0], a.p.f_gpx[1], df, p, fmaxf(0.0f, fminf(1.0f, a0)));
-      atomic_max_pos(a.invdt + ins, (double)((((c + fabsf(ux)) + (c + fabsf(uy))) + (c + fabsf(uz))) * __frcp_rn(d2f_fast(dx))));
+      atomic_max_pos_warp(a.invdt, ins, (double)((((c + fabsf(ux)) + (c + fabsf(uy))) + (c + fabsf(uz))) * __frcp_rn(d2f_fast(dx))));
     }
     else
     {
       double       q[7];
       const double c = prim_fp64<3>(u2, q, a.p);
-      atomic_max_pos(a.invdt + ins, (c + fabs(q[H::QU])) / dx + (c + fabs(q[H::QV])) / dx + (c + fabs(q[H::QW])) / dx);
+      atomic_max_pos_warp(a.invdt, ins, (c + fabs(q[H::QU])) / dx + (c + fabs(q[H::QV])) / dx + (c + fabs(q[H::QW])) / dx);
     }
   }
 }
