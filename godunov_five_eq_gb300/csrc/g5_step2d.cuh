@@ -510,6 +510,7 @@ step2d_kernel(StepArgs a)
   R *          sFy = sFx + 8 * NFF;       // [8][NFF]  Y faces B x (B+1)
   using DtT = typename std::conditional<MIXED, float, double>::type;
   __shared__ DtT sRed[NT / 32];
+  __shared__ int sSlot[8]; // the block's reflux slots (faces 0-3), then its defer slots
   const int         tid = threadIdx.x;
   const PhysParams & P = a.p;
   // a stiffened-gas constant makes the pressure numerator cancel: FP64 there
@@ -521,6 +522,11 @@ step2d_kernel(StepArgs a)
     const int    n = a.work ? a.work[iw] : iw;
     const int    lev = a.m.level[n];
     const int    cx0 = a.m.coord[n * 3 + 0], cy0 = a.m.coord[n * 3 + 1];
+    // coarse/fine slots: loaded now, stored to shared memory at the end of the
+    // gather (their latency hides behind it)
+    int slot_v = -1;
+    if (a.m.reflux_slot && tid < 8)
+      slot_v = tid < 4 ? a.m.reflux_slot[n * 4 + tid] : a.m.defer_slot[n * 4 + tid - 4];
     const int    ins = a.m.inst ? a.m.inst[n] : 0;
     const double dx = P.level_dx[lev];
     R            dtdx_r;
@@ -530,6 +536,8 @@ step2d_kernel(StepArgs a)
       dtdx_r = a.dt[ins] / dx;
 
     // ---------------- phase 1: own cell (coalesced) + halo gather -> primitives
+    // (the own cell's loads are in flight while the halo gather runs; its
+    // primitives are stored last)
     const int ci = tid % B, cj = tid / B;
     double    uin[H::NV];
     {
@@ -537,7 +545,6 @@ step2d_kernel(StepArgs a)
 #pragma unroll
       for (int v = 0; v < H::NV; ++v)
         uin[v] = base[v * NC];
-      store_prim<B, MIXED>(sQ, (ci + 2) + G * (cj + 2), uin, P, stiff);
     }
     for (int h = tid; h < NHALO; h += NT)
     {
@@ -553,6 +560,9 @@ step2d_kernel(StepArgs a)
       }
       store_prim<B, MIXED>(sQ, (gx + 2) + G * (gy + 2), u, P, stiff);
     }
+    store_prim<B, MIXED>(sQ, (ci + 2) + G * (cj + 2), uin, P, stiff);
+    if (tid < 8)
+      sSlot[tid] = slot_v;
     __syncthreads();
     // the next block of this CTA: its own cells and table rows into L2 while
     // this block computes (its gather then hits L2 instead of HBM)
@@ -681,9 +691,10 @@ step2d_kernel(StepArgs a)
     // ---------------- publish coarse/fine records (AMR only)
     if (a.m.reflux_slot)
     {
+#pragma unroll
       for (int face = 0; face < 4; ++face)
       {
-        const int rs = a.m.reflux_slot[n * 4 + face];
+        const int rs = sSlot[face];
         if (rs >= 0 && tid < B)
         {
           // fine block face next to a coarser neighbour: publish its B face fluxes
@@ -695,7 +706,7 @@ step2d_kernel(StepArgs a)
           for (int k = 0; k < 8; ++k)
             dst[k] = (double)src[k * NFF + idx];
         }
-        const int ds = a.m.defer_slot[n * 4 + face];
+        const int ds = sSlot[4 + face];
         if (ds >= 0 && tid < B)
         {
           // coarse cell next to a finer face: save its four own face fluxes
@@ -720,7 +731,7 @@ step2d_kernel(StepArgs a)
     bool deferred = false;
     if (a.m.defer_slot)
     {
-      const int * dsl = a.m.defer_slot + n * 4;
+      const int * dsl = sSlot + 4;
       deferred = (ci == 0 && dsl[0] >= 0) || (ci == B - 1 && dsl[1] >= 0) || (cj == 0 && dsl[2] >= 0) ||
                  (cj == B - 1 && dsl[3] >= 0);
     }

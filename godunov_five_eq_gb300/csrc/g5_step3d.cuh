@@ -297,6 +297,7 @@ step3d_kernel(StepArgs a)
   R *          sF = sN + T::NN * SSS; // [9][NFF] faces of the current direction
   using DtT = typename std::conditional<MIXED, float, double>::type;
   __shared__ DtT     sRed[NT / 32];
+  __shared__ int     sSlot[12]; // the block's reflux slots (faces 0-5), then its defer slots
   const int          tid = threadIdx.x;
   const PhysParams & P = a.p;
   const bool         stiff = P.gpx[0] != 0.0 || P.gpx[1] != 0.0;
@@ -309,6 +310,9 @@ step3d_kernel(StepArgs a)
     const int    ins = a.m.inst ? a.m.inst[n] : 0;
     const double dx = P.level_dx[a.m.level[n]];
     const int    c0[3] = { a.m.coord[n * 3 + 0], a.m.coord[n * 3 + 1], a.m.coord[n * 3 + 2] };
+    int          slot_v = -1; // coarse/fine slots, stored to shared memory after the gather
+    if (a.m.reflux_slot && tid < 12)
+      slot_v = tid < 6 ? a.m.reflux_slot[n * 6 + tid] : a.m.defer_slot[n * 6 + tid - 6];
     R            dtdx_r;
     if constexpr (MIXED)
       dtdx_r = d2f_fast(a.dt[ins]) * __frcp_rn(d2f_fast(dx));
@@ -339,6 +343,8 @@ step3d_kernel(StepArgs a)
       }
       store_prim3<MIXED>(sQ, h, u, P, stiff);
     }
+    if (tid < 12)
+      sSlot[tid] = slot_v;
     __syncthreads();
     // the next block of this CTA: its own cells and table rows into L2
     if (tid < 3 && iw + (int)gridDim.x < nwalk)
@@ -431,7 +437,7 @@ step3d_kernel(StepArgs a)
     __syncthreads();
 
     // deferred cells (next to a finer face) are finished by reflux3d_kernel
-    const int * dsl = a.m.defer_slot ? a.m.defer_slot + n * 6 : nullptr;
+    const int * dsl = a.m.defer_slot ? sSlot + 6 : nullptr;
     bool        deferred = false;
     if (dsl)
     {
@@ -524,8 +530,7 @@ step3d_kernel(StepArgs a)
         for (int side = 0; side < 2; ++side)
         {
           const int face = 2 * dir + side;
-          const int rs = a.m.reflux_slot[n * 6 + face];
-          const int ds = a.m.defer_slot[n * 6 + face];
+          const int rs = sSlot[face];
           // positions along the face: the two transverse coordinates (first, second)
           if (rs >= 0 && tid < B * B)
           {
@@ -540,7 +545,6 @@ step3d_kernel(StepArgs a)
             for (int k = 0; k < 9; ++k)
               dst[k] = (double)sF[k * NFF + fidx];
           }
-          (void)ds;
         }
         // own face fluxes of deferred cells, this direction (left then right)
         if (deferred)
