@@ -10,8 +10,10 @@ namespace g5
 {
 
 // FillOutsideCellFunctor::operator() (border_conditions/FillOutside.cpp:71-170):
-// one thread per outside cell; the faces are visited in order and the last
-// face that applies wins (as in the reference's face loop).
+// one thread per outside cell.  The reference visits the faces in order and
+// every face that applies rewrites the whole cell, so the last such face
+// wins: it is found first (from the outside block's row, read in one wave),
+// then the cell is copied once.
 template <int DIM, int B>
 __global__ void
 fill_outside_kernel(double * U, DevMesh m, PhysParams P)
@@ -24,28 +26,37 @@ fill_outside_kernel(double * U, DevMesh m, PhysParams P)
   const int o = (int)(gid / NC), c = (int)(gid % NC);
   const int nout = m.n_owned + o;
   const int nin = m.out_src[o];
+  int8_t    border[6], normal[3];
+#pragma unroll
+  for (int f = 0; f < 2 * DIM; ++f)
+    border[f] = m.out_border[o * 6 + f];
+#pragma unroll
+  for (int e = 0; e < DIM; ++e)
+    normal[e] = m.out_normal[o * 3 + e];
   if (nin < 0 || nin >= m.n_owned)
     return;
-  const int co[3] = { c % B, (c / B) % B, DIM == 3 ? c / (B * B) : 0 };
+  int last = -1;
+#pragma unroll
   for (int face = 0; face < 2 * DIM; ++face)
-  {
-    const int dir = face >> 1;
-    if (!(m.out_border[o * 6 + face] && m.out_normal[o * 3 + dir] != 0))
-      continue;
-    const int bc = P.bc[face];
-    int       ci[3] = { co[0], co[1], co[2] };
-    if (bc == 2)
-      ci[dir] = (face & 1) ? B - 1 : 0;
-    else if (bc == 3)
-      ci[dir] = B - 1 - co[dir];
-    else
-      continue;
-    const int cin = ci[0] + B * (ci[1] + B * ci[2]);
-    for (int v = 0; v < H::NV; ++v)
-      U[((size_t)nout * H::NV + v) * NC + c] = U[((size_t)nin * H::NV + v) * NC + cin];
-    if (bc == 3)
-      U[((size_t)nout * H::NV + H::IU + dir) * NC + c] *= -1;
-  }
+    if (border[face] && normal[face >> 1] != 0 && (P.bc[face] == 2 || P.bc[face] == 3))
+      last = face;
+  if (last < 0)
+    return;
+  const int dir = last >> 1, bc = P.bc[last];
+  int       ci[3] = { c % B, (c / B) % B, DIM == 3 ? c / (B * B) : 0 };
+  ci[dir] = bc == 2 ? ((last & 1) ? B - 1 : 0) : B - 1 - ci[dir];
+  const int      cin = ci[0] + B * (ci[1] + B * ci[2]);
+  const double * src = U + (size_t)nin * H::NV * NC + cin;
+  double *       dst = U + (size_t)nout * H::NV * NC + c;
+  double         u[H::NV];
+#pragma unroll
+  for (int v = 0; v < H::NV; ++v)
+    u[v] = src[v * NC];
+  if (bc == 3)
+    u[H::IU + dir] = -u[H::IU + dir];
+#pragma unroll
+  for (int v = 0; v < H::NV; ++v)
+    dst[v * NC] = u[v];
 }
 
 // ComputeDtFiveEqFunctor (scheme/ComputeDtFiveEqFunctor.cpp:87-134): one CTA
@@ -401,6 +412,52 @@ remap_kernel(const double * __restrict__ Uold, double * __restrict__ Unew, const
       }
     }
   }
+}
+
+// per-record rows of DeferInfo<DIM> for the records listed in `codes` (one
+// thread per record): everything the reflux pass needs before its data loads
+template <int DIM>
+__global__ void
+defer_info_kernel(DevMesh m, const int32_t * codes, int n, int32_t * info)
+{
+  using D = DeferInfo<DIM>;
+  constexpr int NF = 2 * DIM, NS = DIM == 2 ? 9 : 27, NCH = 1 << DIM;
+  const int     r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n)
+    return;
+  const int code = codes[r];
+  const int nb = code >> 3;
+  int32_t * row = info + (size_t)r * D::STRIDE;
+  row[0] = code;
+  for (int f = 0; f < NF; ++f)
+  {
+    const int ds = m.defer_slot[nb * NF + f];
+    row[1 + f] = ds;
+    const int dir = f >> 1, side = f & 1;
+    int       d[3] = { 0, 0, 0 };
+    d[dir] = side ? 1 : -1;
+    const int s = (d[0] + 1) + 3 * (d[1] + 1) + (DIM == 3 ? 9 * (d[2] + 1) : 0);
+    for (int c = 0; c < D::NCF; ++c)
+    {
+      int rs = -1;
+      if (ds >= 0)
+      {
+        int ch[3] = { 0, 0, 0 };
+        ch[dir] = side ? 0 : 1;
+        const int e1 = dir == 0 ? 1 : 0, e2 = dir == 2 ? 1 : 2;
+        ch[e1] = c & 1;
+        if (DIM == 3)
+          ch[e2] = c >> 1;
+        const int F = m.nbr[((size_t)nb * NS + s) * NCH + ch[0] + 2 * ch[1] + 4 * ch[2]];
+        rs = (F >= 0 && F < m.n_owned) ? m.reflux_slot[F * NF + (f ^ 1)] : -1;
+      }
+      row[D::RS + f * D::NCF + c] = rs;
+    }
+  }
+  row[D::LEVEL] = m.level[nb];
+  row[D::INST] = m.inst ? m.inst[nb] : 0;
+  for (int k = D::INST + 1; k < D::STRIDE; ++k)
+    row[k] = 0;
 }
 
 } // namespace g5

@@ -21,6 +21,7 @@ struct G5Context
   // device block table
   int32_t *d_level = nullptr, *d_coord = nullptr, *d_nbr = nullptr, *d_inst = nullptr;
   int32_t *d_reflux_slot = nullptr, *d_defer_slot = nullptr, *d_defer_list = nullptr, *d_out_src = nullptr;
+  int32_t * d_defer_info = nullptr; // DeferInfo rows, in the order of d_defer_list
   int8_t * d_nbr_rel = nullptr, *d_out_normal = nullptr, *d_out_border = nullptr;
   // scratch
   double *       d_reflux_buf = nullptr, *d_defer_buf = nullptr;
@@ -54,11 +55,11 @@ struct G5Context
     int                  K = 0;
     std::vector<int>     lo;       // [K+1] owned-block bounds of the copy chunks
     std::vector<int>     work_off; // [K+1] launch k steps d_work[work_off[k] .. work_off[k+1])
-    std::vector<int>     rec_off;  // [K+1] launch k refluxes d_recs[rec_off[k] .. rec_off[k+1])
+    std::vector<int>     rec_off;  // [K+1] launch k refluxes records rec_off[k] .. rec_off[k+1] of d_defer_info
     std::vector<int>     out_off;  // [K+1] after launch k copy back chunks out_list[out_off[k] .. out_off[k+1])
     std::vector<int>     out_list;
     int32_t *            d_work = nullptr;
-    int32_t *            d_recs = nullptr;
+    std::vector<int32_t> recs; // record codes in launch order (the order of d_defer_list)
     double *             d_U = nullptr;  // staging of U, n_total blocks (first g5_step_host call)
     double *             d_U2 = nullptr; // staging of U2, n_owned blocks
     static constexpr int kComputeStreams = 8;
@@ -136,7 +137,7 @@ free_mesh(G5Context * c)
   void * ptrs[] = { c->d_level,       c->d_coord,       c->d_nbr,        c->d_inst,       c->d_reflux_slot,
                     c->d_defer_slot,  c->d_defer_list,  c->d_out_src,    c->d_nbr_rel,    c->d_out_normal,
                     c->d_out_border,  c->d_reflux_buf,  c->d_defer_buf,  c->d_dt,         c->d_invdt,
-                    c->d_step,        c->d_urk };
+                    c->d_step,        c->d_urk,         c->d_defer_info };
   for (void * p : ptrs)
     if (p)
       cudaFree(p);
@@ -146,10 +147,11 @@ free_mesh(G5Context * c)
   c->d_reflux_buf = c->d_defer_buf = c->d_dt = c->d_invdt = nullptr;
   c->d_step = nullptr;
   c->d_urk = nullptr;
-  for (void * p : { (void *)c->pipe.d_work, (void *)c->pipe.d_recs, (void *)c->pipe.d_U, (void *)c->pipe.d_U2 })
+  c->d_defer_info = nullptr;
+  for (void * p : { (void *)c->pipe.d_work, (void *)c->pipe.d_U, (void *)c->pipe.d_U2 })
     if (p)
       cudaFree(p);
-  c->pipe.d_work = c->pipe.d_recs = nullptr;
+  c->pipe.d_work = nullptr;
   c->pipe.d_U = c->pipe.d_U2 = nullptr;
   c->pipe.K = 0;
   for (auto & g : c->pipe.graphs)
@@ -175,6 +177,7 @@ dev_mesh(const G5Context * c)
   m.reflux_slot = (c->n_defer > 0) ? c->d_reflux_slot : nullptr;
   m.defer_slot = (c->n_defer > 0) ? c->d_defer_slot : nullptr;
   m.defer_list = c->d_defer_list;
+  m.defer_info = c->d_defer_info;
   m.out_src = c->d_out_src;
   m.out_normal = c->d_out_normal;
   m.out_border = c->d_out_border;
@@ -261,7 +264,9 @@ plan_host_pipe(G5Context * c, const G5Mesh * m, const std::vector<int32_t> & def
         if (nb[ch] >= 0 && nb[ch] < n_owned)
           final_[n] = final_[n] > ready[nb[ch]] ? final_[n] : ready[nb[ch]];
     }
-  std::vector<int32_t> work, recs;
+  std::vector<int32_t>   work;
+  std::vector<int32_t> & recs = hp.recs;
+  recs.clear();
   hp.work_off.assign(K + 1, 0);
   hp.rec_off.assign(K + 1, 0);
   for (int k = 0; k < K; ++k)
@@ -290,10 +295,7 @@ plan_host_pipe(G5Context * c, const G5Mesh * m, const std::vector<int32_t> & def
         hp.out_list.push_back(d);
   }
   hp.out_off[K] = (int)hp.out_list.size();
-  int rc = dev_upload(c, &hp.d_work, work.data(), work.size());
-  if (!recs.empty())
-    rc |= dev_upload(c, &hp.d_recs, recs.data(), recs.size());
-  return rc;
+  return dev_upload(c, &hp.d_work, work.data(), work.size());
 }
 
 } // namespace
@@ -519,7 +521,6 @@ g5_set_mesh(G5Context * c, const G5Mesh * m)
   {
     rc |= dev_upload(c, &c->d_reflux_slot, reflux_slot.data(), reflux_slot.size());
     rc |= dev_upload(c, &c->d_defer_slot, defer_slot.data(), defer_slot.size());
-    rc |= dev_upload(c, &c->d_defer_list, defer_list.data(), defer_list.size());
     rc |= dev_alloc(c, &c->d_reflux_buf, (size_t)n_reflux * face_cells * nf);
     rc |= dev_alloc(c, &c->d_defer_buf, (size_t)n_defer * face_cells * 2 * dim * nf);
   }
@@ -543,6 +544,22 @@ g5_set_mesh(G5Context * c, const G5Mesh * m)
   {
     free_mesh(c);
     return G5_ERR_CUDA;
+  }
+  if (n_defer > 0)
+  {
+    // records in the launch order of g5_step_host, and their reflux-pass rows
+    const std::vector<int32_t> & recs = c->pipe.recs;
+    const int stride = dim == 2 ? g5::DeferInfo<2>::STRIDE : g5::DeferInfo<3>::STRIDE;
+    rc = dev_upload(c, &c->d_defer_list, recs.data(), recs.size());
+    rc |= dev_alloc(c, &c->d_defer_info, recs.size() * (size_t)stride);
+    if (!rc && (g5::launch_defer_info(dim, dev_mesh(c), c->d_defer_list, (int)recs.size(), c->d_defer_info, nullptr) != cudaSuccess ||
+                cudaStreamSynchronize(nullptr) != cudaSuccess))
+      rc = 1;
+    if (rc)
+    {
+      free_mesh(c);
+      return G5_ERR_CUDA;
+    }
   }
   c->has_mesh = true;
   return G5_OK;
@@ -653,7 +670,7 @@ enqueue_host_step(G5Context * c, const double * h_U, double * h_U2, double * d_U
           ok = cudaStreamWaitEvent(q, hp.ev_step[j], 0) == cudaSuccess;
       a.work = hp.d_work; // non-null with n_work == 0: the launcher runs the record pass only
       a.n_work = 0;
-      a.m.defer_list = hp.d_recs + hp.rec_off[k];
+      a.m.defer_info = c->d_defer_info + (size_t)hp.rec_off[k] * (c->dim == 2 ? g5::DeferInfo<2>::STRIDE : g5::DeferInfo<3>::STRIDE);
       a.m.n_defer = n_rec;
       ok = ok && launch(a);
     }

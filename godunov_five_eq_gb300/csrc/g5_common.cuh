@@ -43,11 +43,26 @@ struct DevMesh
   const int32_t * reflux_slot; // [n_owned * 2*dim] slot in reflux_buf, or -1
   const int32_t * defer_slot;  // [n_owned * 2*dim] slot in defer_buf, or -1
   const int32_t * defer_list;  // [n_defer_slots] (block*8 + face) of each deferred record
+  const int32_t * defer_info;  // [n_defer][DEFER_INFO<DIM>] per record: code, defer slots of the
+                               // block, reflux slots of the fine faces, level, instance
   const int32_t * out_src;     // [n_outside]
   const int8_t *  out_normal;  // [n_outside*3]
   const int8_t *  out_border;  // [n_outside*6]
   int             n_owned, n_outside, n_total, n_inst;
   int             n_defer;
+};
+
+// row of the per-record table read by the reflux pass in one wave:
+// [0] block*8 + face, [1 .. 2*DIM] the block's defer slots per face,
+// then per face f and fine child c along the face (2 in 2D, 4 in 3D) the
+// reflux slot of that fine face (-1 if none), then level and instance
+template <int DIM>
+struct DeferInfo
+{
+  static constexpr int NCF = DIM == 2 ? 2 : 4;
+  static constexpr int RS = 1 + 2 * DIM;
+  static constexpr int LEVEL = RS + 2 * DIM * NCF, INST = LEVEL + 1;
+  static constexpr int STRIDE = DIM == 2 ? 16 : 36;
 };
 
 struct StepArgs

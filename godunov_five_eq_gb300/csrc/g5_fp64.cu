@@ -291,4 +291,16 @@ launch_remap(int dim, int b, const double * Uold, double * Unew, const int8_t * 
   return cudaErrorInvalidValue;
 }
 
+cudaError_t
+launch_defer_info(int dim, const DevMesh & m, const int32_t * codes, int n, int32_t * info, cudaStream_t s)
+{
+  if (n <= 0)
+    return cudaSuccess;
+  if (dim == 2)
+    defer_info_kernel<2><<<(n + 127) / 128, 128, 0, s>>>(m, codes, n, info);
+  else
+    defer_info_kernel<3><<<(n + 127) / 128, 128, 0, s>>>(m, codes, n, info);
+  return cudaGetLastError();
+}
+
 } // namespace g5

@@ -31,5 +31,7 @@ cudaError_t launch_refine_flags(int dim, int b, const double * U, const DevMesh 
 // block remap after a mesh adaptation (kind/src validated by the caller)
 cudaError_t launch_remap(int dim, int b, const double * Uold, double * Unew, const int8_t * kind, const int32_t * src, int n_new,
                          cudaStream_t s);
+// per-record rows of the reflux pass (DeferInfo) for `n` record codes
+cudaError_t launch_defer_info(int dim, const DevMesh & m, const int32_t * codes, int n, int32_t * info, cudaStream_t s);
 
 } // namespace g5

@@ -172,6 +172,8 @@ g5_step_static(const G5Params * params,
   off = align256(off + (n_defer > 0 ? sizeof(int32_t) * (size_t)n_owned * nfaces : 0));
   const size_t o_dlist = off;
   off = align256(off + sizeof(int32_t) * (size_t)n_defer);
+  const size_t o_dinfo = off; // DeferInfo rows of the reflux pass, built on the device
+  off = align256(off + sizeof(int32_t) * (size_t)n_defer * (dim == 2 ? g5::DeferInfo<2>::STRIDE : g5::DeferInfo<3>::STRIDE));
   const size_t o_rbuf = off;
   off = align256(off + sizeof(double) * (size_t)n_reflux * face_cells * nf);
   const size_t o_dbuf = off;
@@ -300,11 +302,15 @@ g5_step_static(const G5Params * params,
   a.m.reflux_slot = n_defer > 0 ? reinterpret_cast<const int32_t *>(base + o_rslot) : nullptr;
   a.m.defer_slot = n_defer > 0 ? reinterpret_cast<const int32_t *>(base + o_dslot) : nullptr;
   a.m.defer_list = n_defer > 0 ? reinterpret_cast<const int32_t *>(base + o_dlist) : nullptr;
+  a.m.defer_info = n_defer > 0 ? reinterpret_cast<const int32_t *>(base + o_dinfo) : nullptr;
   a.m.n_owned = n_owned;
   a.m.n_outside = n_outside;
   a.m.n_total = n_total;
   a.m.n_inst = n_inst;
   a.m.n_defer = n_defer;
+  if (n_defer > 0 &&
+      g5::launch_defer_info(dim, a.m, a.m.defer_list, n_defer, reinterpret_cast<int32_t *>(base + o_dinfo), s) != cudaSuccess)
+    return G5_ERR_CUDA;
   int         launches = 0;
   cudaError_t e = mode == G5_MODE_FP64 ? g5::launch_step_fp64(dim, b, a, 0, s, &launches)
                                        : g5::launch_step_mixed(dim, b, a, 0, s, &launches);

@@ -701,10 +701,11 @@ step2d_kernel(StepArgs a)
           const int dir = face >> 1, side = face & 1;
           const int idx = dir == 0 ? (side ? B : 0) + (B + 1) * tid : tid + B * (side ? B : 0);
           const R * src = dir == 0 ? sFx : sFy;
-          double *  dst = a.reflux_buf + ((size_t)rs * B + tid) * 8;
+          // the mixed form keeps the float fluxes (the buffer read as floats)
+          R * dst = reinterpret_cast<R *>(a.reflux_buf) + ((size_t)rs * B + tid) * 8;
 #pragma unroll
           for (int k = 0; k < 8; ++k)
-            dst[k] = (double)src[k * NFF + idx];
+            dst[k] = src[k * NFF + idx];
         }
         const int ds = sSlot[4 + face];
         if (ds >= 0 && tid < B)
@@ -713,15 +714,15 @@ step2d_kernel(StepArgs a)
           const int dir = face >> 1, side = face & 1;
           const int cx = dir == 0 ? (side ? B - 1 : 0) : tid;
           const int cy = dir == 0 ? tid : (side ? B - 1 : 0);
-          double *  dst = a.defer_buf + ((size_t)ds * B + tid) * 32;
+          R *       dst = reinterpret_cast<R *>(a.defer_buf) + ((size_t)ds * B + tid) * 32;
           const int fxl = cx + (B + 1) * cy, fyl = cx + B * cy;
 #pragma unroll
           for (int k = 0; k < 8; ++k)
           {
-            dst[0 * 8 + k] = (double)sFx[k * NFF + fxl];
-            dst[1 * 8 + k] = (double)sFx[k * NFF + fxl + 1];
-            dst[2 * 8 + k] = (double)sFy[k * NFF + fyl];
-            dst[3 * 8 + k] = (double)sFy[k * NFF + fyl + B];
+            dst[0 * 8 + k] = sFx[k * NFF + fxl];
+            dst[1 * 8 + k] = sFx[k * NFF + fxl + 1];
+            dst[2 * 8 + k] = sFy[k * NFF + fyl];
+            dst[3 * 8 + k] = sFy[k * NFF + fyl + B];
           }
         }
       }
@@ -781,85 +782,75 @@ step2d_kernel(StepArgs a)
 // ---------------------------------------------------------------------------
 // MIXED selects the FP32-bulk form of the mixed mode (float-pair increments
 // applied by apply_mixed_2d); the FP64 form replays the reference arithmetic.
-// All loads of a cell are issued in four waves (record, slots and own state,
-// fine-face indices, face fluxes) rather than one dependent chain per face:
-// a thread of this pass is latency-bound, and each L2 round trip counts.
+// A thread of this pass is latency-bound, so its loads come in two waves: the
+// record's DeferInfo row (slots, fine-face reflux slots, level, instance),
+// then the cell's old state and all face fluxes it needs.
 template <int B, bool MIXED>
 __global__ void
 reflux2d_kernel(StepArgs a)
 {
   using H = V<2>;
+  using D = DeferInfo<2>;
   constexpr int NC = B * B;
   const int     gid = blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= a.m.n_defer * B)
     return;
-  const int rec = gid / B, pos = gid % B;
-  const int code = a.m.defer_list[rec];
-  const int n = code >> 3, face = code & 7;
-  const int dirf = face >> 1, sidef = face & 1;
-  const int ci = dirf == 0 ? (sidef ? B - 1 : 0) : pos;
-  const int cj = dirf == 0 ? pos : (sidef ? B - 1 : 0);
-  const int cell = ci + B * cj;
-  // wave 2: the block's record slots, the cell's old state, the fine-face
-  // neighbour of every face (indices within the block's table rows)
-  int dsl[4], Fn[4];
-  double uin[H::NV], u2[H::NV];
+  const int   rec = gid / B, pos = gid % B;
+  const int4 * row = reinterpret_cast<const int4 *>(a.m.defer_info + (size_t)rec * D::STRIDE);
+  const int4  r0 = row[0], r1 = row[1], r2 = row[2], r3 = row[3];
+  const int   code = r0.x;
+  const int   dsl[4] = { r0.y, r0.z, r0.w, r1.x };
+  const int   rsf[4][2] = { { r1.y, r1.z }, { r1.w, r2.x }, { r2.y, r2.z }, { r2.w, r3.x } };
+  const int   n = code >> 3, face = code & 7;
+  const int   ins = r3.z;
+  const double dx = a.p.level_dx[r3.y];
+  const int   dirf = face >> 1, sidef = face & 1;
+  const int   ci = dirf == 0 ? (sidef ? B - 1 : 0) : pos;
+  const int   cj = dirf == 0 ? pos : (sidef ? B - 1 : 0);
+  const int   cell = ci + B * cj;
+  // a cell next to two finer faces is handled by the lower face index
+#pragma unroll
+  for (int f2 = 0; f2 < 4; ++f2)
+    if (f2 < face && dsl[f2] >= 0 && (f2 >> 1 == 0 ? ci : cj) == ((f2 & 1) ? B - 1 : 0))
+      return;
+  bool fine[4];
+  int  rs[4];
 #pragma unroll
   for (int f = 0; f < 4; ++f)
   {
-    dsl[f] = a.m.defer_slot[n * 4 + f];
-    const int dir = f >> 1, side = f & 1;
-    const int ct = dir == 0 ? cj : ci;
-    const int s = dir == 0 ? (side ? 5 : 3) : (side ? 7 : 1);
-    const int cht = (2 * ct) / B;
-    const int chd = side ? 0 : 1;
-    Fn[f] = a.m.nbr[(n * 9 + s) * 4 + (dir == 0 ? chd + 2 * cht : cht + 2 * chd)];
+    const int cd = (f >> 1) == 0 ? ci : cj, ct = (f >> 1) == 0 ? cj : ci;
+    fine[f] = cd == ((f & 1) ? B - 1 : 0) && dsl[f] >= 0;
+    rs[f] = fine[f] ? rsf[f][(2 * ct) / B] : -1;
+    if (fine[f] && rs[f] < 0)
+    {
+      raise_status(a.status, STATUS_MESH);
+      return;
+    }
   }
+  double uin[H::NV], u2[H::NV];
   {
     const double * ub = a.U + (size_t)n * H::NV * NC + cell;
 #pragma unroll
     for (int v = 0; v < H::NV; ++v)
       u2[v] = uin[v] = ub[v * NC];
   }
-  const int    ins = a.m.inst ? a.m.inst[n] : 0;
-  const double dx = a.p.level_dx[a.m.level[n]];
-  // a cell next to two finer faces is handled by the lower face index
-#pragma unroll
-  for (int f2 = 0; f2 < 4; ++f2)
-    if (f2 < face && dsl[f2] >= 0 && (f2 >> 1 == 0 ? ci : cj) == ((f2 & 1) ? B - 1 : 0))
-      return;
-  // wave 3: reflux slots of the fine faces this cell touches
-  bool fine[4];
-  int  rs[4];
+  // second wave (with the state): the face fluxes, own faces from the
+  // record, fine faces from the two fine faces' published fluxes (floats in
+  // the mixed form, doubles in the FP64 form)
+  using R = typename std::conditional<MIXED, float, double>::type;
+  const R * own = reinterpret_cast<const R *>(a.defer_buf) + ((size_t)dsl[face] * B + pos) * 32;
+  R         F0[4][8], F1[4][8];
 #pragma unroll
   for (int f = 0; f < 4; ++f)
   {
-    const int cd = (f >> 1) == 0 ? ci : cj;
-    fine[f] = cd == ((f & 1) ? B - 1 : 0) && dsl[f] >= 0;
-    rs[f] = (fine[f] && Fn[f] >= 0 && Fn[f] < a.m.n_owned) ? a.m.reflux_slot[Fn[f] * 4 + (f ^ 1)] : -1;
-  }
-#pragma unroll
-  for (int f = 0; f < 4; ++f)
-    if (fine[f] && rs[f] < 0)
-    {
-      raise_status(a.status, STATUS_MESH);
-      return;
-    }
-  // wave 4: the face fluxes: own faces from the record, fine faces from the
-  // two fine faces' published fluxes
-  const double * own = a.defer_buf + ((size_t)dsl[face] * B + pos) * 32;
-  double         F0[4][8], F1[4][8];
-#pragma unroll
-  for (int f = 0; f < 4; ++f)
-  {
-    const int      ct = (f >> 1) == 0 ? cj : ci;
-    const int      fl = 2 * ct - ((2 * ct) / B) * B;
-    const double * p0 = fine[f] ? a.reflux_buf + ((size_t)rs[f] * B + fl) * 8 : own + f * 8;
+    const int ct = (f >> 1) == 0 ? cj : ci;
+    const int fl = 2 * ct - ((2 * ct) / B) * B;
+    const R * p0 = fine[f] ? reinterpret_cast<const R *>(a.reflux_buf) + ((size_t)rs[f] * B + fl) * 8 : own + f * 8;
 #pragma unroll
     for (int k = 0; k < 8; ++k)
     {
       F0[f][k] = p0[k];
-      F1[f][k] = fine[f] ? p0[8 + k] : 0.0;
+      F1[f][k] = fine[f] ? p0[8 + k] : R(0);
     }
   }
   if constexpr (MIXED)
@@ -891,13 +882,13 @@ reflux2d_kernel(StepArgs a)
           if (fine[f])
           {
             float sh, sl;
-            two_sum(d2f_fast(F0[f][k]), d2f_fast(F1[f][k]), sh, sl);
+            two_sum(F0[f][k], F1[f][k], sh, sl);
             Fh[side][k] = 0.25f * sh;
             Fl[side][k] = 0.25f * sl;
           }
           else
           {
-            Fh[side][k] = d2f_fast(F0[f][k]);
+            Fh[side][k] = F0[f][k];
             Fl[side][k] = 0.0f;
           }
         }

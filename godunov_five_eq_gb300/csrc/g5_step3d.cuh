@@ -762,30 +762,48 @@ __global__ void
 reflux3d_kernel(StepArgs a)
 {
   using H = V<3>;
+  using D = DeferInfo<3>;
   constexpr int B = 8, NC = 512;
   const int     gid = blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= a.m.n_defer * B * B)
     return;
   const int rec = gid / (B * B), pos = gid % (B * B);
-  const int code = a.m.defer_list[rec];
+  // first wave: the record's DeferInfo row
+  int row[D::STRIDE];
+  {
+    const int4 * r4 = reinterpret_cast<const int4 *>(a.m.defer_info + (size_t)rec * D::STRIDE);
+#pragma unroll
+    for (int q = 0; q < D::STRIDE / 4; ++q)
+    {
+      const int4 v = r4[q];
+      row[4 * q] = v.x;
+      row[4 * q + 1] = v.y;
+      row[4 * q + 2] = v.z;
+      row[4 * q + 3] = v.w;
+    }
+  }
+  const int code = row[0];
   const int n = code >> 3, face = code & 7;
   const int dirf = face >> 1, sidef = face & 1;
   int       cc[3];
   cc[dirf] = sidef ? B - 1 : 0;
   cc[dirf == 0 ? 1 : 0] = pos % B;
   cc[dirf == 2 ? 1 : 2] = pos / B;
-  const int * dsl = a.m.defer_slot + n * 6;
-  for (int f2 = 0; f2 < face; ++f2)
-    if (dsl[f2] >= 0 && cc[f2 >> 1] == ((f2 & 1) ? B - 1 : 0))
+  const int * dsl = row + 1;
+#pragma unroll
+  for (int f2 = 0; f2 < 6; ++f2)
+    if (f2 < face && dsl[f2] >= 0 && cc[f2 >> 1] == ((f2 & 1) ? B - 1 : 0))
       return; // handled by the lower face index
+  // second wave: the cell's old state and the face fluxes
   const double * own = a.defer_buf + ((size_t)dsl[face] * B * B + pos) * 54;
   const int      cell = cc[0] + B * (cc[1] + B * cc[2]);
   const double * ub = a.U + (size_t)n * H::NV * NC + cell;
   double         uin[H::NV], u2[H::NV];
+#pragma unroll
   for (int v = 0; v < H::NV; ++v)
     u2[v] = uin[v] = ub[v * NC];
-  const int    ins = a.m.inst ? a.m.inst[n] : 0;
-  const double dx = a.p.level_dx[a.m.level[n]];
+  const int    ins = row[D::INST];
+  const double dx = a.p.level_dx[row[D::LEVEL]];
   const double a0n = uin[H::IA0], a1n = uin[H::IA1];
   double       st0, st1;
   source_factors_fp64<3>(uin, a.p, st0, st1);
@@ -801,10 +819,7 @@ reflux3d_kernel(StepArgs a)
       const bool fine = cc[dir] == (side ? B - 1 : 0) && dsl[fface] >= 0;
       if (fine)
       {
-        int d3[3] = { 0, 0, 0 };
-        d3[dir] = side ? 1 : -1;
-        const int s = (d3[0] + 1) + 3 * (d3[1] + 1) + 9 * (d3[2] + 1);
-        int       ch[3], fl[3];
+        int ch[3], fl[3];
         ch[dir] = side ? 0 : 1;
         fl[dir] = 0;
         for (int e = 0; e < 3; ++e)
@@ -814,8 +829,7 @@ reflux3d_kernel(StepArgs a)
             ch[e] = f / B;
             fl[e] = f - ch[e] * B;
           }
-        const int F = a.m.nbr[(n * 27 + s) * 8 + ch[0] + 2 * ch[1] + 4 * ch[2]];
-        const int rs = (F >= 0 && F < a.m.n_owned) ? a.m.reflux_slot[F * 6 + (fface ^ 1)] : -1;
+        const int rs = row[D::RS + fface * D::NCF + ch[e1] + 2 * ch[e2]];
         if (rs < 0)
         {
           raise_status(a.status, STATUS_MESH);
