@@ -544,18 +544,19 @@ hllc_fp32(const float * ql, const float * qr, float xi0, float xi1, float gp0, f
 // numerator, and does everything else on the FP32 and integer pipes.
 // ---------------------------------------------------------------------------
 
-// double -> float on the integer pipe: round half away from zero on the
-// magnitude bits, flush below FLT_MIN (values of the state stay far from
-// FLT_MAX).  The hardware conversion issues on the FP64 pipe.
+// double -> float on the integer pipe (the hardware conversion issues on the
+// FP64 pipe, 1.9 per clock per SM on GB300): the exponent and the top 23
+// mantissa bits move into float position with one funnel shift, the exponent
+// is rebiased by flipping its top bit (e - 896 mod 256), the mantissa is
+// truncated; magnitudes below FLT_MIN (zeros included) give a signed zero.
+// Values of the state stay far below FLT_MAX.
 __device__ __forceinline__ float
 d2f_fast(double x)
 {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x) + (1ull << 28);
-  const unsigned           hi = (unsigned)(b >> 32);
-  unsigned                 f = ((unsigned)(b >> 29) - (384u << 23)) & 0x7FFFFFFFu;
-  if ((hi & 0x7FFFFFFFu) < (897u << 20))
-    f = 0u;
-  return __uint_as_float(f | (hi & 0x80000000u));
+  const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+  const unsigned m = __funnelshift_l(lo, hi, 3); // e[8:0] m[51:29]
+  const unsigned f = (((m & 0x7FFFFFFFu) ^ 0x40000000u)) | (hi & 0x80000000u);
+  return __uint_as_float(((hi & 0x7FFFFFFFu) < (897u << 20)) ? (hi & 0x80000000u) : f);
 }
 
 // exact float -> double on the integer pipe (float denormals read as zero,

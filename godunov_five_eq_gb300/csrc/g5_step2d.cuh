@@ -269,6 +269,105 @@ face_state(const typename Step2DTraits<B, MIXED>::R * sQ,
   }
 }
 
+// The mixed form of face_state for a face direction known at compile time:
+// q = (q + hs) + off * dq_dir, with q + hs stored by the slope phase, so a
+// face side reads 11 values of shared memory instead of 21.
+template <int B, int DIR>
+__device__ __forceinline__ void
+face_state_mixed(const float * sQ, const float * sRec, int ci, int cj, int side, const PhysParams & P, float * q)
+{
+  using T = Step2DTraits<B, true>;
+  constexpr int G = T::G, S = T::S, GG = G * G, SS = S * S;
+  const int     gi = (ci + 2) + G * (cj + 2);
+  const int     si = (ci + 1) + S * (cj + 1);
+  const float   off = 0.5f * (float)side;
+  const float * dq = sRec + (DIR == 0 ? 0 : 5 * SS);
+#pragma unroll
+  for (int k = 0; k < 5; ++k)
+    q[k] = sRec[(10 + k) * SS + si] + off * dq[k * SS + si];
+  const float a0 = sQ[5 * GG + gi];
+  q[5] = a0;
+  if (P.thinc)
+  {
+    // THINC (scheme/ComputeFluxesAndStoreTHINCFunctor.cpp:122-283)
+    constexpr int o = DIR == 0 ? 1 : G;
+    const float * A = sQ + 5 * GG;
+    const float   aP = A[gi + o], aM = A[gi - o];
+    const float   mono = (aP - a0) * (a0 - aM);
+    const float   eps = P.f_thinc_eps;
+    if ((a0 > eps) && (a0 < 1.0f - eps) && mono > 0.0f)
+    {
+      const float nd = sRec[(15 + DIR) * SS + si];
+      const float beta = P.f_thinc_beta * nd + 0.01f;
+      const float Aa = (aP + aM) / 2.0f;
+      const float Bb = (aP - aM) / 2.0f;
+      const float C = tanhf(0.5f * beta);
+      const float D = tanhf(0.5f * beta * (a0 - Aa) / Bb);
+      const float bs = (float)side;
+      const float af = Aa + bs * Bb * (C + bs * D / C) / (1.0f + bs * D);
+      const float r0 = sQ[0 * GG + gi], r1 = sQ[1 * GG + gi];
+      // (r + hs) + r / a0 (af - a0): the partial densities rescaled (eq. 45)
+      q[0] = sRec[10 * SS + si] + r0 / a0 * (af - a0);
+      q[1] = sRec[11 * SS + si] + r1 / (1.0f - a0) * (a0 - af);
+      q[5] = af;
+    }
+  }
+  else
+  {
+    q[0] = fmaxf(P.f_smallr, q[0]);
+    q[1] = fmaxf(P.f_smallr, q[1]);
+  }
+}
+
+// HLLC flux of one face of the mixed form, scaled by dt/dx into the shared
+// flux arrays; DIR selects the face set (X faces (B+1) x B, Y faces B x (B+1))
+template <int B, int DIR>
+__device__ __forceinline__ void
+face_flux_mixed(const float * sQ, const float * sRec, float * sF, int ff, float dtdx, const PhysParams & P)
+{
+  using H = V<2>;
+  constexpr int NFF = B * (B + 1);
+  int           li, lj, ri, rj;
+  if (DIR == 0)
+  {
+    const int fi = ff % (B + 1), fj = ff / (B + 1);
+    li = fi - 1;
+    lj = fj;
+    ri = fi;
+    rj = fj;
+  }
+  else
+  {
+    const int fi = ff % B, fj = ff / B;
+    li = fi;
+    lj = fj - 1;
+    ri = fi;
+    rj = fj;
+  }
+  float qL[6], qR[6], fl[8];
+  face_state_mixed<B, DIR>(sQ, sRec, li, lj, +1, P, qL);
+  face_state_mixed<B, DIR>(sQ, sRec, ri, rj, -1, P, qR);
+  if (DIR == 1)
+  {
+    float t = qL[3];
+    qL[3] = qL[4];
+    qL[4] = t;
+    t = qR[3];
+    qR[3] = qR[4];
+    qR[4] = t;
+  }
+  hllc_fp32<2>(qL, qR, P.f_xi[0], P.f_xi[1], P.f_gpx[0], P.f_gpx[1], P.f_smallr, P.f_smallp, P.f_smallc, fl);
+  if (DIR == 1)
+  {
+    const float t = fl[H::FU];
+    fl[H::FU] = fl[H::FV];
+    fl[H::FV] = t;
+  }
+#pragma unroll
+  for (int k = 0; k < 8; ++k)
+    sF[k * NFF + ff] = fl[k] * dtdx;
+}
+
 // ReadFluxesAndConservativeUpdateFunctor (X then Y, update_U with the
 // per-direction clamps, .cpp:115-305, .h:319-349), FixVolumeFractionsNormalization
 // (.cpp:49-72) and the CFL rate of the new state (ComputeDtFiveEqFunctor.cpp:87-134),
@@ -621,11 +720,29 @@ step2d_kernel(StepArgs a)
         const R su0 = (-u * dux - dpx / rr) * dtdx_r + (-v * duy) * dtdy;
         const R sv0 = (-u * dvx) * dtdx_r + (-v * dvy - dpy / rr) * dtdy;
         const R sp0 = (-u * dpx - dux * rr * c * c) * dtdx_r + (-v * dpy - dvy * rr * c * c) * dtdy;
-        sRec[10 * SS + r] = R(0.5) * sr0_0;
-        sRec[11 * SS + r] = R(0.5) * sr0_1;
-        sRec[12 * SS + r] = R(0.5) * sp0;
-        sRec[13 * SS + r] = R(0.5) * su0;
-        sRec[14 * SS + r] = R(0.5) * sv0;
+        if constexpr (MIXED)
+        {
+          // the mixed form stores the predicted centre value q + hs
+          sRec[10 * SS + r] = q[0] + R(0.5) * sr0_0;
+          sRec[11 * SS + r] = q[1] + R(0.5) * sr0_1;
+          sRec[12 * SS + r] = q[2] + R(0.5) * sp0;
+          sRec[13 * SS + r] = q[3] + R(0.5) * su0;
+          sRec[14 * SS + r] = q[4] + R(0.5) * sv0;
+        }
+        else
+        {
+          sRec[10 * SS + r] = R(0.5) * sr0_0;
+          sRec[11 * SS + r] = R(0.5) * sr0_1;
+          sRec[12 * SS + r] = R(0.5) * sp0;
+          sRec[13 * SS + r] = R(0.5) * su0;
+          sRec[14 * SS + r] = R(0.5) * sv0;
+        }
+      }
+      else if constexpr (MIXED)
+      {
+#pragma unroll
+        for (int k = 0; k < 5; ++k)
+          sRec[(10 + k) * SS + r] = q[k];
       }
       if (P.thinc)
       {
@@ -638,6 +755,17 @@ step2d_kernel(StepArgs a)
     __syncthreads();
 
     // ---------------- phase 3: faces (X then Y) -> HLLC -> shared fluxes
+    if constexpr (MIXED)
+    {
+      for (int f = tid; f < 2 * NFF; f += NT)
+      {
+        if (f < NFF)
+          face_flux_mixed<B, 0>(sQ, sRec, sFx, f, dtdx_r, P);
+        else
+          face_flux_mixed<B, 1>(sQ, sRec, sFy, f - NFF, dtdx_r, P);
+      }
+    }
+    else
     for (int f = tid; f < 2 * NFF; f += NT)
     {
       const int dir = f >= NFF ? 1 : 0;
