@@ -28,6 +28,11 @@ struct G5Context
   double *       d_dt = nullptr, *d_invdt = nullptr;
   double *       d_urk = nullptr; // RK2_SSP intermediate stage (SolverGodunovFiveEq.h:349-358 m_U_RK)
   int *          d_step = nullptr;
+  // g5_step_batched: owned blocks grouped by instance (host), the call's work
+  // list and instance mask (device)
+  std::vector<int32_t> inst_blocks, inst_off;
+  int32_t *            d_batch_work = nullptr;
+  uint8_t *            d_inst_active = nullptr;
   unsigned int * d_status = nullptr;
   int64_t        bytes = 0;
   int            ctas_per_sm[2] = { 0, 0 };
@@ -146,6 +151,13 @@ free_mesh(G5Context * c)
   c->d_nbr_rel = c->d_out_normal = c->d_out_border = nullptr;
   c->d_reflux_buf = c->d_defer_buf = c->d_dt = c->d_invdt = nullptr;
   c->d_step = nullptr;
+  for (void * p : { (void *)c->d_batch_work, (void *)c->d_inst_active })
+    if (p)
+      cudaFree(p);
+  c->d_batch_work = nullptr;
+  c->d_inst_active = nullptr;
+  c->inst_blocks.clear();
+  c->inst_off.clear();
   c->d_urk = nullptr;
   c->d_defer_info = nullptr;
   for (void * p : { (void *)c->pipe.d_work, (void *)c->pipe.d_U, (void *)c->pipe.d_U2 })
@@ -545,6 +557,23 @@ g5_set_mesh(G5Context * c, const G5Mesh * m)
     free_mesh(c);
     return G5_ERR_CUDA;
   }
+  // owned blocks grouped by instance (counting sort, block order kept)
+  c->inst_off.assign(n_inst + 1, 0);
+  for (int n = 0; n < n_owned; ++n)
+    ++c->inst_off[(m->inst ? m->inst[n] : 0) + 1];
+  for (int i = 0; i < n_inst; ++i)
+    c->inst_off[i + 1] += c->inst_off[i];
+  c->inst_blocks.assign(n_owned, 0);
+  {
+    std::vector<int32_t> pos(c->inst_off.begin(), c->inst_off.end() - 1);
+    for (int n = 0; n < n_owned; ++n)
+      c->inst_blocks[pos[m->inst ? m->inst[n] : 0]++] = n;
+  }
+  if (dev_alloc(c, &c->d_batch_work, (size_t)n_owned) || dev_alloc(c, &c->d_inst_active, (size_t)n_inst))
+  {
+    free_mesh(c);
+    return G5_ERR_CUDA;
+  }
   if (n_defer > 0)
   {
     // records in the launch order of g5_step_host, and their reflux-pass rows
@@ -698,6 +727,55 @@ enqueue_host_step(G5Context * c, const double * h_U, double * h_U2, double * d_U
   return ok;
 }
 } // namespace
+
+extern "C" int
+g5_step_batched(G5Context * c, const double * d_U, double * d_U2, const double * d_dt, int mode, const int32_t * instances, int n_list,
+                double * d_inv_dt_out, void * stream)
+{
+  if (!c || !c->has_mesh || !d_U || !d_U2 || !d_dt || n_list < 0 || (n_list > 0 && !instances))
+    return G5_ERR_ARG;
+  if (mode != G5_MODE_FP64 && mode != G5_MODE_MIXED)
+    return G5_ERR_ARG;
+  if (!g5::step_supported(c->dim, c->b))
+    return G5_ERR_UNSUPPORTED;
+  std::vector<uint8_t> active((size_t)c->n_inst, 0);
+  for (int k = 0; k < n_list; ++k)
+  {
+    if (instances[k] < 0 || instances[k] >= c->n_inst)
+      return G5_ERR_ARG;
+    active[instances[k]] = 1;
+  }
+  std::vector<int32_t> work;
+  for (int i = 0; i < c->n_inst; ++i)
+    if (active[i])
+      work.insert(work.end(), c->inst_blocks.begin() + c->inst_off[i], c->inst_blocks.begin() + c->inst_off[i + 1]);
+  cudaStream_t s = (cudaStream_t)stream;
+  c->last_launches = 0;
+  if (work.empty())
+    return G5_OK;
+  // pageable sources: the copies are staged before the calls return
+  if (cudaMemcpyAsync(c->d_batch_work, work.data(), work.size() * sizeof(int32_t), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+      cudaMemcpyAsync(c->d_inst_active, active.data(), active.size(), cudaMemcpyHostToDevice, s) != cudaSuccess)
+    return G5_ERR_CUDA;
+  g5::StepArgs a;
+  a.U = d_U;
+  a.U2 = d_U2;
+  a.dt = d_dt;
+  a.reflux_buf = c->d_reflux_buf;
+  a.defer_buf = c->d_defer_buf;
+  a.invdt = d_inv_dt_out;
+  a.status = c->d_status;
+  a.work = c->d_batch_work;
+  a.n_work = (int)work.size();
+  a.inst_active = c->d_inst_active;
+  a.m = dev_mesh(c);
+  a.p = c->phys;
+  int         launches = 0;
+  cudaError_t e = mode == G5_MODE_FP64 ? g5::launch_step_fp64(c->dim, c->b, a, c->ctas_per_sm[0], s, &launches)
+                                       : g5::launch_step_mixed(c->dim, c->b, a, c->ctas_per_sm[1], s, &launches);
+  c->last_launches = launches;
+  return e == cudaSuccess ? G5_OK : G5_ERR_CUDA;
+}
 
 extern "C" int
 g5_step_host(G5Context * c, const double * h_U, double * h_U2, const double * dt_host, int mode, double * h_inv_dt_out, void * stream)

@@ -76,6 +76,7 @@ struct StepArgs
   unsigned int * status;
   const int32_t * work = nullptr; // owned blocks to step (null: all n_owned blocks in order)
   int             n_work = 0;     // entries of work
+  const uint8_t * inst_active = nullptr; // per instance: nonzero = stepped (null: all); read by the reflux pass
   DevMesh        m;
   PhysParams     p;
 };

@@ -931,6 +931,8 @@ reflux2d_kernel(StepArgs a)
   const int   rsf[4][2] = { { r1.y, r1.z }, { r1.w, r2.x }, { r2.y, r2.z }, { r2.w, r3.x } };
   const int   n = code >> 3, face = code & 7;
   const int   ins = r3.z;
+  if (a.inst_active && !a.inst_active[ins])
+    return;
   const double dx = a.p.level_dx[r3.y];
   const int   dirf = face >> 1, sidef = face & 1;
   const int   ci = dirf == 0 ? (sidef ? B - 1 : 0) : pos;

@@ -784,6 +784,8 @@ reflux3d_kernel(StepArgs a)
   }
   const int code = row[0];
   const int n = code >> 3, face = code & 7;
+  if (a.inst_active && !a.inst_active[row[D::INST]])
+    return;
   const int dirf = face >> 1, sidef = face & 1;
   int       cc[3];
   cc[dirf] = sidef ? B - 1 : 0;

@@ -103,6 +103,7 @@ EXPORTS = [
     "g5_step",
     "g5_step_dev",
     "g5_step_host",
+    "g5_step_batched",
     "g5_compute_inv_dt",
     "g5_fill_outside",
     "g5_begin",
@@ -144,6 +145,7 @@ def load_library(build_if_missing: bool = True):
     L.g5_step.argtypes = [vp, vp, vp, vp, ctypes.c_int, vp, vp]
     L.g5_step_dev.argtypes = [vp, vp, vp, vp, ctypes.c_int, vp, vp]
     L.g5_step_host.argtypes = [vp, vp, vp, vp, ctypes.c_int, vp, vp]
+    L.g5_step_batched.argtypes = [vp, vp, vp, vp, ctypes.c_int, vp, ctypes.c_int, vp, vp]
     L.g5_compute_inv_dt.argtypes = [vp, vp, vp, vp]
     L.g5_fill_outside.argtypes = [vp, vp, vp]
     L.g5_run.argtypes = [vp, vp, vp, ctypes.c_int, ctypes.c_int, vp, vp]
@@ -287,6 +289,23 @@ class GodunovImplemGB300:
         )
         if rc != 0:
             raise G5Error(rc, "g5_step_dev")
+
+    def do_time_step_batched(self, U, U2, dt_dev, instances, mode="fp64", inv_dt_out=None, stream=None):
+        """g5_step_batched: one step of the listed instances only (dt_dev[n_inst] on the device)."""
+        inst = np.ascontiguousarray(np.asarray(instances, dtype=np.int32).reshape(-1))
+        rc = self.lib.g5_step_batched(
+            self.ctx,
+            ctypes.c_void_p(_dptr(U)),
+            ctypes.c_void_p(_dptr(U2)),
+            ctypes.c_void_p(_dptr(dt_dev)),
+            MODES[mode],
+            inst.ctypes.data_as(ctypes.c_void_p),
+            int(inst.size),
+            ctypes.c_void_p(_dptr(inv_dt_out)) if inv_dt_out is not None else None,
+            _stream(stream),
+        )
+        if rc != 0:
+            raise G5Error(rc, "g5_step_batched")
 
     def do_time_step_host(self, U_host, U2_host, dt, mode="fp64", inv_dt_out=None, stream=None):
         """g5_step_host: U and U2 are CPU tensors (pinned for overlap); the copies

@@ -141,6 +141,22 @@ int g5_step(G5Context * ctx, const double * d_U, double * d_U2, const double * d
 /* Same as g5_step with dt read from device memory (d_dt[n_inst]). */
 int g5_step_dev(G5Context * ctx, const double * d_U, double * d_U2, const double * d_dt, int mode, double * d_inv_dt_out, void * stream);
 
+/* Batched form of g5_step_dev over a work list of instances: one step of the
+ * owned blocks of the instances listed in instances[n_list] (host array), each
+ * with its own dt (d_dt[instance]); the blocks of the other instances are not
+ * written in U2 and their CFL accumulators in d_inv_dt_out are left as they
+ * are.  Instances are independent meshes batched in one table (G5Mesh.inst),
+ * e.g. runs that reached their end time drop out of the list. */
+int g5_step_batched(G5Context * ctx,
+                    const double * d_U,
+                    double *       d_U2,
+                    const double * d_dt,
+                    int            mode,
+                    const int32_t * instances,
+                    int            n_list,
+                    double *       d_inv_dt_out,
+                    void *         stream);
+
 /* GodunovImplemBase::do_time_step for a caller whose U and U2 live in host
  * memory (pinned, for the copies to overlap): h_U[n_owned + n_outside blocks]
  * (outside blocks filled) is copied to a device staging array and h_U2's
