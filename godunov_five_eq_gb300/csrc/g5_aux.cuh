@@ -460,4 +460,77 @@ defer_info_kernel(DevMesh m, const int32_t * codes, int n, int32_t * info)
     row[k] = 0;
 }
 
+// ComputeDerivedQuantities::run (utils/ComputeDerivedQuantities.h:96-180):
+// one derived quantity per cell of blocks [oct_begin, oct_begin + num_octs),
+// FP64 in the reference's operation order.  quantity: 0 RHO_MIX,
+// 1 THERMAL_PRESSURE, 2 SPEED_OF_SOUND, 3 SPECIFIC_EKIN, 4 LOCAL_MACH_NUMBER,
+// 5 VX, 6 VY, 7 VZ (the DERIVED_QUANTITY enum order).
+template <int DIM, int B>
+__global__ void
+derived_kernel(const double * __restrict__ U, double * __restrict__ out, int quantity, long long oct_begin, long long num_octs,
+               PhysParams P)
+{
+  using H = V<DIM>;
+  constexpr int NC = DIM == 2 ? B * B : B * B * B;
+  const long long total = num_octs * NC;
+  for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (long long)gridDim.x * blockDim.x)
+  {
+    const long long oct = oct_begin + g / NC;
+    const int       cell = (int)(g % NC);
+    double          u[H::NV];
+#pragma unroll
+    for (int v = 0; v < H::NV; ++v)
+      u[v] = U[(oct * H::NV + v) * NC + cell];
+    double r = 0.0;
+    if (quantity == 0)
+      r = u[H::ID];
+    else if (quantity == 1 || quantity == 3)
+    {
+      // compute_mixture_ekin (models/utils.h:124-151): density from ID
+      const double d = fmax(u[H::ID], P.smallr);
+      const double ux = u[H::IU] / d, uy = u[H::IV] / d;
+      double       ekin;
+      if constexpr (DIM == 2)
+        ekin = 0.5 * (ux * ux + uy * uy);
+      else
+      {
+        const double uz = u[H::IW] / d;
+        ekin = 0.5 * (ux * ux + uy * uy + uz * uz);
+      }
+      if (quantity == 3)
+        r = ekin;
+      else
+      {
+        // compute_mixture_pressure (models/utils.h:160-185): density from the partial densities
+        const double dm = fmax(u[H::IAD0] + u[H::IAD1], P.smallr);
+        const double eint = u[H::IE] / dm - ekin;
+        const double a0 = u[H::IA0];
+        r = (dm * eint - eosPI(P, a0, 1 - a0)) / eosS(P, a0, 1 - a0);
+      }
+    }
+    else
+    {
+      double       q[7];
+      const double cs = prim_fp64<DIM>(u, q, P);
+      if (quantity == 2)
+        r = cs;
+      else if (quantity == 4)
+      {
+        double un = q[H::QU] * q[H::QU] + q[H::QV] * q[H::QV];
+        if constexpr (DIM == 3)
+          un += q[H::QW] * q[H::QW];
+        un = sqrt(un);
+        r = un / cs;
+      }
+      else if (quantity == 5)
+        r = q[H::QU];
+      else if (quantity == 6)
+        r = q[H::QV];
+      else if constexpr (DIM == 3)
+        r = q[H::QW];
+    }
+    out[oct * NC + cell] = r;
+  }
+}
+
 } // namespace g5

@@ -919,6 +919,20 @@ g5_step_host(G5Context * c, const double * h_U, double * h_U2, const double * dt
 }
 
 extern "C" int
+g5_derived_quantity(G5Context * c, const double * d_U, int quantity, int64_t oct_begin, int64_t num_octs, double * d_out, void * stream)
+{
+  if (!c || !d_U || !d_out || quantity < 0 || quantity > 7)
+    return G5_ERR_ARG;
+  // ComputeDerivedQuantities::check_args_validity (utils/ComputeDerivedQuantities.h:78-92)
+  const int64_t nq = c->has_mesh ? c->n_total : 0;
+  if (oct_begin < 0 || oct_begin >= nq || oct_begin + num_octs < 0 || oct_begin + num_octs > nq)
+    return G5_ERR_ARG;
+  return g5::launch_derived(c->dim, c->b, d_U, d_out, quantity, oct_begin, num_octs, c->phys, (cudaStream_t)stream) == cudaSuccess
+           ? G5_OK
+           : G5_ERR_CUDA;
+}
+
+extern "C" int
 g5_compute_inv_dt(G5Context * ctx, const double * d_U, double * d_inv_dt, void * stream)
 {
   if (!ctx || !ctx->has_mesh || !d_U || !d_inv_dt)

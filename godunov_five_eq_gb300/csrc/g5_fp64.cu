@@ -303,4 +303,32 @@ launch_defer_info(int dim, const DevMesh & m, const int32_t * codes, int n, int3
   return cudaGetLastError();
 }
 
+template <int DIM, int B>
+static cudaError_t
+derived_t(const double * U, double * out, int quantity, long long oct_begin, long long num_octs, const PhysParams & p, cudaStream_t s)
+{
+  constexpr int   NC = DIM == 2 ? B * B : B * B * B;
+  const long long total = num_octs * NC;
+  if (total <= 0)
+    return cudaSuccess;
+  long long grid = (total + 255) / 256;
+  if (grid > (long long)num_sms() * 16)
+    grid = (long long)num_sms() * 16;
+  derived_kernel<DIM, B><<<(unsigned)grid, 256, 0, s>>>(U, out, quantity, oct_begin, num_octs, p);
+  return cudaGetLastError();
+}
+
+cudaError_t
+launch_derived(int dim, int b, const double * U, double * out, int quantity, long long oct_begin, long long num_octs, const PhysParams & p,
+               cudaStream_t s)
+{
+  if (dim == 2 && b == 16)
+    return derived_t<2, 16>(U, out, quantity, oct_begin, num_octs, p, s);
+  if (dim == 2 && b == 8)
+    return derived_t<2, 8>(U, out, quantity, oct_begin, num_octs, p, s);
+  if (dim == 3 && b == 8)
+    return derived_t<3, 8>(U, out, quantity, oct_begin, num_octs, p, s);
+  return cudaErrorInvalidValue;
+}
+
 } // namespace g5

@@ -33,5 +33,8 @@ cudaError_t launch_remap(int dim, int b, const double * Uold, double * Unew, con
                          cudaStream_t s);
 // per-record rows of the reflux pass (DeferInfo) for `n` record codes
 cudaError_t launch_defer_info(int dim, const DevMesh & m, const int32_t * codes, int n, int32_t * info, cudaStream_t s);
+// derived quantity per cell (ComputeDerivedQuantities)
+cudaError_t launch_derived(int dim, int b, const double * U, double * out, int quantity, long long oct_begin, long long num_octs,
+                           const PhysParams & p, cudaStream_t s);
 
 } // namespace g5

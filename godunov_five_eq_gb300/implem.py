@@ -104,6 +104,7 @@ EXPORTS = [
     "g5_step_dev",
     "g5_step_host",
     "g5_step_batched",
+    "g5_derived_quantity",
     "g5_compute_inv_dt",
     "g5_fill_outside",
     "g5_begin",
@@ -146,6 +147,7 @@ def load_library(build_if_missing: bool = True):
     L.g5_step_dev.argtypes = [vp, vp, vp, vp, ctypes.c_int, vp, vp]
     L.g5_step_host.argtypes = [vp, vp, vp, vp, ctypes.c_int, vp, vp]
     L.g5_step_batched.argtypes = [vp, vp, vp, vp, ctypes.c_int, vp, ctypes.c_int, vp, vp]
+    L.g5_derived_quantity.argtypes = [vp, vp, ctypes.c_int, ctypes.c_int64, ctypes.c_int64, vp, vp]
     L.g5_compute_inv_dt.argtypes = [vp, vp, vp, vp]
     L.g5_fill_outside.argtypes = [vp, vp, vp]
     L.g5_run.argtypes = [vp, vp, vp, ctypes.c_int, ctypes.c_int, vp, vp]
@@ -331,6 +333,25 @@ class GodunovImplemGB300:
         )
         if rc != 0:
             raise G5Error(rc, "g5_step_host")
+
+    DERIVED_QUANTITIES = ("RHO_MIX", "THERMAL_PRESSURE", "SPEED_OF_SOUND", "SPECIFIC_EKIN", "LOCAL_MACH_NUMBER", "VX", "VY", "VZ")
+
+    def derived_quantity(self, U, quantity, oct_begin=0, num_octs=None, out=None, stream=None):
+        """g5_derived_quantity (ComputeDerivedQuantities::run): one quantity per cell
+        of blocks [oct_begin, oct_begin + num_octs) into out[n_blocks, 1, ncell]."""
+        import torch
+
+        q = self.DERIVED_QUANTITIES.index(quantity.upper()) if isinstance(quantity, str) else int(quantity)
+        n = self.table.n_total
+        num_octs = n - oct_begin if num_octs is None else num_octs
+        if out is None:
+            out = torch.zeros((n, 1, self.table.ncell), dtype=torch.float64, device=U.device)
+        rc = self.lib.g5_derived_quantity(
+            self.ctx, ctypes.c_void_p(_dptr(U)), q, int(oct_begin), int(num_octs), ctypes.c_void_p(_dptr(out)), _stream(stream)
+        )
+        if rc != 0:
+            raise G5Error(rc, "g5_derived_quantity")
+        return out
 
     def compute_inv_dt(self, U, out=None, stream=None):
         import torch

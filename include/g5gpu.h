@@ -170,6 +170,24 @@ int g5_step_batched(G5Context * ctx,
  * g5_set_mesh frees them. */
 int g5_step_host(G5Context * ctx, const double * h_U, double * h_U2, const double * dt_host, int mode, double * h_inv_dt_out, void * stream);
 
+/* derived quantities of ComputeDerivedQuantities (utils/ComputeDerivedQuantities.h:
+ * 42-51, the DERIVED_QUANTITY order) */
+#define G5_DQ_RHO_MIX 0
+#define G5_DQ_THERMAL_PRESSURE 1
+#define G5_DQ_SPEED_OF_SOUND 2
+#define G5_DQ_SPECIFIC_EKIN 3
+#define G5_DQ_LOCAL_MACH_NUMBER 4
+#define G5_DQ_VX 5
+#define G5_DQ_VY 6
+#define G5_DQ_VZ 7
+
+/* ComputeDerivedQuantities::run (utils/ComputeDerivedQuantities.h:96-180): one
+ * quantity per cell of blocks [oct_begin, oct_begin + num_octs) of d_U into
+ * d_out[n_blocks][1][bsize^dim] (other blocks of d_out untouched), FP64 in the
+ * reference's order.  The range must lie within the context's block table
+ * (owned + outside blocks), as check_args_validity requires. */
+int g5_derived_quantity(G5Context * ctx, const double * d_U, int quantity, int64_t oct_begin, int64_t num_octs, double * d_out, void * stream);
+
 /* ComputeDtFiveEqFunctor::apply (scheme/ComputeDtFiveEqFunctor.h:113-121):
  * d_inv_dt[n_inst] <- max over owned cells of sum_d (c+|u_d|)/dx. */
 int g5_compute_inv_dt(G5Context * ctx, const double * d_U, double * d_inv_dt, void * stream);

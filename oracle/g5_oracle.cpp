@@ -1552,3 +1552,55 @@ g5o_remap(const G5OParams * prm, int n_new, const int8_t * kind, const int32_t *
 {
   return prm->dim == 2 ? do_remap<2>(prm->b, n_new, kind, src, Uold, Unew) : do_remap<3>(prm->b, n_new, kind, src, Uold, Unew);
 }
+
+/* ---------------------------------------------------------------------------
+ * ComputeDerivedQuantities::run (utils/ComputeDerivedQuantities.h:96-180):
+ * quantity per cell of blocks [begin, begin + count); out[n_blocks][ncell].
+ * ------------------------------------------------------------------------- */
+template <int DIM>
+static int
+do_derived(const G5OParams * prm, const double * U, int quantity, long long begin, long long count, double * out)
+{
+  using H = Ids<DIM>;
+  const Settings s = make_settings(prm);
+  const int      b = prm->b;
+  const int      nc = DIM == 2 ? b * b : b * b * b;
+#pragma omp parallel for schedule(static)
+  for (long long oct = begin; oct < begin + count; ++oct)
+    for (int c = 0; c < nc; ++c)
+    {
+      double u[H::NV];
+      for (int v = 0; v < H::NV; ++v)
+        u[v] = U[(oct * H::NV + v) * nc + c];
+      double q[H::NV];
+      const double cs = computePrimitives<DIM>(u, q, s);
+      double       r = 0.0;
+      switch (quantity)
+      {
+      case 0: r = u[H::ID]; break;
+      case 1: r = compute_mixture_pressure<DIM>(u, s); break;
+      case 2: r = cs; break;
+      case 3: r = compute_mixture_ekin<DIM>(u, s); break;
+      case 4:
+      {
+        double un = q[H::IU] * q[H::IU] + q[H::IV] * q[H::IV];
+        if (DIM == 3)
+          un += q[H::IW] * q[H::IW];
+        un = sqrt(un);
+        r = un / cs;
+        break;
+      }
+      case 5: r = q[H::IU]; break;
+      case 6: r = q[H::IV]; break;
+      default: r = DIM == 3 ? q[H::IW] : 0.0; break;
+      }
+      out[oct * nc + c] = r;
+    }
+  return 0;
+}
+
+extern "C" int
+g5o_derived(const G5OParams * prm, const double * U, int quantity, long long begin, long long count, double * out)
+{
+  return prm->dim == 2 ? do_derived<2>(prm, U, quantity, begin, count, out) : do_derived<3>(prm, U, quantity, begin, count, out);
+}

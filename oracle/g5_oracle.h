@@ -90,6 +90,10 @@ int    g5o_refine_flags(void * ctx,
  * src[j*2^dim .. +2^dim-1]).  returns 0 */
 int    g5o_remap(const G5OParams * prm, int n_new, const int8_t * kind, const int32_t * src, const double * Uold, double * Unew);
 
+/* ComputeDerivedQuantities: quantity (0 RHO_MIX .. 7 VZ) per cell of blocks
+ * [begin, begin + count) into out[n_blocks][ncell].  returns 0 */
+int    g5o_derived(const G5OParams * prm, const double * U, int quantity, long long begin, long long count, double * out);
+
 /* point functions (used by the golden-vector pins) */
 double g5o_compute_primitives(const G5OParams * prm, const double * u, double * q);
 void   g5o_riemann_hllc(const G5OParams * prm, const double * qL, const double * qR, double * out);

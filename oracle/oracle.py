@@ -89,6 +89,7 @@ def lib():
         L.g5o_mixture_sound_speed.restype = ctypes.c_double
         L.g5o_mixture_sound_speed.argtypes = [ctypes.POINTER(G5OParams), ctypes.c_double, ctypes.c_double, ctypes.c_double]
         L.g5o_remap.argtypes = [ctypes.POINTER(G5OParams), ctypes.c_int, vp, vp, vp, vp]
+        L.g5o_derived.argtypes = [ctypes.POINTER(G5OParams), vp, ctypes.c_int, ctypes.c_longlong, ctypes.c_longlong, vp]
         _lib = L
     return _lib
 
@@ -225,6 +226,21 @@ def remap(params, rt, U_old: np.ndarray, n_total_new: int) -> np.ndarray:
     prm = make_params(params)
     lib().g5o_remap(ctypes.byref(prm), rt.n_new, _ptr(kind), _ptr(src), _ptr(U_old), _ptr(U_new))
     return U_new
+
+
+DERIVED_QUANTITIES = ("RHO_MIX", "THERMAL_PRESSURE", "SPEED_OF_SOUND", "SPECIFIC_EKIN", "LOCAL_MACH_NUMBER", "VX", "VY", "VZ")
+
+
+def derived(params, U: np.ndarray, quantity, begin=0, count=None) -> np.ndarray:
+    """ComputeDerivedQuantities on the CPU: out[n_blocks, 1, ncell] (zeros outside the range)."""
+    q = DERIVED_QUANTITIES.index(quantity.upper()) if isinstance(quantity, str) else int(quantity)
+    U = np.ascontiguousarray(U, np.float64)
+    n = U.shape[0]
+    count = n - begin if count is None else count
+    out = np.zeros((n, 1, U.shape[2]))
+    prm = make_params(params)
+    lib().g5o_derived(ctypes.byref(prm), _ptr(U), q, int(begin), int(count), _ptr(out))
+    return out
 
 
 def oracle_flag_fn(indicator=0, eps_refine=0.1, eps_coarsen=0.0125, eps_lohner=0.02):
