@@ -207,8 +207,9 @@ def cpu_baseline(t, p, U, max_seconds=20.0):
 
 
 def run_reference(args):
-    rank = int(os.environ.get("RANK", "0"))
-    if rank != 0:
+    from godunov_five_eq_gb300.replicas import rank_env
+
+    if rank_env()[1] != 0:
         return 0
     from oracle.oracle import Oracle, oracle_flag_fn
 
@@ -332,9 +333,9 @@ def main():
     import torch
     import torch.distributed as dist
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
+    from godunov_five_eq_gb300.replicas import max_over_ranks, rank_env, whole_job_rate
+
+    world, rank, local = rank_env()
     torch.cuda.set_device(local)
     if world > 1:
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
@@ -366,15 +367,12 @@ def main():
         if sampler:
             A, B = _load(impl, A, B, mode, 0.4)
         clocks = sampler.stop() if sampler else None
-        if world > 1:
-            tt = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            total_ms = float(tt.item())
+        total_ms = max_over_ranks(total_ms, device="cuda")
         d_dt = impl.compute_dt_local(A)
         kern_ms = time_kernel(impl, A, B, d_dt, mode, max(5, min(args.steps, 20)), flush, stream)
         res[mode] = dict(total_ms=total_ms, launches=launches, clocks=clocks, kern_ms=kern_ms, impl=impl)
-    value = world * cells * args.steps / (res["mixed"]["total_ms"] * 1e-3)
-    value64 = world * cells * args.steps / (res["fp64"]["total_ms"] * 1e-3)
+    value = whole_job_rate(world, cells, args.steps, res["mixed"]["total_ms"])
+    value64 = whole_job_rate(world, cells, args.steps, res["fp64"]["total_ms"])
 
     # accuracy of the mixed path: L1 against the FP64 path after the config's step count
     l1 = None
@@ -416,7 +414,7 @@ def main():
             e2e_ms += e0.elapsed_time(e1)
     blk = t.nv * t.ncell * 8
     e2e = {
-        "value": world * cells * args.steps / (e2e_ms * 1e-3),
+        "value": whole_job_rate(world, cells, args.steps, max_over_ranks(e2e_ms, device="cuda")),
         "unit": "cell-updates/s",
         "h2d_bytes_per_step": int(t.n_total * blk),
         "d2h_bytes_per_step": int(t.n_owned * blk),
