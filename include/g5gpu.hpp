@@ -12,6 +12,9 @@
 // plus the pieces of SolverGodunovFiveEq the step depends on:
 //   compute_dt_local(U)                ComputeDtFiveEqFunctor + cfl / invDt
 //   fill_outside_quadrants(U)          FillOutsideCellFunctor
+//   remap_block_data(map, Uold, Unew)  UserDataRemapper after a mesh adaptation
+//   compute_derived_quantity(U, q, o)  ComputeDerivedQuantities (output path)
+//   do_time_step_host(hU, hU2, dt)     do_time_step on host-resident arrays
 // Errors from the C ABI are thrown as g5::Error (the reference aborts).
 #pragma once
 
@@ -217,6 +220,23 @@ public:
     cudaFree(d_inv);
     g5::check(rc, "g5_compute_inv_dt");
     return m_params.cfl / inv[0];
+  }
+
+  //! do_time_step for a solver whose U and U2 live in host memory (pinned for the
+  //! copies to overlap the step): g5_step_host, then wait for the result
+  void do_time_step_host(const double * h_U, double * h_U2, double dt)
+  {
+    std::vector<double> dts(m_table.n_inst, dt);
+    g5::check(g5_step_host(m_ctx, h_U, h_U2, dts.data(), m_mode, nullptr, m_stream), "g5_step_host");
+    if (cudaStreamSynchronize(m_stream) != cudaSuccess)
+      throw g5::Error(G5_ERR_CUDA, "cudaStreamSynchronize");
+  }
+
+  //! ComputeDerivedQuantities::run (utils/ComputeDerivedQuantities.h:96-180) on all blocks:
+  //! out[n_blocks][1][bsize^dim] receives quantity G5_DQ_*
+  void compute_derived_quantity(const g5::BlockArray & U, int quantity, const g5::BlockArray & out)
+  {
+    g5::check(g5_derived_quantity(m_ctx, U.data, quantity, 0, U.n_blocks, out.data, m_stream), "g5_derived_quantity");
   }
 
   //! SolverGodunovFiveEq::fill_outside_quadrants

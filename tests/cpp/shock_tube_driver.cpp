@@ -3,7 +3,9 @@
 // godunov_five_eq::GodunovImplemGB300<2> (include/g5gpu.hpp) the way the
 // reference's SolverGodunovFiveEq::godunov_unsplit drives its implementation
 // (fill outside quadrants, dt, do_time_step, swap), checked bit for bit
-// against the CPU oracle on the same block table.  Prints "OK" on success.
+// against the CPU oracle on the same block table; then one step through host
+// buffers (g5_step_host) against the device step and the derived thermal
+// pressure against the oracle.  Prints "OK" on success.
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -132,6 +134,51 @@ main(int argc, char ** argv)
   {
     std::printf("%zu values differ\n", diff);
     return 1;
+  }
+  // ---- one more step through host buffers (g5_step_host) against the device step
+  {
+    double * hU = nullptr;
+    double * hO = nullptr;
+    if (cudaMallocHost(&hU, bytes) != cudaSuccess || cudaMallocHost(&hO, bytes) != cudaSuccess)
+      return 2;
+    impl.fill_outside_quadrants(A);
+    const double dt = impl.compute_dt_local(A);
+    cudaMemcpy(hU, A.data, bytes, cudaMemcpyDeviceToHost);
+    impl.do_time_step_host(hU, hO, dt);
+    impl.do_time_step(A, B, dt);
+    std::vector<double> D(U.size());
+    cudaMemcpy(D.data(), B.data, bytes, cudaMemcpyDeviceToHost);
+    size_t hd = 0;
+    for (size_t i = 0; i < (size_t)t.n_owned * nv * nc; ++i)
+      hd += hO[i] != D[i];
+    cudaFreeHost(hU);
+    cudaFreeHost(hO);
+    if (hd)
+    {
+      std::printf("host-buffer step: %zu values differ\n", hd);
+      return 1;
+    }
+  }
+  // ---- derived quantity (thermal pressure) against the oracle
+  {
+    g5::BlockArray P;
+    P.n_blocks = n_total;
+    if (cudaMalloc(&P.data, (size_t)n_total * nc * sizeof(double)) != cudaSuccess)
+      return 2;
+    impl.compute_derived_quantity(A, G5_DQ_THERMAL_PRESSURE, P);
+    std::vector<double> GP((size_t)n_total * nc), OP((size_t)n_total * nc);
+    cudaMemcpy(GP.data(), P.data, GP.size() * sizeof(double), cudaMemcpyDeviceToHost);
+    cudaMemcpy(G.data(), A.data, bytes, cudaMemcpyDeviceToHost);
+    g5o_derived(&op, G.data(), G5_DQ_THERMAL_PRESSURE, 0, n_total, OP.data());
+    cudaFree(P.data);
+    size_t pd = 0;
+    for (size_t i = 0; i < GP.size(); ++i)
+      pd += GP[i] != OP[i];
+    if (pd)
+    {
+      std::printf("derived pressure: %zu values differ\n", pd);
+      return 1;
+    }
   }
   std::printf("OK %d steps, %d blocks, %zu bytes of context memory\n", nsteps, t.n_owned, (size_t)impl.total_mem_size_in_bytes());
   cudaFree(A.data);
