@@ -2,8 +2,8 @@
 // block, persistent over the block list).
 //
 // Shared memory holds the 12^3 ghosted primitives, the Hancock half-step
-// source (and the THINC |normal|) of the 10^3 ring, and the face fluxes of
-// ONE direction.  The update runs direction by direction (X, Y, Z: the
+// source of the 10^3 ring, and the face fluxes of ONE direction (the THINC
+// normal is evaluated on demand, at interface cells only).  The update runs direction by direction (X, Y, Z: the
 // reference's order, GodunovImplemV0.cpp:121-139, with update_U's clamps after
 // each direction), the running state of each owned cell in registers.
 // Cells next to a finer face are deferred to reflux3d_kernel; fine blocks
@@ -27,10 +27,9 @@ struct Step3DTraits
   static constexpr int S = B + 2, SS = S * S, SSS = S * S * S; // ring extent
   static constexpr int NQ = 7;                                  // r0 r1 p u v w a0
   static constexpr int NHS = 6;                                 // Hancock source r0 r1 p u v w
-  static constexpr int NN = 3;                                  // THINC |n_d|
   static constexpr int NFF = (B + 1) * B * B;                   // faces of one direction
   static constexpr int NF = 9;                                  // r0 r1 a0 a1 e u v w ustar
-  static constexpr size_t smem_bytes = sizeof(R) * (size_t)(NQ * GGG + NHS * SSS + NN * SSS + NF * NFF) + 64;
+  static constexpr size_t smem_bytes = sizeof(R) * (size_t)(NQ * GGG + NHS * SSS + NF * NFF) + 64;
 };
 
 __device__ __forceinline__ bool
@@ -143,11 +142,34 @@ slope_at(const R * Qk, int gi, int o, R st)
 
 // reconstructed state of cell (ci,cj,ck) at its face in direction dir
 // (side +1: right face, side -1: left face); q[7] = r0 r1 p u v w a0
+// |n_dir| of the Youngs normal of the alpha field at ghosted index gi
+// ((1,2,1) x (1,2,1) weighted central differences, unit cell, n = -grad/|grad|),
+// evaluated where THINC needs it (interface cells only)
+template <typename R, int G, int GG>
+__device__ __forceinline__ R
+youngs_abs_3d(const R * A, int gi, int dir)
+{
+  const R w[3] = { R(1), R(2), R(1) };
+  R       g0 = R(0), g1 = R(0), g2 = R(0);
+  for (int cc = -1; cc <= 1; ++cc)
+    for (int bb = -1; bb <= 1; ++bb)
+    {
+      const R ww = w[bb + 1] * w[cc + 1];
+      g0 += ww * (A[gi + 1 + G * bb + GG * cc] - A[gi - 1 + G * bb + GG * cc]);
+      g1 += ww * (A[gi + bb + G + GG * cc] - A[gi + bb - G + GG * cc]);
+      g2 += ww * (A[gi + bb + G * cc + GG] - A[gi + bb + G * cc - GG]);
+    }
+  R nrm = g0 * g0 + g1 * g1;
+  nrm += g2 * g2;
+  nrm = sqrt(nrm);
+  const R gd = dir == 0 ? g0 : (dir == 1 ? g1 : g2);
+  return (nrm > R(0)) ? fabs(-gd / nrm) : R(0);
+}
+
 template <bool MIXED>
 __device__ __forceinline__ void
 face_state3(const typename Step3DTraits<MIXED>::R * sQ,
             const typename Step3DTraits<MIXED>::R * sHS,
-            const typename Step3DTraits<MIXED>::R * sN,
             int                                     ci,
             int                                     cj,
             int                                     ck,
@@ -216,7 +238,7 @@ face_state3(const typename Step3DTraits<MIXED>::R * sQ,
     const bool req = (a0 > thinc_eps) && (a0 < R(1) - thinc_eps) && mono > R(0);
     if (req)
     {
-      const R nd = sN[dir * SSS + si];
+      const R nd = youngs_abs_3d<R, G, GG>(A, gi, dir);
       const R beta = thinc_beta * nd + R(0.01);
       const R Aa = (aP + aM) / R(2);
       const R Bb = (aP - aM) / R(2);
@@ -293,8 +315,7 @@ step3d_kernel(StepArgs a)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   R *          sQ = reinterpret_cast<R *>(smem_raw);
   R *          sHS = sQ + T::NQ * GGG;
-  R *          sN = sHS + T::NHS * SSS;
-  R *          sF = sN + T::NN * SSS; // [9][NFF] faces of the current direction
+  R *          sF = sHS + T::NHS * SSS; // [9][NFF] faces of the current direction
   using DtT = typename std::conditional<MIXED, float, double>::type;
   __shared__ DtT     sRed[NT / 32];
   __shared__ int     sSlot[12]; // the block's reflux slots (faces 0-5), then its defer slots
@@ -412,27 +433,7 @@ step3d_kernel(StepArgs a)
         sHS[4 * SSS + r] = R(0.5) * sv0;
         sHS[5 * SSS + r] = R(0.5) * sw0;
       }
-      if (P.thinc)
-      {
-        // Youngs normal, (1,2,1)x(1,2,1) weights, unit cell
-        const R * A = sQ + 6 * GGG;
-        const R   w[3] = { R(1), R(2), R(1) };
-        R         g0 = R(0), g1 = R(0), g2 = R(0);
-        for (int cc = -1; cc <= 1; ++cc)
-          for (int bb = -1; bb <= 1; ++bb)
-          {
-            const R ww = w[bb + 1] * w[cc + 1];
-            g0 += ww * (A[gi + 1 + G * bb + GG * cc] - A[gi - 1 + G * bb + GG * cc]);
-            g1 += ww * (A[gi + bb + G + GG * cc] - A[gi + bb - G + GG * cc]);
-            g2 += ww * (A[gi + bb + G * cc + GG] - A[gi + bb + G * cc - GG]);
-          }
-        R nrm = g0 * g0 + g1 * g1;
-        nrm += g2 * g2;
-        nrm = sqrt(nrm);
-        sN[0 * SSS + r] = (nrm > R(0)) ? fabs(-g0 / nrm) : R(0);
-        sN[1 * SSS + r] = (nrm > R(0)) ? fabs(-g1 / nrm) : R(0);
-        sN[2 * SSS + r] = (nrm > R(0)) ? fabs(-g2 / nrm) : R(0);
-      }
+
     }
     __syncthreads();
 
@@ -489,8 +490,8 @@ step3d_kernel(StepArgs a)
           fk = f / (B * B);
         }
         R qL[7], qR[7], fl[9];
-        face_state3<MIXED>(sQ, sHS, sN, fi - (dir == 0), fj - (dir == 1), fk - (dir == 2), dir, +1, P, qL);
-        face_state3<MIXED>(sQ, sHS, sN, fi, fj, fk, dir, -1, P, qR);
+        face_state3<MIXED>(sQ, sHS, fi - (dir == 0), fj - (dir == 1), fk - (dir == 2), dir, +1, P, qL);
+        face_state3<MIXED>(sQ, sHS, fi, fj, fk, dir, -1, P, qR);
         const int iw = dir == 1 ? 4 : 5; // component swapped with u
         if (dir > 0)
         {
