@@ -28,7 +28,7 @@ struct Step2DTraits
   static constexpr int G = B + 4;  // ghosted extent
   static constexpr int S = B + 2;  // ring extent
   static constexpr int NQ = 6;     // r0 r1 p u v a0
-  static constexpr int NREC = 17;  // dqx[5] dqy[5] hS[5] |nx| |ny|
+  static constexpr int NREC = 15;  // dqx[5] dqy[5] hS[5] (the THINC normal is evaluated on demand)
   static constexpr int NFF = B * (B + 1);
   static constexpr size_t smem_bytes = sizeof(R) * (size_t)(NQ * G * G + NREC * S * S + 2 * 8 * NFF) + 64;
 };
@@ -231,7 +231,9 @@ face_state(const typename Step2DTraits<B, MIXED>::R * sQ,
     const bool req = (a0 > thinc_eps) && (a0 < R(1) - thinc_eps) && mono > R(0);
     if (req)
     {
-      const R nd = sRec[(15 + dir) * SS + si];
+      R nxa, nya;
+      youngs_abs_2d<R, G>(A, gi, nxa, nya);
+      const R nd = dir == 0 ? nxa : nya;
       const R beta = thinc_beta * nd + R(0.01);
       const R Aa = (aP + aM) / R(2);
       const R Bb = (aP - aM) / R(2);
@@ -297,7 +299,9 @@ face_state_mixed(const float * sQ, const float * sRec, int ci, int cj, int side,
     const float   eps = P.f_thinc_eps;
     if ((a0 > eps) && (a0 < 1.0f - eps) && mono > 0.0f)
     {
-      const float nd = sRec[(15 + DIR) * SS + si];
+      float nxa, nya;
+      youngs_abs_2d<float, G>(A, gi, nxa, nya);
+      const float nd = DIR == 0 ? nxa : nya;
       const float beta = P.f_thinc_beta * nd + 0.01f;
       const float Aa = (aP + aM) / 2.0f;
       const float Bb = (aP - aM) / 2.0f;
@@ -743,13 +747,6 @@ step2d_kernel(StepArgs a)
 #pragma unroll
         for (int k = 0; k < 5; ++k)
           sRec[(10 + k) * SS + r] = q[k];
-      }
-      if (P.thinc)
-      {
-        R nx, ny;
-        youngs_abs_2d<R, G>(sQ + 5 * GG, gi, nx, ny);
-        sRec[15 * SS + r] = nx;
-        sRec[16 * SS + r] = ny;
       }
     }
     __syncthreads();
