@@ -22,6 +22,8 @@ struct G5Context
   int32_t *d_level = nullptr, *d_coord = nullptr, *d_nbr = nullptr, *d_inst = nullptr;
   int32_t *d_reflux_slot = nullptr, *d_defer_slot = nullptr, *d_defer_list = nullptr, *d_out_src = nullptr;
   int32_t * d_defer_info = nullptr; // DeferInfo rows, in the order of d_defer_list
+  int32_t * d_twin_first = nullptr, *d_twin_list = nullptr; // outside blocks per owned source block
+  bool      fused_fill = false;                              // the 2D solver loop fills them in the step
   int8_t * d_nbr_rel = nullptr, *d_out_normal = nullptr, *d_out_border = nullptr;
   // scratch
   double *       d_reflux_buf = nullptr, *d_defer_buf = nullptr;
@@ -142,7 +144,7 @@ free_mesh(G5Context * c)
   void * ptrs[] = { c->d_level,       c->d_coord,       c->d_nbr,        c->d_inst,       c->d_reflux_slot,
                     c->d_defer_slot,  c->d_defer_list,  c->d_out_src,    c->d_nbr_rel,    c->d_out_normal,
                     c->d_out_border,  c->d_reflux_buf,  c->d_defer_buf,  c->d_dt,         c->d_invdt,
-                    c->d_step,        c->d_urk,         c->d_defer_info };
+                    c->d_step,        c->d_urk,         c->d_defer_info, c->d_twin_first, c->d_twin_list };
   for (void * p : ptrs)
     if (p)
       cudaFree(p);
@@ -160,6 +162,8 @@ free_mesh(G5Context * c)
   c->inst_off.clear();
   c->d_urk = nullptr;
   c->d_defer_info = nullptr;
+  c->d_twin_first = c->d_twin_list = nullptr;
+  c->fused_fill = false;
   for (void * p : { (void *)c->pipe.d_work, (void *)c->pipe.d_U, (void *)c->pipe.d_U2 })
     if (p)
       cudaFree(p);
@@ -190,6 +194,8 @@ dev_mesh(const G5Context * c)
   m.defer_slot = (c->n_defer > 0) ? c->d_defer_slot : nullptr;
   m.defer_list = c->d_defer_list;
   m.defer_info = c->d_defer_info;
+  m.twin_first = c->d_twin_first;
+  m.twin_list = c->d_twin_list;
   m.out_src = c->d_out_src;
   m.out_normal = c->d_out_normal;
   m.out_border = c->d_out_border;
@@ -202,7 +208,7 @@ dev_mesh(const G5Context * c)
 }
 
 int
-do_step(G5Context * c, const double * U, double * U2, const double * d_dt, int mode, double * invdt, cudaStream_t s)
+do_step(G5Context * c, const double * U, double * U2, const double * d_dt, int mode, double * invdt, cudaStream_t s, bool fill_twins = false)
 {
   if (!c || !c->has_mesh || !U || !U2 || !d_dt)
     return G5_ERR_ARG;
@@ -220,6 +226,7 @@ do_step(G5Context * c, const double * U, double * U2, const double * d_dt, int m
   a.status = c->d_status;
   a.m = dev_mesh(c);
   a.p = c->phys;
+  a.fill_twins = fill_twins ? 1 : 0;
   int         launches = 0;
   cudaError_t e = mode == G5_MODE_FP64 ? g5::launch_step_fp64(c->dim, c->b, a, c->ctas_per_sm[0], s, &launches)
                                        : g5::launch_step_mixed(c->dim, c->b, a, c->ctas_per_sm[1], s, &launches);
@@ -573,6 +580,40 @@ g5_set_mesh(G5Context * c, const G5Mesh * m)
   {
     free_mesh(c);
     return G5_ERR_CUDA;
+  }
+  // outside blocks per owned source block, with the face whose rule the
+  // boundary fill applies last (FillOutside.cpp:71-170)
+  {
+    std::vector<int32_t> first((size_t)n_owned + 1, 0), list;
+    std::vector<int32_t> entry((size_t)m->n_outside, -1);
+    for (int o = 0; o < m->n_outside; ++o)
+    {
+      int last = -1;
+      for (int f = 0; f < 2 * dim; ++f)
+        if (m->out_border[o * 6 + f] && m->out_normal[o * 3 + (f >> 1)] != 0 && (c->prm.bc[f] == 2 || c->prm.bc[f] == 3))
+          last = f;
+      if (last >= 0)
+      {
+        entry[o] = (n_owned + o) * 8 + last;
+        ++first[m->out_src[o] + 1];
+      }
+    }
+    for (int n = 0; n < n_owned; ++n)
+      first[n + 1] += first[n];
+    list.assign((size_t)first[n_owned], 0);
+    std::vector<int32_t> pos(first.begin(), first.end() - 1);
+    for (int o = 0; o < m->n_outside; ++o)
+      if (entry[o] >= 0)
+        list[pos[m->out_src[o]]++] = entry[o];
+    int trc = dev_upload(c, &c->d_twin_first, first.data(), first.size());
+    if (!list.empty())
+      trc |= dev_upload(c, &c->d_twin_list, list.data(), list.size());
+    if (trc)
+    {
+      free_mesh(c);
+      return G5_ERR_CUDA;
+    }
+    c->fused_fill = dim == 2 && m->n_outside > 0;
   }
   if (n_defer > 0)
   {
@@ -1054,11 +1095,13 @@ loop_step(G5Context * c, const double * U, double * U2, int mode, double * dt_ou
     }
     return G5_OK;
   }
-  int rc = do_step(c, U, U2, c->d_dt, mode, c->d_invdt, s);
+  // 2D: the step kernel fills the outside blocks of U2 itself (and the
+  // reflux pass patches the cells it finishes), so no separate fill launch
+  int rc = do_step(c, U, U2, c->d_dt, mode, c->d_invdt, s, c->fused_fill);
   if (rc)
     return rc;
   *launches += c->last_launches;
-  if (c->n_outside > 0)
+  if (c->n_outside > 0 && !c->fused_fill)
   {
     if (g5::launch_fill_outside(c->dim, c->b, U2, dev_mesh(c), c->phys, s) != cudaSuccess)
       return G5_ERR_CUDA;

@@ -45,6 +45,8 @@ struct DevMesh
   const int32_t * defer_list;  // [n_defer_slots] (block*8 + face) of each deferred record
   const int32_t * defer_info;  // [n_defer][DEFER_INFO<DIM>] per record: code, defer slots of the
                                // block, reflux slots of the fine faces, level, instance
+  const int32_t * twin_first;  // [n_owned + 1] CSR over the outside blocks filled from each owned block
+  const int32_t * twin_list;   // (outside block) * 8 + the last applicable face of FillOutside
   const int32_t * out_src;     // [n_outside]
   const int8_t *  out_normal;  // [n_outside*3]
   const int8_t *  out_border;  // [n_outside*6]
@@ -77,6 +79,7 @@ struct StepArgs
   const int32_t * work = nullptr; // owned blocks to step (null: all n_owned blocks in order)
   int             n_work = 0;     // entries of work
   const uint8_t * inst_active = nullptr; // per instance: nonzero = stepped (null: all); read by the reflux pass
+  int             fill_twins = 0;        // also fill U2's outside blocks (the solver loop's fill after the step)
   DevMesh        m;
   PhysParams     p;
 };

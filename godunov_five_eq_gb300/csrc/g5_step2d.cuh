@@ -613,7 +613,8 @@ step2d_kernel(StepArgs a)
   R *          sFy = sFx + 8 * NFF;       // [8][NFF]  Y faces B x (B+1)
   using DtT = typename std::conditional<MIXED, float, double>::type;
   __shared__ DtT sRed[NT / 32];
-  __shared__ int sSlot[8]; // the block's reflux slots (faces 0-3), then its defer slots
+  __shared__ int sSlot[10]; // the block's reflux slots (faces 0-3), its defer slots, its outside-twin range
+  static_assert(T::NREC * T::S * T::S * sizeof(R) >= H::NV * B * B * sizeof(double), "twin staging does not fit the slope area");
   const int         tid = threadIdx.x;
   const PhysParams & P = a.p;
   // a stiffened-gas constant makes the pressure numerator cancel: FP64 there
@@ -630,6 +631,8 @@ step2d_kernel(StepArgs a)
     int slot_v = -1;
     if (a.m.reflux_slot && tid < 8)
       slot_v = tid < 4 ? a.m.reflux_slot[n * 4 + tid] : a.m.defer_slot[n * 4 + tid - 4];
+    if (tid == 8 || tid == 9)
+      slot_v = a.fill_twins ? a.m.twin_first[n + tid - 8] : 0;
     const int    ins = a.m.inst ? a.m.inst[n] : 0;
     const double dx = P.level_dx[lev];
     R            dtdx_r;
@@ -664,7 +667,7 @@ step2d_kernel(StepArgs a)
       store_prim<B, MIXED>(sQ, (gx + 2) + G * (gy + 2), u, P, stiff);
     }
     store_prim<B, MIXED>(sQ, (ci + 2) + G * (cj + 2), uin, P, stiff);
-    if (tid < 8)
+    if (tid < 10)
       sSlot[tid] = slot_v;
     __syncthreads();
     // the next block of this CTA: its own cells and table rows into L2 while
@@ -861,10 +864,10 @@ step2d_kernel(StepArgs a)
       deferred = (ci == 0 && dsl[0] >= 0) || (ci == B - 1 && dsl[1] >= 0) || (cj == 0 && dsl[2] >= 0) ||
                  (cj == B - 1 && dsl[3] >= 0);
     }
-    DtT m_inv = DtT(0);
+    DtT    m_inv = DtT(0);
+    double u2[H::NV];
     if (!deferred)
     {
-      double u2[H::NV];
       if constexpr (MIXED)
         m_inv = update_mixed<B>(uin, u2, sFx, sFy, ci, cj, d2f_fast(dx), P, stiff, a.invdt != nullptr);
       else
@@ -879,6 +882,39 @@ step2d_kernel(StepArgs a)
       }
       if (!finite)
         raise_status(a.status, STATUS_NONPHYSICAL);
+    }
+    else
+    {
+#pragma unroll
+      for (int v = 0; v < H::NV; ++v)
+        u2[v] = uin[v]; // the reflux pass finishes the cell (and its twin cells)
+    }
+    if (sSlot[9] > sSlot[8])
+    {
+      // the solver loop's boundary fill of the outside blocks mirroring this
+      // block (FillOutside: the last applicable face's copy rule), from the
+      // new state staged in the (now free) slope area
+      double * sTw = reinterpret_cast<double *>(sRec);
+#pragma unroll
+      for (int v = 0; v < H::NV; ++v)
+        sTw[v * NC + tid] = u2[v];
+      __syncthreads();
+      for (int t = sSlot[8]; t < sSlot[9]; ++t)
+      {
+        const int e = a.m.twin_list[t];
+        const int o = e >> 3, face = e & 7, dir = face >> 1, bc = P.bc[face];
+        const int edge = (face & 1) ? B - 1 : 0;
+        const int sx = dir == 0 ? (bc == 2 ? edge : B - 1 - ci) : ci;
+        const int sy = dir == 1 ? (bc == 2 ? edge : B - 1 - cj) : cj;
+        const double * src = sTw + sx + B * sy;
+        double *       dst = a.U2 + (size_t)o * H::NV * NC + tid;
+#pragma unroll
+        for (int v = 0; v < H::NV; ++v)
+        {
+          const double val = src[v * NC];
+          dst[v * NC] = (bc == 3 && v == H::IU + dir) ? -val : val;
+        }
+      }
     }
     if (a.invdt)
     {
@@ -905,6 +941,44 @@ step2d_kernel(StepArgs a)
 // entry).  Replays update_U with the fine face sums of
 // get_flux_from_fine_neighbor (ReadFluxesAndConservativeUpdateFunctor.h:256-307).
 // ---------------------------------------------------------------------------
+// The outside-block cells that copy the refluxed cell (ci, cj) of block n in
+// the solver loop's boundary fill (the step kernel filled them from the
+// pre-reflux state): ZERO_GRADIENT copies the boundary row into every layer,
+// WALL mirrors one cell and negates the normal momentum.
+template <int B>
+__device__ __forceinline__ void
+patch_twins_2d(const StepArgs & a, int n, int ci, int cj, const double * u2)
+{
+  using H = V<2>;
+  constexpr int NC = B * B;
+  const int     t0 = a.m.twin_first[n], t1 = a.m.twin_first[n + 1];
+  for (int t = t0; t < t1; ++t)
+  {
+    const int e = a.m.twin_list[t];
+    const int o = e >> 3, face = e & 7, dir = face >> 1, bc = a.p.bc[face];
+    double *  base = a.U2 + (size_t)o * H::NV * NC;
+    if (bc == 2)
+    {
+      if ((dir == 0 ? ci : cj) != ((face & 1) ? B - 1 : 0))
+        continue;
+      for (int k = 0; k < B; ++k)
+      {
+        const int c = dir == 0 ? k + B * cj : ci + B * k;
+#pragma unroll
+        for (int v = 0; v < H::NV; ++v)
+          base[v * NC + c] = u2[v];
+      }
+    }
+    else
+    {
+      const int c = dir == 0 ? (B - 1 - ci) + B * cj : ci + B * (B - 1 - cj);
+#pragma unroll
+      for (int v = 0; v < H::NV; ++v)
+        base[v * NC + c] = v == H::IU + dir ? -u2[v] : u2[v];
+    }
+  }
+}
+
 // MIXED selects the FP32-bulk form of the mixed mode (float-pair increments
 // applied by apply_mixed_2d); the FP64 form replays the reference arithmetic.
 // A thread of this pass is latency-bound, so its loads come in two waves: the
@@ -1043,6 +1117,8 @@ reflux2d_kernel(StepArgs a)
     }
     if (!finite)
       raise_status(a.status, STATUS_NONPHYSICAL);
+    if (a.fill_twins)
+      patch_twins_2d<B>(a, n, ci, cj, u2);
     if (a.invdt)
       atomic_max_pos_warp(a.invdt, ins, (double)m_inv);
   }
@@ -1145,6 +1221,8 @@ reflux2d_kernel(StepArgs a)
     }
     if (!finite)
       raise_status(a.status, STATUS_NONPHYSICAL);
+    if (a.fill_twins)
+      patch_twins_2d<B>(a, n, ci, cj, u2);
     if (a.invdt)
     {
       double       q[6];
