@@ -386,10 +386,19 @@ def main():
             impl.run(A, B, nst, mode)
             torch.cuda.synchronize()
             outs[mode] = A.cpu().numpy()
-        from godunov_five_eq_gb300.metrics import l1_relative
+        from godunov_five_eq_gb300.metrics import interface_error, l1_relative, linf_relative
 
         errs = [float(e) for e in l1_relative(t, outs["mixed"], outs["fp64"])]
-        l1 = {"steps": nst, "max": max(errs), "per_variable": errs, "norm": "volume-weighted relative L1 (momentum by |rho u|)"}
+        linf = [float(e) for e in linf_relative(t, outs["mixed"], outs["fp64"])]
+        l1 = {
+            "steps": nst,
+            "max": max(errs),
+            "per_variable": errs,
+            "norm": "volume-weighted relative L1 (momentum by |rho u|)",
+            "linf_max": max(linf),
+            "linf_per_variable": linf,
+            "interface": interface_error(t, outs["mixed"], outs["fp64"]),
+        }
 
     # end to end through the C ABI with host buffers: g5_step_host copies the
     # pinned host U (owned + outside blocks) to the device and the owned blocks
