@@ -29,7 +29,7 @@ struct G5Context
   double *       d_reflux_buf = nullptr, *d_defer_buf = nullptr;
   double *       d_dt = nullptr, *d_invdt = nullptr;
   double *       d_urk = nullptr; // RK2_SSP intermediate stage (SolverGodunovFiveEq.h:349-358 m_U_RK)
-  int *          d_step = nullptr;
+  unsigned int * d_ticket = nullptr; // block claiming counter of the step kernels (zero between launches)
   // g5_step_batched: owned blocks grouped by instance (host), the call's work
   // list and instance mask (device)
   std::vector<int32_t> inst_blocks, inst_off;
@@ -144,7 +144,7 @@ free_mesh(G5Context * c)
   void * ptrs[] = { c->d_level,       c->d_coord,       c->d_nbr,        c->d_inst,       c->d_reflux_slot,
                     c->d_defer_slot,  c->d_defer_list,  c->d_out_src,    c->d_nbr_rel,    c->d_out_normal,
                     c->d_out_border,  c->d_reflux_buf,  c->d_defer_buf,  c->d_dt,         c->d_invdt,
-                    c->d_step,        c->d_urk,         c->d_defer_info, c->d_twin_first, c->d_twin_list };
+                    c->d_ticket,      c->d_urk,         c->d_defer_info, c->d_twin_first, c->d_twin_list };
   for (void * p : ptrs)
     if (p)
       cudaFree(p);
@@ -152,7 +152,7 @@ free_mesh(G5Context * c)
   c->d_reflux_slot = c->d_defer_slot = c->d_defer_list = c->d_out_src = nullptr;
   c->d_nbr_rel = c->d_out_normal = c->d_out_border = nullptr;
   c->d_reflux_buf = c->d_defer_buf = c->d_dt = c->d_invdt = nullptr;
-  c->d_step = nullptr;
+  c->d_ticket = nullptr;
   for (void * p : { (void *)c->d_batch_work, (void *)c->d_inst_active })
     if (p)
       cudaFree(p);
@@ -227,6 +227,7 @@ do_step(G5Context * c, const double * U, double * U2, const double * d_dt, int m
   a.m = dev_mesh(c);
   a.p = c->phys;
   a.fill_twins = fill_twins ? 1 : 0;
+  a.ticket = c->d_ticket;
   int         launches = 0;
   cudaError_t e = mode == G5_MODE_FP64 ? g5::launch_step_fp64(c->dim, c->b, a, c->ctas_per_sm[0], s, &launches)
                                        : g5::launch_step_mixed(c->dim, c->b, a, c->ctas_per_sm[1], s, &launches);
@@ -545,7 +546,9 @@ g5_set_mesh(G5Context * c, const G5Mesh * m)
   }
   rc |= dev_alloc(c, &c->d_dt, (size_t)n_inst);
   rc |= dev_alloc(c, &c->d_invdt, (size_t)n_inst);
-  rc |= dev_alloc(c, &c->d_step, 1);
+  rc |= dev_alloc(c, &c->d_ticket, 1);
+  if (!rc && cudaMemset(c->d_ticket, 0, sizeof(unsigned int)) != cudaSuccess)
+    rc = G5_ERR_CUDA;
   if (c->prm.integrator == 2)
     rc |= dev_alloc(c, &c->d_urk, (size_t)n_total * c->nv * (dim == 2 ? c->b * c->b : c->b * c->b * c->b));
   if (rc)
@@ -809,6 +812,7 @@ g5_step_batched(G5Context * c, const double * d_U, double * d_U2, const double *
   a.work = c->d_batch_work;
   a.n_work = (int)work.size();
   a.inst_active = c->d_inst_active;
+  a.ticket = c->d_ticket;
   a.m = dev_mesh(c);
   a.p = c->phys;
   int         launches = 0;

@@ -80,9 +80,35 @@ struct StepArgs
   int             n_work = 0;     // entries of work
   const uint8_t * inst_active = nullptr; // per instance: nonzero = stepped (null: all); read by the reflux pass
   int             fill_twins = 0;        // also fill U2's outside blocks (the solver loop's fill after the step)
+  // Dynamic block claiming (null: CTA b steps blocks b, b + grid, ...): CTA b
+  // steps block b, then claims further blocks with tickets of this counter;
+  // the CTA drawing the launch's last ticket resets it to 0.
+  unsigned int * ticket = nullptr;
   DevMesh        m;
   PhysParams     p;
 };
+
+// Next block of a persistent step CTA (returns >= nwalk when done).  CTA b
+// steps blocks b and b + grid (the CTAs start in step, so a shared counter
+// would be drawn by all of them at once), then claims the remaining
+// M = nwalk - 2 grid blocks in order with tickets, so that CTAs that finish
+// early take more of the tail.  Each of the K = min(grid, nwalk - grid) CTAs
+// with a second block draws one ticket per block from its second on, the last
+// draw failing: a launch draws M + K tickets and the drawer of the last one
+// resets the counter.
+__device__ __forceinline__ int
+claim_next(const StepArgs & a, int iw, int nwalk)
+{
+  const int G = (int)gridDim.x;
+  if (!a.ticket || iw < G)
+    return iw + G;
+  const int      M = nwalk - 2 * G > 0 ? nwalk - 2 * G : 0;
+  const int      K = nwalk - G < G ? nwalk - G : G;
+  const unsigned t = atomicAdd(a.ticket, 1u);
+  if (t == (unsigned)(M + K - 1))
+    *a.ticket = 0u;
+  return t < (unsigned)M ? 2 * G + (int)t : nwalk;
+}
 
 // number of blocks a step launch walks
 __host__ __device__ inline int

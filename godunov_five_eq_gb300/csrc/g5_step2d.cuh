@@ -614,6 +614,7 @@ step2d_kernel(StepArgs a)
   using DtT = typename std::conditional<MIXED, float, double>::type;
   __shared__ DtT sRed[NT / 32];
   __shared__ int sSlot[10]; // the block's reflux slots (faces 0-3), its defer slots, its outside-twin range
+  __shared__ int sNext;     // the CTA's next block
   static_assert(T::NREC * T::S * T::S * sizeof(R) >= H::NV * B * B * sizeof(double), "twin staging does not fit the slope area");
   const int         tid = threadIdx.x;
   const PhysParams & P = a.p;
@@ -621,11 +622,13 @@ step2d_kernel(StepArgs a)
   const bool stiff = P.gpx[0] != 0.0 || P.gpx[1] != 0.0;
 
   const int nwalk = step_count(a);
-  for (int iw = blockIdx.x; iw < nwalk; iw += gridDim.x)
+  for (int iw = blockIdx.x; iw < nwalk;)
   {
     const int    n = a.work ? a.work[iw] : iw;
     const int    lev = a.m.level[n];
     const int    cx0 = a.m.coord[n * 3 + 0], cy0 = a.m.coord[n * 3 + 1];
+    // the next block is claimed now (the ticket's latency hides behind the gather)
+    const int    next_v = tid == 10 ? claim_next(a, iw, nwalk) : 0;
     // coarse/fine slots: loaded now, stored to shared memory at the end of the
     // gather (their latency hides behind it)
     int slot_v = -1;
@@ -669,12 +672,14 @@ step2d_kernel(StepArgs a)
     store_prim<B, MIXED>(sQ, (ci + 2) + G * (cj + 2), uin, P, stiff);
     if (tid < 10)
       sSlot[tid] = slot_v;
+    if (tid == 10)
+      sNext = next_v;
     __syncthreads();
     // the next block of this CTA: its own cells and table rows into L2 while
     // this block computes (its gather then hits L2 instead of HBM)
-    if (tid < 3 && iw + (int)gridDim.x < nwalk)
+    if (tid < 3 && sNext < nwalk)
     {
-      const int nn = a.work ? a.work[iw + gridDim.x] : iw + (int)gridDim.x;
+      const int nn = a.work ? a.work[sNext] : sNext;
       if (tid == 0)
         prefetch_l2_range(a.U + (size_t)nn * H::NV * NC, (unsigned)(H::NV * NC * sizeof(double)));
       else if (tid == 1)
@@ -932,7 +937,9 @@ step2d_kernel(StepArgs a)
         atomic_max_pos(a.invdt + ins, (double)mm);
       }
     }
+    const int next = sNext; // read before the barrier: the next block's claim overwrites it
     __syncthreads();
+    iw = next;
   }
 }
 

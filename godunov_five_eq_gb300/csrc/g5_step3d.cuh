@@ -319,15 +319,18 @@ step3d_kernel(StepArgs a)
   using DtT = typename std::conditional<MIXED, float, double>::type;
   __shared__ DtT     sRed[NT / 32];
   __shared__ int     sSlot[12]; // the block's reflux slots (faces 0-5), then its defer slots
+  __shared__ int     sNext;     // the CTA's next block
   const int          tid = threadIdx.x;
   const PhysParams & P = a.p;
   const bool         stiff = P.gpx[0] != 0.0 || P.gpx[1] != 0.0;
   const int          ci = tid % B, cj = (tid / B) % B, ck = tid / (B * B);
 
   const int nwalk = step_count(a);
-  for (int iw = blockIdx.x; iw < nwalk; iw += gridDim.x)
+  for (int iw = blockIdx.x; iw < nwalk;)
   {
     const int    n = a.work ? a.work[iw] : iw;
+    // the next block is claimed now (the ticket's latency hides behind the gather)
+    const int    next_v = tid == 12 ? claim_next(a, iw, nwalk) : 0;
     const int    ins = a.m.inst ? a.m.inst[n] : 0;
     const double dx = P.level_dx[a.m.level[n]];
     const int    c0[3] = { a.m.coord[n * 3 + 0], a.m.coord[n * 3 + 1], a.m.coord[n * 3 + 2] };
@@ -366,11 +369,13 @@ step3d_kernel(StepArgs a)
     }
     if (tid < 12)
       sSlot[tid] = slot_v;
+    if (tid == 12)
+      sNext = next_v;
     __syncthreads();
     // the next block of this CTA: its own cells and table rows into L2
-    if (tid < 3 && iw + (int)gridDim.x < nwalk)
+    if (tid < 3 && sNext < nwalk)
     {
-      const int nn = a.work ? a.work[iw + gridDim.x] : iw + (int)gridDim.x;
+      const int nn = a.work ? a.work[sNext] : sNext;
       if (tid == 0)
         prefetch_l2_range(a.U + (size_t)nn * H::NV * NC, (unsigned)(H::NV * NC * sizeof(double)));
       else if (tid == 1)
@@ -751,7 +756,9 @@ step3d_kernel(StepArgs a)
         atomic_max_pos(a.invdt + ins, (double)mm);
       }
     }
+    const int next = sNext; // read before the barrier: the next block's claim overwrites it
     __syncthreads();
+    iw = next;
   }
 }
 
