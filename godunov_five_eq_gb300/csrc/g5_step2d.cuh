@@ -1028,7 +1028,7 @@ reflux2d_kernel(StepArgs a)
   {
     const int cd = (f >> 1) == 0 ? ci : cj, ct = (f >> 1) == 0 ? cj : ci;
     fine[f] = cd == ((f & 1) ? B - 1 : 0) && dsl[f] >= 0;
-    rs[f] = fine[f] ? rsf[f][(2 * ct) / B] : -1;
+    rs[f] = fine[f] ? ((2 * ct) / B ? rsf[f][1] : rsf[f][0]) : -1;
     if (fine[f] && rs[f] < 0)
     {
       raise_status(a.status, STATUS_MESH);
@@ -1045,20 +1045,36 @@ reflux2d_kernel(StepArgs a)
   // second wave (with the state): the face fluxes, own faces from the
   // record, fine faces from the two fine faces' published fluxes (floats in
   // the mixed form, doubles in the FP64 form)
+  // (rows of 8 fluxes start on 32-byte boundaries: 16-byte vector loads)
   using R = typename std::conditional<MIXED, float, double>::type;
-  const R * own = reinterpret_cast<const R *>(a.defer_buf) + ((size_t)dsl[face] * B + pos) * 32;
+  using R2 = typename std::conditional<MIXED, float4, double2>::type;
+  constexpr int RV = sizeof(R2) / sizeof(R);
+  const int dslf = face == 0 ? dsl[0] : face == 1 ? dsl[1] : face == 2 ? dsl[2] : dsl[3];
+  const R * own = reinterpret_cast<const R *>(a.defer_buf) + ((size_t)dslf * B + pos) * 32;
   R         F0[4][8], F1[4][8];
 #pragma unroll
   for (int f = 0; f < 4; ++f)
   {
-    const int ct = (f >> 1) == 0 ? cj : ci;
-    const int fl = 2 * ct - ((2 * ct) / B) * B;
-    const R * p0 = fine[f] ? reinterpret_cast<const R *>(a.reflux_buf) + ((size_t)rs[f] * B + fl) * 8 : own + f * 8;
+    const int  ct = (f >> 1) == 0 ? cj : ci;
+    const int  fl = 2 * ct - ((2 * ct) / B) * B;
+    const R *  p0 = fine[f] ? reinterpret_cast<const R *>(a.reflux_buf) + ((size_t)rs[f] * B + fl) * 8 : own + f * 8;
+    const R2 * q = reinterpret_cast<const R2 *>(p0);
 #pragma unroll
-    for (int k = 0; k < 8; ++k)
+    for (int k = 0; k < 8 / RV; ++k)
     {
-      F0[f][k] = p0[k];
-      F1[f][k] = fine[f] ? p0[8 + k] : R(0);
+      const R2 x = q[k];
+      const R2 y = fine[f] ? q[8 / RV + k] : R2{};
+      F0[f][RV * k] = x.x;
+      F0[f][RV * k + 1] = x.y;
+      F1[f][RV * k] = y.x;
+      F1[f][RV * k + 1] = y.y;
+      if constexpr (RV == 4)
+      {
+        F0[f][RV * k + 2] = x.z;
+        F0[f][RV * k + 3] = x.w;
+        F1[f][RV * k + 2] = y.z;
+        F1[f][RV * k + 3] = y.w;
+      }
     }
   }
   if constexpr (MIXED)
