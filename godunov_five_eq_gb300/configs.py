@@ -51,19 +51,74 @@ class HydroParams:
     prolongation: int = 0  # SIMPLE_COPY
     bc: tuple = (BC_PERIODIC,) * 6
     level_dx: np.ndarray = field(default_factory=lambda: np.zeros(32))
+    # material laws: EOS_* per material and the law parameters (G5Params.mg)
+    eos: tuple = (0, 0)
+    mg: tuple = ((0.0,) * 8, (0.0,) * 8)
+
+
+# material laws (G5Params.eos / .mg); the device and the oracle restate them
+EOS = {"STIFFENED": 0, "JWL": 1, "SHOCKWAVE": 2, "SHOCKWAVE2": 3}
+
+
+def mg_law(params: HydroParams, k: int, rho):
+    """G(rho) and f(rho) of material k's law written p = G rho e + f (numpy;
+    initial states only)."""
+    rho = np.asarray(rho, dtype=np.float64)
+    kind, c = params.eos[k], params.mg[k]
+    if kind == EOS["JWL"]:
+        rho0, w, A1, A2, R1, R2, e0 = c[:7]
+        x1, x2 = R1 * rho0 / rho, R2 * rho0 / rho
+        f = A1 * (1.0 - w / x1) * np.exp(-x1) + A2 * (1.0 - w / x2) * np.exp(-x2) - w * rho * e0
+        return np.full_like(rho, w), f
+    if kind == EOS["SHOCKWAVE"]:
+        rho0, g0, c0, s1, s2, s3, b, e0 = c[:8]
+        mu = rho / rho0 - 1.0
+        m1 = mu + 1.0
+        N = 1.0 + (1.0 - 0.5 * g0) * mu - 0.5 * b * mu * mu
+        D = 1.0 - (s1 - 1.0) * mu - s2 * mu * mu / m1 - s3 * mu**3 / (m1 * m1)
+        K = rho0 * c0 * c0
+        pc = np.where(mu > 0.0, K * mu * N / (D * D), K * mu)
+        gr = (g0 + b * mu) * rho0
+        return gr / rho, pc - gr * e0
+    if kind == EOS["SHOCKWAVE2"]:
+        rho0, g0, c0, s, al, e0, p0 = c[:7]
+        eta = 1.0 - rho0 / rho
+        pH = p0 + rho0 * c0 * c0 * eta / (1.0 - s * eta) ** 2
+        eH = e0 + (pH + p0) * eta / (2.0 * rho0)
+        G = g0 * (rho0 / rho) ** al
+        return G, pH - G * rho * eH
+    return np.full_like(rho, params.gamma[k] - 1.0), np.full_like(rho, -params.gamma[k] * params.pinf[k])
+
+
+def mixture_S_PI(params: HydroParams, a0, ar0, ar1):
+    """S and PI of the pressure-equilibrium mixture (p = (rho e - PI)/S)."""
+    a0 = np.asarray(a0, dtype=np.float64)
+    S = np.zeros(np.broadcast_shapes(a0.shape, np.shape(ar0), np.shape(ar1)))
+    PI = np.zeros_like(S)
+    for k, (a, ar) in enumerate(((a0, ar0), (1.0 - a0, ar1))):
+        rho0 = params.mg[k][0] if params.eos[k] != EOS["STIFFENED"] else 1.0
+        rho = np.where(a > 0.0, np.maximum(np.asarray(ar) / np.where(a > 0.0, a, 1.0), params.smallr), rho0)
+        G, f = mg_law(params, k, rho)
+        xi = 1.0 / G
+        S = S + a * xi
+        PI = PI - a * xi * f
+    return S, PI
 
 
 def prim_to_cons(dim, params: HydroParams, a0, ar0, ar1, p, vel):
-    """Conservative vector [nv, ...] from primitive fields (stiffened-gas mixture)."""
+    """Conservative vector [nv, ...] from primitive fields (pressure-equilibrium mixture)."""
     I = ids(dim)
     a0 = np.asarray(a0, dtype=np.float64)
     shape = np.broadcast_shapes(a0.shape, np.shape(ar0), np.shape(ar1), np.shape(p), *[np.shape(v) for v in vel])
     U = np.zeros((I["NV"],) + shape)
-    xi = [1.0 / (g - 1.0) for g in params.gamma]
-    gpx = [params.gamma[k] * params.pinf[k] * xi[k] for k in range(2)]
     a1 = 1.0 - a0
-    S = a0 * xi[0] + a1 * xi[1]
-    PI = a0 * gpx[0] + a1 * gpx[1]
+    if params.eos == (0, 0):
+        xi = [1.0 / (g - 1.0) for g in params.gamma]
+        gpx = [params.gamma[k] * params.pinf[k] * xi[k] for k in range(2)]
+        S = a0 * xi[0] + a1 * xi[1]
+        PI = a0 * gpx[0] + a1 * gpx[1]
+    else:
+        S, PI = mixture_S_PI(params, a0, ar0, ar1)
     rho = ar0 + ar1
     rhoe = p * S + PI
     ek = 0.0
@@ -127,6 +182,64 @@ def gas_water_shock_tube(bsize=16, nx_blocks=32, ny_blocks=2):
     ar1 = (1.0 - a0) * 50.0
     p = np.where(left, 1e9, 1e5)
     U[: table.n_owned] = np.moveaxis(prim_to_cons(2, params, a0, ar0, ar1, p, (0.0 * p, 0.0 * p)), 0, 1)
+    return mesh, table, params, U
+
+
+# ----------------------------------------------------------------------------
+# Mie-Grueneisen two-material shock tubes (the decks' JWL and shock-wave laws)
+# ----------------------------------------------------------------------------
+MG_LAWS = {
+    # LX-17-like detonation products, JWL {rho0, Gamma0, A1, A2, R1, R2, e0}
+    "jwl": (EOS["JWL"], (1905.0, 0.8938, 6.321e13, -4.472e9, 11.3, 1.13, 0.0, 0.0)),
+    # aluminium, Grueneisen with a cubic Us-up fit {rho0, Gamma0, c0, s1, s2, s3, b, e0}
+    "shockwave": (EOS["SHOCKWAVE"], (2700.0, 1.97, 5328.0, 1.4, 0.0, 0.0, 0.48, 0.0)),
+    # aluminium, linear Us-up Hugoniot {rho0, Gamma0, c0, s, alpha, e0, p0}
+    "shockwave2": (EOS["SHOCKWAVE2"], (2785.0, 2.0, 5328.0, 1.338, 1.0, 0.0, 0.0, 0.0)),
+}
+
+
+def mg_shock_tube(law="jwl", other=None, bsize=16, nx_blocks=16, ny_blocks=2, source_term=0, dim=2):
+    """Two-material shock tube with Mie-Grueneisen laws: material 0 (law) at
+    x < 0.5 compressed to 1.6 rho0 at high pressure, material 1 (other: a law
+    name, or None for the same law, or "air" for an ideal gas) at x > 0.5 at
+    rho0 and low pressure.  ZERO_GRADIENT in x, periodic across."""
+    level = 1
+    trees = [max(1, nx_blocks >> level), max(1, ny_blocks >> level)] + ([max(1, ny_blocks >> level)] if dim == 3 else [])
+    per = (False, True) + ((True,) if dim == 3 else ())
+    mesh = BlockMesh(dim, bsize, tuple(trees), per, level, level, scaling=1.0 / trees[0])
+    table = mesh.build()
+    k0, c0 = MG_LAWS[law]
+    if other == "air":
+        k1, c1, gamma1 = EOS["STIFFENED"], (0.0,) * 8, 1.4
+    else:
+        k1, c1 = MG_LAWS[other or law]
+        gamma1 = 3.0
+    params = HydroParams(
+        dim=dim,
+        bsize=bsize,
+        gamma=(3.0, gamma1),
+        pinf=(0.0, 0.0),
+        slope_type=1.0,
+        cfl=0.4,
+        integrator=INTEGRATOR["HANCOCK"],
+        source_term=source_term,
+        bc=(BC_ZERO_GRADIENT, BC_ZERO_GRADIENT) + (BC_PERIODIC,) * 4,
+        level_dx=table.level_dx,
+        eos=(k0, k1),
+        mg=(tuple(c0), tuple(c1)),
+    )
+    U = _alloc_U(table)
+    xc = cell_centers(mesh, table)
+    left = xc[:, 0] < 0.5
+    eps = 1e-6
+    rho0_0 = c0[0]
+    rho0_1 = c1[0] if k1 != EOS["STIFFENED"] else 1.0
+    a0 = np.where(left, 1.0 - eps, eps)
+    ar0 = a0 * 1.6 * rho0_0
+    ar1 = (1.0 - a0) * rho0_1
+    p = np.where(left, 2e10, 1e5)
+    vel = tuple(0.0 * p for _ in range(dim))
+    U[: table.n_owned] = np.moveaxis(prim_to_cons(dim, params, a0, ar0, ar1, p, vel), 0, 1)
     return mesh, table, params, U
 
 

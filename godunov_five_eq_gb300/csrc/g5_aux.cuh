@@ -505,7 +505,14 @@ derived_kernel(const double * __restrict__ U, double * __restrict__ out, int qua
         const double dm = fmax(u[H::IAD0] + u[H::IAD1], P.smallr);
         const double eint = u[H::IE] / dm - ekin;
         const double a0 = u[H::IA0];
-        r = (dm * eint - eosPI(P, a0, 1 - a0)) / eosS(P, a0, 1 - a0);
+        if (!P.mg_any)
+          r = (dm * eint - eosPI(P, a0, 1 - a0)) / eosS(P, a0, 1 - a0);
+        else
+        {
+          double S, PI, C1, C0;
+          mg_mixture(P, a0, 1 - a0, u[H::IAD0], u[H::IAD1], S, PI, C1, C0);
+          r = (dm * eint - PI) / S;
+        }
       }
     }
     else

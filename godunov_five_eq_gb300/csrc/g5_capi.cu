@@ -8,6 +8,7 @@
 
 #include "../../include/g5gpu.h"
 #include "g5_launch.h"
+#include "g5_phys.h"
 
 struct G5Context
 {
@@ -214,6 +215,8 @@ do_step(G5Context * c, const double * U, double * U2, const double * d_dt, int m
     return G5_ERR_ARG;
   if (mode != G5_MODE_FP64 && mode != G5_MODE_MIXED)
     return G5_ERR_ARG;
+  if (mode == G5_MODE_MIXED && c->phys.mg_any)
+    return G5_ERR_UNSUPPORTED; // the FP32-bulk form is written for stiffened gases
   if (!g5::step_supported(c->dim, c->b))
     return G5_ERR_UNSUPPORTED;
   g5::StepArgs a;
@@ -345,6 +348,8 @@ g5_create(const G5Params * params, G5Context ** out_ctx)
   for (int k = 0; k < 2; ++k)
     if (!(params->gamma[k] > 1.0))
       return G5_ERR_ARG;
+  if (!g5::eos_params_valid(params))
+    return G5_ERR_ARG;
   G5Context * c = new G5Context;
   c->prm = *params;
   c->dim = params->dim;
@@ -353,41 +358,7 @@ g5_create(const G5Params * params, G5Context ** out_ctx)
   c->ns = params->dim == 2 ? 9 : 27;
   c->nch = params->dim == 2 ? 4 : 8;
   cudaGetDevice(&c->device);
-  g5::PhysParams & p = c->phys;
-  p.smallr = params->smallr;
-  p.smallc = params->smallc;
-  p.smallp = params->smallc * params->smallc;
-  p.slope_type = params->slope_type;
-  for (int k = 0; k < 2; ++k)
-  {
-    p.gamma[k] = params->gamma[k];
-    p.pinf[k] = params->pinf[k];
-    p.xi[k] = 1.0 / (params->gamma[k] - 1.0);
-    p.gpx[k] = params->gamma[k] * params->pinf[k] * p.xi[k];
-  }
-  p.cfl = params->cfl;
-  p.thinc_beta = params->thinc_beta;
-  p.thinc_eps = params->thinc_eps;
-  p.integrator = params->integrator;
-  p.thinc = params->thinc;
-  p.source_term = params->source_term;
-  for (int f = 0; f < 6; ++f)
-    p.bc[f] = params->bc[f];
-  for (int l = 0; l < 32; ++l)
-    p.level_dx[l] = params->level_dx[l];
-  p.f_smallr = (float)p.smallr;
-  p.f_smallc = (float)p.smallc;
-  p.f_smallp = (float)p.smallp;
-  p.f_slope_type = (float)p.slope_type;
-  p.f_thinc_beta = (float)p.thinc_beta;
-  p.f_thinc_eps = (float)p.thinc_eps;
-  for (int k = 0; k < 2; ++k)
-  {
-    p.f_xi[k] = (float)p.xi[k];
-    p.f_gpx[k] = (float)p.gpx[k];
-  }
-  p.f_dxi = (float)(p.xi[0] - p.xi[1]);
-  p.dgpx = p.gpx[0] - p.gpx[1];
+  c->phys = g5::make_phys(params);
   if (cudaMalloc((void **)&c->d_status, sizeof(unsigned int)) != cudaSuccess ||
       cudaMemset(c->d_status, 0, sizeof(unsigned int)) != cudaSuccess)
   {
@@ -780,6 +751,8 @@ g5_step_batched(G5Context * c, const double * d_U, double * d_U2, const double *
     return G5_ERR_ARG;
   if (mode != G5_MODE_FP64 && mode != G5_MODE_MIXED)
     return G5_ERR_ARG;
+  if (mode == G5_MODE_MIXED && c->phys.mg_any)
+    return G5_ERR_UNSUPPORTED; // the FP32-bulk form is written for stiffened gases
   if (!g5::step_supported(c->dim, c->b))
     return G5_ERR_UNSUPPORTED;
   std::vector<uint8_t> active((size_t)c->n_inst, 0);
@@ -829,6 +802,8 @@ g5_step_host(G5Context * c, const double * h_U, double * h_U2, const double * dt
     return G5_ERR_ARG;
   if (mode != G5_MODE_FP64 && mode != G5_MODE_MIXED)
     return G5_ERR_ARG;
+  if (mode == G5_MODE_MIXED && c->phys.mg_any)
+    return G5_ERR_UNSUPPORTED; // the FP32-bulk form is written for stiffened gases
   for (int i = 0; i < c->n_inst; ++i)
     if (!(dt_host[i] > 0.0))
       return G5_ERR_ARG;
@@ -1135,6 +1110,8 @@ g5_advance(G5Context * c, const double * d_U, double * d_U2, int mode, double * 
     return G5_ERR_ARG;
   if (mode != G5_MODE_FP64 && mode != G5_MODE_MIXED)
     return G5_ERR_ARG;
+  if (mode == G5_MODE_MIXED && c->phys.mg_any)
+    return G5_ERR_UNSUPPORTED; // the FP32-bulk form is written for stiffened gases
   cudaStream_t s = (cudaStream_t)stream;
   // cached graph of one loop step for (U, U2, mode, dt_out)
   G5Context::GraphSlot * slot = nullptr;
@@ -1195,6 +1172,8 @@ g5_run(G5Context * c, double * d_U, double * d_U2, int nsteps, int mode, double 
     return G5_ERR_ARG;
   if (mode != G5_MODE_FP64 && mode != G5_MODE_MIXED)
     return G5_ERR_ARG;
+  if (mode == G5_MODE_MIXED && c->phys.mg_any)
+    return G5_ERR_UNSUPPORTED; // the FP32-bulk form is written for stiffened gases
   cudaStream_t s = (cudaStream_t)stream;
   int          rc = g5_begin(c, d_U, stream);
   if (rc)
@@ -1246,6 +1225,8 @@ g5_tune(G5Context * c, const double * d_U, double * d_U2, int mode, void * strea
 {
   if (!c || !c->has_mesh || !d_U || !d_U2 || (mode != G5_MODE_FP64 && mode != G5_MODE_MIXED))
     return G5_ERR_ARG;
+  if (mode == G5_MODE_MIXED && c->phys.mg_any)
+    return G5_ERR_UNSUPPORTED; // the FP32-bulk form is written for stiffened gases
   cudaStream_t s = (cudaStream_t)stream;
   const int    occ = mode == G5_MODE_FP64 ? g5::step_max_ctas_per_sm_fp64(c->dim, c->b) : g5::step_max_ctas_per_sm_mixed(c->dim, c->b);
   if (occ <= 0)

@@ -31,6 +31,13 @@ struct PhysParams
   float f_smallr, f_smallc, f_smallp, f_slope_type, f_thinc_beta, f_thinc_eps;
   float f_xi[2], f_gpx[2], f_dxi; // f_dxi = xi0 - xi1
   double dgpx;                    // gpx0 - gpx1
+  // Mie-Grueneisen material laws (mg_law): kind per material (0 stiffened
+  // gas), parameters, reference densities, and whether any law is not the
+  // stiffened gas (then every EOS evaluation takes the general path)
+  int    eos_kind[2];
+  int    mg_any;
+  double mg[2][8];
+  double mg_rho0[2];
 };
 
 struct DevMesh
@@ -204,6 +211,237 @@ sound_speed_f(float xi0, float xi1, float gp0, float gp1, float rho, float p, fl
 }
 
 // ---------------------------------------------------------------------------
+// exp and log without the CUDA math library, the same algorithms as the
+// oracle (IEEE +, -, *, / and exact frexp/ldexp only, so the FP64 path stays
+// bit-reproducible against it):
+//   exp: Cody-Waite reduction x = k ln2 + r, |r| <= ln2/2, degree-16 Taylor
+//        polynomial of expm1(r), then 2^k (1 + expm1(r));
+//   log: x = m 2^e with m in [sqrt(1/2), sqrt(2)), log m = 2 atanh(t),
+//        t = (m-1)/(m+1), odd series to t^25, plus e ln2 (split hi/lo).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double
+expm1_small_d(double r)
+{
+  const double c[17] = { 1.0,
+                         1.0,
+                         0.5,
+                         0.16666666666666666,
+                         0.041666666666666664,
+                         0.008333333333333333,
+                         0.001388888888888889,
+                         0.0001984126984126984,
+                         2.48015873015873e-05,
+                         2.7557319223985893e-06,
+                         2.755731922398589e-07,
+                         2.505210838544172e-08,
+                         2.08767569878681e-09,
+                         1.6059043836821613e-10,
+                         1.1470745597729725e-11,
+                         7.647163731819816e-13,
+                         4.779477332387385e-14 };
+  double       p = c[16];
+#pragma unroll
+  for (int k = 15; k >= 1; --k)
+    p = p * r + c[k];
+  return p * r;
+}
+
+__device__ __forceinline__ double
+exp_d(double x)
+{
+  if (x != x)
+    return x;
+  if (x < -745.5)
+    return 0.0;
+  if (x > 709.7)
+    return __longlong_as_double(0x7ff0000000000000LL);
+  const double k = floor(x * 1.4426950408889634 + 0.5);
+  const double r = (x - k * 0.6931471824645996) - k * -1.904654299957768e-09;
+  return ldexp(expm1_small_d(r) + 1.0, (int)k);
+}
+
+__device__ __forceinline__ double
+log_d(double x)
+{
+  int    e;
+  double m = frexp(x, &e);
+  if (m < 0.7071067811865476)
+  {
+    m = m * 2.0;
+    e = e - 1;
+  }
+  const double t = (m - 1.0) / (m + 1.0);
+  const double t2 = t * t;
+  const double c[13] = { 1.0 / 1.0,  1.0 / 3.0,  1.0 / 5.0,  1.0 / 7.0,  1.0 / 9.0,  1.0 / 11.0, 1.0 / 13.0,
+                         1.0 / 15.0, 1.0 / 17.0, 1.0 / 19.0, 1.0 / 21.0, 1.0 / 23.0, 1.0 / 25.0 };
+  double       sr = c[12];
+#pragma unroll
+  for (int j = 11; j >= 0; --j)
+    sr = sr * t2 + c[j];
+  const double de = (double)e;
+  return (2.0 * t * sr + de * 0.6931471824645996) + de * -1.904654299957768e-09;
+}
+
+// ---------------------------------------------------------------------------
+// Mie-Grueneisen material laws (restated from their published forms; the
+// reference's core::eos::MieGruneisenMixture is external).  Each law is
+// written p = G(rho) rho e + f(rho) and gives G, dG/drho, f and df/drho:
+//   stiffened gas  G = gamma - 1, f = -gamma pinf
+//   JWL (Lee, Hornig & Kury 1968), x_i = R_i rho0 / rho:
+//       G = Gamma0, f = sum_i A_i (1 - Gamma0/x_i) exp(-x_i) - Gamma0 rho e0
+//   SHOCKWAVE (Grueneisen form with a cubic Us-up Hugoniot fit, Steinberg),
+//   mu = rho/rho0 - 1:  G rho = (Gamma0 + b mu) rho0,
+//       f = pc - (Gamma0 + b mu) rho0 e0,
+//       pc = rho0 c0^2 mu N / D^2 (mu > 0), rho0 c0^2 mu (mu <= 0),
+//       N = 1 + (1 - Gamma0/2) mu - b mu^2/2,
+//       D = 1 - (s1-1) mu - s2 mu^2/(mu+1) - s3 mu^3/(mu+1)^2
+//   SHOCKWAVE2 (linear Us-up Hugoniot as the reference curve), eta = 1 - rho0/rho:
+//       pH = p0 + rho0 c0^2 eta / (1 - s eta)^2, eH = e0 + (pH + p0) eta / (2 rho0),
+//       G = Gamma0 (rho0/rho)^alpha, f = pH - G rho eH
+// Mixture under pressure equilibrium (Allaire, Clerc & Kokh 2002), material
+// densities rho_k = (alpha rho)_k / alpha_k (rho0_k when alpha_k = 0), xi_k = 1/G_k:
+//   S = sum a_k xi_k, PI = -sum a_k xi_k f_k:  p = (rho e - PI)/S, rho e = p S + PI
+//   rho c^2 S = sum a_k xi_k rho_k c_k^2 = p C1 + C0 with
+//   rho_k c_k^2 = (1 + rho_k G'_k xi_k)(p - f_k) + rho_k f'_k + G_k p,
+//   C1 = sum a_k (xi_k (1 + rho_k G'_k xi_k) + 1),
+//   C0 = sum a_k (xi_k rho_k f'_k - xi_k (1 + rho_k G'_k xi_k) f_k).
+// With stiffened gases only these reduce to the forms above (S, PI and
+// c^2 = (p (S+1) + PI)/(rho S)), which the code keeps for that case.
+// ---------------------------------------------------------------------------
+constexpr int EOS_STIFFENED = 0, EOS_JWL = 1, EOS_SHOCKWAVE = 2, EOS_SHOCKWAVE2 = 3;
+
+__device__ __forceinline__ void
+mg_law(const PhysParams & P, int k, double rho, double & G, double & dG, double & f, double & df)
+{
+  const double * c = P.mg[k];
+  const int      kind = P.eos_kind[k];
+  if (kind == EOS_JWL)
+  {
+    const double rho0 = c[0], w = c[1], A1 = c[2], A2 = c[3], R1 = c[4], R2 = c[5], e0 = c[6];
+    const double x1 = R1 * rho0 / rho, x2 = R2 * rho0 / rho;
+    const double E1 = exp_d(-x1), E2 = exp_d(-x2);
+    G = w;
+    dG = 0.0;
+    f = A1 * (1.0 - w / x1) * E1 + A2 * (1.0 - w / x2) * E2 - w * rho * e0;
+    df = (A1 * E1 * (x1 - w - w / x1) + A2 * E2 * (x2 - w - w / x2)) / rho - w * e0;
+  }
+  else if (kind == EOS_SHOCKWAVE)
+  {
+    const double rho0 = c[0], g0 = c[1], c0 = c[2], s1 = c[3], s2 = c[4], s3 = c[5], b = c[6], e0 = c[7];
+    const double mu = rho / rho0 - 1.0;
+    const double K = rho0 * c0 * c0;
+    double       pc, dpc;
+    if (mu > 0.0)
+    {
+      const double m1 = mu + 1.0;
+      const double N = 1.0 + (1.0 - 0.5 * g0) * mu - 0.5 * b * mu * mu;
+      const double Np = (1.0 - 0.5 * g0) - b * mu;
+      const double D = 1.0 - (s1 - 1.0) * mu - s2 * mu * mu / m1 - s3 * mu * mu * mu / (m1 * m1);
+      const double Dp = -(s1 - 1.0) - s2 * (mu * mu + 2.0 * mu) / (m1 * m1) - s3 * (mu * mu * mu + 3.0 * mu * mu) / (m1 * m1 * m1);
+      pc = K * mu * N / (D * D);
+      dpc = K * ((N + mu * Np) / (D * D) - 2.0 * mu * N * Dp / (D * D * D));
+    }
+    else
+    {
+      pc = K * mu;
+      dpc = K;
+    }
+    const double gr = (g0 + b * mu) * rho0;
+    G = gr / rho;
+    dG = b / rho - G / rho;
+    f = pc - gr * e0;
+    df = dpc / rho0 - b * e0;
+  }
+  else if (kind == EOS_SHOCKWAVE2)
+  {
+    const double rho0 = c[0], g0 = c[1], c0 = c[2], s = c[3], al = c[4], e0 = c[5], p0 = c[6];
+    const double eta = 1.0 - rho0 / rho;
+    const double w = 1.0 - s * eta;
+    const double K = rho0 * c0 * c0;
+    const double pH = p0 + K * eta / (w * w);
+    const double eH = e0 + (pH + p0) * eta / (2.0 * rho0);
+    const double v = rho0 / rho;
+    double       gp;
+    if (al == 1.0)
+      gp = v;
+    else if (al == 0.0)
+      gp = 1.0;
+    else
+      gp = exp_d(al * log_d(v));
+    G = g0 * gp;
+    dG = -al * G / rho;
+    const double dpH = K * (1.0 + s * eta) / (w * w * w);
+    const double deH = (dpH * eta + pH + p0) / (2.0 * rho0);
+    const double deta = rho0 / (rho * rho);
+    f = pH - G * rho * eH;
+    df = dpH * deta - (dG * rho + G) * eH - G * rho * deH * deta;
+  }
+  else
+  {
+    G = P.gamma[k] - 1.0;
+    dG = 0.0;
+    f = -P.gamma[k] * P.pinf[k];
+    df = 0.0;
+  }
+}
+
+// material density of the mixture rules (the law's reference density when
+// the material is absent)
+__device__ __forceinline__ double
+mg_material_density(const PhysParams & P, int k, double a, double ar)
+{
+  return a > 0.0 ? fmax(ar / a, P.smallr) : P.mg_rho0[k];
+}
+
+// S, PI, C1, C0 of the mixture rules above for volume fractions a0, a1 and
+// partial densities ar0, ar1
+__device__ __forceinline__ void
+mg_mixture(const PhysParams & P, double a0, double a1, double ar0, double ar1, double & S, double & PI, double & C1, double & C0)
+{
+  S = 0.0;
+  PI = 0.0;
+  C1 = 0.0;
+  C0 = 0.0;
+#pragma unroll
+  for (int k = 0; k < 2; ++k)
+  {
+    const double a = k == 0 ? a0 : a1;
+    const double rho = mg_material_density(P, k, a, k == 0 ? ar0 : ar1);
+    double       G, dG, f, df;
+    mg_law(P, k, rho, G, dG, f, df);
+    const double xi = 1.0 / G;
+    const double h = xi * (1.0 + rho * dG * xi);
+    S = S + a * xi;
+    PI = PI - a * xi * f;
+    C1 = C1 + a * (h + 1.0);
+    C0 = C0 + a * (xi * rho * df - h * f);
+  }
+}
+
+// bulk modulus rho_k c_k^2 of material k at pressure p (Miller-Puckett)
+__device__ __forceinline__ double
+mg_bulk_modulus(const PhysParams & P, int k, double a, double ar, double p)
+{
+  const double rho = mg_material_density(P, k, a, ar);
+  double       G, dG, f, df;
+  mg_law(P, k, rho, G, dG, f, df);
+  return (1.0 + rho * dG / G) * (p - f) + rho * df + G * p;
+}
+
+// mixture sound speed for either path: the stiffened-gas form, or the
+// general one from the partial densities
+__device__ __forceinline__ double
+sound_speed_mix(const PhysParams & P, double rho, double p, double a0, double a1, double ar0, double ar1)
+{
+  if (!P.mg_any)
+    return sound_speed_d(P, rho, p, a0, a1);
+  double S, PI, C1, C0;
+  mg_mixture(P, a0, a1, ar0, ar1, S, PI, C1, C0);
+  const double c2 = (p * C1 + C0) / (rho * S);
+  return sqrt(fmax(c2, 0.0));
+}
+
+// ---------------------------------------------------------------------------
 // conservative (FP64) -> primitive, models/utils.h:200-250 (computePrimitives)
 // q[] receives the shared-memory components (r0 r1 p u v (w) alpha0).
 // Returns the mixture sound speed c; ux/uy/uz are the velocities.
@@ -227,7 +465,15 @@ prim_fp64(const double * u, double * q, const PhysParams & P)
   }
   const double eint = u[H::IE] / d - ekin;
   const double a0u = u[H::IA0];
-  const double p = (d * eint - eosPI(P, a0u, 1.0 - a0u)) / eosS(P, a0u, 1.0 - a0u);
+  double       p;
+  if (!P.mg_any)
+    p = (d * eint - eosPI(P, a0u, 1.0 - a0u)) / eosS(P, a0u, 1.0 - a0u);
+  else
+  {
+    double S, PI, C1, C0;
+    mg_mixture(P, a0u, 1.0 - a0u, u[H::IAD0], u[H::IAD1], S, PI, C1, C0);
+    p = (d * eint - PI) / S;
+  }
   double       a0 = fmax(0.0, fmin(1.0, a0u));
   double       r0 = u[H::IAD0], r1 = u[H::IAD1];
   const double eps = 1e-12;
@@ -247,7 +493,7 @@ prim_fp64(const double * u, double * q, const PhysParams & P)
   if constexpr (DIM == 3)
     q[H::QW] = uz;
   q[H::QA] = a0;
-  return sound_speed_d(P, d, p, a0, 1.0 - a0);
+  return sound_speed_mix(P, d, p, a0, 1.0 - a0, r0, r1);
 }
 
 // Volume-fraction source-term factors st_k of get_source_term_factor
@@ -278,9 +524,21 @@ source_factors_fp64(const double * u, const PhysParams & P, double & st0, double
   }
   const double eint = u[H::IE] / d - ekin;
   const double a0 = u[H::IA0];
-  const double p = (d * eint - eosPI(P, a0, 1 - a0)) / eosS(P, a0, 1 - a0);
-  const double K0 = P.gamma[0] * (p + P.pinf[0]);
-  const double K1 = P.gamma[1] * (p + P.pinf[1]);
+  double       p, K0, K1;
+  if (!P.mg_any)
+  {
+    p = (d * eint - eosPI(P, a0, 1 - a0)) / eosS(P, a0, 1 - a0);
+    K0 = P.gamma[0] * (p + P.pinf[0]);
+    K1 = P.gamma[1] * (p + P.pinf[1]);
+  }
+  else
+  {
+    double S, PI, C1, C0;
+    mg_mixture(P, a0, 1 - a0, u[H::IAD0], u[H::IAD1], S, PI, C1, C0);
+    p = (d * eint - PI) / S;
+    K0 = mg_bulk_modulus(P, 0, u[H::IA0], u[H::IAD0], p);
+    K1 = mg_bulk_modulus(P, 1, u[H::IA1], u[H::IAD1], p);
+  }
   const double kbar = 1.0 / (u[H::IA0] / K0 + u[H::IA1] / K1);
   st0 = 1.0 - kbar / K0;
   st1 = 1.0 - kbar / K1;
@@ -309,33 +567,6 @@ slope_scalar(R q, R qPlus, R qMinus, R slope_type)
 // tanh: same algorithm as the oracle (Cody-Waite reduced Taylor expm1),
 // FP64, bit-reproducible on IEEE hardware without contraction.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ double
-expm1_small_d(double r)
-{
-  const double c[17] = { 1.0,
-                         1.0,
-                         0.5,
-                         0.16666666666666666,
-                         0.041666666666666664,
-                         0.008333333333333333,
-                         0.001388888888888889,
-                         0.0001984126984126984,
-                         2.48015873015873e-05,
-                         2.7557319223985893e-06,
-                         2.755731922398589e-07,
-                         2.505210838544172e-08,
-                         2.08767569878681e-09,
-                         1.6059043836821613e-10,
-                         1.1470745597729725e-11,
-                         7.647163731819816e-13,
-                         4.779477332387385e-14 };
-  double       p = c[16];
-#pragma unroll
-  for (int k = 15; k >= 1; --k)
-    p = p * r + c[k];
-  return p * r;
-}
-
 __device__ __forceinline__ double
 tanh_d(double x)
 {
@@ -374,8 +605,23 @@ hllc_fp64(const double * ql, const double * qr, const PhysParams & P, double * f
   using H = V<DIM>;
   const double smallr = P.smallr, smallp = P.smallp, smallc = P.smallc;
   const double al = ql[H::QA], ar = qr[H::QA];
-  const double Sl = eosS(P, al, 1 - al), PIl = eosPI(P, al, 1 - al);
-  const double Sr = eosS(P, ar, 1 - ar), PIr = eosPI(P, ar, 1 - ar);
+  double       Sl, PIl, Sr, PIr, C1l, C0l, C1r, C0r;
+  if (!P.mg_any)
+  {
+    Sl = eosS(P, al, 1 - al);
+    PIl = eosPI(P, al, 1 - al);
+    Sr = eosS(P, ar, 1 - ar);
+    PIr = eosPI(P, ar, 1 - ar);
+    C1l = Sl + 1.0;
+    C0l = PIl;
+    C1r = Sr + 1.0;
+    C0r = PIr;
+  }
+  else
+  {
+    mg_mixture(P, al, 1 - al, ql[H::QR0], ql[H::QR1], Sl, PIl, C1l, C0l);
+    mg_mixture(P, ar, 1 - ar, qr[H::QR0], qr[H::QR1], Sr, PIr, C1r, C0r);
+  }
 
   const double rl = fmax(ql[H::QR0] + ql[H::QR1], smallr);
   double       pl = fmax(ql[H::QP], rl * smallp);
@@ -386,7 +632,7 @@ hllc_fp64(const double * ql, const double * qr, const PhysParams & P, double * f
   ecinl += 0.5 * rl * ql[H::QV] * ql[H::QV];
   if constexpr (DIM == 3)
     ecinl += 0.5 * rl * ql[H::QW] * ql[H::QW];
-  const double cl2 = (pl * (Sl + 1.0) + PIl) / (rl * Sl);
+  const double cl2 = (pl * C1l + C0l) / (rl * Sl);
   const double cl = sqrt(fmax(cl2, 0.0));
   const double etotl = rl * eintl + ecinl;
   const double ptotl = pl;
@@ -400,7 +646,7 @@ hllc_fp64(const double * ql, const double * qr, const PhysParams & P, double * f
   ecinr += 0.5 * rr * qr[H::QV] * qr[H::QV];
   if constexpr (DIM == 3)
     ecinr += 0.5 * rr * qr[H::QW] * qr[H::QW];
-  const double cr2 = (pr * (Sr + 1.0) + PIr) / (rr * Sr);
+  const double cr2 = (pr * C1r + C0r) / (rr * Sr);
   const double cr = sqrt(fmax(cr2, 0.0));
   const double etotr = rr * eintr + ecinr;
   const double ptotr = pr;

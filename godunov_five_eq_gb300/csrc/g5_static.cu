@@ -20,6 +20,7 @@
 
 #include "../../include/g5gpu.h"
 #include "g5_launch.h"
+#include "g5_phys.h"
 
 namespace
 {
@@ -93,8 +94,10 @@ g5_step_static(const G5Params * params,
     return G5_ERR_UNSUPPORTED;
   if ((params->integrator != 0 && params->integrator != 1) || params->source_term != 0 || params->prolongation != 0)
     return G5_ERR_UNSUPPORTED;
-  if (!(params->gamma[0] > 1.0) || !(params->gamma[1] > 1.0))
+  if (!(params->gamma[0] > 1.0) || !(params->gamma[1] > 1.0) || !g5::eos_params_valid(params))
     return G5_ERR_ARG;
+  if (mode == G5_MODE_MIXED && (params->eos[0] != G5_EOS_STIFFENED || params->eos[1] != G5_EOS_STIFFENED))
+    return G5_ERR_UNSUPPORTED; // the FP32-bulk form is written for stiffened gases
   const int n_owned = mesh->n_owned, n_outside = mesh->n_outside;
   const int n_total = n_owned + n_outside, n_inst = mesh->n_inst > 0 ? mesh->n_inst : 1;
   if (n_owned <= 0 || n_outside < 0 || !mesh->level || !mesh->coord || !mesh->nbr || !mesh->nbr_rel)
@@ -251,38 +254,7 @@ g5_step_static(const G5Params * params,
     return G5_ERR_CUDA;
 
   // ---- the step, with every scratch pointer inside the static array
-  g5::PhysParams p;
-  std::memset(&p, 0, sizeof(p));
-  p.smallr = params->smallr;
-  p.smallc = params->smallc;
-  p.smallp = params->smallc * params->smallc;
-  p.slope_type = params->slope_type;
-  for (int k = 0; k < 2; ++k)
-  {
-    p.gamma[k] = params->gamma[k];
-    p.pinf[k] = params->pinf[k];
-    p.xi[k] = 1.0 / (params->gamma[k] - 1.0);
-    p.gpx[k] = params->gamma[k] * params->pinf[k] * p.xi[k];
-    p.f_xi[k] = (float)p.xi[k];
-    p.f_gpx[k] = (float)p.gpx[k];
-  }
-  p.cfl = params->cfl;
-  p.thinc_beta = params->thinc_beta;
-  p.thinc_eps = params->thinc_eps;
-  p.integrator = params->integrator;
-  p.thinc = params->thinc;
-  for (int f = 0; f < 6; ++f)
-    p.bc[f] = params->bc[f];
-  for (int l = 0; l < 32; ++l)
-    p.level_dx[l] = params->level_dx[l];
-  p.f_smallr = (float)p.smallr;
-  p.f_smallc = (float)p.smallc;
-  p.f_smallp = (float)p.smallp;
-  p.f_slope_type = (float)p.slope_type;
-  p.f_thinc_beta = (float)p.thinc_beta;
-  p.f_thinc_eps = (float)p.thinc_eps;
-  p.f_dxi = (float)(p.xi[0] - p.xi[1]);
-  p.dgpx = p.gpx[0] - p.gpx[1];
+  const g5::PhysParams p = g5::make_phys(params);
 
   g5::StepArgs a;
   std::memset(&a, 0, sizeof(a));

@@ -722,7 +722,7 @@ step2d_kernel(StepArgs a)
         if constexpr (MIXED)
           c = sound_speed_f(P.f_xi[0], P.f_xi[1], P.f_gpx[0], P.f_gpx[1], rr, p, a0);
         else
-          c = sound_speed_d(P, rr, p, a0, 1 - a0);
+          c = sound_speed_mix(P, rr, p, a0, 1 - a0, r0, r1);
         const R drx0 = dqx[0], drx1 = dqx[1], dpx = dqx[2], dux = dqx[3], dvx = dqx[4];
         const R dry0 = dqy[0], dry1 = dqy[1], dpy = dqy[2], duy = dqy[3], dvy = dqy[4];
         const R dtdy = dtdx_r;

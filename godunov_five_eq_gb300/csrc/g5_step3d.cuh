@@ -416,7 +416,7 @@ step3d_kernel(StepArgs a)
         if constexpr (MIXED)
           c = sound_speed_f(P.f_xi[0], P.f_xi[1], P.f_gpx[0], P.f_gpx[1], rr, p, a0);
         else
-          c = sound_speed_d(P, rr, p, a0, 1 - a0);
+          c = sound_speed_mix(P, rr, p, a0, 1 - a0, r0, r1);
         const R drx0 = dq[0][0], drx1 = dq[0][1], dpx = dq[0][2], dux = dq[0][3], dvx = dq[0][4], dwx = dq[0][5];
         const R dry0 = dq[1][0], dry1 = dq[1][1], dpy = dq[1][2], duy = dq[1][3], dvy = dq[1][4], dwy = dq[1][5];
         const R drz0 = dq[2][0], drz1 = dq[2][1], dpz = dq[2][2], duz = dq[2][3], dvz = dq[2][4], dwz = dq[2][5];

@@ -65,6 +65,8 @@ class G5Params(ctypes.Structure):
         ("thinc_beta", ctypes.c_double),
         ("thinc_eps", ctypes.c_double),
         ("level_dx", ctypes.c_double * 32),
+        ("eos", ctypes.c_int32 * 2),
+        ("mg", (ctypes.c_double * 8) * 2),
     ]
 
 
@@ -184,6 +186,10 @@ def make_params(p) -> G5Params:
     o.thinc_eps = p.thinc_eps
     for i in range(32):
         o.level_dx[i] = float(p.level_dx[i])
+    for k in range(2):
+        o.eos[k] = int(p.eos[k])
+        for j in range(8):
+            o.mg[k][j] = float(p.mg[k][j]) if j < len(p.mg[k]) else 0.0
     return o
 
 

@@ -79,7 +79,22 @@ typedef struct G5Params
   double  thinc_beta;
   double  thinc_eps;
   double  level_dx[32];
+  /* Material laws (Mie-Grueneisen family), per material k.  G5_EOS_STIFFENED
+   * uses gamma[k] and pinf[k] (ideal gas: pinf 0); the other laws read mg[k]:
+   *   G5_EOS_JWL         {rho0, Gamma0, A1, A2, R1, R2, e0}
+   *   G5_EOS_SHOCKWAVE   {rho0, Gamma0, c0, s1, s2, s3, b, e0}
+   *   G5_EOS_SHOCKWAVE2  {rho0, Gamma0, c0, s, alpha, e0, p0}
+   * (the [material<k>_mie_gruneisen_jwl/_sw/_sw2] sections of the decks).
+   * A non-stiffened law is stepped in G5_MODE_FP64 only; gamma[k] must still
+   * be > 1 (unused by those laws). */
+  int32_t eos[2];
+  double  mg[2][8];
 } G5Params;
+
+#define G5_EOS_STIFFENED 0
+#define G5_EOS_JWL 1
+#define G5_EOS_SHOCKWAVE 2
+#define G5_EOS_SHOCKWAVE2 3
 
 /*
  * Block table (host pointers; copied to the device by g5_set_mesh).  It

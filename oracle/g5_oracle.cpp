@@ -50,6 +50,8 @@ struct Settings
 {
   double smallr, smallc, smallp, slope_type;
   double gamma[2], pinf[2], xi[2], gpx[2];
+  int    kind[2], mg_any;
+  double mg[2][8], mg_rho0[2];
 };
 
 static Settings
@@ -67,7 +69,12 @@ make_settings(const G5OParams * p)
     s.pinf[k] = p->pinf[k];
     s.xi[k] = 1.0 / (p->gamma[k] - 1.0);
     s.gpx[k] = p->gamma[k] * p->pinf[k] * s.xi[k];
+    s.kind[k] = p->eos[k];
+    for (int j = 0; j < 8; ++j)
+      s.mg[k][j] = p->mg[k][j];
+    s.mg_rho0[k] = p->eos[k] != 0 ? p->mg[k][0] : 1.0;
   }
+  s.mg_any = p->eos[0] != 0 || p->eos[1] != 0;
   return s;
 }
 
@@ -89,35 +96,218 @@ eos_PI(const Settings & s, double a0, double a1)
 {
   return a0 * s.gpx[0] + a1 * s.gpx[1];
 }
+/* Mie-Grueneisen material laws (restated from their published forms; the
+ * reference's core::eos::MieGruneisenMixture is external), each written
+ * p = G(rho) rho e + f(rho), giving G, dG/drho, f, df/drho:
+ *   stiffened gas: G = gamma - 1, f = -gamma pinf
+ *   JWL (Lee, Hornig & Kury 1968), mg = {rho0, Gamma0, A1, A2, R1, R2, e0},
+ *     x_i = R_i rho0/rho: G = Gamma0, f = sum_i A_i (1 - Gamma0/x_i) exp(-x_i) - Gamma0 rho e0
+ *   SHOCKWAVE (Grueneisen form, cubic Us-up Hugoniot fit, Steinberg),
+ *     mg = {rho0, Gamma0, c0, s1, s2, s3, b, e0}, mu = rho/rho0 - 1:
+ *     G rho = (Gamma0 + b mu) rho0, f = pc - (Gamma0 + b mu) rho0 e0,
+ *     pc = rho0 c0^2 mu N/D^2 (mu > 0) else rho0 c0^2 mu,
+ *     N = 1 + (1 - Gamma0/2) mu - b mu^2/2, D = 1 - (s1-1) mu - s2 mu^2/(mu+1) - s3 mu^3/(mu+1)^2
+ *   SHOCKWAVE2 (linear Us-up Hugoniot reference), mg = {rho0, Gamma0, c0, s, alpha, e0, p0},
+ *     eta = 1 - rho0/rho: pH = p0 + rho0 c0^2 eta/(1 - s eta)^2,
+ *     eH = e0 + (pH + p0) eta/(2 rho0), G = Gamma0 (rho0/rho)^alpha, f = pH - G rho eH
+ * Mixture under pressure equilibrium (Allaire, Clerc & Kokh 2002), material
+ * densities rho_k = (alpha rho)_k/alpha_k (rho0_k when alpha_k = 0), xi_k = 1/G_k:
+ *   S = sum a_k xi_k, PI = -sum a_k xi_k f_k: p = (rho e - PI)/S
+ *   rho c^2 S = p C1 + C0, C1 = sum a_k (h_k + 1), C0 = sum a_k (xi_k rho_k f'_k - h_k f_k),
+ *   h_k = xi_k (1 + rho_k G'_k xi_k); bulk modulus rho_k c_k^2 = (1 + rho_k G'_k/G_k)(p - f_k) + rho_k f'_k + G_k p.
+ * exp/log use only IEEE +,-,*,/ and exact frexp/ldexp (exp: Cody-Waite + the
+ * Taylor expm1 below; log: 2 atanh((m-1)/(m+1)) series), so the values are the
+ * same bits on any IEEE machine. */
+static inline double expm1_small(double r);
+
 static inline double
-mixture_pressure(const Settings & s, double rho, double eint, double a0, double a1)
+g5_exp(double x)
 {
-  return (rho * eint - eos_PI(s, a0, a1)) / eos_S(s, a0, a1);
+  if (x != x)
+    return x;
+  if (x < -745.5)
+    return 0.0;
+  if (x > 709.7)
+    return HUGE_VAL;
+  const double k = floor(x * 1.4426950408889634 + 0.5);
+  const double r = (x - k * 0.6931471824645996) - k * -1.904654299957768e-09;
+  return ldexp(expm1_small(r) + 1.0, (int)k);
+}
+
+static inline double
+g5_log(double x)
+{
+  int    e;
+  double m = frexp(x, &e);
+  if (m < 0.7071067811865476)
+  {
+    m = m * 2.0;
+    e = e - 1;
+  }
+  const double t = (m - 1.0) / (m + 1.0);
+  const double t2 = t * t;
+  static const double c[13] = { 1.0 / 1.0,  1.0 / 3.0,  1.0 / 5.0,  1.0 / 7.0,  1.0 / 9.0,  1.0 / 11.0, 1.0 / 13.0,
+                                1.0 / 15.0, 1.0 / 17.0, 1.0 / 19.0, 1.0 / 21.0, 1.0 / 23.0, 1.0 / 25.0 };
+  double              sr = c[12];
+  for (int j = 11; j >= 0; --j)
+    sr = sr * t2 + c[j];
+  const double de = (double)e;
+  return (2.0 * t * sr + de * 0.6931471824645996) + de * -1.904654299957768e-09;
+}
+
+static inline void
+mg_law(const Settings & s, int k, double rho, double & G, double & dG, double & f, double & df)
+{
+  const double * c = s.mg[k];
+  if (s.kind[k] == 1)
+  {
+    const double rho0 = c[0], w = c[1], A1 = c[2], A2 = c[3], R1 = c[4], R2 = c[5], e0 = c[6];
+    const double x1 = R1 * rho0 / rho, x2 = R2 * rho0 / rho;
+    const double E1 = g5_exp(-x1), E2 = g5_exp(-x2);
+    G = w;
+    dG = 0.0;
+    f = A1 * (1.0 - w / x1) * E1 + A2 * (1.0 - w / x2) * E2 - w * rho * e0;
+    df = (A1 * E1 * (x1 - w - w / x1) + A2 * E2 * (x2 - w - w / x2)) / rho - w * e0;
+  }
+  else if (s.kind[k] == 2)
+  {
+    const double rho0 = c[0], g0 = c[1], c0 = c[2], s1 = c[3], s2 = c[4], s3 = c[5], b = c[6], e0 = c[7];
+    const double mu = rho / rho0 - 1.0;
+    const double K = rho0 * c0 * c0;
+    double       pc, dpc;
+    if (mu > 0.0)
+    {
+      const double m1 = mu + 1.0;
+      const double N = 1.0 + (1.0 - 0.5 * g0) * mu - 0.5 * b * mu * mu;
+      const double Np = (1.0 - 0.5 * g0) - b * mu;
+      const double D = 1.0 - (s1 - 1.0) * mu - s2 * mu * mu / m1 - s3 * mu * mu * mu / (m1 * m1);
+      const double Dp = -(s1 - 1.0) - s2 * (mu * mu + 2.0 * mu) / (m1 * m1) - s3 * (mu * mu * mu + 3.0 * mu * mu) / (m1 * m1 * m1);
+      pc = K * mu * N / (D * D);
+      dpc = K * ((N + mu * Np) / (D * D) - 2.0 * mu * N * Dp / (D * D * D));
+    }
+    else
+    {
+      pc = K * mu;
+      dpc = K;
+    }
+    const double gr = (g0 + b * mu) * rho0;
+    G = gr / rho;
+    dG = b / rho - G / rho;
+    f = pc - gr * e0;
+    df = dpc / rho0 - b * e0;
+  }
+  else if (s.kind[k] == 3)
+  {
+    const double rho0 = c[0], g0 = c[1], c0 = c[2], sl = c[3], al = c[4], e0 = c[5], p0 = c[6];
+    const double eta = 1.0 - rho0 / rho;
+    const double w = 1.0 - sl * eta;
+    const double K = rho0 * c0 * c0;
+    const double pH = p0 + K * eta / (w * w);
+    const double eH = e0 + (pH + p0) * eta / (2.0 * rho0);
+    const double v = rho0 / rho;
+    double       gp;
+    if (al == 1.0)
+      gp = v;
+    else if (al == 0.0)
+      gp = 1.0;
+    else
+      gp = g5_exp(al * g5_log(v));
+    G = g0 * gp;
+    dG = -al * G / rho;
+    const double dpH = K * (1.0 + sl * eta) / (w * w * w);
+    const double deH = (dpH * eta + pH + p0) / (2.0 * rho0);
+    const double deta = rho0 / (rho * rho);
+    f = pH - G * rho * eH;
+    df = dpH * deta - (dG * rho + G) * eH - G * rho * deH * deta;
+  }
+  else
+  {
+    G = s.gamma[k] - 1.0;
+    dG = 0.0;
+    f = -s.gamma[k] * s.pinf[k];
+    df = 0.0;
+  }
+}
+
+static inline double
+mg_material_density(const Settings & s, int k, double a, double ar)
+{
+  return a > 0.0 ? fmax(ar / a, s.smallr) : s.mg_rho0[k];
+}
+
+static inline void
+mg_mixture(const Settings & s, double a0, double a1, double ar0, double ar1, double & S, double & PI, double & C1, double & C0)
+{
+  S = 0.0;
+  PI = 0.0;
+  C1 = 0.0;
+  C0 = 0.0;
+  for (int k = 0; k < 2; ++k)
+  {
+    const double a = k == 0 ? a0 : a1;
+    const double rho = mg_material_density(s, k, a, k == 0 ? ar0 : ar1);
+    double       G, dG, f, df;
+    mg_law(s, k, rho, G, dG, f, df);
+    const double xi = 1.0 / G;
+    const double h = xi * (1.0 + rho * dG * xi);
+    S = S + a * xi;
+    PI = PI - a * xi * f;
+    C1 = C1 + a * (h + 1.0);
+    C0 = C0 + a * (xi * rho * df - h * f);
+  }
+}
+
+/* mixture EOS entry points: (a0, a1) volume fractions, (ar0, ar1) partial
+ * densities (read by the Mie-Grueneisen laws only) */
+static inline double
+mixture_pressure(const Settings & s, double rho, double eint, double a0, double a1, double ar0, double ar1)
+{
+  if (!s.mg_any)
+    return (rho * eint - eos_PI(s, a0, a1)) / eos_S(s, a0, a1);
+  double S, PI, C1, C0;
+  mg_mixture(s, a0, a1, ar0, ar1, S, PI, C1, C0);
+  return (rho * eint - PI) / S;
 }
 static inline double
-mixture_specific_eint(const Settings & s, double rho, double p, double a0, double a1)
+mixture_specific_eint(const Settings & s, double rho, double p, double a0, double a1, double ar0, double ar1)
 {
-  return (p * eos_S(s, a0, a1) + eos_PI(s, a0, a1)) / rho;
+  if (!s.mg_any)
+    return (p * eos_S(s, a0, a1) + eos_PI(s, a0, a1)) / rho;
+  double S, PI, C1, C0;
+  mg_mixture(s, a0, a1, ar0, ar1, S, PI, C1, C0);
+  return (p * S + PI) / rho;
 }
 static inline double
-mixture_sound_speed(const Settings & s, double rho, double p, double a0, double a1)
+mixture_sound_speed(const Settings & s, double rho, double p, double a0, double a1, double ar0, double ar1)
 {
-  const double S = eos_S(s, a0, a1);
-  const double c2 = (p * (S + 1.0) + eos_PI(s, a0, a1)) / (rho * S);
+  if (!s.mg_any)
+  {
+    const double S = eos_S(s, a0, a1);
+    const double c2 = (p * (S + 1.0) + eos_PI(s, a0, a1)) / (rho * S);
+    return sqrt(fmax(c2, 0.0));
+  }
+  double S, PI, C1, C0;
+  mg_mixture(s, a0, a1, ar0, ar1, S, PI, C1, C0);
+  const double c2 = (p * C1 + C0) / (rho * S);
   return sqrt(fmax(c2, 0.0));
 }
 
-/* Miller-Puckett factor pieces (restated for the stiffened gas):
- * K_k = gamma_k (p + pinf_k), 1/Kbar = a0/K0 + a1/K1 */
+/* Miller-Puckett factor pieces: K_k = rho_k c_k^2 (stiffened gas:
+ * gamma_k (p + pinf_k)), 1/Kbar = a0/K0 + a1/K1 */
 static inline double
-material_bulk_modulus(const Settings & s, int k, double p)
+material_bulk_modulus(const Settings & s, int k, double p, double a, double ar)
 {
-  return s.gamma[k] * (p + s.pinf[k]);
+  if (!s.mg_any)
+    return s.gamma[k] * (p + s.pinf[k]);
+  const double rho = mg_material_density(s, k, a, ar);
+  double       G, dG, f, df;
+  mg_law(s, k, rho, G, dG, f, df);
+  return (1.0 + rho * dG / G) * (p - f) + rho * df + G * p;
 }
 static inline double
-mixture_bulk_modulus(const Settings & s, double p, double a0, double a1)
+mixture_bulk_modulus(const Settings & s, double p, double a0, double a1, double ar0, double ar1)
 {
-  return 1.0 / (a0 / material_bulk_modulus(s, 0, p) + a1 / material_bulk_modulus(s, 1, p));
+  return 1.0 / (a0 / material_bulk_modulus(s, 0, p, a0, ar0) + a1 / material_bulk_modulus(s, 1, p, a1, ar1));
 }
 
 /* ---------------------------------------------------------------------------
@@ -227,7 +417,7 @@ compute_mixture_pressure(const double * u, const Settings & s) // models/utils.h
   const double d = fmax(u[H::IAD0] + u[H::IAD1], s.smallr);
   const double ekin = compute_mixture_ekin<DIM>(u, s);
   const double eint = u[H::IE] / d - ekin;
-  return mixture_pressure(s, d, eint, u[H::IA0], 1 - u[H::IA0]);
+  return mixture_pressure(s, d, eint, u[H::IA0], 1 - u[H::IA0], u[H::IAD0], u[H::IAD1]);
 }
 
 template <int DIM>
@@ -240,7 +430,7 @@ computePrimitives(const double * u, double * q, const Settings & s) // models/ut
   const double uy = u[H::IV] / d;
   const double ekin = compute_mixture_ekin<DIM>(u, s);
   const double eint = u[H::IE] / d - ekin;
-  const double p = mixture_pressure(s, d, eint, u[H::IA0], 1.0 - u[H::IA0]);
+  const double p = mixture_pressure(s, d, eint, u[H::IA0], 1.0 - u[H::IA0], u[H::IAD0], u[H::IAD1]);
   q[H::ID] = d;
   q[H::IP] = p;
   q[H::IU] = ux;
@@ -252,7 +442,7 @@ computePrimitives(const double * u, double * q, const Settings & s) // models/ut
   q[H::IA1] = 1.0 - q[H::IA0];
   q[H::IAD1] = u[H::IAD1];
   hydro_sanitizer<DIM>(q);
-  return mixture_sound_speed(s, d, p, q[H::IA0], 1.0 - q[H::IA0]);
+  return mixture_sound_speed(s, d, p, q[H::IA0], 1.0 - q[H::IA0], q[H::IAD0], q[H::IAD1]);
 }
 
 /* ---------------------------------------------------------------------------
@@ -269,26 +459,26 @@ riemann_hllc(const double * ql, const double * qr, const Settings & s, double * 
   const double rl = fmax(ql[H::IAD0] + ql[H::IAD1], smallr);
   double       pl = fmax(ql[H::IP], rl * smallp);
   const double ul = ql[H::IU];
-  const double eintl = mixture_specific_eint(s, rl, pl, ql[H::IA0], 1 - ql[H::IA0]);
-  pl = mixture_pressure(s, rl, eintl, ql[H::IA0], 1 - ql[H::IA0]);
+  const double eintl = mixture_specific_eint(s, rl, pl, ql[H::IA0], 1 - ql[H::IA0], ql[H::IAD0], ql[H::IAD1]);
+  pl = mixture_pressure(s, rl, eintl, ql[H::IA0], 1 - ql[H::IA0], ql[H::IAD0], ql[H::IAD1]);
   double ecinl = 0.5 * rl * ul * ul;
   ecinl += 0.5 * rl * ql[H::IV] * ql[H::IV];
   if (DIM == 3)
     ecinl += 0.5 * rl * ql[H::IW] * ql[H::IW];
-  const double cl = mixture_sound_speed(s, rl, pl, ql[H::IA0], 1 - ql[H::IA0]);
+  const double cl = mixture_sound_speed(s, rl, pl, ql[H::IA0], 1 - ql[H::IA0], ql[H::IAD0], ql[H::IAD1]);
   const double etotl = rl * eintl + ecinl;
   const double ptotl = pl;
 
   const double rr = fmax(qr[H::IAD0] + qr[H::IAD1], smallr);
   double       pr = fmax(qr[H::IP], rr * smallp);
   const double ur = qr[H::IU];
-  const double eintr = mixture_specific_eint(s, rr, pr, qr[H::IA0], 1 - qr[H::IA0]);
-  pr = mixture_pressure(s, rr, eintr, qr[H::IA0], 1 - qr[H::IA0]);
+  const double eintr = mixture_specific_eint(s, rr, pr, qr[H::IA0], 1 - qr[H::IA0], qr[H::IAD0], qr[H::IAD1]);
+  pr = mixture_pressure(s, rr, eintr, qr[H::IA0], 1 - qr[H::IA0], qr[H::IAD0], qr[H::IAD1]);
   double ecinr = 0.5 * rr * ur * ur;
   ecinr += 0.5 * rr * qr[H::IV] * qr[H::IV];
   if (DIM == 3)
     ecinr += 0.5 * rr * qr[H::IW] * qr[H::IW];
-  const double cr = mixture_sound_speed(s, rr, pr, qr[H::IA0], 1 - qr[H::IA0]);
+  const double cr = mixture_sound_speed(s, rr, pr, qr[H::IA0], 1 - qr[H::IA0], qr[H::IAD0], qr[H::IAD1]);
   const double etotr = rr * eintr + ecinr;
   const double ptotr = pr;
 
@@ -584,7 +774,7 @@ reconstruct_muscl(const Ctx & x, const double * q, const double * const * sl, co
   const double r = r0 + r1;
   const double p = q[H::IP], u = q[H::IU], v = q[H::IV];
   const double w = DIM == 3 ? q[H::IW] : 0.0;
-  const double c = mixture_sound_speed(x.s, r, p, q[H::IA0], 1 - q[H::IA0]);
+  const double c = mixture_sound_speed(x.s, r, p, q[H::IA0], 1 - q[H::IA0], r0, r1);
   // sl[d][var]
   const double drx0 = sl[0][H::IAD0], drx1 = sl[0][H::IAD1], dpx = sl[0][H::IP], dux = sl[0][H::IU], dvx = sl[0][H::IV];
   const double dry0 = sl[1][H::IAD0], dry1 = sl[1][H::IAD1], dpy = sl[1][H::IP], duy = sl[1][H::IU], dvy = sl[1][H::IV];
@@ -712,7 +902,7 @@ reconstruct_thinc(const Ctx &            x,
   const double p = q[H::IP], u = q[H::IU], v = q[H::IV];
   const double w = DIM == 3 ? q[H::IW] : 0.0;
   const double r = r0 + r1;
-  const double c = mixture_sound_speed(x.s, r, p, q[H::IA0], 1 - q[H::IA0]);
+  const double c = mixture_sound_speed(x.s, r, p, q[H::IA0], 1 - q[H::IA0], r0, r1);
   const double dpx = sl[0][H::IP], dux = sl[0][H::IU], dvx = sl[0][H::IV];
   const double dpy = sl[1][H::IP], duy = sl[1][H::IU], dvy = sl[1][H::IV];
   if (DIM == 2)
@@ -980,9 +1170,9 @@ read_fluxes_and_update(Ctx & x, const double * Uin, double * Uout, int dir)
         for (int v = 0; v < H::NV; ++v)
           u[v] = U_in(v);
         const double pressure = compute_mixture_pressure<DIM>(u, x.s);
-        const double kbar = mixture_bulk_modulus(x.s, pressure, u[H::IA0], u[H::IA1]);
-        st0 = 1.0 - kbar / material_bulk_modulus(x.s, 0, pressure);
-        st1 = 1.0 - kbar / material_bulk_modulus(x.s, 1, pressure);
+        const double kbar = mixture_bulk_modulus(x.s, pressure, u[H::IA0], u[H::IA1], u[H::IAD0], u[H::IAD1]);
+        st0 = 1.0 - kbar / material_bulk_modulus(x.s, 0, pressure, u[H::IA0], u[H::IAD0]);
+        st1 = 1.0 - kbar / material_bulk_modulus(x.s, 1, pressure, u[H::IA1], u[H::IAD1]);
       }
       double acc[H::NV];
       for (int v = 0; v < H::NV; ++v)
@@ -1456,17 +1646,17 @@ g5o_tanh(double x)
 }
 
 extern "C" double
-g5o_mixture_pressure(const G5OParams * prm, double rho, double eint, double a0)
+g5o_mixture_pressure(const G5OParams * prm, double rho, double eint, double a0, double ar0, double ar1)
 {
   const Settings s = make_settings(prm);
-  return mixture_pressure(s, rho, eint, a0, 1.0 - a0);
+  return mixture_pressure(s, rho, eint, a0, 1.0 - a0, ar0, ar1);
 }
 
 extern "C" double
-g5o_mixture_sound_speed(const G5OParams * prm, double rho, double p, double a0)
+g5o_mixture_sound_speed(const G5OParams * prm, double rho, double p, double a0, double ar0, double ar1)
 {
   const Settings s = make_settings(prm);
-  return mixture_sound_speed(s, rho, p, a0, 1.0 - a0);
+  return mixture_sound_speed(s, rho, p, a0, 1.0 - a0, ar0, ar1);
 }
 
 /* ---------------------------------------------------------------------------

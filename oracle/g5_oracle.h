@@ -46,6 +46,8 @@ typedef struct G5OParams
   double  thinc_beta;
   double  thinc_eps;
   double  level_dx[32]; /* cell length per AMR level (already scaled) */
+  int32_t eos[2];       /* material law per material: 0 stiffened gas, 1 JWL, 2 SHOCKWAVE, 3 SHOCKWAVE2 */
+  double  mg[2][8];     /* law parameters (see g5_oracle.cpp, mg_law) */
 } G5OParams;
 
 typedef struct G5OMesh
@@ -99,8 +101,8 @@ double g5o_compute_primitives(const G5OParams * prm, const double * u, double * 
 void   g5o_riemann_hllc(const G5OParams * prm, const double * qL, const double * qR, double * out);
 double g5o_slope(const G5OParams * prm, double q, double qp, double qm);
 double g5o_tanh(double x);
-double g5o_mixture_pressure(const G5OParams * prm, double rho, double eint, double a0);
-double g5o_mixture_sound_speed(const G5OParams * prm, double rho, double p, double a0);
+double g5o_mixture_pressure(const G5OParams * prm, double rho, double eint, double a0, double ar0, double ar1);
+double g5o_mixture_sound_speed(const G5OParams * prm, double rho, double p, double a0, double ar0, double ar1);
 
 #ifdef __cplusplus
 }

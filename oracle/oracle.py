@@ -41,6 +41,8 @@ class G5OParams(ctypes.Structure):
         ("thinc_beta", ctypes.c_double),
         ("thinc_eps", ctypes.c_double),
         ("level_dx", ctypes.c_double * 32),
+        ("eos", ctypes.c_int32 * 2),
+        ("mg", (ctypes.c_double * 8) * 2),
     ]
 
 
@@ -85,9 +87,9 @@ def lib():
         L.g5o_tanh.restype = ctypes.c_double
         L.g5o_tanh.argtypes = [ctypes.c_double]
         L.g5o_mixture_pressure.restype = ctypes.c_double
-        L.g5o_mixture_pressure.argtypes = [ctypes.POINTER(G5OParams), ctypes.c_double, ctypes.c_double, ctypes.c_double]
+        L.g5o_mixture_pressure.argtypes = [ctypes.POINTER(G5OParams)] + [ctypes.c_double] * 5
         L.g5o_mixture_sound_speed.restype = ctypes.c_double
-        L.g5o_mixture_sound_speed.argtypes = [ctypes.POINTER(G5OParams), ctypes.c_double, ctypes.c_double, ctypes.c_double]
+        L.g5o_mixture_sound_speed.argtypes = [ctypes.POINTER(G5OParams)] + [ctypes.c_double] * 5
         L.g5o_remap.argtypes = [ctypes.POINTER(G5OParams), ctypes.c_int, vp, vp, vp, vp]
         L.g5o_derived.argtypes = [ctypes.POINTER(G5OParams), vp, ctypes.c_int, ctypes.c_longlong, ctypes.c_longlong, vp]
         _lib = L
@@ -116,6 +118,10 @@ def make_params(p) -> G5OParams:
     o.thinc_eps = p.thinc_eps
     for i in range(32):
         o.level_dx[i] = float(p.level_dx[i])
+    for k in range(2):
+        o.eos[k] = int(p.eos[k])
+        for j in range(8):
+            o.mg[k][j] = float(p.mg[k][j]) if j < len(p.mg[k]) else 0.0
     return o
 
 
