@@ -1,5 +1,6 @@
 // g5_capi.cu — the C ABI (include/g5gpu.h): context, block-table upload,
 // scratch sizing, launches, the graph-replayed solver loop and the autotuner.
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <vector>
@@ -24,6 +25,7 @@ struct G5Context
   int32_t *d_reflux_slot = nullptr, *d_defer_slot = nullptr, *d_defer_list = nullptr, *d_out_src = nullptr;
   int32_t * d_defer_info = nullptr; // DeferInfo rows, in the order of d_defer_list
   int32_t * d_twin_first = nullptr, *d_twin_list = nullptr; // outside blocks per owned source block
+  int32_t * d_walk = nullptr;                                // block order of the full-mesh step
   bool      fused_fill = false;                              // the 2D solver loop fills them in the step
   int8_t * d_nbr_rel = nullptr, *d_out_normal = nullptr, *d_out_border = nullptr;
   // scratch
@@ -145,7 +147,7 @@ free_mesh(G5Context * c)
   void * ptrs[] = { c->d_level,       c->d_coord,       c->d_nbr,        c->d_inst,       c->d_reflux_slot,
                     c->d_defer_slot,  c->d_defer_list,  c->d_out_src,    c->d_nbr_rel,    c->d_out_normal,
                     c->d_out_border,  c->d_reflux_buf,  c->d_defer_buf,  c->d_dt,         c->d_invdt,
-                    c->d_ticket,      c->d_urk,         c->d_defer_info, c->d_twin_first, c->d_twin_list };
+                    c->d_ticket,      c->d_urk,         c->d_defer_info, c->d_twin_first, c->d_twin_list, c->d_walk };
   for (void * p : ptrs)
     if (p)
       cudaFree(p);
@@ -163,7 +165,7 @@ free_mesh(G5Context * c)
   c->inst_off.clear();
   c->d_urk = nullptr;
   c->d_defer_info = nullptr;
-  c->d_twin_first = c->d_twin_list = nullptr;
+  c->d_twin_first = c->d_twin_list = c->d_walk = nullptr;
   c->fused_fill = false;
   for (void * p : { (void *)c->pipe.d_work, (void *)c->pipe.d_U, (void *)c->pipe.d_U2 })
     if (p)
@@ -231,6 +233,8 @@ do_step(G5Context * c, const double * U, double * U2, const double * d_dt, int m
   a.p = c->phys;
   a.fill_twins = fill_twins ? 1 : 0;
   a.ticket = c->d_ticket;
+  a.work = c->d_walk;
+  a.n_work = c->n_owned;
   int         launches = 0;
   cudaError_t e = mode == G5_MODE_FP64 ? g5::launch_step_fp64(c->dim, c->b, a, c->ctas_per_sm[0], s, &launches)
                                        : g5::launch_step_mixed(c->dim, c->b, a, c->ctas_per_sm[1], s, &launches);
@@ -588,6 +592,25 @@ g5_set_mesh(G5Context * c, const G5Mesh * m)
       return G5_ERR_CUDA;
     }
     c->fused_fill = dim == 2 && m->n_outside > 0;
+  }
+  {
+    // walk order of the full-mesh step: blocks with more neighbour slots at
+    // another level first (their gathers restrict or prolong, they publish or
+    // defer coarse/fine records: they cost more), so that the last round of
+    // the persistent grid holds cheap same-level blocks
+    std::vector<int32_t> order(n_owned), score(n_owned, 0);
+    for (int n = 0; n < n_owned; ++n)
+    {
+      order[n] = n;
+      for (int sl = 0; sl < ns; ++sl)
+        score[n] += m->nbr_rel[(size_t)n * ns + sl] != 0;
+    }
+    std::stable_sort(order.begin(), order.end(), [&](int32_t x, int32_t y) { return score[x] > score[y]; });
+    if (n_owned > 0 && dev_upload(c, &c->d_walk, order.data(), order.size()))
+    {
+      free_mesh(c);
+      return G5_ERR_CUDA;
+    }
   }
   if (n_defer > 0)
   {
