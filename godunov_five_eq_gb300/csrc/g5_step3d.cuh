@@ -43,6 +43,36 @@ neg_zero(float x)
   return __float_as_uint(x) == 0x80000000u;
 }
 
+// halo cell h (0 .. 1215) of an 8^3 block -> ghosted offsets (-2 .. 9): the
+// four z layers outside the block, then the four y rows outside it in each
+// inner z layer, then the four x cells outside it in each inner row (x
+// fastest everywhere, so a warp reads consecutive cells of a neighbour)
+__device__ __forceinline__ void
+halo_coords_3d(int h, int * g)
+{
+  if (h < 576)
+  {
+    const int layer = h / 144, rem = h - layer * 144;
+    g[2] = layer < 2 ? layer - 2 : layer + 6;
+    g[1] = rem / 12 - 2;
+    g[0] = rem % 12 - 2;
+  }
+  else if (h < 960)
+  {
+    const int i = h - 576, z = i / 48, rem = i - z * 48, row = rem / 12;
+    g[2] = z;
+    g[1] = row < 2 ? row - 2 : row + 6;
+    g[0] = rem % 12 - 2;
+  }
+  else
+  {
+    const int i = h - 960, z = i >> 5, rem = i & 31, xs = rem & 3;
+    g[2] = z;
+    g[1] = rem >> 2;
+    g[0] = xs < 2 ? xs - 2 : xs + 6;
+  }
+}
+
 // conservative state seen by ghost cell g of block n (3D); false on a bad index
 __device__ __forceinline__ bool
 gather_ghost_3d(const StepArgs & a, int n, const int * c0, const int * g, double * u)
@@ -344,19 +374,20 @@ step3d_kernel(StepArgs a)
       dtdx_r = a.dt[ins] / dx;
 
     // ---------------- phase 1: own cell (coalesced) + halo -> primitives
+    // (the own cell's loads are in flight while the halo gather runs; its
+    // primitives are stored last)
     double uin[H::NV];
     {
       const double * base = a.U + (size_t)n * H::NV * NC + tid;
 #pragma unroll
       for (int v = 0; v < H::NV; ++v)
         uin[v] = base[v * NC];
-      store_prim3<MIXED>(sQ, (ci + 2) + G * (cj + 2) + GG * (ck + 2), uin, P, stiff);
     }
-    for (int h = tid; h < GGG; h += NT)
+    constexpr int NHALO = GGG - NC;
+    for (int h = tid; h < NHALO; h += NT)
     {
-      const int g[3] = { h % G - 2, (h / G) % G - 2, h / GG - 2 };
-      if (g[0] >= 0 && g[0] < B && g[1] >= 0 && g[1] < B && g[2] >= 0 && g[2] < B)
-        continue;
+      int g[3];
+      halo_coords_3d(h, g);
       double u[H::NV];
       if (!gather_ghost_3d(a, n, c0, g, u))
       {
@@ -365,8 +396,9 @@ step3d_kernel(StepArgs a)
         for (int v = 0; v < H::NV; ++v)
           u[v] = uin[v];
       }
-      store_prim3<MIXED>(sQ, h, u, P, stiff);
+      store_prim3<MIXED>(sQ, (g[0] + 2) + G * (g[1] + 2) + GG * (g[2] + 2), u, P, stiff);
     }
+    store_prim3<MIXED>(sQ, (ci + 2) + G * (cj + 2) + GG * (ck + 2), uin, P, stiff);
     if (tid < 12)
       sSlot[tid] = slot_v;
     if (tid == 12)
@@ -379,7 +411,7 @@ step3d_kernel(StepArgs a)
       if (tid == 0)
         prefetch_l2_range(a.U + (size_t)nn * H::NV * NC, (unsigned)(H::NV * NC * sizeof(double)));
       else if (tid == 1)
-        prefetch_l2_line(a.m.nbr + (size_t)nn * 27 * 8);
+        prefetch_l2_range(a.m.nbr + (size_t)nn * 27 * 8, 27 * 8 * sizeof(int32_t));
       else
         prefetch_l2_line(a.m.nbr_rel + (size_t)nn * 27);
     }
