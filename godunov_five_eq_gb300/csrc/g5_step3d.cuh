@@ -29,7 +29,10 @@ struct Step3DTraits
   static constexpr int NHS = 6;                                 // Hancock source r0 r1 p u v w
   static constexpr int NFF = (B + 1) * B * B;                   // faces of one direction
   static constexpr int NF = 9;                                  // r0 r1 a0 a1 e u v w ustar
-  static constexpr size_t smem_bytes = sizeof(R) * (size_t)(NQ * GGG + NHS * SSS + NF * NFF) + 64;
+  // face-flux buffers: the FP32-bulk form computes the X and Y faces in one
+  // pass (1,152 faces over 512 threads: 3 rounds instead of 2 + 2), Z alone
+  static constexpr int NBUF = MIXED ? 2 : 1;
+  static constexpr size_t smem_bytes = sizeof(R) * (size_t)(NQ * GGG + NHS * SSS + NBUF * NF * NFF) + 64;
 };
 
 __device__ __forceinline__ bool
@@ -72,6 +75,13 @@ halo_coords_3d(int h, int * g)
     g[0] = xs < 2 ? xs - 2 : xs + 6;
   }
 }
+
+// HLLC flux of face f of direction DIR (normal velocity swapped into u and
+// back), scaled by dt/dx into the face buffer sFd ([9][NFF])
+template <bool MIXED, int DIR>
+__device__ __forceinline__ void face_flux3(const typename Step3DTraits<MIXED>::R * sQ, const typename Step3DTraits<MIXED>::R * sHS,
+                                           int f, typename Step3DTraits<MIXED>::R * sFd, typename Step3DTraits<MIXED>::R dtdx_r,
+                                           const PhysParams & P);
 
 // conservative state seen by ghost cell g of block n (3D); false on a bad index
 __device__ __forceinline__ bool
@@ -305,6 +315,63 @@ face_state3(const typename Step3DTraits<MIXED>::R * sQ,
   }
 }
 
+template <bool MIXED, int DIR>
+__device__ __forceinline__ void
+face_flux3(const typename Step3DTraits<MIXED>::R * sQ, const typename Step3DTraits<MIXED>::R * sHS, int f,
+           typename Step3DTraits<MIXED>::R * sFd, typename Step3DTraits<MIXED>::R dtdx_r, const PhysParams & P)
+{
+  using T = Step3DTraits<MIXED>;
+  using R = typename T::R;
+  using H = V<3>;
+  constexpr int B = T::B, NFF = T::NFF;
+  int           fi, fj, fk;
+  if (DIR == 0)
+  {
+    fi = f % (B + 1);
+    fj = (f / (B + 1)) % B;
+    fk = f / ((B + 1) * B);
+  }
+  else if (DIR == 1)
+  {
+    fi = f % B;
+    fj = (f / B) % (B + 1);
+    fk = f / (B * (B + 1));
+  }
+  else
+  {
+    fi = f % B;
+    fj = (f / B) % B;
+    fk = f / (B * B);
+  }
+  R qL[7], qR[7], fl[9];
+  face_state3<MIXED>(sQ, sHS, fi - (DIR == 0), fj - (DIR == 1), fk - (DIR == 2), DIR, +1, P, qL);
+  face_state3<MIXED>(sQ, sHS, fi, fj, fk, DIR, -1, P, qR);
+  if (DIR > 0)
+  {
+    constexpr int iw = DIR == 1 ? 4 : 5; // component swapped with u
+    R             t = qL[3];
+    qL[3] = qL[iw];
+    qL[iw] = t;
+    t = qR[3];
+    qR[3] = qR[iw];
+    qR[iw] = t;
+  }
+  if constexpr (MIXED)
+    hllc_fp32<3>(qL, qR, P.f_xi[0], P.f_xi[1], P.f_gpx[0], P.f_gpx[1], P.f_smallr, P.f_smallp, P.f_smallc, fl);
+  else
+    hllc_fp64<3>(qL, qR, P, fl);
+  if (DIR > 0)
+  {
+    constexpr int fw = DIR == 1 ? H::FV : H::FW;
+    const R       t = fl[H::FU];
+    fl[H::FU] = fl[fw];
+    fl[fw] = t;
+  }
+#pragma unroll
+  for (int k = 0; k < 9; ++k)
+    sFd[k * NFF + f] = fl[k] * dtdx_r;
+}
+
 // one direction of update_U (FP64, reference order); returns nothing, u2 updated
 __device__ __forceinline__ void
 apply_dir_fp64(double * u2, const double * acc)
@@ -502,59 +569,53 @@ step3d_kernel(StepArgs a)
     float hh[3][2], ll[3][2], dA[3][2];
     float es[4] = { 0.f, 0.f, 0.f, 0.f }, et[4] = { 0.f, 0.f, 0.f, 0.f };
 
-    for (int dir = 0; dir < 3; ++dir)
-    {
-      // ---------------- phase 3: faces of this direction
-      for (int f = tid; f < NFF; f += NT)
-      {
-        int fi, fj, fk;
-        if (dir == 0)
-        {
-          fi = f % (B + 1);
-          fj = (f / (B + 1)) % B;
-          fk = f / ((B + 1) * B);
-        }
-        else if (dir == 1)
-        {
-          fi = f % B;
-          fj = (f / B) % (B + 1);
-          fk = f / (B * (B + 1));
-        }
-        else
-        {
-          fi = f % B;
-          fj = (f / B) % B;
-          fk = f / (B * B);
-        }
-        R qL[7], qR[7], fl[9];
-        face_state3<MIXED>(sQ, sHS, fi - (dir == 0), fj - (dir == 1), fk - (dir == 2), dir, +1, P, qL);
-        face_state3<MIXED>(sQ, sHS, fi, fj, fk, dir, -1, P, qR);
-        const int iw = dir == 1 ? 4 : 5; // component swapped with u
-        if (dir > 0)
-        {
-          R t = qL[3];
-          qL[3] = qL[iw];
-          qL[iw] = t;
-          t = qR[3];
-          qR[3] = qR[iw];
-          qR[iw] = t;
-        }
-        if constexpr (MIXED)
-          hllc_fp32<3>(qL, qR, P.f_xi[0], P.f_xi[1], P.f_gpx[0], P.f_gpx[1], P.f_smallr, P.f_smallp, P.f_smallc, fl);
-        else
-          hllc_fp64<3>(qL, qR, P, fl);
-        if (dir > 0)
-        {
-          const int fw = dir == 1 ? H::FV : H::FW;
-          const R   t = fl[H::FU];
-          fl[H::FU] = fl[fw];
-          fl[fw] = t;
-        }
+    // passes of face directions: FP32-bulk {X, Y} then {Z}; FP64 X, Y, Z
 #pragma unroll
-        for (int k = 0; k < 9; ++k)
-          sF[k * NFF + f] = fl[k] * dtdx_r;
+    for (int pass = 0; pass < (MIXED ? 2 : 3); ++pass)
+    {
+      const int d0 = MIXED ? 2 * pass : pass;
+      const int nd = MIXED ? 2 - pass : 1;
+      // ---------------- phase 3: faces of this pass's directions
+      if constexpr (MIXED)
+      {
+        constexpr int XR = NFF - NT; // X faces of the second round
+        if (pass == 0)
+        {
+          face_flux3<MIXED, 0>(sQ, sHS, tid, sF, dtdx_r, P);
+          if (tid < XR)
+            face_flux3<MIXED, 0>(sQ, sHS, tid + NT, sF, dtdx_r, P);
+          else
+            face_flux3<MIXED, 1>(sQ, sHS, tid - XR, sF + T::NF * NFF, dtdx_r, P);
+          constexpr int YR = 2 * NFF - 2 * NT; // Y faces of the third round
+          if (tid < YR)
+            face_flux3<MIXED, 1>(sQ, sHS, tid + NT - XR, sF + T::NF * NFF, dtdx_r, P);
+        }
+        else
+        {
+          face_flux3<MIXED, 2>(sQ, sHS, tid, sF, dtdx_r, P);
+          if (tid < XR)
+            face_flux3<MIXED, 2>(sQ, sHS, tid + NT, sF, dtdx_r, P);
+        }
+      }
+      else
+      {
+        for (int f = tid; f < NFF; f += NT)
+        {
+          if (pass == 0)
+            face_flux3<MIXED, 0>(sQ, sHS, f, sF, dtdx_r, P);
+          else if (pass == 1)
+            face_flux3<MIXED, 1>(sQ, sHS, f, sF, dtdx_r, P);
+          else
+            face_flux3<MIXED, 2>(sQ, sHS, f, sF, dtdx_r, P);
+        }
       }
       __syncthreads();
+
+#pragma unroll
+    for (int dsub = 0; dsub < nd; ++dsub)
+    {
+      const int dir = d0 + dsub;
+      R *       sFd = sF + dsub * T::NF * NFF;
 
       // face index of the owned cell's left/right face in this direction
       const int ext0 = B + (dir == 0), ext1 = B + (dir == 1);
@@ -581,7 +642,7 @@ step3d_kernel(StepArgs a)
             double *  dst = a.reflux_buf + ((size_t)rs * B * B + tid) * 9;
 #pragma unroll
             for (int k = 0; k < 9; ++k)
-              dst[k] = (double)sF[k * NFF + fidx];
+              dst[k] = (double)sFd[k * NFF + fidx];
           }
         }
         // own face fluxes of deferred cells, this direction (left then right)
@@ -598,8 +659,8 @@ step3d_kernel(StepArgs a)
 #pragma unroll
             for (int k = 0; k < 9; ++k)
             {
-              dst[k] = (double)sF[k * NFF + il];
-              dst[9 + k] = (double)sF[k * NFF + ir];
+              dst[k] = (double)sFd[k * NFF + il];
+              dst[9 + k] = (double)sFd[k * NFF + ir];
             }
           }
         }
@@ -612,14 +673,14 @@ step3d_kernel(StepArgs a)
         double       acc[8];
 #pragma unroll
         for (int k = 0; k < 8; ++k)
-          acc[k] = 0.0 + sF[k * NFF + il];
-        const double usl = sF[H::FUS * NFF + il];
+          acc[k] = 0.0 + sFd[k * NFF + il];
+        const double usl = sFd[H::FUS * NFF + il];
         acc[H::FA0] -= st0 * usl * a0n;
         acc[H::FA1] -= st1 * usl * a1n;
 #pragma unroll
         for (int k = 0; k < 8; ++k)
-          acc[k] = acc[k] - sF[k * NFF + ir];
-        const double usr = sF[H::FUS * NFF + ir];
+          acc[k] = acc[k] - sFd[k * NFF + ir];
+        const double usr = sFd[H::FUS * NFF + ir];
         acc[H::FA0] += st0 * usr * a0n;
         acc[H::FA1] += st1 * usr * a1n;
         apply_dir_fp64(u2, acc);
@@ -627,21 +688,22 @@ step3d_kernel(StepArgs a)
       else
       {
         const float a0f = d2f_fast(uin[H::IA0]) * fst0, a1f = d2f_fast(uin[H::IA1]) * fst1;
-        two_diff(sF[H::FR0 * NFF + il], sF[H::FR0 * NFF + ir], hh[dir][0], ll[dir][0]);
-        two_diff(sF[H::FR1 * NFF + il], sF[H::FR1 * NFF + ir], hh[dir][1], ll[dir][1]);
+        two_diff(sFd[H::FR0 * NFF + il], sFd[H::FR0 * NFF + ir], hh[dir][0], ll[dir][0]);
+        two_diff(sFd[H::FR1 * NFF + il], sFd[H::FR1 * NFF + ir], hh[dir][1], ll[dir][1]);
         const int ke[4] = { H::FE, H::FU, H::FV, H::FW };
 #pragma unroll
         for (int e = 0; e < 4; ++e)
         {
           float h, l, t;
-          two_diff(sF[ke[e] * NFF + il], sF[ke[e] * NFF + ir], h, l);
+          two_diff(sFd[ke[e] * NFF + il], sFd[ke[e] * NFF + ir], h, l);
           two_sum(es[e], h, es[e], t);
           et[e] += t + l;
         }
-        const float usl = sF[H::FUS * NFF + il], usr = sF[H::FUS * NFF + ir];
-        dA[dir][0] = ((sF[H::FA0 * NFF + il] - usl * a0f) - sF[H::FA0 * NFF + ir]) + usr * a0f;
-        dA[dir][1] = ((sF[H::FA1 * NFF + il] - usl * a1f) - sF[H::FA1 * NFF + ir]) + usr * a1f;
+        const float usl = sFd[H::FUS * NFF + il], usr = sFd[H::FUS * NFF + ir];
+        dA[dir][0] = ((sFd[H::FA0 * NFF + il] - usl * a0f) - sFd[H::FA0 * NFF + ir]) + usr * a0f;
+        dA[dir][1] = ((sFd[H::FA1 * NFF + il] - usl * a1f) - sFd[H::FA1 * NFF + ir]) + usr * a1f;
       }
+    }
       __syncthreads();
     }
 
