@@ -482,6 +482,20 @@ step3d_kernel(StepArgs a)
       else
         prefetch_l2_line(a.m.nbr_rel + (size_t)nn * 27);
     }
+    // and its same-level or coarser face neighbours (most of its halo), from
+    // the last warp (its table loads stall only that warp)
+    if (tid >= NT - 6 && sNext < nwalk)
+    {
+      const int nn = a.work ? a.work[sNext] : sNext;
+      const int fs = NT - 1 - tid; // face 0..5
+      const int slot = 13 + ((fs & 1) ? 1 : -1) * ((fs >> 1) == 0 ? 1 : ((fs >> 1) == 1 ? 3 : 9));
+      if (a.m.nbr_rel[(size_t)nn * 27 + slot] <= 0)
+      {
+        const int src = a.m.nbr[((size_t)nn * 27 + slot) * 8];
+        if (src >= 0 && src < a.m.n_total)
+          prefetch_l2_range(a.U + (size_t)src * H::NV * NC, (unsigned)(H::NV * NC * sizeof(double)));
+      }
+    }
 
     // ---------------- phase 2: ring cells: Hancock source (and THINC |n|)
     for (int r = tid; r < SSS; r += NT)
