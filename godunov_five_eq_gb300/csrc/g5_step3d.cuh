@@ -626,98 +626,98 @@ step3d_kernel(StepArgs a)
       __syncthreads();
 
 #pragma unroll
-    for (int dsub = 0; dsub < nd; ++dsub)
-    {
-      const int dir = d0 + dsub;
-      R *       sFd = sF + dsub * T::NF * NFF;
-
-      // face index of the owned cell's left/right face in this direction
-      const int ext0 = B + (dir == 0), ext1 = B + (dir == 1);
-      const int il = ci + ext0 * (cj + ext1 * ck);
-      const int step = dir == 0 ? 1 : (dir == 1 ? ext0 : ext0 * ext1);
-      const int ir = il + step;
-
-      // ---------------- publish coarse/fine records of this direction (AMR only)
-      if (a.m.reflux_slot)
+      for (int dsub = 0; dsub < nd; ++dsub)
       {
-        for (int side = 0; side < 2; ++side)
+        const int dir = d0 + dsub;
+        R *       sFd = sF + dsub * T::NF * NFF;
+
+        // face index of the owned cell's left/right face in this direction
+        const int ext0 = B + (dir == 0), ext1 = B + (dir == 1);
+        const int il = ci + ext0 * (cj + ext1 * ck);
+        const int step = dir == 0 ? 1 : (dir == 1 ? ext0 : ext0 * ext1);
+        const int ir = il + step;
+
+        // ---------------- publish coarse/fine records of this direction (AMR only)
+        if (a.m.reflux_slot)
         {
-          const int face = 2 * dir + side;
-          const int rs = sSlot[face];
-          // positions along the face: the two transverse coordinates (first, second)
-          if (rs >= 0 && tid < B * B)
+          for (int side = 0; side < 2; ++side)
           {
-            const int t1 = tid % B, t2 = tid / B;
-            int       c3[3];
-            c3[dir] = side ? B : 0;
-            c3[dir == 0 ? 1 : 0] = t1;
-            c3[dir == 2 ? 1 : 2] = t2;
-            const int fidx = c3[0] + ext0 * (c3[1] + ext1 * c3[2]);
-            double *  dst = a.reflux_buf + ((size_t)rs * B * B + tid) * 9;
-#pragma unroll
-            for (int k = 0; k < 9; ++k)
-              dst[k] = (double)sFd[k * NFF + fidx];
-          }
-        }
-        // own face fluxes of deferred cells, this direction (left then right)
-        if (deferred)
-        {
-          const int cc[3] = { ci, cj, ck };
-          for (int f = 0; f < 6; ++f)
-          {
-            if (dsl[f] < 0 || cc[f >> 1] != ((f & 1) ? B - 1 : 0))
-              continue;
-            const int d2 = f >> 1;
-            const int t1 = cc[d2 == 0 ? 1 : 0], t2 = cc[d2 == 2 ? 1 : 2];
-            double *  dst = a.defer_buf + (((size_t)dsl[f] * B * B + t1 + B * t2) * 6 + 2 * dir) * 9;
-#pragma unroll
-            for (int k = 0; k < 9; ++k)
+            const int face = 2 * dir + side;
+            const int rs = sSlot[face];
+            // positions along the face: the two transverse coordinates (first, second)
+            if (rs >= 0 && tid < B * B)
             {
-              dst[k] = (double)sFd[k * NFF + il];
-              dst[9 + k] = (double)sFd[k * NFF + ir];
+              const int t1 = tid % B, t2 = tid / B;
+              int       c3[3];
+              c3[dir] = side ? B : 0;
+              c3[dir == 0 ? 1 : 0] = t1;
+              c3[dir == 2 ? 1 : 2] = t2;
+              const int fidx = c3[0] + ext0 * (c3[1] + ext1 * c3[2]);
+              double *  dst = a.reflux_buf + ((size_t)rs * B * B + tid) * 9;
+#pragma unroll
+              for (int k = 0; k < 9; ++k)
+                dst[k] = (double)sFd[k * NFF + fidx];
+            }
+          }
+          // own face fluxes of deferred cells, this direction (left then right)
+          if (deferred)
+          {
+            const int cc[3] = { ci, cj, ck };
+            for (int f = 0; f < 6; ++f)
+            {
+              if (dsl[f] < 0 || cc[f >> 1] != ((f & 1) ? B - 1 : 0))
+                continue;
+              const int d2 = f >> 1;
+              const int t1 = cc[d2 == 0 ? 1 : 0], t2 = cc[d2 == 2 ? 1 : 2];
+              double *  dst = a.defer_buf + (((size_t)dsl[f] * B * B + t1 + B * t2) * 6 + 2 * dir) * 9;
+#pragma unroll
+              for (int k = 0; k < 9; ++k)
+              {
+                dst[k] = (double)sFd[k * NFF + il];
+                dst[9 + k] = (double)sFd[k * NFF + ir];
+              }
             }
           }
         }
-      }
 
-      // ---------------- phase 4: this direction's update of the owned cell
-      if constexpr (!MIXED)
-      {
-        const double a0n = uin[H::IA0], a1n = uin[H::IA1];
-        double       acc[8];
-#pragma unroll
-        for (int k = 0; k < 8; ++k)
-          acc[k] = 0.0 + sFd[k * NFF + il];
-        const double usl = sFd[H::FUS * NFF + il];
-        acc[H::FA0] -= st0 * usl * a0n;
-        acc[H::FA1] -= st1 * usl * a1n;
-#pragma unroll
-        for (int k = 0; k < 8; ++k)
-          acc[k] = acc[k] - sFd[k * NFF + ir];
-        const double usr = sFd[H::FUS * NFF + ir];
-        acc[H::FA0] += st0 * usr * a0n;
-        acc[H::FA1] += st1 * usr * a1n;
-        apply_dir_fp64(u2, acc);
-      }
-      else
-      {
-        const float a0f = d2f_fast(uin[H::IA0]) * fst0, a1f = d2f_fast(uin[H::IA1]) * fst1;
-        two_diff(sFd[H::FR0 * NFF + il], sFd[H::FR0 * NFF + ir], hh[dir][0], ll[dir][0]);
-        two_diff(sFd[H::FR1 * NFF + il], sFd[H::FR1 * NFF + ir], hh[dir][1], ll[dir][1]);
-        const int ke[4] = { H::FE, H::FU, H::FV, H::FW };
-#pragma unroll
-        for (int e = 0; e < 4; ++e)
+        // ---------------- phase 4: this direction's update of the owned cell
+        if constexpr (!MIXED)
         {
-          float h, l, t;
-          two_diff(sFd[ke[e] * NFF + il], sFd[ke[e] * NFF + ir], h, l);
-          two_sum(es[e], h, es[e], t);
-          et[e] += t + l;
+          const double a0n = uin[H::IA0], a1n = uin[H::IA1];
+          double       acc[8];
+#pragma unroll
+          for (int k = 0; k < 8; ++k)
+            acc[k] = 0.0 + sFd[k * NFF + il];
+          const double usl = sFd[H::FUS * NFF + il];
+          acc[H::FA0] -= st0 * usl * a0n;
+          acc[H::FA1] -= st1 * usl * a1n;
+#pragma unroll
+          for (int k = 0; k < 8; ++k)
+            acc[k] = acc[k] - sFd[k * NFF + ir];
+          const double usr = sFd[H::FUS * NFF + ir];
+          acc[H::FA0] += st0 * usr * a0n;
+          acc[H::FA1] += st1 * usr * a1n;
+          apply_dir_fp64(u2, acc);
         }
-        const float usl = sFd[H::FUS * NFF + il], usr = sFd[H::FUS * NFF + ir];
-        dA[dir][0] = ((sFd[H::FA0 * NFF + il] - usl * a0f) - sFd[H::FA0 * NFF + ir]) + usr * a0f;
-        dA[dir][1] = ((sFd[H::FA1 * NFF + il] - usl * a1f) - sFd[H::FA1 * NFF + ir]) + usr * a1f;
+        else
+        {
+          const float a0f = d2f_fast(uin[H::IA0]) * fst0, a1f = d2f_fast(uin[H::IA1]) * fst1;
+          two_diff(sFd[H::FR0 * NFF + il], sFd[H::FR0 * NFF + ir], hh[dir][0], ll[dir][0]);
+          two_diff(sFd[H::FR1 * NFF + il], sFd[H::FR1 * NFF + ir], hh[dir][1], ll[dir][1]);
+          const int ke[4] = { H::FE, H::FU, H::FV, H::FW };
+#pragma unroll
+          for (int e = 0; e < 4; ++e)
+          {
+            float h, l, t;
+            two_diff(sFd[ke[e] * NFF + il], sFd[ke[e] * NFF + ir], h, l);
+            two_sum(es[e], h, es[e], t);
+            et[e] += t + l;
+          }
+          const float usl = sFd[H::FUS * NFF + il], usr = sFd[H::FUS * NFF + ir];
+          dA[dir][0] = ((sFd[H::FA0 * NFF + il] - usl * a0f) - sFd[H::FA0 * NFF + ir]) + usr * a0f;
+          dA[dir][1] = ((sFd[H::FA1 * NFF + il] - usl * a1f) - sFd[H::FA1 * NFF + ir]) + usr * a1f;
+        }
       }
-    }
       __syncthreads();
     }
 
