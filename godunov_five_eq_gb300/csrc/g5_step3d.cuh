@@ -583,32 +583,39 @@ step3d_kernel(StepArgs a)
     float hh[3][2], ll[3][2], dA[3][2];
     float es[4] = { 0.f, 0.f, 0.f, 0.f }, et[4] = { 0.f, 0.f, 0.f, 0.f };
 
-    // passes of face directions: FP32-bulk {X, Y} then {Z}; FP64 X, Y, Z
+    // passes of face directions.  FP32-bulk: 1,728 faces in 4 rounds of 512
+    // threads over two flux buffers: pass 0 computes all X faces (buffer 0)
+    // and the first 448 Y faces (buffer 1) and updates X; pass 1 the other
+    // 128 Y faces and all Z faces (into buffer 0) and updates Y and Z.  FP64:
+    // one direction per pass.
 #pragma unroll
     for (int pass = 0; pass < (MIXED ? 2 : 3); ++pass)
     {
-      const int d0 = MIXED ? 2 * pass : pass;
-      const int nd = MIXED ? 2 - pass : 1;
-      // ---------------- phase 3: faces of this pass's directions
+      const int nd = MIXED ? pass + 1 : 1;
+      // ---------------- phase 3: faces of this pass
       if constexpr (MIXED)
       {
-        constexpr int XR = NFF - NT; // X faces of the second round
+        static_assert(NFF > NT && NFF - NT < NT && 3 * NFF - 2 * NT <= 2 * NT, "two rounds of faces per pass");
+        constexpr int XR = NFF - NT;      // X faces of pass 0's second round (64)
+        constexpr int YA = NT - XR;       // Y faces of pass 0 (448)
+        constexpr int YB = NFF - YA;      // Y faces of pass 1 (128)
+        R *           sF1 = sF + T::NF * NFF;
         if (pass == 0)
         {
           face_flux3<MIXED, 0>(sQ, sHS, tid, sF, dtdx_r, P);
           if (tid < XR)
             face_flux3<MIXED, 0>(sQ, sHS, tid + NT, sF, dtdx_r, P);
           else
-            face_flux3<MIXED, 1>(sQ, sHS, tid - XR, sF + T::NF * NFF, dtdx_r, P);
-          constexpr int YR = 2 * NFF - 2 * NT; // Y faces of the third round
-          if (tid < YR)
-            face_flux3<MIXED, 1>(sQ, sHS, tid + NT - XR, sF + T::NF * NFF, dtdx_r, P);
+            face_flux3<MIXED, 1>(sQ, sHS, tid - XR, sF1, dtdx_r, P);
         }
         else
         {
-          face_flux3<MIXED, 2>(sQ, sHS, tid, sF, dtdx_r, P);
-          if (tid < XR)
-            face_flux3<MIXED, 2>(sQ, sHS, tid + NT, sF, dtdx_r, P);
+          if (tid < YB)
+            face_flux3<MIXED, 1>(sQ, sHS, tid + YA, sF1, dtdx_r, P);
+          else
+            face_flux3<MIXED, 2>(sQ, sHS, tid - YB, sF, dtdx_r, P);
+          if (tid < NFF - (NT - YB))
+            face_flux3<MIXED, 2>(sQ, sHS, tid + NT - YB, sF, dtdx_r, P);
         }
       }
       else
@@ -628,8 +635,8 @@ step3d_kernel(StepArgs a)
 #pragma unroll
       for (int dsub = 0; dsub < nd; ++dsub)
       {
-        const int dir = d0 + dsub;
-        R *       sFd = sF + dsub * T::NF * NFF;
+        const int dir = MIXED ? (pass == 0 ? 0 : 1 + dsub) : pass;
+        R *       sFd = sF + (MIXED && dir == 1 ? T::NF * NFF : 0);
 
         // face index of the owned cell's left/right face in this direction
         const int ext0 = B + (dir == 0), ext1 = B + (dir == 1);
