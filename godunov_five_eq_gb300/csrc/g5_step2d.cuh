@@ -110,15 +110,17 @@ gather_ghost_2d(const StepArgs & a, int n, int cx0, int cy0, int gx, int gy, dou
   const int      lx = fx - chx * B, ly = fy - chy * B;
   const double * base = a.U + (size_t)src * H::NV * NC + lx + B * ly;
   const int      vars[6] = { H::IE, H::IU, H::IV, H::IAD0, H::IAD1, H::IA0 };
+  // lx is even: each pair of fine cells in x is one 16-byte load
 #pragma unroll
   for (int t = 0; t < 6; ++t)
   {
-    const double * p = base + vars[t] * NC;
-    double         sum = 0.0;
-    sum += p[0];
-    sum += p[1];
-    sum += p[B];
-    sum += p[B + 1];
+    const double2 * p = reinterpret_cast<const double2 *>(base + vars[t] * NC);
+    const double2   r0 = p[0], r1 = p[B / 2];
+    double          sum = 0.0;
+    sum += r0.x;
+    sum += r0.y;
+    sum += r1.x;
+    sum += r1.y;
     u[vars[t]] = sum / 4.0;
   }
   u[H::IA1] = 1.0 - u[H::IA0];

@@ -130,6 +130,7 @@ gather_ghost_3d(const StepArgs & a, int n, const int * c0, const int * g, double
     return false;
   const double * base = a.U + (size_t)src * H::NV * NC + f0[0] + B * (f0[1] + B * f0[2]);
   const int      vars[7] = { H::IE, H::IU, H::IV, H::IW, H::IAD0, H::IAD1, H::IA0 };
+  // f0[0] is even: each pair of fine cells in x is one 16-byte load
 #pragma unroll
   for (int t = 0; t < 7; ++t)
   {
@@ -139,9 +140,11 @@ gather_ghost_3d(const StepArgs & a, int n, const int * c0, const int * g, double
     for (int oz = 0; oz < 2; ++oz)
 #pragma unroll
       for (int oy = 0; oy < 2; ++oy)
-#pragma unroll
-        for (int ox = 0; ox < 2; ++ox)
-          sum += p[ox + B * (oy + B * oz)];
+      {
+        const double2 r = *reinterpret_cast<const double2 *>(p + B * (oy + B * oz));
+        sum += r.x;
+        sum += r.y;
+      }
     u[vars[t]] = sum / 8.0;
   }
   u[H::IA1] = 1.0 - u[H::IA0];
