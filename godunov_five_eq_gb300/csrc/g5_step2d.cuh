@@ -276,7 +276,7 @@ face_state(const typename Step2DTraits<B, MIXED>::R * sQ,
 // The mixed form of face_state for a face direction known at compile time:
 // q = (q + hs) + off * dq_dir, with q + hs stored by the slope phase, so a
 // face side reads 11 values of shared memory instead of 21.
-template <int B, int DIR>
+template <int B, int DIR, bool THINC>
 __device__ __forceinline__ void
 face_state_mixed(const float * sQ, const float * sRec, int ci, int cj, int side, const PhysParams & P, float * q)
 {
@@ -291,7 +291,7 @@ face_state_mixed(const float * sQ, const float * sRec, int ci, int cj, int side,
     q[k] = sRec[(10 + k) * SS + si] + off * dq[k * SS + si];
   const float a0 = sQ[5 * GG + gi];
   q[5] = a0;
-  if (P.thinc)
+  if constexpr (THINC)
   {
     // THINC (scheme/ComputeFluxesAndStoreTHINCFunctor.cpp:122-283)
     constexpr int o = DIR == 0 ? 1 : G;
@@ -327,7 +327,7 @@ face_state_mixed(const float * sQ, const float * sRec, int ci, int cj, int side,
 
 // HLLC flux of one face of the mixed form, scaled by dt/dx into the shared
 // flux arrays; DIR selects the face set (X faces (B+1) x B, Y faces B x (B+1))
-template <int B, int DIR>
+template <int B, int DIR, bool THINC>
 __device__ __forceinline__ void
 face_flux_mixed(const float * sQ, const float * sRec, float * sF, int ff, float dtdx, const PhysParams & P)
 {
@@ -351,8 +351,8 @@ face_flux_mixed(const float * sQ, const float * sRec, float * sF, int ff, float 
     rj = fj;
   }
   float qL[6], qR[6], fl[8];
-  face_state_mixed<B, DIR>(sQ, sRec, li, lj, +1, P, qL);
-  face_state_mixed<B, DIR>(sQ, sRec, ri, rj, -1, P, qR);
+  face_state_mixed<B, DIR, THINC>(sQ, sRec, li, lj, +1, P, qL);
+  face_state_mixed<B, DIR, THINC>(sQ, sRec, ri, rj, -1, P, qR);
   if (DIR == 1)
   {
     float t = qL[3];
@@ -598,7 +598,10 @@ update_mixed(const double * uin, double * u2, const float * sFx, const float * s
 // 4 CTAs per SM in the FP32-bulk form (64 registers), so that CTAs in the
 // FP64-heavy update overlap with CTAs in the FP32 face phase; 2 CTAs per SM
 // (128 registers) in the FP64 form
-template <int B, bool MIXED>
+// THINC: the FP32-bulk form is compiled with and without the THINC
+// reconstruction (P.thinc picks the kernel), so the MUSCL kernel carries no
+// THINC code; the FP64 form tests P.thinc at run time
+template <int B, bool MIXED, bool THINC = false>
 __global__ void __launch_bounds__(B * B, MIXED ? (B == 16 ? 4 : 8) : (B == 16 ? 2 : 8))
 step2d_kernel(StepArgs a)
 {
@@ -767,9 +770,9 @@ step2d_kernel(StepArgs a)
       for (int f = tid; f < 2 * NFF; f += NT)
       {
         if (f < NFF)
-          face_flux_mixed<B, 0>(sQ, sRec, sFx, f, dtdx_r, P);
+          face_flux_mixed<B, 0, THINC>(sQ, sRec, sFx, f, dtdx_r, P);
         else
-          face_flux_mixed<B, 1>(sQ, sRec, sFy, f - NFF, dtdx_r, P);
+          face_flux_mixed<B, 1, THINC>(sQ, sRec, sFy, f - NFF, dtdx_r, P);
       }
     }
     else
