@@ -23,7 +23,7 @@ num_sms_m()
   return n;
 }
 
-template <int B, bool THINC>
+template <int B, bool THINC, int STIFF>
 static cudaError_t
 launch_step2d_m(const StepArgs & a, int ctas_per_sm, cudaStream_t s, int * launches)
 {
@@ -32,10 +32,10 @@ launch_step2d_m(const StepArgs & a, int ctas_per_sm, cudaStream_t s, int * launc
   static int  occ = 1;
   if (!configured)
   {
-    cudaError_t e = cudaFuncSetAttribute(step2d_kernel<B, true, THINC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::smem_bytes);
+    cudaError_t e = cudaFuncSetAttribute(step2d_kernel<B, true, THINC, STIFF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::smem_bytes);
     if (e != cudaSuccess)
       return e;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, step2d_kernel<B, true, THINC>, T::NT, T::smem_bytes);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, step2d_kernel<B, true, THINC, STIFF>, T::NT, T::smem_bytes);
     if (occ < 1)
       occ = 1;
     configured = true;
@@ -47,7 +47,7 @@ launch_step2d_m(const StepArgs & a, int ctas_per_sm, cudaStream_t s, int * launc
   cudaError_t e = cudaSuccess;
   if (grid >= 1)
   {
-    step2d_kernel<B, true, THINC><<<grid, T::NT, T::smem_bytes, s>>>(a);
+    step2d_kernel<B, true, THINC, STIFF><<<grid, T::NT, T::smem_bytes, s>>>(a);
     ++*launches;
     e = cudaGetLastError();
     if (e != cudaSuccess)
@@ -68,12 +68,18 @@ static int
 occupancy2d_m()
 {
   using T = Step2DTraits<B, true>;
-  cudaFuncSetAttribute(step2d_kernel<B, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::smem_bytes);
-  cudaFuncSetAttribute(step2d_kernel<B, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::smem_bytes);
-  int occ = 0, occ_t = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, step2d_kernel<B, true, false>, T::NT, T::smem_bytes);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_t, step2d_kernel<B, true, true>, T::NT, T::smem_bytes);
-  return occ < occ_t ? occ : occ_t;
+  int occ = 1 << 20;
+  auto one = [&](const void * k) {
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::smem_bytes);
+    int o = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k, T::NT, T::smem_bytes);
+    occ = o < occ ? o : occ;
+  };
+  one((const void *)step2d_kernel<B, true, false, 0>);
+  one((const void *)step2d_kernel<B, true, false, 1>);
+  one((const void *)step2d_kernel<B, true, true, 0>);
+  one((const void *)step2d_kernel<B, true, true, 1>);
+  return occ;
 }
 
 static cudaError_t
@@ -146,10 +152,21 @@ launch_step_mixed(int dim, int b, const StepArgs & a, int ctas_per_sm, cudaStrea
 {
   if (dim == 3 && b == 8)
     return launch_step3d_m(a, ctas_per_sm, s, launches);
-  if (dim == 2 && b == 16)
-    return a.p.thinc ? launch_step2d_m<16, true>(a, ctas_per_sm, s, launches) : launch_step2d_m<16, false>(a, ctas_per_sm, s, launches);
-  if (dim == 2 && b == 8)
-    return a.p.thinc ? launch_step2d_m<8, true>(a, ctas_per_sm, s, launches) : launch_step2d_m<8, false>(a, ctas_per_sm, s, launches);
+  if (dim == 2)
+  {
+    const bool stiff = a.p.gpx[0] != 0.0 || a.p.gpx[1] != 0.0;
+    const int  v = (a.p.thinc ? 2 : 0) + (stiff ? 1 : 0);
+    if (b == 16)
+      return v == 0 ? launch_step2d_m<16, false, 0>(a, ctas_per_sm, s, launches)
+           : v == 1 ? launch_step2d_m<16, false, 1>(a, ctas_per_sm, s, launches)
+           : v == 2 ? launch_step2d_m<16, true, 0>(a, ctas_per_sm, s, launches)
+                    : launch_step2d_m<16, true, 1>(a, ctas_per_sm, s, launches);
+    if (b == 8)
+      return v == 0 ? launch_step2d_m<8, false, 0>(a, ctas_per_sm, s, launches)
+           : v == 1 ? launch_step2d_m<8, false, 1>(a, ctas_per_sm, s, launches)
+           : v == 2 ? launch_step2d_m<8, true, 0>(a, ctas_per_sm, s, launches)
+                    : launch_step2d_m<8, true, 1>(a, ctas_per_sm, s, launches);
+  }
   return cudaErrorInvalidValue;
 }
 

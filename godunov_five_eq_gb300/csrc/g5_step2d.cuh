@@ -598,10 +598,11 @@ update_mixed(const double * uin, double * u2, const float * sFx, const float * s
 // 4 CTAs per SM in the FP32-bulk form (64 registers), so that CTAs in the
 // FP64-heavy update overlap with CTAs in the FP32 face phase; 2 CTAs per SM
 // (128 registers) in the FP64 form
-// THINC: the FP32-bulk form is compiled with and without the THINC
-// reconstruction (P.thinc picks the kernel), so the MUSCL kernel carries no
-// THINC code; the FP64 form tests P.thinc at run time
-template <int B, bool MIXED, bool THINC = false>
+// THINC, STIFF: the FP32-bulk form is compiled with and without the THINC
+// reconstruction and the stiffened-gas pressure path (P picks the kernel), so
+// a kernel carries only the code its case runs; the FP64 form tests both at
+// run time (STIFF = -1)
+template <int B, bool MIXED, bool THINC = false, int STIFF = -1>
 __global__ void __launch_bounds__(B * B, MIXED ? (B == 16 ? 4 : 8) : (B == 16 ? 2 : 8))
 step2d_kernel(StepArgs a)
 {
@@ -624,7 +625,7 @@ step2d_kernel(StepArgs a)
   const int         tid = threadIdx.x;
   const PhysParams & P = a.p;
   // a stiffened-gas constant makes the pressure numerator cancel: FP64 there
-  const bool stiff = P.gpx[0] != 0.0 || P.gpx[1] != 0.0;
+  const bool stiff = STIFF < 0 ? (P.gpx[0] != 0.0 || P.gpx[1] != 0.0) : STIFF == 1;
 
   const int nwalk = step_count(a);
   for (int iw = blockIdx.x; iw < nwalk;)
