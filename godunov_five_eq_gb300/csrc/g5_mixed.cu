@@ -82,6 +82,7 @@ occupancy2d_m()
   return occ;
 }
 
+template <int THINC, int STIFF>
 static cudaError_t
 launch_step3d_m(const StepArgs & a, int ctas_per_sm, cudaStream_t s, int * launches)
 {
@@ -90,10 +91,10 @@ launch_step3d_m(const StepArgs & a, int ctas_per_sm, cudaStream_t s, int * launc
   static int  occ = 1;
   if (!configured)
   {
-    cudaError_t e = cudaFuncSetAttribute(step3d_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::smem_bytes);
+    cudaError_t e = cudaFuncSetAttribute(step3d_kernel<true, THINC, STIFF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::smem_bytes);
     if (e != cudaSuccess)
       return e;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, step3d_kernel<true>, T::NT, T::smem_bytes);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, step3d_kernel<true, THINC, STIFF>, T::NT, T::smem_bytes);
     if (occ < 1)
       occ = 1;
     configured = true;
@@ -105,7 +106,7 @@ launch_step3d_m(const StepArgs & a, int ctas_per_sm, cudaStream_t s, int * launc
   cudaError_t e = cudaSuccess;
   if (grid >= 1)
   {
-    step3d_kernel<true><<<grid, T::NT, T::smem_bytes, s>>>(a);
+    step3d_kernel<true, THINC, STIFF><<<grid, T::NT, T::smem_bytes, s>>>(a);
     ++*launches;
     e = cudaGetLastError();
     if (e != cudaSuccess)
@@ -151,7 +152,14 @@ cudaError_t
 launch_step_mixed(int dim, int b, const StepArgs & a, int ctas_per_sm, cudaStream_t s, int * launches)
 {
   if (dim == 3 && b == 8)
-    return launch_step3d_m(a, ctas_per_sm, s, launches);
+  {
+    const bool stiff = a.p.gpx[0] != 0.0 || a.p.gpx[1] != 0.0;
+    const int  v = (a.p.thinc ? 2 : 0) + (stiff ? 1 : 0);
+    return v == 0 ? launch_step3d_m<0, 0>(a, ctas_per_sm, s, launches)
+         : v == 1 ? launch_step3d_m<0, 1>(a, ctas_per_sm, s, launches)
+         : v == 2 ? launch_step3d_m<1, 0>(a, ctas_per_sm, s, launches)
+                  : launch_step3d_m<1, 1>(a, ctas_per_sm, s, launches);
+  }
   if (dim == 2)
   {
     const bool stiff = a.p.gpx[0] != 0.0 || a.p.gpx[1] != 0.0;
@@ -180,9 +188,17 @@ step_max_ctas_per_sm_mixed(int dim, int b)
   if (dim == 3 && b == 8)
   {
     using T = Step3DTraits<true>;
-    cudaFuncSetAttribute(step3d_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::smem_bytes);
-    int occ = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, step3d_kernel<true>, T::NT, T::smem_bytes);
+    int  occ = 1 << 20;
+    auto one = [&](const void * k) {
+      cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::smem_bytes);
+      int o = 0;
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k, T::NT, T::smem_bytes);
+      occ = o < occ ? o : occ;
+    };
+    one((const void *)step3d_kernel<true, 0, 0>);
+    one((const void *)step3d_kernel<true, 0, 1>);
+    one((const void *)step3d_kernel<true, 1, 0>);
+    one((const void *)step3d_kernel<true, 1, 1>);
     return occ;
   }
   return 0;

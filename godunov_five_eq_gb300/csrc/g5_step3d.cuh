@@ -78,7 +78,7 @@ halo_coords_3d(int h, int * g)
 
 // HLLC flux of face f of direction DIR (normal velocity swapped into u and
 // back), scaled by dt/dx into the face buffer sFd ([9][NFF])
-template <bool MIXED, int DIR>
+template <bool MIXED, int DIR, int THINC>
 __device__ __forceinline__ void face_flux3(const typename Step3DTraits<MIXED>::R * sQ, const typename Step3DTraits<MIXED>::R * sHS,
                                            int f, typename Step3DTraits<MIXED>::R * sFd, typename Step3DTraits<MIXED>::R dtdx_r,
                                            const PhysParams & P);
@@ -209,7 +209,7 @@ youngs_abs_3d(const R * A, int gi, int dir)
   return (nrm > R(0)) ? fabs(-gd / nrm) : R(0);
 }
 
-template <bool MIXED>
+template <bool MIXED, int THINC = -1>
 __device__ __forceinline__ void
 face_state3(const typename Step3DTraits<MIXED>::R * sQ,
             const typename Step3DTraits<MIXED>::R * sHS,
@@ -273,7 +273,7 @@ face_state3(const typename Step3DTraits<MIXED>::R * sQ,
   }
   const R a0 = sQ[6 * GGG + gi];
   q[6] = a0;
-  if (P.thinc)
+  if (THINC < 0 ? P.thinc != 0 : THINC == 1)
   {
     const R *  A = sQ + 6 * GGG;
     const R    aP = A[gi + o], aM = A[gi - o];
@@ -318,7 +318,7 @@ face_state3(const typename Step3DTraits<MIXED>::R * sQ,
   }
 }
 
-template <bool MIXED, int DIR>
+template <bool MIXED, int DIR, int THINC>
 __device__ __forceinline__ void
 face_flux3(const typename Step3DTraits<MIXED>::R * sQ, const typename Step3DTraits<MIXED>::R * sHS, int f,
            typename Step3DTraits<MIXED>::R * sFd, typename Step3DTraits<MIXED>::R dtdx_r, const PhysParams & P)
@@ -347,8 +347,8 @@ face_flux3(const typename Step3DTraits<MIXED>::R * sQ, const typename Step3DTrai
     fk = f / (B * B);
   }
   R qL[7], qR[7], fl[9];
-  face_state3<MIXED>(sQ, sHS, fi - (DIR == 0), fj - (DIR == 1), fk - (DIR == 2), DIR, +1, P, qL);
-  face_state3<MIXED>(sQ, sHS, fi, fj, fk, DIR, -1, P, qR);
+  face_state3<MIXED, THINC>(sQ, sHS, fi - (DIR == 0), fj - (DIR == 1), fk - (DIR == 2), DIR, +1, P, qL);
+  face_state3<MIXED, THINC>(sQ, sHS, fi, fj, fk, DIR, -1, P, qR);
   if (DIR > 0)
   {
     constexpr int iw = DIR == 1 ? 4 : 5; // component swapped with u
@@ -403,7 +403,9 @@ apply_dir_fp64(double * u2, const double * acc)
   u2[H::IW] += acc[H::FW];
 }
 
-template <bool MIXED>
+// THINC, STIFF: compile-time cases of the FP32-bulk form (-1: tested at run
+// time, the FP64 form)
+template <bool MIXED, int THINC = -1, int STIFF = -1>
 __global__ void __launch_bounds__(512, MIXED ? 2 : 1)
 step3d_kernel(StepArgs a)
 {
@@ -422,7 +424,7 @@ step3d_kernel(StepArgs a)
   __shared__ int     sNext;     // the CTA's next block
   const int          tid = threadIdx.x;
   const PhysParams & P = a.p;
-  const bool         stiff = P.gpx[0] != 0.0 || P.gpx[1] != 0.0;
+  const bool         stiff = STIFF < 0 ? (P.gpx[0] != 0.0 || P.gpx[1] != 0.0) : STIFF == 1;
   const int          ci = tid % B, cj = (tid / B) % B, ck = tid / (B * B);
 
   const int nwalk = step_count(a);
@@ -605,20 +607,20 @@ step3d_kernel(StepArgs a)
         R *           sF1 = sF + T::NF * NFF;
         if (pass == 0)
         {
-          face_flux3<MIXED, 0>(sQ, sHS, tid, sF, dtdx_r, P);
+          face_flux3<MIXED, 0, THINC>(sQ, sHS, tid, sF, dtdx_r, P);
           if (tid < XR)
-            face_flux3<MIXED, 0>(sQ, sHS, tid + NT, sF, dtdx_r, P);
+            face_flux3<MIXED, 0, THINC>(sQ, sHS, tid + NT, sF, dtdx_r, P);
           else
-            face_flux3<MIXED, 1>(sQ, sHS, tid - XR, sF1, dtdx_r, P);
+            face_flux3<MIXED, 1, THINC>(sQ, sHS, tid - XR, sF1, dtdx_r, P);
         }
         else
         {
           if (tid < YB)
-            face_flux3<MIXED, 1>(sQ, sHS, tid + YA, sF1, dtdx_r, P);
+            face_flux3<MIXED, 1, THINC>(sQ, sHS, tid + YA, sF1, dtdx_r, P);
           else
-            face_flux3<MIXED, 2>(sQ, sHS, tid - YB, sF, dtdx_r, P);
+            face_flux3<MIXED, 2, THINC>(sQ, sHS, tid - YB, sF, dtdx_r, P);
           if (tid < NFF - (NT - YB))
-            face_flux3<MIXED, 2>(sQ, sHS, tid + NT - YB, sF, dtdx_r, P);
+            face_flux3<MIXED, 2, THINC>(sQ, sHS, tid + NT - YB, sF, dtdx_r, P);
         }
       }
       else
@@ -626,11 +628,11 @@ step3d_kernel(StepArgs a)
         for (int f = tid; f < NFF; f += NT)
         {
           if (pass == 0)
-            face_flux3<MIXED, 0>(sQ, sHS, f, sF, dtdx_r, P);
+            face_flux3<MIXED, 0, THINC>(sQ, sHS, f, sF, dtdx_r, P);
           else if (pass == 1)
-            face_flux3<MIXED, 1>(sQ, sHS, f, sF, dtdx_r, P);
+            face_flux3<MIXED, 1, THINC>(sQ, sHS, f, sF, dtdx_r, P);
           else
-            face_flux3<MIXED, 2>(sQ, sHS, f, sF, dtdx_r, P);
+            face_flux3<MIXED, 2, THINC>(sQ, sHS, f, sF, dtdx_r, P);
         }
       }
       __syncthreads();
