@@ -427,7 +427,7 @@ def main():
         "unit": "cell-updates/s",
         "h2d_bytes_per_step": int(t.n_total * blk),
         "d2h_bytes_per_step": int(t.n_owned * blk),
-        "api": "g5_step_host: pinned host U copied in 8 chunks, chunk steps on 8 streams as neighbours arrive, U2 stored by the kernels into pinned host memory (one CUDA graph)",
+        "api": "g5_step_host: pinned host U copied in chunks of about 3.5 MB (8 to 16), chunk steps on 8 streams as neighbours arrive, U2 stored by the kernels into pinned host memory (one CUDA graph)",
     }
     peak, peak_kind = measured_peaks()
     kern_s = res["mixed"]["kern_ms"] * 1e-3
