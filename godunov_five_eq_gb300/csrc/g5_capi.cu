@@ -249,14 +249,15 @@ plan_host_pipe(G5Context * c, const G5Mesh * m, const std::vector<int32_t> & def
   G5Context::HostPipe & hp = c->pipe;
   const int             n_owned = m->n_owned, ns = c->ns, nch = c->nch, nfaces = 2 * c->dim;
   const int             center = c->dim == 2 ? 4 : 13;
-  // 8 chunks of at least 64 blocks, or more (up to 16) when the chunks would
-  // exceed about 3.5 MB (the copy of chunk 0 is the pipeline's start-up
-  // latency, each chunk's step launch has a fixed cost)
+  // 8 chunks of at least 64 blocks, or in 2D more (up to 16) when the chunks
+  // would exceed about 3.5 MB (the copy of chunk 0 is the pipeline's start-up
+  // latency, each chunk's step launch has a fixed cost; 3D chunks of that size
+  // hold too few blocks whose 26 neighbours have all arrived)
   const double          mbytes = (double)(n_owned + m->n_outside) * c->nv * (c->dim == 2 ? c->b * c->b : c->b * c->b * c->b) * 8.0 / (1 << 20);
   int                   K = n_owned / 64;
   K = K > 8 ? 8 : K;
   const int             Kb = (int)(mbytes / 3.5 + 0.5);
-  K = Kb > K && Kb <= n_owned / 64 ? Kb : K;
+  K = c->dim == 2 && Kb > K && Kb <= n_owned / 64 ? Kb : K;
   K = K < 1 ? 1 : (K > 16 ? 16 : K);
   hp.K = K;
   hp.lo.assign(K + 1, 0);
