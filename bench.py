@@ -60,10 +60,27 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--profile", action="store_true", help="one FP64 and one mixed step kernel launch, for ncu")
     ap.add_argument("--no-clocks", action="store_true", help="skip the nvidia-smi clock sampling (and its bracketing load)")
+    ap.add_argument(
+        "--prolongation",
+        type=int,
+        choices=[0, 1, 2, 3],
+        default=0,
+        help="ghost cells in coarser neighbours: 0 SIMPLE_COPY, 1 minmod extrapolation, 2/3 conservative order 2/4",
+    )
     return ap.parse_args()
 
 
-def build_workload(name, flag_fn):
+def build_workload(name, flag_fn, prolongation=0):
+    desc, t, p, U = _workload(name, flag_fn)
+    if prolongation:
+        import dataclasses
+
+        p = dataclasses.replace(p, prolongation=prolongation)
+        desc += ("", "_minmod_prolongation", "_conservative_o2_prolongation", "_conservative_o4_prolongation")[prolongation]
+    return desc, t, p, U
+
+
+def _workload(name, flag_fn):
     from godunov_five_eq_gb300 import configs
 
     if name == "shock_bubble":
@@ -213,7 +230,7 @@ def run_reference(args):
         return 0
     from oracle.oracle import Oracle, oracle_flag_fn
 
-    desc, t, p, U = build_workload(args.workload, oracle_flag_fn())
+    desc, t, p, U = build_workload(args.workload, oracle_flag_fn(), args.prolongation)
     cores = os.cpu_count() or 1
     o = Oracle(t, p, nthreads=cores)
     A = U.copy()
@@ -310,7 +327,7 @@ def run_profile_case(args):
 
     from godunov_five_eq_gb300 import GodunovImplemGB300, gpu_flag_fn
 
-    desc, t, p, U = build_workload(args.workload, gpu_flag_fn())
+    desc, t, p, U = build_workload(args.workload, gpu_flag_fn(), args.prolongation)
     impl = GodunovImplemGB300(p, t)
     A = torch.from_numpy(U.copy()).cuda()
     B = torch.zeros_like(A)
@@ -341,7 +358,7 @@ def main():
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     from godunov_five_eq_gb300 import GodunovImplemGB300, gpu_flag_fn
 
-    desc, t, p, U = build_workload(args.workload, gpu_flag_fn())
+    desc, t, p, U = build_workload(args.workload, gpu_flag_fn(), args.prolongation)
     cells = t.n_owned * t.ncell
     stream = torch.cuda.current_stream()
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float64, device="cuda")  # 512 MB > L2

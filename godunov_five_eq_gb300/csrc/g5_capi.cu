@@ -26,6 +26,8 @@ struct G5Context
   int32_t * d_defer_info = nullptr; // DeferInfo rows, in the order of d_defer_list
   int32_t * d_twin_first = nullptr, *d_twin_list = nullptr; // outside blocks per owned source block
   int32_t * d_walk = nullptr;                                // block order of the full-mesh step
+  int32_t * d_pg_slot = nullptr;                             // prolonged-ghost slot per owned block (DevMesh::pg_slot)
+  double *  d_pg = nullptr;                                  // prolonged ghost states (DevMesh::pg)
   bool      fused_fill = false;                              // the 2D solver loop fills them in the step
   int8_t * d_nbr_rel = nullptr, *d_out_normal = nullptr, *d_out_border = nullptr;
   // scratch
@@ -147,7 +149,8 @@ free_mesh(G5Context * c)
   void * ptrs[] = { c->d_level,       c->d_coord,       c->d_nbr,        c->d_inst,       c->d_reflux_slot,
                     c->d_defer_slot,  c->d_defer_list,  c->d_out_src,    c->d_nbr_rel,    c->d_out_normal,
                     c->d_out_border,  c->d_reflux_buf,  c->d_defer_buf,  c->d_dt,         c->d_invdt,
-                    c->d_ticket,      c->d_urk,         c->d_defer_info, c->d_twin_first, c->d_twin_list, c->d_walk };
+                    c->d_ticket,      c->d_urk,         c->d_defer_info, c->d_twin_first, c->d_twin_list, c->d_walk,
+                    c->d_pg_slot,     c->d_pg };
   for (void * p : ptrs)
     if (p)
       cudaFree(p);
@@ -165,7 +168,8 @@ free_mesh(G5Context * c)
   c->inst_off.clear();
   c->d_urk = nullptr;
   c->d_defer_info = nullptr;
-  c->d_twin_first = c->d_twin_list = c->d_walk = nullptr;
+  c->d_twin_first = c->d_twin_list = c->d_walk = c->d_pg_slot = nullptr;
+  c->d_pg = nullptr;
   c->fused_fill = false;
   for (void * p : { (void *)c->pipe.d_work, (void *)c->pipe.d_U, (void *)c->pipe.d_U2 })
     if (p)
@@ -207,6 +211,8 @@ dev_mesh(const G5Context * c)
   m.n_total = c->n_total;
   m.n_inst = c->n_inst;
   m.n_defer = c->n_defer;
+  m.pg_slot = c->d_pg_slot;
+  m.pg = c->d_pg;
   return m;
 }
 
@@ -355,7 +361,14 @@ g5_create(const G5Params * params, G5Context ** out_ctx)
     return G5_ERR_UNSUPPORTED;
   if (params->integrator < 0 || params->integrator > 2)
     return G5_ERR_UNSUPPORTED;
-  if ((params->source_term != 0 && params->source_term != 1) || params->prolongation != 0)
+  if (params->source_term != 0 && params->source_term != 1)
+    return G5_ERR_UNSUPPORTED;
+  if (params->prolongation < G5_PROLONG_SIMPLE_COPY || params->prolongation > G5_PROLONG_CONSERVATIVE_O4)
+    return G5_ERR_ARG;
+  // order 4 reaches 3 coarse cells around a block: past the children of a
+  // finer neighbour that touch it (the only ones the block table lists)
+  // unless the blocks have 16 cells per edge
+  if (params->prolongation == G5_PROLONG_CONSERVATIVE_O4 && params->bsize < 16)
     return G5_ERR_UNSUPPORTED;
   for (int k = 0; k < 2; ++k)
     if (!(params->gamma[k] > 1.0))
@@ -534,6 +547,23 @@ g5_set_mesh(G5Context * c, const G5Mesh * m)
     rc = G5_ERR_CUDA;
   if (c->prm.integrator == 2)
     rc |= dev_alloc(c, &c->d_urk, (size_t)n_total * c->nv * (dim == 2 ? c->b * c->b : c->b * c->b * c->b));
+  if (c->prm.prolongation != G5_PROLONG_SIMPLE_COPY)
+  {
+    // one slot of prolonged ghost states per owned block with a coarser neighbour
+    std::vector<int32_t> pg_slot(n_owned, -1);
+    int                  n_pg = 0;
+    for (int n = 0; n < n_owned; ++n)
+      for (int s = 0; s < ns; ++s)
+        if (m->nbr_rel[(size_t)n * ns + s] < 0)
+        {
+          pg_slot[n] = n_pg++;
+          break;
+        }
+    const size_t ng = dim == 2 ? (size_t)(c->b + 4) * (c->b + 4) : (size_t)(c->b + 4) * (c->b + 4) * (c->b + 4);
+    rc |= dev_upload(c, &c->d_pg_slot, pg_slot.data(), pg_slot.size());
+    if (n_pg > 0)
+      rc |= dev_alloc(c, &c->d_pg, (size_t)n_pg * c->nv * ng);
+  }
   if (rc)
   {
     free_mesh(c);

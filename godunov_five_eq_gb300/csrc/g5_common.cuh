@@ -38,6 +38,9 @@ struct PhysParams
   int    mg_any;
   double mg[2][8];
   double mg_rho0[2];
+  // ghost cells in a coarser neighbour: 0 SIMPLE_COPY, 1 EXTRAPOLATE_LINEAR_MINMOD,
+  // 2 / 3 CONSERVATIVE_INTERPOLATION_ORDER_2 / 4
+  int prolong;
 };
 
 struct DevMesh
@@ -59,6 +62,11 @@ struct DevMesh
   const int8_t *  out_border;  // [n_outside*6]
   int             n_owned, n_outside, n_total, n_inst;
   int             n_defer;
+  // prolonged ghost states (prolongation other than SIMPLE_COPY; null
+  // otherwise): pg_slot[n] = the owned block's slot in pg, or -1 when no
+  // neighbour is coarser; pg = [slot][NV][(b+4)^dim ghosted cells]
+  const int32_t * pg_slot = nullptr;
+  double *        pg = nullptr;
 };
 
 // row of the per-record table read by the reflux pass in one wave:

@@ -2,6 +2,7 @@
 // product and sum is rounded separately, as in the reference's arithmetic.
 #include "g5_aux.cuh"
 #include "g5_launch.h"
+#include "g5_prolong.cuh"
 #include "g5_step2d.cuh"
 #include "g5_step3d.cuh"
 
@@ -132,9 +133,45 @@ step_supported(int dim, int b)
   return (dim == 2 && (b == 8 || b == 16)) || (dim == 3 && b == 8);
 }
 
+template <int DIM, int B, int MODE>
+static cudaError_t
+prolong_t(const StepArgs & a, cudaStream_t s, int * launches)
+{
+  using T = ProlongTraits<DIM, B, MODE>;
+  int grid = num_sms() * 8;
+  if (grid > step_count(a))
+    grid = step_count(a);
+  if (grid < 1)
+    return cudaSuccess;
+  prolong_kernel<DIM, B, MODE><<<grid, T::NT, T::smem_bytes, s>>>(a);
+  ++*launches;
+  return cudaGetLastError();
+}
+
+cudaError_t
+launch_prolong(int dim, int b, const StepArgs & a, cudaStream_t s, int * launches)
+{
+  if (!a.m.pg)
+    return cudaSuccess;
+  const int mode = a.p.prolong;
+  if (dim == 2 && b == 16)
+    return mode == 1 ? prolong_t<2, 16, 1>(a, s, launches)
+         : mode == 2 ? prolong_t<2, 16, 2>(a, s, launches)
+         : mode == 3 ? prolong_t<2, 16, 3>(a, s, launches)
+                     : cudaErrorInvalidValue;
+  if (dim == 2 && b == 8)
+    return mode == 1 ? prolong_t<2, 8, 1>(a, s, launches) : mode == 2 ? prolong_t<2, 8, 2>(a, s, launches) : cudaErrorInvalidValue;
+  if (dim == 3 && b == 8)
+    return mode == 1 ? prolong_t<3, 8, 1>(a, s, launches) : mode == 2 ? prolong_t<3, 8, 2>(a, s, launches) : cudaErrorInvalidValue;
+  return cudaErrorInvalidValue;
+}
+
 cudaError_t
 launch_step_fp64(int dim, int b, const StepArgs & a, int ctas_per_sm, cudaStream_t s, int * launches)
 {
+  const cudaError_t e = launch_prolong(dim, b, a, s, launches);
+  if (e != cudaSuccess)
+    return e;
   if (dim == 2 && b == 16)
     return launch_step2d<16, false>(a, ctas_per_sm, s, launches);
   if (dim == 2 && b == 8)

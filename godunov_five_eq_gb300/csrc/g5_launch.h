@@ -13,6 +13,9 @@ namespace g5
 // ctas_per_sm <= 0 selects the occupancy maximum.  Returns the launch error.
 cudaError_t launch_step_fp64(int dim, int b, const StepArgs & a, int ctas_per_sm, cudaStream_t s, int * launches);
 cudaError_t launch_step_mixed(int dim, int b, const StepArgs & a, int ctas_per_sm, cudaStream_t s, int * launches);
+// ghost cells in coarser neighbours prolonged into a.m.pg (nothing when
+// a.m.pg is null, i.e. SIMPLE_COPY); launched by both step launchers first
+cudaError_t launch_prolong(int dim, int b, const StepArgs & a, cudaStream_t s, int * launches);
 // whether the (dim, b) pair is compiled
 bool step_supported(int dim, int b);
 // occupancy (CTAs per SM) of the fused step kernel

@@ -151,6 +151,9 @@ launch_rk2_combine_mixed(int dim, int b, const double * U, double * U2, const De
 cudaError_t
 launch_step_mixed(int dim, int b, const StepArgs & a, int ctas_per_sm, cudaStream_t s, int * launches)
 {
+  const cudaError_t e = launch_prolong(dim, b, a, s, launches);
+  if (e != cudaSuccess)
+    return e;
   if (dim == 3 && b == 8)
   {
     const bool stiff = a.p.gpx[0] != 0.0 || a.p.gpx[1] != 0.0;

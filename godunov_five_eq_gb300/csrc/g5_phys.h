@@ -73,6 +73,7 @@ make_phys(const G5Params * params)
     p.mg_rho0[k] = params->eos[k] != G5_EOS_STIFFENED ? params->mg[k][0] : 1.0;
   }
   p.mg_any = params->eos[0] != G5_EOS_STIFFENED || params->eos[1] != G5_EOS_STIFFENED;
+  p.prolong = params->prolongation;
   return p;
 }
 

@@ -90,6 +90,19 @@ gather_ghost_2d(const StepArgs & a, int n, int cx0, int cy0, int gx, int gy, dou
   }
   if (rel < 0)
   {
+    if (a.m.pg)
+    {
+      // prolonged by the pre-pass (minmod extrapolation or conservative interpolation)
+      constexpr int GG = (B + 4) * (B + 4);
+      const int     ps = a.m.pg_slot[n];
+      if (ps < 0)
+        return false;
+      const double * base = a.m.pg + (size_t)ps * H::NV * GG + (gx + 2) + (B + 4) * (gy + 2);
+#pragma unroll
+      for (int v = 0; v < H::NV; ++v)
+        u[v] = base[v * GG];
+      return true;
+    }
     const int src = nb[0];
     if (src < 0 || src >= a.m.n_total)
       return false;

@@ -102,6 +102,19 @@ gather_ghost_3d(const StepArgs & a, int n, const int * c0, const int * g, double
   const int4  nb_lo = *reinterpret_cast<const int4 *>(a.m.nbr + (n * 27 + s) * 8);
   const int4  nb_hi = *reinterpret_cast<const int4 *>(a.m.nbr + (n * 27 + s) * 8 + 4);
   const int   nb[8] = { nb_lo.x, nb_lo.y, nb_lo.z, nb_lo.w, nb_hi.x, nb_hi.y, nb_hi.z, nb_hi.w };
+  if (rel < 0 && a.m.pg)
+  {
+    // prolonged by the pre-pass (minmod extrapolation or conservative interpolation)
+    constexpr int G = B + 4, GGG = G * G * G;
+    const int     ps = a.m.pg_slot[n];
+    if (ps < 0)
+      return false;
+    const double * base = a.m.pg + (size_t)ps * H::NV * GGG + (g[0] + 2) + G * ((g[1] + 2) + G * (g[2] + 2));
+#pragma unroll
+    for (int k = 0; k < H::NV; ++k)
+      u[k] = base[k * GGG];
+    return true;
+  }
   if (rel <= 0)
   {
     const int src = nb[0];

@@ -68,7 +68,7 @@ typedef struct G5Params
   int32_t integrator;   /* 0 HANCOCK, 1 RK1, 2 RK2_SSP (two stages in g5_advance / g5_run) */
   int32_t thinc;        /* 0 MUSCL, 1 THINC interface reconstruction */
   int32_t source_term;  /* 0 ALLAIRE_KOKH, 1 MILLER_PUCKETT */
-  int32_t prolongation; /* 0 SIMPLE_COPY (only value implemented) */
+  int32_t prolongation; /* ghost cells in a coarser neighbour: G5_PROLONG_* below */
   int32_t bc[6];        /* xmin xmax ymin ymax zmin zmax */
   double  gamma[2];
   double  pinf[2];
@@ -95,6 +95,18 @@ typedef struct G5Params
 #define G5_EOS_JWL 1
 #define G5_EOS_SHOCKWAVE 2
 #define G5_EOS_SHOCKWAVE2 3
+
+/* CellCenteredProlongationType of the ghost fill
+ * (scheme/ConvertToPrimitivesVariablesFunctor.cpp:893-917).  SIMPLE_COPY
+ * copies the coarse cell; the others are computed by a pass before each step
+ * kernel launch (g5_step, g5_step_batched, g5_step_host, g5_advance, g5_run)
+ * from the coarse cells around the block.  CONSERVATIVE_O4 needs bsize 16
+ * (g5_create returns G5_ERR_UNSUPPORTED otherwise); g5_step_static supports
+ * SIMPLE_COPY only. */
+#define G5_PROLONG_SIMPLE_COPY 0
+#define G5_PROLONG_EXTRAPOLATE_LINEAR_MINMOD 1
+#define G5_PROLONG_CONSERVATIVE_O2 2
+#define G5_PROLONG_CONSERVATIVE_O4 3
 
 /*
  * Block table (host pointers; copied to the device by g5_set_mesh).  It

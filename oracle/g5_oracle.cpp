@@ -17,7 +17,9 @@
  *   - Youngs normal (3x3(x3) weighted central differences, unit cell);
  *   - stencil semantics: restriction = mean of the 2^dim fine cells,
  *     prolongation = SIMPLE_COPY of the coarse cell containing the ghost
- *     cell centre, coarse/fine face sums over the 2^(dim-1) fine faces;
+ *     cell centre, or the minmod extrapolation / conservative order-2 and
+ *     order-4 interpolation of prolong_ghost, coarse/fine face sums over the
+ *     2^(dim-1) fine faces;
  *   - tanh evaluated by g5o_tanh (Cody-Waite reduced Taylor expm1).
  */
 #include "g5_oracle.h"
@@ -627,13 +629,169 @@ load_u(const Ctx & x, const double * U, int n, int c, double * u)
 }
 
 /* ---------------------------------------------------------------------------
+ * Prolongation of a ghost cell that lies in a coarser neighbour
+ * (ConvertToPrimitivesVariablesFunctor.cpp:893-917).  The stencil helpers the
+ * reference calls (getNeighLoc, compute_minmod_slopes,
+ * compute_linear_combination, the ConservativeInterpolation coefficient
+ * tables) live in the external kalypsso core; restated here:
+ *
+ *  - a stencil point is a level-(l-1) cell q of the coarse grid around owned
+ *    block n (l = the block's level; q in coarse cells relative to the block,
+ *    whose footprint is [0, b/2)^dim).  Its value is the cell of the
+ *    coarser neighbour that holds it, the mean of the 2^dim level-l cells
+ *    that cover it (the block itself or a same-level neighbour), or, in a
+ *    finer neighbour, the mean of those 2^dim means of 2^dim level-(l+1)
+ *    cells (sums x fastest, then divided by 2^dim, as the restriction);
+ *  - EXTRAPOLATE_LINEAR_MINMOD (:278-300, :544-620): the coarse value plus
+ *    0.25 * (+-1) * the minmod slope (ComputeLimitedSlopesFunctor's slope with
+ *    slope_type 1) per direction, +1 for the upper half of the coarse cell;
+ *  - CONSERVATIVE_INTERPOLATION_ORDER_2/4 (:341-488): the half-cell averages
+ *    of the quadratic (quartic) polynomial whose cell averages match 3 (5)
+ *    coarse cells, applied along x, then y (then z):
+ *    lower half (1/8, 1, -1/8), (-3/128, 22/128, 1, -22/128, 3/128), upper
+ *    half the same reversed; sums left to right.
+ * ID = IAD0 + IAD1 and IA1 = 1 - IA0 are recomputed as the reference does.
+ * ------------------------------------------------------------------------- */
+template <int DIM>
+static double
+coarse_cell_value(const Ctx & x, const double * U, int n, const int * q, int var)
+{
+  using H = Ids<DIM>;
+  const Geo<DIM> geo(x.b);
+  const int      b = x.b, h = b / 2;
+  int            s[3] = { 0, 0, 0 }, f[3] = { 0, 0, 0 };
+  bool           own = true;
+  for (int e = 0; e < DIM; ++e)
+  {
+    s[e] = q[e] < 0 ? -1 : (q[e] >= h ? 1 : 0);
+    f[e] = 2 * q[e] - s[e] * b; // first level-l cell of q in the slot's same-level block
+    if (s[e] != 0)
+      own = false;
+  }
+  auto cellv = [&](int blk, int i, int j, int k) { return U[((size_t)blk * H::NV + var) * geo.ncell() + geo.cell(i, j, k)]; };
+  auto mean = [&](int blk, int i0, int j0, int k0) {
+    double sum = 0.0;
+    for (int oz = 0; oz < (DIM == 3 ? 2 : 1); ++oz)
+      for (int oy = 0; oy < 2; ++oy)
+        for (int ox = 0; ox < 2; ++ox)
+          sum += cellv(blk, i0 + ox, j0 + oy, k0 + oz);
+    return sum / (double)(1 << DIM);
+  };
+  if (own)
+    return mean(n, f[0], f[1], f[2]);
+  const int       slot = slot_index(DIM, s);
+  const int       rel = x.nbr_rel[(size_t)n * x.ns + slot];
+  const int32_t * nb = &x.nbr[((size_t)n * x.ns + slot) * x.nc];
+  if (rel == 0)
+    return mean(nb[0], f[0], f[1], f[2]);
+  if (rel < 0)
+  {
+    int cc[3] = { 0, 0, 0 };
+    for (int e = 0; e < DIM; ++e)
+      cc[e] = ((x.coord[(size_t)n * 3 + e] + s[e]) & 1) * h + (f[e] >> 1);
+    return cellv(nb[0], cc[0], cc[1], cc[2]);
+  }
+  int ch[3] = { 0, 0, 0 }, l[3] = { 0, 0, 0 };
+  for (int e = 0; e < DIM; ++e)
+  {
+    ch[e] = f[e] >= h ? 1 : 0;
+    l[e] = 2 * (f[e] - ch[e] * h);
+  }
+  const int F = nb[DIM == 2 ? ch[0] + 2 * ch[1] : ch[0] + 2 * ch[1] + 4 * ch[2]];
+  double    sum = 0.0;
+  for (int oz = 0; oz < (DIM == 3 ? 2 : 1); ++oz)
+    for (int oy = 0; oy < 2; ++oy)
+      for (int ox = 0; ox < 2; ++ox)
+        sum += mean(F, l[0] + 2 * ox, l[1] + 2 * oy, l[2] + 2 * oz);
+  return sum / (double)(1 << DIM);
+}
+
+static const double kConsO2[2][3] = { { 0.125, 1.0, -0.125 }, { -0.125, 1.0, 0.125 } };
+static const double kConsO4[2][5] = { { -3.0 / 128.0, 22.0 / 128.0, 1.0, -22.0 / 128.0, 3.0 / 128.0 },
+                                      { 3.0 / 128.0, -22.0 / 128.0, 1.0, 22.0 / 128.0, -3.0 / 128.0 } };
+
+static inline double
+lin_comb(const double * c, const double * v, int np)
+{
+  double r = c[0] * v[0];
+  for (int i = 1; i < np; ++i)
+    r = r + c[i] * v[i];
+  return r;
+}
+
+/* conservative state of ghost cell g (block coords, in a coarser slot) */
+template <int DIM>
+static void
+prolong_ghost(const Ctx & x, const double * U, int n, const int * g, double * u)
+{
+  using H = Ids<DIM>;
+  int q[3] = { 0, 0, 0 }, pos[3] = { 0, 0, 0 };
+  for (int e = 0; e < DIM; ++e)
+  {
+    q[e] = (g[e] + 2) / 2 - 1; // coarse cell holding the ghost cell
+    pos[e] = (g[e] + 2) & 1;   // 0 lower, 1 upper half
+  }
+  const int vars[7] = { H::IAD0, H::IAD1, H::IA0, H::IE, H::IU, H::IV, H::IW };
+  const int nvars = DIM == 2 ? 6 : 7;
+  const int mode = x.prm.prolongation;
+  for (int t = 0; t < nvars; ++t)
+  {
+    const int var = vars[t];
+    double    r;
+    if (mode == 1)
+    {
+      const double u0 = coarse_cell_value<DIM>(x, U, n, q, var);
+      double       sl[3] = { 0.0, 0.0, 0.0 };
+      for (int e = 0; e < DIM; ++e)
+      {
+        int qp[3] = { q[0], q[1], q[2] }, qm[3] = { q[0], q[1], q[2] };
+        qp[e] += 1;
+        qm[e] -= 1;
+        sl[e] = slope_unsplit_scalar(
+          u0, coarse_cell_value<DIM>(x, U, n, qp, var), coarse_cell_value<DIM>(x, U, n, qm, var), 1.0);
+      }
+      r = u0;
+      for (int e = 0; e < DIM; ++e)
+        r = r + 0.25 * (double)(pos[e] ? 1 : -1) * sl[e];
+    }
+    else
+    {
+      const int      rr = mode == 2 ? 1 : 2, np = 2 * rr + 1;
+      const double * cx = mode == 2 ? kConsO2[pos[0]] : kConsO4[pos[0]];
+      const double * cy = mode == 2 ? kConsO2[pos[1]] : kConsO4[pos[1]];
+      const double * cz = mode == 2 ? kConsO2[DIM == 3 ? pos[2] : 0] : kConsO4[DIM == 3 ? pos[2] : 0];
+      double         valy[5];
+      for (int k = (DIM == 3 ? -rr : 0); k <= (DIM == 3 ? rr : 0); ++k)
+      {
+        double valx[5];
+        for (int j = -rr; j <= rr; ++j)
+        {
+          double pts[5];
+          for (int i = -rr; i <= rr; ++i)
+          {
+            const int qq[3] = { q[0] + i, q[1] + j, q[2] + k };
+            pts[i + rr] = coarse_cell_value<DIM>(x, U, n, qq, var);
+          }
+          valx[j + rr] = lin_comb(cx, pts, np);
+        }
+        valy[DIM == 3 ? k + rr : 0] = lin_comb(cy, valx, np);
+      }
+      r = DIM == 3 ? lin_comb(cz, valy, np) : valy[0];
+    }
+    u[var] = r;
+  }
+  u[H::ID] = u[H::IAD0] + u[H::IAD1];
+  u[H::IA1] = 1.0 - u[H::IA0];
+}
+
+/* ---------------------------------------------------------------------------
  * ConvertToPrimitivesVariablesFunctor::fill_ghosts
  * (scheme/ConvertToPrimitivesVariablesFunctor.cpp:833-926): one ghosted cell
  * (g = cell coords relative to the block, in [-2, b+2)) of owned block n.
  * ------------------------------------------------------------------------- */
 template <int DIM>
 static void
-fill_ghost_cell(const Ctx & x, const double * U, int n, const int * g, double * q)
+ghost_state(const Ctx & x, const double * U, int n, const int * g, double * u)
 {
   using H = Ids<DIM>;
   const Geo<DIM> geo(x.b);
@@ -647,7 +805,6 @@ fill_ghost_cell(const Ctx & x, const double * U, int n, const int * g, double * 
     if (d[e] != 0)
       inner = false;
   }
-  double u[H::NV];
   if (inner)
   {
     // fill_inner, :494-510
@@ -662,6 +819,12 @@ fill_ghost_cell(const Ctx & x, const double * U, int n, const int * g, double * 
     {
       // same level: plain copy (fill_ghost_copy without restriction, :516-537)
       load_u<DIM>(x, U, nb[0], geo.cell(v[0], v[1], v[2]), u);
+    }
+    else if (rel < 0 && x.prm.prolongation != 0)
+    {
+      // coarser neighbour, EXTRAPOLATE_LINEAR_MINMOD or conservative
+      // interpolation (:898-912)
+      prolong_ghost<DIM>(x, U, n, g, u);
     }
     else if (rel < 0)
     {
@@ -710,6 +873,15 @@ fill_ghost_cell(const Ctx & x, const double * U, int n, const int * g, double * 
       u[H::ID] = u[H::IAD0] + u[H::IAD1];
     }
   }
+}
+
+template <int DIM>
+static void
+fill_ghost_cell(const Ctx & x, const double * U, int n, const int * g, double * q)
+{
+  using H = Ids<DIM>;
+  double u[H::NV];
+  ghost_state<DIM>(x, U, n, g, u);
   double qq[H::NV];
   computePrimitives<DIM>(u, qq, x.s);
   // set_primitive_vars, :252-270
@@ -1576,6 +1748,25 @@ extern "C" void
 g5o_destroy(void * ctx)
 {
   delete static_cast<Ctx *>(ctx);
+}
+
+/* conservative state that the ghost fill of owned block n gives ghosted cell
+ * g (block cell coordinates, -2 .. b+1; g[2] = 0 in 2D) before the
+ * conversion to primitives */
+extern "C" int
+g5o_ghost_state(void * ctx, const double * U, int n, const int * g, double * u)
+{
+  Ctx * x = static_cast<Ctx *>(ctx);
+  if (n < 0 || n >= x->n_owned)
+    return -1;
+  for (int e = 0; e < x->dim; ++e)
+    if (g[e] < -2 || g[e] >= x->b + 2)
+      return -1;
+  if (x->dim == 2)
+    ghost_state<2>(*x, U, n, g, u);
+  else
+    ghost_state<3>(*x, U, n, g, u);
+  return 0;
 }
 
 extern "C" int

@@ -35,7 +35,7 @@ typedef struct G5OParams
   int32_t integrator;   /* 0 HANCOCK, 1 RK1 */
   int32_t thinc;        /* 0 MUSCL, 1 THINC */
   int32_t source_term;  /* 0 ALLAIRE_KOKH, 1 MILLER_PUCKETT */
-  int32_t prolongation; /* 0 SIMPLE_COPY */
+  int32_t prolongation; /* 0 SIMPLE_COPY, 1 EXTRAPOLATE_LINEAR_MINMOD, 2/3 CONSERVATIVE_INTERPOLATION_ORDER_2/4 */
   int32_t bc[6];        /* per face (xmin,xmax,ymin,ymax,zmin,zmax): 0 NONE 1 PERIODIC 2 ZERO_GRADIENT 3 WALL */
   double  gamma[2];
   double  pinf[2];
@@ -71,6 +71,9 @@ void * g5o_create(const G5OMesh * mesh, const G5OParams * prm, int nthreads);
 void   g5o_destroy(void * ctx);
 /* U2 owned blocks <- one step of U; dt[inst] per instance.  returns 0 */
 int    g5o_step(void * ctx, const double * U, double * U2, const double * dt);
+/* conservative state the ghost fill of owned block n gives its ghosted cell
+ * g (g[e] in -2 .. b+1; g[2] = 0 in 2D), before the primitive conversion */
+int    g5o_ghost_state(void * ctx, const double * U, int n, const int * g, double * u);
 /* max over owned cells of sum_d (c+|u_d|)/dx, per instance */
 int    g5o_inv_dt(void * ctx, const double * U, double * inv_dt);
 /* fill outside blocks of U from inside blocks (boundary conditions) */

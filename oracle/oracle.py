@@ -78,6 +78,7 @@ def lib():
         L.g5o_step.argtypes = [vp, vp, vp, vp]
         L.g5o_inv_dt.argtypes = [vp, vp, vp]
         L.g5o_fill_outside.argtypes = [vp, vp]
+        L.g5o_ghost_state.argtypes = [vp, vp, ctypes.c_int, vp, vp]
         L.g5o_refine_flags.argtypes = [vp, vp, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int, vp]
         L.g5o_compute_primitives.restype = ctypes.c_double
         L.g5o_compute_primitives.argtypes = [ctypes.POINTER(G5OParams), vp, vp]
@@ -171,6 +172,17 @@ class Oracle:
     def fill_outside(self, U: np.ndarray) -> None:
         assert U.dtype == np.float64 and U.flags.c_contiguous
         lib().g5o_fill_outside(self.ctx, _ptr(U))
+
+    def ghost_state(self, U: np.ndarray, n: int, g) -> np.ndarray:
+        """Conservative state the ghost fill of owned block n gives its
+        ghosted cell g (block cell coordinates, -2 .. b+1)."""
+        assert U.dtype == np.float64 and U.flags.c_contiguous
+        gg = np.zeros(3, np.int32)
+        gg[: len(g)] = g
+        out = np.zeros(self.table.nv)
+        if lib().g5o_ghost_state(self.ctx, _ptr(U), int(n), _ptr(gg), _ptr(out)) != 0:
+            raise ValueError("ghost cell out of range")
+        return out
 
     def inv_dt(self, U: np.ndarray) -> np.ndarray:
         out = np.zeros(self.table.n_inst)
