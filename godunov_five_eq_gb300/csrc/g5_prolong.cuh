@@ -169,16 +169,60 @@ prolong_coef(int mode, int upper, int i)
   }
 }
 
+// linear combination sum_i c(i) v(i), i = -R .. R, left to right
+template <int R, typename F>
+__device__ __forceinline__ double
+prolong_lin(int mode, int upper, F v)
+{
+  double acc = prolong_coef(mode, upper, -R) * v(-R);
+#pragma unroll
+  for (int i = -R + 1; i <= R; ++i)
+    acc = acc + prolong_coef(mode, upper, i) * v(i);
+  return acc;
+}
+
+// One CTA per walked block with a coarser neighbour:
+//  1. the coarser slots and the prefix of their coarse-cell counts;
+//  2. the patch cells some stencil reads, packed into a list (warp ballots);
+//  3. their values for the NVI prolonged variables into shared memory;
+//  4. work items (variable, coarse cell): the 2^dim children of the coarse
+//     cell for that variable, the per-direction combinations shared by the
+//     children (slopes, or the x then y then z sums);
+//  5. ID = IAD0 + IAD1 and IA1 = 1 - IA0 per ghost cell.
+// FP64 instructions cost the same with idle lanes: the items are packed
+// into full warps.
 template <int DIM, int B, int MODE>
 __global__ void __launch_bounds__(128)
 prolong_kernel(StepArgs a)
 {
   using T = ProlongTraits<DIM, B, MODE>;
   using H = V<DIM>;
-  constexpr int R = T::R, P = T::P, NP = T::NP, G = T::G, NG = T::NG, NC = T::NC;
+  constexpr int R = T::R, P = T::P, NP = T::NP, G = T::G, NG = T::NG, NC = T::NC, NT = T::NT;
+  constexpr int HB = B / 2, NCHILD = 1 << DIM;
   extern __shared__ __align__(16) double sP[]; // [NVI][NP]
-  const int vars[7] = { H::IAD0, H::IAD1, H::IA0, H::IE, H::IU, H::IV, H::IW };
-  const int nwalk = step_count(a);
+  __shared__ int sOff[T::NS + 1];              // coarse cells of the coarser slots before slot k
+  __shared__ int sSlot[T::NS];
+  __shared__ int sNslot, sCount;
+  __shared__ int sList[NP]; // patch cells to load
+  const int      vars[7] = { H::IAD0, H::IAD1, H::IA0, H::IE, H::IU, H::IV, H::IW };
+  const int      tid = threadIdx.x, lane = tid & 31;
+  const int      nwalk = step_count(a);
+  // coarse cell (block coarse coordinates) of item w's slot-local index
+  auto slot_cell = [&](int js, int loc, int * q) {
+    const int sl = sSlot[js];
+#pragma unroll
+    for (int e = 0, p3 = 1; e < DIM; ++e, p3 *= 3)
+    {
+      const int d = (sl / p3) % 3 - 1;
+      if (d == 0)
+      {
+        q[e] = loc % HB;
+        loc /= HB;
+      }
+      else
+        q[e] = d < 0 ? -1 : HB;
+    }
+  };
   for (int iw = blockIdx.x; iw < nwalk; iw += gridDim.x)
   {
     const int n = a.work ? a.work[iw] : iw;
@@ -186,11 +230,67 @@ prolong_kernel(StepArgs a)
     if (ps < 0)
       continue;
     const int c0[3] = { a.m.coord[n * 3 + 0], a.m.coord[n * 3 + 1], DIM == 3 ? a.m.coord[n * 3 + 2] : 0 };
-    __syncthreads(); // the previous block's patch is read
-    for (int i = threadIdx.x; i < NP; i += T::NT)
+    __syncthreads(); // the previous block's lists and patch are read
+    if (tid == 0)
     {
-      int q[3] = { i % P - 1 - R, (i / P) % P - 1 - R, DIM == 3 ? i / (P * P) - 1 - R : 0 };
-      int kind, src, c;
+      int tot = 0, k = 0;
+      for (int sl = 0; sl < T::NS; ++sl)
+      {
+        if (sl == T::NS / 2 || a.m.nbr_rel[(size_t)n * T::NS + sl] >= 0)
+          continue;
+        int cnt = 1;
+#pragma unroll
+        for (int e = 0, p3 = 1; e < DIM; ++e, p3 *= 3)
+          cnt *= (sl / p3) % 3 == 1 ? HB : 1;
+        sSlot[k] = sl;
+        sOff[k] = tot;
+        tot += cnt;
+        ++k;
+      }
+      sOff[k] = tot;
+      sNslot = k;
+      sCount = 0;
+    }
+    __syncthreads();
+    const int nslot = sNslot, ncc = sOff[nslot];
+    // 2. patch cells within R of a coarse cell of a coarser slot
+    for (int base = 0; base < NP; base += NT)
+    {
+      const int i = base + tid;
+      bool      need = false;
+      if (i < NP)
+      {
+        const int q[3] = { i % P - 1 - R, (i / P) % P - 1 - R, DIM == 3 ? i / (P * P) - 1 - R : 0 };
+        for (int js = 0; js < nslot && !need; ++js)
+        {
+          const int sl = sSlot[js];
+          bool      in = true;
+#pragma unroll
+          for (int e = 0, p3 = 1; e < DIM; ++e, p3 *= 3)
+          {
+            const int d = (sl / p3) % 3 - 1;
+            const int lo = d < 0 ? -1 : (d == 0 ? 0 : HB), hi = d < 0 ? -1 : (d == 0 ? HB - 1 : HB);
+            in = in && q[e] >= lo - R && q[e] <= hi + R;
+          }
+          need = in;
+        }
+      }
+      const unsigned mask = __ballot_sync(0xffffffffu, need);
+      int            wbase = 0;
+      if (lane == 0 && mask)
+        wbase = atomicAdd(&sCount, __popc(mask));
+      wbase = __shfl_sync(0xffffffffu, wbase, 0);
+      if (need)
+        sList[wbase + __popc(mask & ((1u << lane) - 1u))] = i;
+    }
+    __syncthreads();
+    // 3. their values
+    const int nload = sCount;
+    for (int k = tid; k < nload; k += NT)
+    {
+      const int i = sList[k];
+      const int q[3] = { i % P - 1 - R, (i / P) % P - 1 - R, DIM == 3 ? i / (P * P) - 1 - R : 0 };
+      int       kind, src, c;
       coarse_cell_ref<DIM, B>(a.m, n, c0, q, kind, src, c);
       if (kind < 0)
         raise_status(a.status, STATUS_MESH);
@@ -199,91 +299,97 @@ prolong_kernel(StepArgs a)
         sP[t * NP + i] = kind < 0 ? 0.0 : coarse_cell_value<DIM, B>(a.U + ((size_t)src * H::NV + vars[t]) * NC, kind, c);
     }
     __syncthreads();
+    // 4. items (variable t, coarse cell cc): the cell's 2^dim children
     double * out = a.m.pg + (size_t)ps * H::NV * NG;
-    for (int gi = threadIdx.x; gi < NG; gi += T::NT)
+    for (int w = tid; w < T::NVI * ncc; w += NT)
     {
-      int g[3] = { gi % G - 2, (gi / G) % G - 2, DIM == 3 ? gi / (G * G) - 2 : 0 };
-      int s[3] = { 0, 0, 0 };
-      bool inner = true;
-#pragma unroll
-      for (int e = 0; e < DIM; ++e)
+      const int t = w / ncc, cc = w - t * ncc;
+      int       js = 0;
+      while (js + 1 < nslot && sOff[js + 1] <= cc)
+        ++js;
+      int q[3] = { 0, 0, 0 };
+      slot_cell(js, cc - sOff[js], q);
+      const double * Pv = sP + t * NP + (q[0] + 1 + R) + P * ((q[1] + 1 + R) + (DIM == 3 ? P * (q[2] + 1 + R) : 0));
+      auto at = [&](int i, int j, int k) { return Pv[i + P * (j + (DIM == 3 ? P * k : 0))]; };
+      double ch[NCHILD]; // child (ux, uy, uz) at ux + 2 uy + 4 uz
+      if constexpr (MODE == 1)
       {
-        s[e] = g[e] < 0 ? -1 : (g[e] >= B ? 1 : 0);
-        inner = inner && s[e] == 0;
-      }
-      if (inner)
-        continue;
-      const int slot = DIM == 2 ? (s[0] + 1) + 3 * (s[1] + 1) : (s[0] + 1) + 3 * (s[1] + 1) + 9 * (s[2] + 1);
-      if (a.m.nbr_rel[(size_t)n * T::NS + slot] >= 0)
-        continue;
-      int pc[3] = { 0, 0, 0 }, up[3] = { 0, 0, 0 };
+        const double u0 = at(0, 0, 0);
+        double       sl[3];
+        sl[0] = slope_scalar<double>(u0, at(1, 0, 0), at(-1, 0, 0), 1.0);
+        sl[1] = slope_scalar<double>(u0, at(0, 1, 0), at(0, -1, 0), 1.0);
+        if constexpr (DIM == 3)
+          sl[2] = slope_scalar<double>(u0, at(0, 0, 1), at(0, 0, -1), 1.0);
 #pragma unroll
-      for (int e = 0; e < DIM; ++e)
-      {
-        pc[e] = (g[e] + 2) / 2 - 1 + 1 + R; // holding coarse cell, in patch coordinates
-        up[e] = (g[e] + 2) & 1;
-      }
-      double u[H::NV];
-#pragma unroll
-      for (int t = 0; t < T::NVI; ++t)
-      {
-        const double * Pv = sP + t * NP;
-        auto at = [&](int i, int j, int k) { return Pv[(pc[0] + i) + P * ((pc[1] + j) + (DIM == 3 ? P * (pc[2] + k) : 0))]; };
-        double r;
-        if constexpr (MODE == 1)
+        for (int c = 0; c < NCHILD; ++c)
         {
-          const double u0 = at(0, 0, 0);
-          const double sx = slope_scalar<double>(u0, at(1, 0, 0), at(-1, 0, 0), 1.0);
-          const double sy = slope_scalar<double>(u0, at(0, 1, 0), at(0, -1, 0), 1.0);
-          r = u0;
-          r = r + 0.25 * (double)(up[0] ? 1 : -1) * sx;
-          r = r + 0.25 * (double)(up[1] ? 1 : -1) * sy;
-          if constexpr (DIM == 3)
-          {
-            const double sz = slope_scalar<double>(u0, at(0, 0, 1), at(0, 0, -1), 1.0);
-            r = r + 0.25 * (double)(up[2] ? 1 : -1) * sz;
-          }
+          double r = u0;
+#pragma unroll
+          for (int e = 0; e < DIM; ++e)
+            r = r + 0.25 * (double)(((c >> e) & 1) ? 1 : -1) * sl[e];
+          ch[c] = r;
         }
-        else
-        {
-          double valy[2 * R + 1];
+      }
+      else if constexpr (DIM == 2)
+      {
 #pragma unroll
-          for (int k = (DIM == 3 ? -R : 0); k <= (DIM == 3 ? R : 0); ++k)
-          {
-            double valx[2 * R + 1];
+        for (int ux = 0; ux < 2; ++ux)
+        {
+          double X[2 * R + 1];
+#pragma unroll
+          for (int j = -R; j <= R; ++j)
+            X[j + R] = prolong_lin<R>(MODE, ux, [&](int i) { return at(i, j, 0); });
+#pragma unroll
+          for (int uy = 0; uy < 2; ++uy)
+            ch[ux + 2 * uy] = prolong_lin<R>(MODE, uy, [&](int j) { return X[j + R]; });
+        }
+      }
+      else
+      {
+#pragma unroll
+        for (int ux = 0; ux < 2; ++ux)
+        {
+          double X[2 * R + 1][2 * R + 1]; // [k][j]
+#pragma unroll
+          for (int k = -R; k <= R; ++k)
 #pragma unroll
             for (int j = -R; j <= R; ++j)
-            {
-              double acc = prolong_coef(MODE, up[0], -R) * at(-R, j, k);
+              X[k + R][j + R] = prolong_lin<R>(MODE, ux, [&](int i) { return at(i, j, k); });
 #pragma unroll
-              for (int i = -R + 1; i <= R; ++i)
-                acc = acc + prolong_coef(MODE, up[0], i) * at(i, j, k);
-              valx[j + R] = acc;
-            }
-            double acc = prolong_coef(MODE, up[1], -R) * valx[0];
-#pragma unroll
-            for (int j = -R + 1; j <= R; ++j)
-              acc = acc + prolong_coef(MODE, up[1], j) * valx[j + R];
-            valy[DIM == 3 ? k + R : 0] = acc;
-          }
-          if constexpr (DIM == 3)
+          for (int uy = 0; uy < 2; ++uy)
           {
-            double acc = prolong_coef(MODE, up[2], -R) * valy[0];
+            double Y[2 * R + 1];
 #pragma unroll
-            for (int k = -R + 1; k <= R; ++k)
-              acc = acc + prolong_coef(MODE, up[2], k) * valy[k + R];
-            r = acc;
+            for (int k = -R; k <= R; ++k)
+              Y[k + R] = prolong_lin<R>(MODE, uy, [&](int j) { return X[k + R][j + R]; });
+#pragma unroll
+            for (int uz = 0; uz < 2; ++uz)
+              ch[ux + 2 * uy + 4 * uz] = prolong_lin<R>(MODE, uz, [&](int k) { return Y[k + R]; });
           }
-          else
-            r = valy[0];
         }
-        u[vars[t]] = r;
       }
-      u[H::ID] = u[H::IAD0] + u[H::IAD1];
-      u[H::IA1] = 1.0 - u[H::IA0];
+      double * o = out + (size_t)vars[t] * NG;
 #pragma unroll
-      for (int v = 0; v < H::NV; ++v)
-        out[(size_t)v * NG + gi] = u[v];
+      for (int c = 0; c < NCHILD; ++c)
+      {
+        const int gx = 2 * q[0] + (c & 1), gy = 2 * q[1] + ((c >> 1) & 1), gz = DIM == 3 ? 2 * q[2] + ((c >> 2) & 1) : 0;
+        o[DIM == 2 ? (gx + 2) + G * (gy + 2) : (gx + 2) + G * ((gy + 2) + G * (gz + 2))] = ch[c];
+      }
+    }
+    __syncthreads();
+    // 5. the two derived variables of every ghost cell
+    for (int w = tid; w < ncc * NCHILD; w += NT)
+    {
+      const int cc = w / NCHILD, c = w - cc * NCHILD;
+      int       js = 0;
+      while (js + 1 < nslot && sOff[js + 1] <= cc)
+        ++js;
+      int q[3] = { 0, 0, 0 };
+      slot_cell(js, cc - sOff[js], q);
+      const int gx = 2 * q[0] + (c & 1), gy = 2 * q[1] + ((c >> 1) & 1), gz = DIM == 3 ? 2 * q[2] + ((c >> 2) & 1) : 0;
+      double *  o = out + (DIM == 2 ? (gx + 2) + G * (gy + 2) : (gx + 2) + G * ((gy + 2) + G * (gz + 2)));
+      o[(size_t)H::ID * NG] = o[(size_t)H::IAD0 * NG] + o[(size_t)H::IAD1 * NG];
+      o[(size_t)H::IA1 * NG] = 1.0 - o[(size_t)H::IA0 * NG];
     }
   }
 }
