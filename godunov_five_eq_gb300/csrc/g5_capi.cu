@@ -1075,6 +1075,37 @@ g5_remap(G5Context * ctx, const G5Remap * r, const double * d_Uold, double * d_U
     if (k == 1 && (s[1] < 0 || s[1] >= nch))
       return G5_ERR_MESH;
   }
+  // refined blocks under a prolongation other than SIMPLE_COPY: prolonged over
+  // the old mesh, which the context must still hold (g5_remap before
+  // g5_set_mesh of the adapted mesh); one row per refined old block
+  std::vector<int32_t> refine_rows;
+  if (ctx->prm.prolongation != G5_PROLONG_SIMPLE_COPY)
+  {
+    std::vector<int32_t> row_of;
+    for (int j = 0; j < r->n_new; ++j)
+    {
+      if (r->kind[j] != 1)
+        continue;
+      if (!ctx->has_mesh || r->n_old != ctx->n_owned)
+        return G5_ERR_ARG;
+      if (row_of.empty())
+        row_of.assign(r->n_old, -1);
+      const int32_t * s = r->src + (size_t)j * nch;
+      if (row_of[s[0]] < 0)
+      {
+        row_of[s[0]] = (int)(refine_rows.size() / (nch + 1));
+        refine_rows.push_back(s[0]);
+        refine_rows.insert(refine_rows.end(), nch, -1);
+      }
+      int32_t & slot = refine_rows[(size_t)row_of[s[0]] * (nch + 1) + 1 + s[1]];
+      if (slot >= 0)
+        return G5_ERR_MESH;
+      slot = j;
+    }
+    for (int32_t v : refine_rows)
+      if (v < 0)
+        return G5_ERR_MESH; // a refined block without all its children
+  }
   cudaStream_t st = (cudaStream_t)stream;
   int8_t *     d_kind = nullptr;
   int32_t *    d_src = nullptr;
@@ -1094,6 +1125,19 @@ g5_remap(G5Context * ctx, const G5Remap * r, const double * d_Uold, double * d_U
   cudaFreeAsync(d_kind, st);
   cudaFreeAsync(d_src, st);
   ctx->last_launches = 1;
+  if (rc == G5_OK && !refine_rows.empty())
+  {
+    int32_t *    d_rows = nullptr;
+    const size_t nb = refine_rows.size() * sizeof(int32_t);
+    if (cudaMallocAsync((void **)&d_rows, nb, st) != cudaSuccess)
+      return G5_ERR_CUDA;
+    if (cudaMemcpyAsync(d_rows, refine_rows.data(), nb, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        g5::launch_remap_prolong(ctx->dim, ctx->b, ctx->prm.prolongation, d_Uold, d_Unew, dev_mesh(ctx), d_rows,
+                                 (int)(refine_rows.size() / (nch + 1)), ctx->d_status, st) != cudaSuccess)
+      rc = G5_ERR_CUDA;
+    cudaFreeAsync(d_rows, st);
+    ctx->last_launches = 2;
+  }
   return rc;
 }
 

@@ -166,6 +166,48 @@ launch_prolong(int dim, int b, const StepArgs & a, cudaStream_t s, int * launche
   return cudaErrorInvalidValue;
 }
 
+template <int DIM, int B, int MODE>
+static cudaError_t
+refine_t(const double * Uold, double * Unew, const DevMesh & m, const int32_t * list, int n_ref, unsigned int * status, cudaStream_t s)
+{
+  using T = RefineTraits<DIM, B, MODE>;
+  static bool configured = false;
+  if (!configured)
+  {
+    const cudaError_t e = cudaFuncSetAttribute(prolong_refine_kernel<DIM, B, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::smem_bytes);
+    if (e != cudaSuccess)
+      return e;
+    configured = true;
+  }
+  int grid = num_sms() * 4;
+  if (grid > n_ref)
+    grid = n_ref;
+  if (grid < 1)
+    return cudaSuccess;
+  prolong_refine_kernel<DIM, B, MODE><<<grid, T::NT, T::smem_bytes, s>>>(Uold, Unew, m, list, n_ref, status);
+  return cudaGetLastError();
+}
+
+cudaError_t
+launch_remap_prolong(int dim, int b, int mode, const double * Uold, double * Unew, const DevMesh & m, const int32_t * list, int n_ref,
+                     unsigned int * status, cudaStream_t s)
+{
+  if (dim == 2 && b == 16)
+    return mode == 1 ? refine_t<2, 16, 1>(Uold, Unew, m, list, n_ref, status, s)
+         : mode == 2 ? refine_t<2, 16, 2>(Uold, Unew, m, list, n_ref, status, s)
+         : mode == 3 ? refine_t<2, 16, 3>(Uold, Unew, m, list, n_ref, status, s)
+                     : cudaErrorInvalidValue;
+  if (dim == 2 && b == 8)
+    return mode == 1 ? refine_t<2, 8, 1>(Uold, Unew, m, list, n_ref, status, s)
+         : mode == 2 ? refine_t<2, 8, 2>(Uold, Unew, m, list, n_ref, status, s)
+                     : cudaErrorInvalidValue;
+  if (dim == 3 && b == 8)
+    return mode == 1 ? refine_t<3, 8, 1>(Uold, Unew, m, list, n_ref, status, s)
+         : mode == 2 ? refine_t<3, 8, 2>(Uold, Unew, m, list, n_ref, status, s)
+                     : cudaErrorInvalidValue;
+  return cudaErrorInvalidValue;
+}
+
 cudaError_t
 launch_step_fp64(int dim, int b, const StepArgs & a, int ctas_per_sm, cudaStream_t s, int * launches)
 {

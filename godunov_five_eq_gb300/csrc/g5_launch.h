@@ -34,6 +34,10 @@ cudaError_t launch_refine_flags(int dim, int b, const double * U, const DevMesh 
 // block remap after a mesh adaptation (kind/src validated by the caller)
 cudaError_t launch_remap(int dim, int b, const double * Uold, double * Unew, const int8_t * kind, const int32_t * src, int n_new,
                          cudaStream_t s);
+// refined blocks of a remap prolonged over the old mesh m (prolongation mode
+// 1-3); list rows: old block, then the new block of each child
+cudaError_t launch_remap_prolong(int dim, int b, int mode, const double * Uold, double * Unew, const DevMesh & m, const int32_t * list,
+                                 int n_ref, unsigned int * status, cudaStream_t s);
 // per-record rows of the reflux pass (DeferInfo) for `n` record codes
 cudaError_t launch_defer_info(int dim, const DevMesh & m, const int32_t * codes, int n, int32_t * info, cudaStream_t s);
 // derived quantity per cell (ComputeDerivedQuantities)

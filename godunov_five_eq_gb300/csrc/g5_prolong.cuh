@@ -181,6 +181,75 @@ prolong_lin(int mode, int upper, F v)
   return acc;
 }
 
+// the 2^dim children of the coarse value at Pv in a shared-memory patch
+// (strides 1, P, P^2), child (ux, uy, uz) at ch[ux + 2 uy + 4 uz]: minmod
+// slopes, or the x, then y, then z sums of the conservative interpolation
+// shared by the children (the same operands and order as the per-child sums
+// of the CPU restatement)
+template <int DIM, int MODE, int P>
+__device__ __forceinline__ void
+prolong_children(const double * Pv, double * ch)
+{
+  constexpr int R = MODE == 3 ? 2 : 1, NCHILD = 1 << DIM;
+  auto at = [&](int i, int j, int k) { return Pv[i + P * (j + (DIM == 3 ? P * k : 0))]; };
+  if constexpr (MODE == 1)
+  {
+    const double u0 = at(0, 0, 0);
+    double       sl[3];
+    sl[0] = slope_scalar<double>(u0, at(1, 0, 0), at(-1, 0, 0), 1.0);
+    sl[1] = slope_scalar<double>(u0, at(0, 1, 0), at(0, -1, 0), 1.0);
+    if constexpr (DIM == 3)
+      sl[2] = slope_scalar<double>(u0, at(0, 0, 1), at(0, 0, -1), 1.0);
+#pragma unroll
+    for (int c = 0; c < NCHILD; ++c)
+    {
+      double r = u0;
+#pragma unroll
+      for (int e = 0; e < DIM; ++e)
+        r = r + 0.25 * (double)(((c >> e) & 1) ? 1 : -1) * sl[e];
+      ch[c] = r;
+    }
+  }
+  else if constexpr (DIM == 2)
+  {
+#pragma unroll
+    for (int ux = 0; ux < 2; ++ux)
+    {
+      double X[2 * R + 1];
+#pragma unroll
+      for (int j = -R; j <= R; ++j)
+        X[j + R] = prolong_lin<R>(MODE, ux, [&](int i) { return at(i, j, 0); });
+#pragma unroll
+      for (int uy = 0; uy < 2; ++uy)
+        ch[ux + 2 * uy] = prolong_lin<R>(MODE, uy, [&](int j) { return X[j + R]; });
+    }
+  }
+  else
+  {
+#pragma unroll
+    for (int ux = 0; ux < 2; ++ux)
+    {
+      double X[2 * R + 1][2 * R + 1]; // [k][j]
+#pragma unroll
+      for (int k = -R; k <= R; ++k)
+#pragma unroll
+        for (int j = -R; j <= R; ++j)
+          X[k + R][j + R] = prolong_lin<R>(MODE, ux, [&](int i) { return at(i, j, k); });
+#pragma unroll
+      for (int uy = 0; uy < 2; ++uy)
+      {
+        double Y[2 * R + 1];
+#pragma unroll
+        for (int k = -R; k <= R; ++k)
+          Y[k + R] = prolong_lin<R>(MODE, uy, [&](int j) { return X[k + R][j + R]; });
+#pragma unroll
+        for (int uz = 0; uz < 2; ++uz)
+          ch[ux + 2 * uy + 4 * uz] = prolong_lin<R>(MODE, uz, [&](int k) { return Y[k + R]; });
+      }
+    }
+  }
+}
+
 // One CTA per walked block with a coarser neighbour:
 //  1. the coarser slots and the prefix of their coarse-cell counts;
 //  2. the patch cells some stencil reads, packed into a list (warp ballots);
@@ -310,64 +379,8 @@ prolong_kernel(StepArgs a)
       int q[3] = { 0, 0, 0 };
       slot_cell(js, cc - sOff[js], q);
       const double * Pv = sP + t * NP + (q[0] + 1 + R) + P * ((q[1] + 1 + R) + (DIM == 3 ? P * (q[2] + 1 + R) : 0));
-      auto at = [&](int i, int j, int k) { return Pv[i + P * (j + (DIM == 3 ? P * k : 0))]; };
-      double ch[NCHILD]; // child (ux, uy, uz) at ux + 2 uy + 4 uz
-      if constexpr (MODE == 1)
-      {
-        const double u0 = at(0, 0, 0);
-        double       sl[3];
-        sl[0] = slope_scalar<double>(u0, at(1, 0, 0), at(-1, 0, 0), 1.0);
-        sl[1] = slope_scalar<double>(u0, at(0, 1, 0), at(0, -1, 0), 1.0);
-        if constexpr (DIM == 3)
-          sl[2] = slope_scalar<double>(u0, at(0, 0, 1), at(0, 0, -1), 1.0);
-#pragma unroll
-        for (int c = 0; c < NCHILD; ++c)
-        {
-          double r = u0;
-#pragma unroll
-          for (int e = 0; e < DIM; ++e)
-            r = r + 0.25 * (double)(((c >> e) & 1) ? 1 : -1) * sl[e];
-          ch[c] = r;
-        }
-      }
-      else if constexpr (DIM == 2)
-      {
-#pragma unroll
-        for (int ux = 0; ux < 2; ++ux)
-        {
-          double X[2 * R + 1];
-#pragma unroll
-          for (int j = -R; j <= R; ++j)
-            X[j + R] = prolong_lin<R>(MODE, ux, [&](int i) { return at(i, j, 0); });
-#pragma unroll
-          for (int uy = 0; uy < 2; ++uy)
-            ch[ux + 2 * uy] = prolong_lin<R>(MODE, uy, [&](int j) { return X[j + R]; });
-        }
-      }
-      else
-      {
-#pragma unroll
-        for (int ux = 0; ux < 2; ++ux)
-        {
-          double X[2 * R + 1][2 * R + 1]; // [k][j]
-#pragma unroll
-          for (int k = -R; k <= R; ++k)
-#pragma unroll
-            for (int j = -R; j <= R; ++j)
-              X[k + R][j + R] = prolong_lin<R>(MODE, ux, [&](int i) { return at(i, j, k); });
-#pragma unroll
-          for (int uy = 0; uy < 2; ++uy)
-          {
-            double Y[2 * R + 1];
-#pragma unroll
-            for (int k = -R; k <= R; ++k)
-              Y[k + R] = prolong_lin<R>(MODE, uy, [&](int j) { return X[k + R][j + R]; });
-#pragma unroll
-            for (int uz = 0; uz < 2; ++uz)
-              ch[ux + 2 * uy + 4 * uz] = prolong_lin<R>(MODE, uz, [&](int k) { return Y[k + R]; });
-          }
-        }
-      }
+      double ch[NCHILD];
+      prolong_children<DIM, MODE, P>(Pv, ch);
       double * o = out + (size_t)vars[t] * NG;
 #pragma unroll
       for (int c = 0; c < NCHILD; ++c)
@@ -390,6 +403,137 @@ prolong_kernel(StepArgs a)
       double *  o = out + (DIM == 2 ? (gx + 2) + G * (gy + 2) : (gx + 2) + G * ((gy + 2) + G * (gz + 2)));
       o[(size_t)H::ID * NG] = o[(size_t)H::IAD0 * NG] + o[(size_t)H::IAD1 * NG];
       o[(size_t)H::IA1 * NG] = 1.0 - o[(size_t)H::IA0 * NG];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Refined blocks of a mesh adaptation prolonged with the same types
+// (map_userdata_after_adapt, SolverGodunovFiveEq.cpp:1137-1169: the
+// UserDataRemapper keeps the old orchard keys for the stencil of this
+// prolongation, :286-289): every fine cell of the children of an old block
+// from its parent cell and the parent's neighbours at the old level, over the
+// old block table.  A stencil point q (old-level cell coordinates relative to
+// the old block, -R .. b+R-1) is the old block's cell, a same-level
+// neighbour's cell, the coarser neighbour's cell holding it, or the mean of
+// the 2^dim cells of a finer neighbour covering it — the values the ghost
+// fill gives those cells.
+// ---------------------------------------------------------------------------
+template <int DIM, int B>
+__device__ __forceinline__ void
+level_cell_ref(const DevMesh & m, int n, const int * c0, const int * q, int & kind, int & src, int & c)
+{
+  constexpr int NS = DIM == 2 ? 9 : 27, NCH = DIM == 2 ? 4 : 8, H = B / 2;
+  int           s[3] = { 0, 0, 0 }, v[3] = { 0, 0, 0 };
+  bool          own = true;
+#pragma unroll
+  for (int e = 0; e < DIM; ++e)
+  {
+    s[e] = q[e] < 0 ? -1 : (q[e] >= B ? 1 : 0);
+    v[e] = q[e] - s[e] * B;
+    own = own && s[e] == 0;
+  }
+  auto cell = [&](const int * x) { return DIM == 2 ? x[0] + B * x[1] : x[0] + B * (x[1] + B * x[2]); };
+  kind = 1;
+  src = n;
+  c = cell(v);
+  if (own)
+    return;
+  const int       slot = DIM == 2 ? (s[0] + 1) + 3 * (s[1] + 1) : (s[0] + 1) + 3 * (s[1] + 1) + 9 * (s[2] + 1);
+  const int       rel = m.nbr_rel[(size_t)n * NS + slot];
+  const int32_t * nb = m.nbr + ((size_t)n * NS + slot) * NCH;
+  if (rel == 0)
+    src = nb[0];
+  else if (rel < 0)
+  {
+    int cc[3] = { 0, 0, 0 };
+#pragma unroll
+    for (int e = 0; e < DIM; ++e)
+      cc[e] = ((c0[e] + s[e]) & 1) * H + (v[e] >> 1);
+    src = nb[0];
+    c = cell(cc);
+  }
+  else
+  {
+    int ch[3] = { 0, 0, 0 }, l[3] = { 0, 0, 0 };
+#pragma unroll
+    for (int e = 0; e < DIM; ++e)
+    {
+      const int f = 2 * v[e];
+      ch[e] = f >= B ? 1 : 0;
+      l[e] = f - ch[e] * B;
+    }
+    kind = 0;
+    src = nb[DIM == 2 ? ch[0] + 2 * ch[1] : ch[0] + 2 * ch[1] + 4 * ch[2]];
+    c = cell(l);
+  }
+  if (src < 0 || src >= m.n_total)
+    kind = -1;
+}
+
+template <int DIM, int B, int MODE>
+struct RefineTraits
+{
+  static constexpr int R = MODE == 3 ? 2 : 1;
+  static constexpr int P = B + 2 * R; // patch: the old block and R cells around it
+  static constexpr int NP = DIM == 2 ? P * P : P * P * P;
+  static constexpr int NVI = DIM == 2 ? 6 : 7;
+  static constexpr int NC = DIM == 2 ? B * B : B * B * B;
+  static constexpr int NT = 256;
+  static constexpr size_t smem_bytes = sizeof(double) * (size_t)NVI * NP;
+  static_assert(2 * R <= B, "the patch reaches past the children of a finer slot that touch the block");
+};
+
+// list[r * (1 + 2^DIM)]: the refined old block, then the new block of each
+// of its children (child index x + 2 y + 4 z)
+template <int DIM, int B, int MODE>
+__global__ void __launch_bounds__(256)
+prolong_refine_kernel(const double * __restrict__ Uold, double * __restrict__ Unew, DevMesh m, const int32_t * __restrict__ list,
+                      int n_ref, unsigned int * status)
+{
+  using T = RefineTraits<DIM, B, MODE>;
+  using H = V<DIM>;
+  constexpr int R = T::R, P = T::P, NP = T::NP, NC = T::NC, NT = T::NT, HB = B / 2, NCHILD = 1 << DIM;
+  extern __shared__ __align__(16) double sP[]; // [NVI][NP]
+  const int vars[7] = { H::IAD0, H::IAD1, H::IA0, H::IE, H::IU, H::IV, H::IW };
+  for (int r = blockIdx.x; r < n_ref; r += gridDim.x)
+  {
+    const int32_t * row = list + (size_t)r * (1 + NCHILD);
+    const int       n = row[0];
+    const int       c0[3] = { m.coord[n * 3 + 0], m.coord[n * 3 + 1], DIM == 3 ? m.coord[n * 3 + 2] : 0 };
+    __syncthreads(); // the previous block's patch is read
+    for (int i = threadIdx.x; i < NP; i += NT)
+    {
+      const int q[3] = { i % P - R, (i / P) % P - R, DIM == 3 ? i / (P * P) - R : 0 };
+      int       kind, src, c;
+      level_cell_ref<DIM, B>(m, n, c0, q, kind, src, c);
+      if (kind < 0)
+        raise_status(status, STATUS_MESH);
+#pragma unroll
+      for (int t = 0; t < T::NVI; ++t)
+        sP[t * NP + i] = kind < 0 ? 0.0 : coarse_cell_value<DIM, B>(Uold + ((size_t)src * H::NV + vars[t]) * NC, kind, c);
+    }
+    __syncthreads();
+    // items (variable t, old cell): the cell's 2^dim fine cells
+    for (int w = threadIdx.x; w < T::NVI * NC; w += NT)
+    {
+      const int t = w / NC, oc = w - t * NC;
+      const int q[3] = { oc % B, (oc / B) % B, DIM == 3 ? oc / (B * B) : 0 };
+      double    ch[NCHILD];
+      prolong_children<DIM, MODE, P>(sP + t * NP + (q[0] + R) + P * ((q[1] + R) + (DIM == 3 ? P * (q[2] + R) : 0)), ch);
+      const int cb = (q[0] >= HB ? 1 : 0) + (q[1] >= HB ? 2 : 0) + (DIM == 3 && q[2] >= HB ? 4 : 0);
+      double *  o = Unew + ((size_t)row[1 + cb] * H::NV + vars[t]) * NC;
+      const int f0 = 2 * (q[0] % HB), f1 = 2 * (q[1] % HB), f2 = DIM == 3 ? 2 * (q[2] % HB) : 0;
+#pragma unroll
+      for (int c = 0; c < NCHILD; ++c)
+        o[(f0 + (c & 1)) + B * ((f1 + ((c >> 1) & 1)) + (DIM == 3 ? B * (f2 + ((c >> 2) & 1)) : 0))] = ch[c];
+    }
+    __syncthreads();
+    for (int w = threadIdx.x; w < NCHILD * NC; w += NT)
+    {
+      double * o = Unew + (size_t)row[1 + w / NC] * H::NV * NC + (w % NC);
+      o[(size_t)H::ID * NC] = o[(size_t)H::IAD0 * NC] + o[(size_t)H::IAD1 * NC];
+      o[(size_t)H::IA1 * NC] = 1.0 - o[(size_t)H::IA0 * NC];
     }
   }
 }

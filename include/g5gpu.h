@@ -278,7 +278,11 @@ typedef struct G5Remap
  * 1137-1169): the owned blocks of d_Unew from those of d_Uold.  Refined blocks
  * take the SIMPLE_COPY prolongation of their parent, coarsened blocks the
  * restriction of get_conservative_vars_restriction (mean of the 2^dim fine
- * cells; IA1 = 1 - IA0, ID = IAD0 + IAD1).  Outside blocks of d_Unew are not
+ * cells; IA1 = 1 - IA0, ID = IAD0 + IAD1).  Under another G5Params.prolongation
+ * the refined blocks are prolonged with it from the parent cell and its
+ * neighbours at the old level: the context must still hold the old mesh
+ * (call g5_remap before g5_set_mesh of the adapted mesh; G5_ERR_ARG
+ * otherwise) and d_Uold's outside blocks must be filled.  Outside blocks of d_Unew are not
  * written (g5_set_mesh with the new table, then g5_fill_outside).  The map is
  * validated on the host (G5_ERR_MESH) and copied to stream-ordered device
  * memory (cudaMallocAsync/cudaFreeAsync on `stream`): not capturable. */

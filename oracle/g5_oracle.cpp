@@ -719,36 +719,33 @@ lin_comb(const double * c, const double * v, int np)
   return r;
 }
 
-/* conservative state of ghost cell g (block coords, in a coarser slot) */
 template <int DIM>
+static void ghost_state(const Ctx & x, const double * U, int n, const int * g, double * u, int prolongation);
+
+/* prolonged conservative state of the fine cell at position pos (0 lower,
+ * 1 upper half per direction) of the coarse cell q, whose stencil values
+ * V(q', var) come from the caller */
+template <int DIM, typename Val>
 static void
-prolong_ghost(const Ctx & x, const double * U, int n, const int * g, double * u)
+prolong_point(int mode, Val V, const int * q, const int * pos, double * u)
 {
   using H = Ids<DIM>;
-  int q[3] = { 0, 0, 0 }, pos[3] = { 0, 0, 0 };
-  for (int e = 0; e < DIM; ++e)
-  {
-    q[e] = (g[e] + 2) / 2 - 1; // coarse cell holding the ghost cell
-    pos[e] = (g[e] + 2) & 1;   // 0 lower, 1 upper half
-  }
   const int vars[7] = { H::IAD0, H::IAD1, H::IA0, H::IE, H::IU, H::IV, H::IW };
   const int nvars = DIM == 2 ? 6 : 7;
-  const int mode = x.prm.prolongation;
   for (int t = 0; t < nvars; ++t)
   {
     const int var = vars[t];
     double    r;
     if (mode == 1)
     {
-      const double u0 = coarse_cell_value<DIM>(x, U, n, q, var);
+      const double u0 = V(q, var);
       double       sl[3] = { 0.0, 0.0, 0.0 };
       for (int e = 0; e < DIM; ++e)
       {
         int qp[3] = { q[0], q[1], q[2] }, qm[3] = { q[0], q[1], q[2] };
         qp[e] += 1;
         qm[e] -= 1;
-        sl[e] = slope_unsplit_scalar(
-          u0, coarse_cell_value<DIM>(x, U, n, qp, var), coarse_cell_value<DIM>(x, U, n, qm, var), 1.0);
+        sl[e] = slope_unsplit_scalar(u0, V(qp, var), V(qm, var), 1.0);
       }
       r = u0;
       for (int e = 0; e < DIM; ++e)
@@ -770,7 +767,7 @@ prolong_ghost(const Ctx & x, const double * U, int n, const int * g, double * u)
           for (int i = -rr; i <= rr; ++i)
           {
             const int qq[3] = { q[0] + i, q[1] + j, q[2] + k };
-            pts[i + rr] = coarse_cell_value<DIM>(x, U, n, qq, var);
+            pts[i + rr] = V(qq, var);
           }
           valx[j + rr] = lin_comb(cx, pts, np);
         }
@@ -784,6 +781,43 @@ prolong_ghost(const Ctx & x, const double * U, int n, const int * g, double * u)
   u[H::IA1] = 1.0 - u[H::IA0];
 }
 
+/* conservative state of ghost cell g (block coords, in a coarser slot) */
+template <int DIM>
+static void
+prolong_ghost(const Ctx & x, const double * U, int n, const int * g, double * u)
+{
+  int q[3] = { 0, 0, 0 }, pos[3] = { 0, 0, 0 };
+  for (int e = 0; e < DIM; ++e)
+  {
+    q[e] = (g[e] + 2) / 2 - 1; // coarse cell holding the ghost cell
+    pos[e] = (g[e] + 2) & 1;   // 0 lower, 1 upper half
+  }
+  prolong_point<DIM>(
+    x.prm.prolongation, [&](const int * qq, int var) { return coarse_cell_value<DIM>(x, U, n, qq, var); }, q, pos, u);
+}
+
+/* value of variable var at cell q of the grid of owned block n's own level
+ * around the block (q in [-2, b+2)): the block's cell, a same-level
+ * neighbour's cell, the coarser neighbour's cell holding it or the mean of the
+ * 2^dim cells of a finer neighbour covering it (the ghost fill's values) */
+template <int DIM>
+static double
+level_cell_value(const Ctx & x, const double * U, int n, const int * q, int var)
+{
+  int  g[3] = { q[0], q[1], DIM == 3 ? q[2] : 0 };
+  bool inner = true;
+  for (int e = 0; e < DIM; ++e)
+    inner = inner && q[e] >= 0 && q[e] < x.b;
+  double u[Ids<DIM>::NV];
+  if (inner)
+  {
+    const Geo<DIM> geo(x.b);
+    return U[((size_t)n * Ids<DIM>::NV + var) * geo.ncell() + geo.cell(q[0], q[1], DIM == 3 ? q[2] : 0)];
+  }
+  // outside the block: the SIMPLE_COPY / restriction ghost fill of that cell
+  ghost_state<DIM>(x, U, n, g, u, 0);
+  return u[var];
+}
 /* ---------------------------------------------------------------------------
  * ConvertToPrimitivesVariablesFunctor::fill_ghosts
  * (scheme/ConvertToPrimitivesVariablesFunctor.cpp:833-926): one ghosted cell
@@ -791,7 +825,7 @@ prolong_ghost(const Ctx & x, const double * U, int n, const int * g, double * u)
  * ------------------------------------------------------------------------- */
 template <int DIM>
 static void
-ghost_state(const Ctx & x, const double * U, int n, const int * g, double * u)
+ghost_state(const Ctx & x, const double * U, int n, const int * g, double * u, int prolongation)
 {
   using H = Ids<DIM>;
   const Geo<DIM> geo(x.b);
@@ -820,7 +854,7 @@ ghost_state(const Ctx & x, const double * U, int n, const int * g, double * u)
       // same level: plain copy (fill_ghost_copy without restriction, :516-537)
       load_u<DIM>(x, U, nb[0], geo.cell(v[0], v[1], v[2]), u);
     }
-    else if (rel < 0 && x.prm.prolongation != 0)
+    else if (rel < 0 && prolongation != 0)
     {
       // coarser neighbour, EXTRAPOLATE_LINEAR_MINMOD or conservative
       // interpolation (:898-912)
@@ -881,7 +915,7 @@ fill_ghost_cell(const Ctx & x, const double * U, int n, const int * g, double * 
 {
   using H = Ids<DIM>;
   double u[H::NV];
-  ghost_state<DIM>(x, U, n, g, u);
+  ghost_state<DIM>(x, U, n, g, u, x.prm.prolongation);
   double qq[H::NV];
   computePrimitives<DIM>(u, qq, x.s);
   // set_primitive_vars, :252-270
@@ -1763,9 +1797,9 @@ g5o_ghost_state(void * ctx, const double * U, int n, const int * g, double * u)
     if (g[e] < -2 || g[e] >= x->b + 2)
       return -1;
   if (x->dim == 2)
-    ghost_state<2>(*x, U, n, g, u);
+    ghost_state<2>(*x, U, n, g, u, x->prm.prolongation);
   else
-    ghost_state<3>(*x, U, n, g, u);
+    ghost_state<3>(*x, U, n, g, u, x->prm.prolongation);
   return 0;
 }
 
@@ -1932,6 +1966,59 @@ extern "C" int
 g5o_remap(const G5OParams * prm, int n_new, const int8_t * kind, const int32_t * src, const double * Uold, double * Unew)
 {
   return prm->dim == 2 ? do_remap<2>(prm->b, n_new, kind, src, Uold, Unew) : do_remap<3>(prm->b, n_new, kind, src, Uold, Unew);
+}
+
+/* refined blocks prolonged with the context's prolongation over the old
+ * mesh (the context's mesh): each fine cell from its parent cell and the
+ * parent's neighbours at the old level (the stencil the UserDataRemapper
+ * keeps the old orchard keys for, SolverGodunovFiveEq.cpp:286-289) */
+template <int DIM>
+static void
+do_remap_refined(const Ctx & x, int n_new, const int8_t * kind, const int32_t * src, const double * Uold, double * Unew)
+{
+  using H = Ids<DIM>;
+  const Geo<DIM> geo(x.b);
+  const int      nc = geo.ncell(), nch = 1 << DIM, h = x.b / 2;
+#pragma omp parallel for schedule(static)
+  for (int j = 0; j < n_new; ++j)
+  {
+    if (kind[j] != 1)
+      continue;
+    const int32_t * s = src + (size_t)j * nch;
+    double *        out = Unew + (size_t)j * H::NV * nc;
+    for (int c = 0; c < nc; ++c)
+    {
+      const int cc[3] = { c % x.b, (c / x.b) % x.b, DIM == 3 ? c / (x.b * x.b) : 0 };
+      int       q[3] = { 0, 0, 0 }, pos[3] = { 0, 0, 0 };
+      for (int e = 0; e < DIM; ++e)
+      {
+        q[e] = ((s[1] >> e) & 1) * h + (cc[e] >> 1);
+        pos[e] = cc[e] & 1;
+      }
+      double u[H::NV];
+      prolong_point<DIM>(
+        x.prm.prolongation, [&](const int * qq, int var) { return level_cell_value<DIM>(x, Uold, s[0], qq, var); }, q, pos, u);
+      for (int v = 0; v < H::NV; ++v)
+        out[(size_t)v * nc + c] = u[v];
+    }
+  }
+}
+
+extern "C" int
+g5o_remap_mesh(void * ctx, int n_new, const int8_t * kind, const int32_t * src, const double * Uold, double * Unew)
+{
+  Ctx * x = static_cast<Ctx *>(ctx);
+  const int rc = g5o_remap(&x->prm, n_new, kind, src, Uold, Unew);
+  if (rc != 0 || x->prm.prolongation == 0)
+    return rc;
+  for (int j = 0; j < n_new; ++j)
+    if (kind[j] == 1 && (src[(size_t)j << x->dim] < 0 || src[(size_t)j << x->dim] >= x->n_owned))
+      return -1;
+  if (x->dim == 2)
+    do_remap_refined<2>(*x, n_new, kind, src, Uold, Unew);
+  else
+    do_remap_refined<3>(*x, n_new, kind, src, Uold, Unew);
+  return 0;
 }
 
 /* ---------------------------------------------------------------------------

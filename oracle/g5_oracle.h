@@ -94,6 +94,10 @@ int    g5o_refine_flags(void * ctx,
  * src[j*2^dim+1] of old block src[j*2^dim]; 2 restriction of the old children
  * src[j*2^dim .. +2^dim-1]).  returns 0 */
 int    g5o_remap(const G5OParams * prm, int n_new, const int8_t * kind, const int32_t * src, const double * Uold, double * Unew);
+/* as g5o_remap, then the refined blocks prolonged with the context's
+ * prolongation (if not SIMPLE_COPY) over the context's mesh, which must be
+ * the old mesh (src[j*2^dim] its owned blocks) */
+int g5o_remap_mesh(void * ctx, int n_new, const int8_t * kind, const int32_t * src, const double * Uold, double * Unew);
 
 /* ComputeDerivedQuantities: quantity (0 RHO_MIX .. 7 VZ) per cell of blocks
  * [begin, begin + count) into out[n_blocks][ncell].  returns 0 */

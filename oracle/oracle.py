@@ -92,6 +92,7 @@ def lib():
         L.g5o_mixture_sound_speed.restype = ctypes.c_double
         L.g5o_mixture_sound_speed.argtypes = [ctypes.POINTER(G5OParams)] + [ctypes.c_double] * 5
         L.g5o_remap.argtypes = [ctypes.POINTER(G5OParams), ctypes.c_int, vp, vp, vp, vp]
+        L.g5o_remap_mesh.argtypes = [vp, ctypes.c_int, vp, vp, vp, vp]
         L.g5o_derived.argtypes = [ctypes.POINTER(G5OParams), vp, ctypes.c_int, ctypes.c_longlong, ctypes.c_longlong, vp]
         _lib = L
     return _lib
@@ -183,6 +184,20 @@ class Oracle:
         if lib().g5o_ghost_state(self.ctx, _ptr(U), int(n), _ptr(gg), _ptr(out)) != 0:
             raise ValueError("ghost cell out of range")
         return out
+
+    def remap(self, rt, U_old: np.ndarray, n_total_new: int) -> np.ndarray:
+        """Owned blocks of the adapted mesh from the old state, this context's
+        mesh being the old one: as the module-level remap, and under a
+        prolongation other than SIMPLE_COPY the refined blocks prolonged over
+        the old mesh (U_old's outside blocks filled)."""
+        nv = 8 if rt.dim == 2 else 9
+        U_old = np.ascontiguousarray(U_old, np.float64)
+        U_new = np.zeros((n_total_new, nv, rt.bsize**rt.dim))
+        kind = np.ascontiguousarray(rt.kind, np.int8)
+        src = np.ascontiguousarray(rt.src, np.int32)
+        if lib().g5o_remap_mesh(self.ctx, rt.n_new, _ptr(kind), _ptr(src), _ptr(U_old), _ptr(U_new)) != 0:
+            raise ValueError("remap map does not match the context's mesh")
+        return U_new
 
     def inv_dt(self, U: np.ndarray) -> np.ndarray:
         out = np.zeros(self.table.n_inst)

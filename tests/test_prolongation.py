@@ -184,3 +184,146 @@ def test_gpu_host_step_and_mixed(dim, b, mode):
     torch.cuda.synchronize()
     assert impl.status() == 0
     assert l1_relative(t, d_U.cpu().numpy(), refn).max() <= L1_TOL_MIXED
+
+
+# ------------------------------------------------- refined blocks of a remap
+def _family_flags(mesh, seed):
+    rng = np.random.default_rng(seed)
+    draw, out = {}, []
+    for k in mesh.ordered_leaves():
+        parent = (k[0] - 1,) + tuple(c >> 1 for c in k[1:])
+        if parent not in draw:
+            draw[parent] = rng.choice(np.array([0, 1, 2], np.int8), p=[0.5, 0.3, 0.2])
+        out.append(draw[parent])
+    return np.array(out, np.int8)
+
+
+def _refine_case(dim, b, seed, mode, linear=False):
+    mesh, t_old = _mesh(dim, b)
+    p = water_air_params(t_old, dim=dim, b=b, bc=(2, 2, 3, 3, 2, 3), prolongation=mode)
+    o = Oracle(t_old, p)
+    if linear:
+        ncell = b**dim
+        cells = np.arange(ncell)
+        ijk = [(cells // b**e) % b for e in range(dim)]
+        dx = t_old.level_dx[t_old.level]
+        X = [(t_old.coord[:, e][:, None] * b + ijk[e][None, :] + 0.5) * dx[:, None] for e in range(dim)]
+        coefs = np.random.default_rng(seed).uniform(-1, 1, size=(t_old.nv, dim))
+        U = np.zeros((t_old.n_total, t_old.nv, ncell))
+        for v in range(t_old.nv):
+            U[:, v] = 1.0 + sum(coefs[v, e] * X[e] for e in range(dim))
+    else:
+        U = smooth_state(mesh, t_old, p, seed=seed, interface=False)
+        o.fill_outside(U)
+        coefs = None
+    rt = mesh.adapt(_family_flags(mesh, seed + 10))
+    t_new = mesh.build()
+    return mesh, t_old, t_new, p, o, U, rt, coefs
+
+
+@pytest.mark.parametrize("dim,b,mode", CPU_CASES)
+def test_oracle_refined_blocks_linear_exact(dim, b, mode):
+    """Refined blocks of a linear field: every fine cell is the field at its
+    centre when no neighbour of the parent is coarser (a coarser neighbour
+    gives its stencil points the value of the coarse cell holding them, as
+    the ghost fill does, which is first order)."""
+    mesh, t_old, t_new, p, o, U, rt, coefs = _refine_case(dim, b, 3, mode, linear=True)
+    V = o.remap(rt, U, t_new.n_total)
+    ref_idx = [j for j in np.nonzero(rt.kind == 1)[0] if (t_old.nbr_rel[rt.src[j, 0]] >= 0).all()]
+    assert len(ref_idx) > 0
+    ncell = b**dim
+    cells = np.arange(ncell)
+    ijk = [(cells // b**e) % b for e in range(dim)]
+    vars_ = _interpolated_vars(dim)
+    for j in ref_idx:
+        dx = t_new.level_dx[t_new.level[j]]
+        X = [(t_new.coord[j, e] * b + ijk[e] + 0.5) * dx for e in range(dim)]
+        ref = 1.0 + coefs @ np.array(X)
+        assert np.abs(V[j][vars_] - ref[vars_]).max() < 1e-13
+
+
+@pytest.mark.parametrize("dim,b,mode", [(2, 8, O2), (2, 16, O4), (3, 8, O2)])
+def test_oracle_refined_blocks_conservative(dim, b, mode):
+    """Conservative interpolation: the 2^dim fine cells of a parent cell
+    average to it (SIMPLE_COPY refinement gives every fine cell the parent)."""
+    mesh, t_old, t_new, p, o, U, rt, _ = _refine_case(dim, b, 4, mode)
+    from oracle.oracle import remap as remap_copy
+
+    V = o.remap(rt, U, t_new.n_total)
+    V0 = remap_copy(p, rt, U, t_new.n_total)
+    scale = np.abs(U).max(axis=(0, 2))
+    vars_ = _interpolated_vars(dim)
+    ref_idx = np.nonzero(rt.kind == 1)[0]
+    assert ref_idx.size > 0
+    for j in ref_idx:
+        for v in vars_:
+            arr = V[j, v].reshape((b,) * dim)  # [z][y][x] or [y][x]
+            blocks = arr.reshape(*[m for _ in range(dim) for m in (b // 2, 2)])
+            mean = blocks.mean(axis=tuple(range(1, 2 * dim, 2)))
+            par = V0[j, v].reshape((b,) * dim)[tuple(slice(0, None, 2) for _ in range(dim))]
+            assert np.abs(mean - par).max() <= 1e-14 * scale[v]
+    # copied and coarsened blocks are untouched by the prolongation
+    other = rt.kind != 1
+    assert np.array_equal(V[: t_new.n_owned][other], V0[: t_new.n_owned][other])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dim,b,mode", GPU_CASES)
+def test_gpu_remap_refined_bit_exact(dim, b, mode):
+    torch = pytest.importorskip("torch")
+    from godunov_five_eq_gb300.implem import GodunovImplemGB300
+
+    mesh, t_old, t_new, p, o, U, rt, _ = _refine_case(dim, b, 7, mode)
+    V = o.remap(rt, U, t_new.n_total)
+    impl = GodunovImplemGB300(p, t_old)
+    d_U = torch.from_numpy(U).cuda()
+    d_V = torch.zeros((t_new.n_total, t_new.nv, t_new.ncell), dtype=torch.float64, device="cuda")
+    impl.remap(rt, d_U, d_V)
+    torch.cuda.synchronize()
+    assert impl.status() == 0
+    n = t_new.n_owned
+    assert np.array_equal(d_V.cpu().numpy()[:n], V[:n])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", [MINMOD, O2])
+def test_gpu_amr_cycles_with_prolongation_bit_exact(mode):
+    """Three cycles of (5 steps, GPU flags, host adaptation, GPU remap) on
+    the 8-cell shock-bubble with a prolongation in the ghost fill and the
+    refinement, against the same loop on the oracle (FP64, bit-exact)."""
+    torch = pytest.importorskip("torch")
+    import dataclasses
+
+    from godunov_five_eq_gb300 import configs
+    from godunov_five_eq_gb300.implem import GodunovImplemGB300
+
+    def case():
+        mesh, t, p, U = configs.shock_bubble(level_min=2, level_max=4, bsize=8, initial_level=3)
+        return mesh, t, dataclasses.replace(p, prolongation=mode), U
+
+    mesh_g, t, p, U0 = case()
+    mesh_o, _, _, _ = case()
+    o = Oracle(t, p)
+    impl = GodunovImplemGB300(p, t)
+    A = torch.from_numpy(U0).cuda()
+    Uo = U0.copy()
+    for cycle in range(3):
+        B = torch.empty_like(A)
+        impl.begin(A)
+        for _ in range(5):
+            impl.advance(A, B)
+            A, B = B, A
+        Uo, _ = o.run(Uo, 5)
+        A, t_g, rt_g = impl.do_amr_cycle(mesh_g, A, 0, 0.1, 0.0125, 0.02)
+        o.fill_outside(Uo)
+        f = o.refine_flags(Uo, 0, 0.1, 0.0125, 0.02, mesh_o.level_min, mesh_o.level_max)
+        rt_o = mesh_o.adapt(f)
+        t_o = mesh_o.build()
+        assert np.array_equal(rt_g.kind, rt_o.kind) and np.array_equal(rt_g.src, rt_o.src)
+        Uo = o.remap(rt_o, Uo, t_o.n_total)
+        o.close()
+        o = Oracle(t_o, p)
+        o.fill_outside(Uo)
+        torch.cuda.synchronize()
+        assert np.array_equal(A.cpu().numpy(), Uo), f"cycle {cycle}"
+    assert impl.status() == 0
