@@ -1,10 +1,11 @@
 """In-tree build of libg5gpu.so (sm_103a) with nvcc.
 
-Four translation units compiled in parallel:
+Five translation units compiled in parallel:
   g5_fp64.cu   FP64 kernels, --fmad=false (bit-reproducible reference arithmetic)
   g5_mixed.cu  FP32-bulk kernels, --use_fast_math
   g5_capi.cu   the C ABI (include/g5gpu.h)
   g5_static.cu the allocation-free g5_step_static and its fixed scratch array
+  g5_forest.cpp the host block forest of the dynamic AMR cycle
 """
 from __future__ import annotations
 
@@ -24,6 +25,7 @@ UNITS = {
     "g5_mixed.cu": ["--use_fast_math"],
     "g5_capi.cu": [],
     "g5_static.cu": [],
+    "g5_forest.cpp": [],
 }
 
 
@@ -53,7 +55,7 @@ def build(force: bool = False, verbose: bool = False, extra: list[str] | None = 
     procs = []
     objs = []
     for unit, flags in UNITS.items():
-        obj = os.path.join(BUILD, unit.replace(".cu", ".o"))
+        obj = os.path.join(BUILD, os.path.splitext(unit)[0] + ".o")
         objs.append(obj)
         cmd = [cc, *ARCH, "-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-c", os.path.join(CSRC, unit), "-o", obj, *flags]
         if extra:

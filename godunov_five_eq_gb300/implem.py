@@ -87,6 +87,17 @@ class G5Mesh(ctypes.Structure):
     ]
 
 
+class G5ForestSpec(ctypes.Structure):
+    _fields_ = [
+        ("dim", ctypes.c_int32),
+        ("bsize", ctypes.c_int32),
+        ("nbrick", ctypes.c_int32 * 3),
+        ("periodic", ctypes.c_int32 * 3),
+        ("level_min", ctypes.c_int32),
+        ("level_max", ctypes.c_int32),
+    ]
+
+
 class G5Remap(ctypes.Structure):
     _fields_ = [
         ("n_old", ctypes.c_int32),
@@ -118,6 +129,15 @@ EXPORTS = [
     "g5_last_launch_count",
     "g5_step_static",
     "g5_remap",
+    "g5_forest_create",
+    "g5_forest_destroy",
+    "g5_forest_num_leaves",
+    "g5_forest_leaves",
+    "g5_forest_refine",
+    "g5_forest_balance",
+    "g5_forest_adapt",
+    "g5_forest_table_sizes",
+    "g5_forest_table",
 ]
 
 _lib = None
@@ -161,6 +181,17 @@ def load_library(build_if_missing: bool = True):
     L.g5_last_launch_count.argtypes = [vp]
     L.g5_remap.argtypes = [vp, ctypes.POINTER(G5Remap), vp, vp, vp]
     L.g5_step_static.argtypes = [ctypes.POINTER(G5Params), ctypes.POINTER(G5Mesh), vp, vp, vp, ctypes.c_int, vp, vp, vp]
+    L.g5_forest_create.argtypes = [ctypes.POINTER(G5ForestSpec), vp, ctypes.c_int64, ctypes.POINTER(vp)]
+    L.g5_forest_destroy.argtypes = [vp]
+    L.g5_forest_num_leaves.restype = ctypes.c_int64
+    L.g5_forest_num_leaves.argtypes = [vp]
+    L.g5_forest_leaves.argtypes = [vp, vp]
+    L.g5_forest_refine.argtypes = [vp, vp, ctypes.c_int64]
+    L.g5_forest_balance.argtypes = [vp]
+    L.g5_forest_adapt.restype = ctypes.c_int64
+    L.g5_forest_adapt.argtypes = [vp, vp, ctypes.c_int64, vp, vp, ctypes.c_int64]
+    L.g5_forest_table_sizes.argtypes = [vp, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)]
+    L.g5_forest_table.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp]
     _lib = L
     return L
 

@@ -336,6 +336,60 @@ int g5_step_static(const G5Params * params,
                    unsigned int *   d_status_out,
                    void *           stream);
 
+/*
+ * Block forest of the dynamic AMR cycle (host only; no device call).  It
+ * stands where the reference adapts its p4est forest
+ * (AMRManager::rebuild_from_context, SolverGodunovFiveEq.cpp:258-314) and
+ * rebuilds the neighbour hashmap the stencils read: refinement, 2:1 balance
+ * across faces, edges and corners, adaptation from ComputeRefineFlags codes
+ * with the old -> new block map of g5_remap, and the G5Mesh block table.
+ * Leaves are rows (level, x, y, z) in block units of their level (z = 0 in
+ * 2D) on a brick of nbrick level-0 trees; leaf order (and owned-block order
+ * of the table): brick tree, then the Morton index of the leaf's origin at the
+ * finest level present.
+ */
+typedef struct G5Forest G5Forest;
+typedef struct G5ForestSpec
+{
+  int32_t dim;
+  int32_t bsize;
+  int32_t nbrick[3];
+  int32_t periodic[3];
+  int32_t level_min;
+  int32_t level_max;
+} G5ForestSpec;
+
+/* n_leaves == 0: uniform at level_min.  G5_ERR_MESH for a leaf outside the
+ * brick or the level range. */
+int g5_forest_create(const G5ForestSpec * spec, const int32_t * leaves, int64_t n_leaves, G5Forest ** out);
+int g5_forest_destroy(G5Forest * forest);
+int64_t g5_forest_num_leaves(const G5Forest * forest);
+/* the leaves in table order, 4 int32 each */
+int g5_forest_leaves(const G5Forest * forest, int32_t * out);
+/* refine the given leaves below level_max; returns how many */
+int g5_forest_refine(G5Forest * forest, const int32_t * keys, int64_t n);
+/* refine until 2:1 balanced; returns how many refinements */
+int g5_forest_balance(G5Forest * forest);
+/* one adaptation: flags[i] for the i-th leaf in table order (2 refine, 0
+ * coarsen, else keep).  Refines flagged leaves below level_max, restores the
+ * balance by refining, coarsens complete families flagged 0 above level_min
+ * that were not refined unless the coarse block would touch a leaf two levels
+ * finer.  Writes kind[j] / src[j * 2^dim ..] of every new leaf (G5Remap's
+ * arrays, capacity cap >= n_flags * 2^dim) and returns the new leaf count. */
+int64_t g5_forest_adapt(G5Forest * forest, const int8_t * flags, int64_t n_flags, int8_t * kind, int32_t * src, int64_t cap);
+/* block table of the leaves (G5Mesh arrays: level and coord for owned then
+ * outside blocks, nbr / nbr_rel per owned block, the outside twins'
+ * out_src / out_normal / out_border); sizes first */
+int g5_forest_table_sizes(G5Forest * forest, int32_t * n_owned, int32_t * n_outside);
+int g5_forest_table(G5Forest * forest,
+                    int32_t *  level,
+                    int32_t *  coord,
+                    int32_t *  nbr,
+                    int8_t *   nbr_rel,
+                    int32_t *  out_src,
+                    int8_t *   out_normal,
+                    int8_t *   out_border);
+
 #ifdef __cplusplus
 }
 #endif
