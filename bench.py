@@ -61,6 +61,12 @@ def parse():
     ap.add_argument("--profile", action="store_true", help="one FP64 and one mixed step kernel launch, for ncu")
     ap.add_argument("--no-clocks", action="store_true", help="skip the nvidia-smi clock sampling (and its bracketing load)")
     ap.add_argument(
+        "--amr-cycles",
+        type=int,
+        default=0,
+        help="time N dynamic AMR cycles (10 steps + flags, adaptation, remap, table upload) instead of the benchmark",
+    )
+    ap.add_argument(
         "--prolongation",
         type=int,
         choices=[0, 1, 2, 3],
@@ -70,14 +76,14 @@ def parse():
     return ap.parse_args()
 
 
-def build_workload(name, flag_fn, prolongation=0):
-    desc, t, p, U = _workload(name, flag_fn)
+def build_workload(name, flag_fn, prolongation=0, with_mesh=False):
+    desc, t, p, U, mesh = _workload(name, flag_fn)
     if prolongation:
         import dataclasses
 
         p = dataclasses.replace(p, prolongation=prolongation)
         desc += ("", "_minmod_prolongation", "_conservative_o2_prolongation", "_conservative_o4_prolongation")[prolongation]
-    return desc, t, p, U
+    return (desc, t, p, U, mesh) if with_mesh else (desc, t, p, U)
 
 
 def _workload(name, flag_fn):
@@ -101,12 +107,14 @@ def _workload(name, flag_fn):
     elif name == "droplets32":
         _, t, p, U, _ = configs.droplet_instances(n_inst=32)
         U = np.ascontiguousarray(U)
+        mesh = None
         desc = "droplet_advection_2d_32_instances_16x16"
     else:
         _, t, p, U, _ = configs.droplet_instances()
         U = np.ascontiguousarray(U)
+        mesh = None
         desc = "droplet_advection_2d_256_instances_16x16"
-    return desc, t, p, U
+    return desc, t, p, U, mesh
 
 
 class ClockSampler:
@@ -341,12 +349,82 @@ def run_profile_case(args):
     return 0 if st == 0 else 1
 
 
+def run_amr_case(args):
+    """Dynamic AMR: N cycles of 10 mixed steps (the decks' cycle_frequency)
+    then SolverGodunovFiveEq::do_amr_cycle's phases, each timed on the host
+    with the device synchronised: boundary fill + refine flags + flag copy,
+    forest adaptation, block table build, remap, table upload, boundary fill."""
+    import time
+
+    import torch
+
+    from godunov_five_eq_gb300 import GodunovImplemGB300, gpu_flag_fn
+
+    desc, t, p, U, mesh = build_workload(args.workload, gpu_flag_fn(), args.prolongation, with_mesh=True)
+    if mesh is None:
+        raise SystemExit("--amr-cycles needs a single-mesh workload")
+    impl = GodunovImplemGB300(p, t)
+    A = torch.from_numpy(U.copy()).cuda()
+    phases = {k: [] for k in ("steps", "flags", "adapt", "build", "remap", "set_mesh", "fill")}
+    blocks = []
+
+    def now():
+        torch.cuda.synchronize()
+        return time.perf_counter()
+
+    for cycle in range(args.amr_cycles + 1):
+        B = torch.empty_like(A)
+        impl.begin(A)
+        t0 = now()
+        for _ in range(10):
+            impl.advance(A, B, "mixed")
+            A, B = B, A
+        t1 = now()
+        impl.fill_outside_quadrants(A)
+        flags = impl.refine_flags(A, 0, 0.1, 0.0125, 0.02, mesh.level_min, mesh.level_max).cpu().numpy()
+        t2 = now()
+        rt = mesh.adapt(flags)
+        t3 = now()
+        table = mesh.build()
+        t4 = now()
+        A2 = torch.empty((table.n_total, table.nv, table.ncell), dtype=torch.float64, device="cuda")
+        impl.remap(rt, A, A2)
+        t5 = now()
+        impl.resize_auxiliary_data(table)
+        t6 = now()
+        impl.fill_outside_quadrants(A2)
+        t7 = now()
+        A = A2
+        if cycle == 0:
+            continue  # warm-up cycle
+        for k, v in zip(phases, (t1 - t0, t2 - t1, t3 - t2, t4 - t3, t5 - t4, t6 - t5, t7 - t6)):
+            phases[k].append(v * 1e3)
+        blocks.append(table.n_owned)
+    st = impl.status()
+    ms = {k: round(float(np.median(v)), 3) for k, v in phases.items()}
+    print(
+        json.dumps(
+            {
+                "amr_cycles": args.amr_cycles,
+                "workload": desc,
+                "median_ms": ms,
+                "cycle_ms": round(sum(ms.values()) - ms["steps"], 3),
+                "blocks": blocks,
+                "status": st,
+            }
+        )
+    )
+    return 0 if st == 0 else 1
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
     if args.profile:
         return run_profile_case(args)
+    if args.amr_cycles > 0:
+        return run_amr_case(args)
     import torch
     import torch.distributed as dist
 

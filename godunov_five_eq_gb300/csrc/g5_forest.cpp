@@ -69,8 +69,63 @@ struct G5Forest
   KeySet leaves;
   Table  table;          // block table of the leaves, built on demand
   bool   table_valid = false;
+  // leaf membership per level on a dense grid with a one-block margin (the
+  // outside twins' positions), used when the level grids are small; the hash
+  // set stays the list of leaves
+  bool                 dense = false;
+  std::vector<uint8_t> occ[32];
+  int64_t              gx[32], gxy[32]; // grid strides per level
 
   int extent(int L, int e) const { return nbrick[e] << L; }
+
+  void init_dense()
+  {
+    int64_t total = 0;
+    for (int L = lmin; L <= lmax; ++L)
+      total += (int64_t)(extent(L, 0) + 2) * (extent(L, 1) + 2) * (dim == 3 ? extent(L, 2) + 2 : 1);
+    dense = total <= (int64_t)1 << 26;
+    if (!dense)
+      return;
+    for (int L = lmin; L <= lmax; ++L)
+    {
+      gx[L] = extent(L, 0) + 2;
+      gxy[L] = gx[L] * (extent(L, 1) + 2);
+      occ[L].assign((size_t)(gxy[L] * (dim == 3 ? extent(L, 2) + 2 : 1)), 0);
+    }
+  }
+
+  // position of k on its level's grid, or -1 outside it
+  int64_t grid_index(const Key & k) const
+  {
+    if (k.L < lmin || k.L > lmax)
+      return -1;
+    for (int e = 0; e < dim; ++e)
+      if (k.c(e) < -1 || k.c(e) > extent(k.L, e))
+        return -1;
+    return (k.x + 1) + gx[k.L] * (k.y + 1) + (dim == 3 ? gxy[k.L] * (k.z + 1) : 0);
+  }
+
+  bool has(const Key & k) const
+  {
+    if (!dense)
+      return leaves.count(k) != 0;
+    const int64_t i = grid_index(k);
+    return i >= 0 && occ[k.L][(size_t)i];
+  }
+  void add(const Key & k)
+  {
+    leaves.insert(k);
+    const int64_t i = dense ? grid_index(k) : -1;
+    if (i >= 0)
+      occ[k.L][(size_t)i] = 1;
+  }
+  void del(const Key & k)
+  {
+    leaves.erase(k);
+    const int64_t i = dense ? grid_index(k) : -1;
+    if (i >= 0)
+      occ[k.L][(size_t)i] = 0;
+  }
 
   // periodic wrap of same-level coordinates; true when outside a non-periodic face
   bool wrap(int L, const int * c, int * out) const
@@ -107,7 +162,7 @@ struct G5Forest
     {
       const int s = L - l;
       const Key k{ l, c[0] >> s, c[1] >> s, dim == 3 ? c[2] >> s : 0 };
-      if (leaves.count(k))
+      if (has(k))
       {
         out = k;
         return true;
@@ -152,11 +207,11 @@ struct G5Forest
     table_valid = false;
     int n = 0;
     for (const Key & k : keys)
-      if (leaves.count(k) && k.L < lmax)
+      if (has(k) && k.L < lmax)
       {
-        leaves.erase(k);
+        del(k);
         for (int ci = 0; ci < nchild(); ++ci)
-          leaves.insert(child(k, ci));
+          add(child(k, ci));
         ++n;
       }
     return n;
@@ -281,6 +336,7 @@ g5_forest_create(const G5ForestSpec * spec, const int32_t * leaves, int64_t n_le
     f->nbrick[e] = e < spec->dim ? spec->nbrick[e] : 1;
     f->periodic[e] = e < spec->dim ? (spec->periodic[e] != 0) : 0;
   }
+  f->init_dense();
   if (n_leaves == 0)
   {
     // uniform at level_min
@@ -288,7 +344,7 @@ g5_forest_create(const G5ForestSpec * spec, const int32_t * leaves, int64_t n_le
     for (int z = 0; z < (f->dim == 3 ? f->extent(L, 2) : 1); ++z)
       for (int y = 0; y < f->extent(L, 1); ++y)
         for (int x = 0; x < f->extent(L, 0); ++x)
-          f->leaves.insert(Key{ L, x, y, z });
+          f->add(Key{ L, x, y, z });
   }
   else
   {
@@ -301,7 +357,7 @@ g5_forest_create(const G5ForestSpec * spec, const int32_t * leaves, int64_t n_le
         delete f;
         return G5_ERR_MESH;
       }
-      f->leaves.insert(k);
+      f->add(k);
     }
   }
   *out = f;
@@ -381,11 +437,11 @@ g5_forest_adapt(G5Forest * f, const int8_t * flags, int64_t n_flags, int8_t * ki
       twice = true;
       return;
     }
-    f->leaves.erase(k);
+    f->del(k);
     for (int ci = 0; ci < nc; ++ci)
     {
       const Key ch = f->child(k, ci);
-      f->leaves.insert(ch);
+      f->add(ch);
       refined_from[ch] = k;
     }
   };
@@ -420,7 +476,7 @@ g5_forest_adapt(G5Forest * f, const int8_t * flags, int64_t n_flags, int8_t * ki
     {
       const Key ch = f->child(P, ci);
       auto      it = old_index.find(ch);
-      all = f->leaves.count(ch) && it != old_index.end() && flags[it->second] == 0;
+      all = f->has(ch) && it != old_index.end() && flags[it->second] == 0;
       kids.push_back(ch);
     }
     if (all)
@@ -429,8 +485,8 @@ g5_forest_adapt(G5Forest * f, const int8_t * flags, int64_t n_flags, int8_t * ki
   for (auto & fam : families)
   {
     for (const Key & ch : fam.second)
-      f->leaves.erase(ch);
-    f->leaves.insert(fam.first);
+      f->del(ch);
+    f->add(fam.first);
   }
   for (;;)
   {
@@ -442,9 +498,9 @@ g5_forest_adapt(G5Forest * f, const int8_t * flags, int64_t n_flags, int8_t * ki
       break;
     for (const Key & P : undo)
     {
-      f->leaves.erase(P);
+      f->del(P);
       for (const Key & ch : families[P])
-        f->leaves.insert(ch);
+        f->add(ch);
       families.erase(P);
     }
   }
@@ -490,10 +546,35 @@ build_table(const G5Forest * f, Table & t)
 {
   const int dim = f->dim, ns = dim == 2 ? 9 : 27, nc = f->nchild();
   t.owned = f->ordered();
-  KeyMap<int> index;
-  index.reserve(t.owned.size() * 3);
+  // block index by key: the forest's level grids when dense, else a hash map
+  KeyMap<int>          hindex;
+  std::vector<int32_t> dindex[32];
+  if (f->dense)
+    for (int L = f->lmin; L <= f->lmax; ++L)
+      dindex[L].assign(f->occ[L].size(), -1);
+  else
+    hindex.reserve(t.owned.size() * 3);
+  auto put = [&](const Key & k, int v) {
+    if (!f->dense)
+      hindex[k] = v;
+    else
+    {
+      const int64_t gi = f->grid_index(k);
+      if (gi >= 0)
+        dindex[k.L][(size_t)gi] = v;
+    }
+  };
+  auto find = [&](const Key & k) -> int {
+    if (!f->dense)
+    {
+      auto it = hindex.find(k);
+      return it == hindex.end() ? -1 : it->second;
+    }
+    const int64_t gi = f->grid_index(k);
+    return gi < 0 ? -1 : dindex[k.L][(size_t)gi];
+  };
   for (size_t i = 0; i < t.owned.size(); ++i)
-    index[t.owned[i]] = (int)i;
+    put(t.owned[i], (int)i);
   // outside twins: per owned block touching a non-periodic face, one twin per
   // non-zero normal over {0} + {-1 at the min face} + {+1 at the max face}
   for (size_t i = 0; i < t.owned.size(); ++i)
@@ -537,7 +618,11 @@ build_table(const G5Forest * f, Table & t)
   }
   const int n_owned = (int)t.owned.size();
   for (size_t j = 0; j < t.outside.size(); ++j)
-    index[t.outside[j]] = n_owned + (int)j;
+  {
+    if (f->dense && f->grid_index(t.outside[j]) < 0)
+      return G5_ERR_MESH;
+    put(t.outside[j], n_owned + (int)j);
+  }
   t.nbr.assign((size_t)n_owned * ns * nc, -1);
   t.rel.assign((size_t)n_owned * ns, 0);
   for (int i = 0; i < n_owned; ++i)
@@ -554,19 +639,19 @@ build_table(const G5Forest * f, Table & t)
           int       c[3] = { k.x + sx, k.y + sy, dim == 3 ? k.z + sz : 0 }, cw[3];
           f->wrap(k.L, c, cw);
           int32_t * nb = &t.nbr[((size_t)i * ns + s) * nc];
-          auto      it = index.find(make_key(k.L, cw));
-          if (it != index.end())
+          int       hit = find(make_key(k.L, cw));
+          if (hit >= 0)
           {
             t.rel[(size_t)i * ns + s] = 0;
-            nb[0] = it->second;
+            nb[0] = hit;
             continue;
           }
           const Key pk{ k.L - 1, cw[0] >> 1, cw[1] >> 1, dim == 3 ? cw[2] >> 1 : 0 };
-          it = index.find(pk);
-          if (it != index.end())
+          hit = find(pk);
+          if (hit >= 0)
           {
             t.rel[(size_t)i * ns + s] = -1;
-            nb[0] = it->second;
+            nb[0] = hit;
             continue;
           }
           bool found = false;
@@ -579,10 +664,10 @@ build_table(const G5Forest * f, Table & t)
             if (!touch)
               continue;
             const Key ck{ k.L + 1, 2 * cw[0] + ch[0], 2 * cw[1] + ch[1], dim == 3 ? 2 * cw[2] + ch[2] : 0 };
-            auto      ct = index.find(ck);
-            if (ct == index.end())
+            const int ct = find(ck);
+            if (ct < 0)
               return G5_ERR_MESH; // not 2:1 balanced
-            nb[ci] = ct->second;
+            nb[ci] = ct;
             found = true;
           }
           if (!found)

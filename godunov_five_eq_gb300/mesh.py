@@ -170,6 +170,7 @@ class BlockMesh:
         return kids
 
     def refine(self, keys) -> int:
+        self._drop_forest()
         n = 0
         for k in keys:
             if k in self.leaves and k[0] < self.level_max:
@@ -188,24 +189,46 @@ class BlockMesh:
         return None
 
     def _forest(self):
-        """A native forest (libg5gpu.so) holding the current leaves."""
+        """The native forest (libg5gpu.so) holding the current leaves: the one
+        the last native operation left when `leaves` is still the set it
+        produced (same object, same size), else a new one from `leaves`."""
         import ctypes
 
         from godunov_five_eq_gb300 import implem
 
         lib = implem.load_library()
+        cache = getattr(self, "_fcache", None)
+        if cache is not None and cache[1] is self.leaves and cache[2] == len(self.leaves):
+            return lib, cache[0]
+        self._drop_forest()
         spec = implem.G5ForestSpec()
         spec.dim, spec.bsize = self.dim, self.bsize
         for e in range(3):
             spec.nbrick[e] = self.nbrick[e] if e < self.dim else 1
             spec.periodic[e] = int(self.periodic[e]) if e < self.dim else 0
         spec.level_min, spec.level_max = self.level_min, self.level_max
-        keys = np.ascontiguousarray(np.array(list(self.leaves), np.int32).reshape(-1, 4))
+        n = len(self.leaves)
+        keys = np.fromiter(itertools.chain.from_iterable(self.leaves), dtype=np.int32, count=4 * n)
         h = ctypes.c_void_p()
-        rc = lib.g5_forest_create(ctypes.byref(spec), keys.ctypes.data_as(ctypes.c_void_p), keys.shape[0], ctypes.byref(h))
+        rc = lib.g5_forest_create(ctypes.byref(spec), keys.ctypes.data_as(ctypes.c_void_p), n, ctypes.byref(h))
         if rc != 0:
             raise RuntimeError(f"g5_forest_create failed ({rc})")
+        self._fcache = (h, self.leaves, n)
         return lib, h
+
+    def _drop_forest(self) -> None:
+        cache = getattr(self, "_fcache", None)
+        self._fcache = None
+        if cache is not None:
+            from godunov_five_eq_gb300 import implem
+
+            implem.load_library().g5_forest_destroy(cache[0])
+
+    def __del__(self):
+        try:
+            self._drop_forest()
+        except Exception:
+            pass
 
     @staticmethod
     def _forest_leaves(lib, h) -> np.ndarray:
@@ -217,16 +240,18 @@ class BlockMesh:
         return out
 
     def _set_leaves(self, arr: np.ndarray) -> None:
-        self.leaves = set(map(tuple, arr.tolist()))
+        """`leaves` from the native forest's rows (which stays the cache)."""
+        h = self._fcache[0]
+        self.leaves = set(zip(*arr.T.tolist()))
+        self._fcache = (h, self.leaves, len(self.leaves))
 
     def balance(self) -> int:
         """Enforce 2:1 balance across faces, edges and corners (native forest)."""
         lib, h = self._forest()
-        try:
-            n = lib.g5_forest_balance(h)
-            self._set_leaves(self._forest_leaves(lib, h))
-        finally:
-            lib.g5_forest_destroy(h)
+        n = lib.g5_forest_balance(h)
+        if n < 0:
+            raise RuntimeError(f"g5_forest_balance failed ({n})")
+        self._set_leaves(self._forest_leaves(lib, h))
         return int(n)
 
     # ------------------------------------------------------------ adaptation
@@ -255,15 +280,13 @@ class BlockMesh:
         kind = np.zeros(cap, np.int8)
         src = np.full((cap, nc), -1, np.int32)
         lib, h = self._forest()
-        try:
-            n_new = lib.g5_forest_adapt(
-                h, flags.ctypes.data_as(ctypes.c_void_p), flags.shape[0], kind.ctypes.data_as(ctypes.c_void_p), src.ctypes.data_as(ctypes.c_void_p), cap
-            )
-            if n_new < 0:
-                raise RuntimeError(f"g5_forest_adapt failed ({n_new})")
-            self._set_leaves(self._forest_leaves(lib, h))
-        finally:
-            lib.g5_forest_destroy(h)
+        n_new = lib.g5_forest_adapt(
+            h, flags.ctypes.data_as(ctypes.c_void_p), flags.shape[0], kind.ctypes.data_as(ctypes.c_void_p), src.ctypes.data_as(ctypes.c_void_p), cap
+        )
+        if n_new < 0:
+            self._drop_forest()  # the forest may be half-adapted
+            raise RuntimeError(f"g5_forest_adapt failed ({n_new})")
+        self._set_leaves(self._forest_leaves(lib, h))
         return RemapTable(dim=self.dim, bsize=self.bsize, n_old=flags.shape[0], kind=kind[:n_new].copy(), src=src[:n_new].copy())
 
     # ------------------------------------------------------------------ tables
@@ -271,11 +294,8 @@ class BlockMesh:
         """Leaves in table order: brick tree (x fastest), then Morton order of
         the leaf origin at the finest level present (native forest)."""
         lib, h = self._forest()
-        try:
-            arr = self._forest_leaves(lib, h)
-        finally:
-            lib.g5_forest_destroy(h)
-        return [tuple(r) for r in arr.tolist()]
+        arr = self._forest_leaves(lib, h)
+        return list(zip(*arr.T.tolist()))
 
     def build(self) -> BlockTable:
         """The block table of the current leaves (g5_forest_table): owned
@@ -283,26 +303,23 @@ class BlockMesh:
         import ctypes
 
         lib, h = self._forest()
-        try:
-            n_owned, n_outside = ctypes.c_int32(), ctypes.c_int32()
-            rc = lib.g5_forest_table_sizes(h, ctypes.byref(n_owned), ctypes.byref(n_outside))
-            if rc != 0:
-                raise RuntimeError(f"mesh not 2:1 balanced (g5_forest_table_sizes {rc})")
-            no, nt = n_owned.value, n_outside.value
-            ns, nc = 3**self.dim, 2**self.dim
-            level = np.empty(no + nt, np.int32)
-            coord = np.empty((no + nt, 3), np.int32)
-            nbr = np.empty((no, ns, nc), np.int32)
-            rel = np.empty((no, ns), np.int8)
-            out_src = np.empty(nt, np.int32)
-            out_normal = np.empty((nt, 3), np.int8)
-            out_border = np.empty((nt, 6), np.int8)
-            ptr = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
-            rc = lib.g5_forest_table(h, ptr(level), ptr(coord), ptr(nbr), ptr(rel), ptr(out_src), ptr(out_normal), ptr(out_border))
-            if rc != 0:
-                raise RuntimeError(f"g5_forest_table failed ({rc})")
-        finally:
-            lib.g5_forest_destroy(h)
+        n_owned, n_outside = ctypes.c_int32(), ctypes.c_int32()
+        rc = lib.g5_forest_table_sizes(h, ctypes.byref(n_owned), ctypes.byref(n_outside))
+        if rc != 0:
+            raise RuntimeError(f"mesh not 2:1 balanced (g5_forest_table_sizes {rc})")
+        no, nt = n_owned.value, n_outside.value
+        ns, nc = 3**self.dim, 2**self.dim
+        level = np.empty(no + nt, np.int32)
+        coord = np.empty((no + nt, 3), np.int32)
+        nbr = np.empty((no, ns, nc), np.int32)
+        rel = np.empty((no, ns), np.int8)
+        out_src = np.empty(nt, np.int32)
+        out_normal = np.empty((nt, 3), np.int8)
+        out_border = np.empty((nt, 6), np.int8)
+        ptr = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+        rc = lib.g5_forest_table(h, ptr(level), ptr(coord), ptr(nbr), ptr(rel), ptr(out_src), ptr(out_normal), ptr(out_border))
+        if rc != 0:
+            raise RuntimeError(f"g5_forest_table failed ({rc})")
         return BlockTable(
             dim=self.dim,
             bsize=self.bsize,

@@ -30,6 +30,9 @@ CASES = [
     (2, 8, (3, 2, 1), False, 0, 4, 2),
     (3, 8, (2, 1, 1), True, 1, 3, 3),
     (3, 8, (2, 2, 2), False, 0, 3, 4),
+    # level grids too large for the dense lookup: the hash-map path
+    (3, 8, (1, 1, 1), False, 0, 20, 5),
+    (2, 16, (2, 1, 1), True, 0, 24, 6),
 ]
 
 
@@ -37,7 +40,7 @@ CASES = [
 def test_native_forest_matches_restatement(dim, b, nbrick, periodic, lmin, lmax, seed):
     rng = np.random.default_rng(seed)
     nat, py = _pair(dim, b, nbrick, periodic, lmin, lmax)
-    for _ in range(lmax - lmin):
+    for _ in range(min(lmax - lmin, 4)):
         leaves = sorted(nat.leaves)
         pick = rng.choice(len(leaves), size=min(4, len(leaves)), replace=False)
         keys = [leaves[i] for i in pick]
