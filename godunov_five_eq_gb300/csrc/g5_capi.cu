@@ -3,6 +3,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <unordered_map>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -42,6 +43,12 @@ struct G5Context
   uint8_t *            d_inst_active = nullptr;
   unsigned int * d_status = nullptr;
   int64_t        bytes = 0;
+  struct PoolEntry
+  {
+    void * p = nullptr;
+    size_t cap = 0;
+  };
+  std::unordered_map<const void *, PoolEntry> pool; // device buffers by field (dev_alloc)
   int            ctas_per_sm[2] = { 0, 0 };
   int            last_launches = 0;
   // cached one-step graphs of g5_advance
@@ -107,6 +114,10 @@ struct G5Context
 namespace
 {
 
+// Device buffers of the context, one per field (keyed by the field's
+// address): a new mesh reuses a buffer that is large enough, so that an AMR
+// cycle's table upload costs copies, not frees (each a device-wide
+// synchronisation) and allocations.  The pool is released by g5_destroy.
 template <typename T>
 int
 dev_alloc(G5Context * c, T ** p, size_t count)
@@ -114,10 +125,37 @@ dev_alloc(G5Context * c, T ** p, size_t count)
   *p = nullptr;
   if (count == 0)
     return G5_OK;
-  if (cudaMalloc((void **)p, count * sizeof(T)) != cudaSuccess)
+  const size_t           bytes = count * sizeof(T);
+  G5Context::PoolEntry & e = c->pool[(const void *)p];
+  if (e.p && e.cap >= bytes)
+  {
+    *p = static_cast<T *>(e.p);
+    return G5_OK;
+  }
+  if (e.p)
+  {
+    cudaFree(e.p);
+    c->bytes -= (int64_t)e.cap;
+    e = G5Context::PoolEntry();
+  }
+  void * np = nullptr;
+  if (cudaMalloc(&np, bytes) != cudaSuccess)
     return G5_ERR_CUDA;
-  c->bytes += (int64_t)(count * sizeof(T));
+  e.p = np;
+  e.cap = bytes;
+  c->bytes += (int64_t)bytes;
+  *p = static_cast<T *>(np);
   return G5_OK;
+}
+
+void
+free_pool(G5Context * c)
+{
+  for (auto & kv : c->pool)
+    if (kv.second.p)
+      cudaFree(kv.second.p);
+  c->pool.clear();
+  c->bytes = c->d_status ? (int64_t)sizeof(unsigned int) : 0;
 }
 
 template <typename T>
@@ -143,25 +181,15 @@ drop_graphs(G5Context * c)
   }
 }
 
+// the context forgets its mesh; the buffers stay in the pool for the next one
 void
 free_mesh(G5Context * c)
 {
-  void * ptrs[] = { c->d_level,       c->d_coord,       c->d_nbr,        c->d_inst,       c->d_reflux_slot,
-                    c->d_defer_slot,  c->d_defer_list,  c->d_out_src,    c->d_nbr_rel,    c->d_out_normal,
-                    c->d_out_border,  c->d_reflux_buf,  c->d_defer_buf,  c->d_dt,         c->d_invdt,
-                    c->d_ticket,      c->d_urk,         c->d_defer_info, c->d_twin_first, c->d_twin_list, c->d_walk,
-                    c->d_pg_slot,     c->d_pg };
-  for (void * p : ptrs)
-    if (p)
-      cudaFree(p);
   c->d_level = c->d_coord = c->d_nbr = c->d_inst = nullptr;
   c->d_reflux_slot = c->d_defer_slot = c->d_defer_list = c->d_out_src = nullptr;
   c->d_nbr_rel = c->d_out_normal = c->d_out_border = nullptr;
   c->d_reflux_buf = c->d_defer_buf = c->d_dt = c->d_invdt = nullptr;
   c->d_ticket = nullptr;
-  for (void * p : { (void *)c->d_batch_work, (void *)c->d_inst_active })
-    if (p)
-      cudaFree(p);
   c->d_batch_work = nullptr;
   c->d_inst_active = nullptr;
   c->inst_blocks.clear();
@@ -171,9 +199,6 @@ free_mesh(G5Context * c)
   c->d_twin_first = c->d_twin_list = c->d_walk = c->d_pg_slot = nullptr;
   c->d_pg = nullptr;
   c->fused_fill = false;
-  for (void * p : { (void *)c->pipe.d_work, (void *)c->pipe.d_U, (void *)c->pipe.d_U2 })
-    if (p)
-      cudaFree(p);
   c->pipe.d_work = nullptr;
   c->pipe.d_U = c->pipe.d_U2 = nullptr;
   c->pipe.K = 0;
@@ -185,7 +210,6 @@ free_mesh(G5Context * c)
   }
   drop_graphs(c);
   c->has_mesh = false;
-  c->bytes = c->d_status ? (int64_t)sizeof(unsigned int) : 0;
 }
 
 g5::DevMesh
@@ -401,6 +425,7 @@ g5_destroy(G5Context * ctx)
   if (!ctx)
     return G5_ERR_ARG;
   free_mesh(ctx);
+  free_pool(ctx);
   if (ctx->d_status)
     cudaFree(ctx->d_status);
   G5Context::HostPipe & hp = ctx->pipe;
@@ -518,6 +543,10 @@ g5_set_mesh(G5Context * c, const G5Mesh * m)
     }
 
   free_mesh(c);
+  // work of the previous mesh may still run on another stream: the buffers
+  // are reused in place below
+  if (cudaDeviceSynchronize() != cudaSuccess)
+    return G5_ERR_CUDA;
   const size_t face_cells = dim == 2 ? (size_t)c->b : (size_t)c->b * c->b;
   const size_t nf = dim == 2 ? 8 : 9;
   int          rc = 0;
