@@ -125,11 +125,34 @@ class BlockMesh:
         self.level_min = int(level_min)
         self.level_max = int(level_max)
         self.scaling = float(scaling)
-        self.leaves: set = set()
+        self._fcache = None  # (native forest, the leaf set it holds or None, leaf count)
+        self._leaves: set | None = set()
         L = self.level_min
         ranges = [range(self.nbrick[e] << L) for e in range(dim)]
         for c in itertools.product(*ranges):
-            self.leaves.add((L,) + tuple(c) + (0,) * (3 - dim))
+            self._leaves.add((L,) + tuple(c) + (0,) * (3 - dim))
+
+    @property
+    def leaves(self) -> set:
+        """The leaves as a set of (level, x, y, z).  After a native operation
+        they live in the native forest until read here.  Change them through
+        the methods or by assigning a new set."""
+        if self._leaves is None:
+            from godunov_five_eq_gb300 import implem
+
+            h = self._fcache[0]
+            arr = self._forest_leaves(implem.load_library(), h)
+            self._leaves = set(zip(*arr.T.tolist()))
+            self._fcache = (h, self._leaves, len(self._leaves))
+        return self._leaves
+
+    @leaves.setter
+    def leaves(self, value) -> None:
+        self.leaves  # noqa: B018  (a forest-only state is read out before it is replaced)
+        self._leaves = value
+
+    def _num_leaves(self) -> int:
+        return len(self._leaves) if self._leaves is not None else self._fcache[2]
 
     # ------------------------------------------------------------------ geometry
     def extent(self, level: int, e: int) -> int:
@@ -197,8 +220,8 @@ class BlockMesh:
         from godunov_five_eq_gb300 import implem
 
         lib = implem.load_library()
-        cache = getattr(self, "_fcache", None)
-        if cache is not None and cache[1] is self.leaves and cache[2] == len(self.leaves):
+        cache = self._fcache
+        if cache is not None and (self._leaves is None or (cache[1] is self._leaves and cache[2] == len(self._leaves))):
             return lib, cache[0]
         self._drop_forest()
         spec = implem.G5ForestSpec()
@@ -213,20 +236,26 @@ class BlockMesh:
         rc = lib.g5_forest_create(ctypes.byref(spec), keys.ctypes.data_as(ctypes.c_void_p), n, ctypes.byref(h))
         if rc != 0:
             raise RuntimeError(f"g5_forest_create failed ({rc})")
-        self._fcache = (h, self.leaves, n)
+        self._fcache = (h, self._leaves, n)
         return lib, h
 
     def _drop_forest(self) -> None:
-        cache = getattr(self, "_fcache", None)
-        self._fcache = None
-        if cache is not None:
-            from godunov_five_eq_gb300 import implem
+        """Release the native forest (its leaves read out first when only it holds them)."""
+        if self._fcache is None:
+            return
+        self.leaves  # noqa: B018
+        from godunov_five_eq_gb300 import implem
 
-            implem.load_library().g5_forest_destroy(cache[0])
+        h, self._fcache = self._fcache[0], None
+        implem.load_library().g5_forest_destroy(h)
 
     def __del__(self):
         try:
-            self._drop_forest()
+            if getattr(self, "_fcache", None) is not None:
+                from godunov_five_eq_gb300 import implem
+
+                implem.load_library().g5_forest_destroy(self._fcache[0])
+                self._fcache = None
         except Exception:
             pass
 
@@ -239,11 +268,10 @@ class BlockMesh:
         lib.g5_forest_leaves(h, out.ctypes.data_as(ctypes.c_void_p))
         return out
 
-    def _set_leaves(self, arr: np.ndarray) -> None:
-        """`leaves` from the native forest's rows (which stays the cache)."""
-        h = self._fcache[0]
-        self.leaves = set(zip(*arr.T.tolist()))
-        self._fcache = (h, self.leaves, len(self.leaves))
+    def _leaves_changed(self, lib, h) -> None:
+        """The native forest changed the leaves: they live there until read."""
+        self._leaves = None
+        self._fcache = (h, None, int(lib.g5_forest_num_leaves(h)))
 
     def balance(self) -> int:
         """Enforce 2:1 balance across faces, edges and corners (native forest)."""
@@ -251,7 +279,7 @@ class BlockMesh:
         n = lib.g5_forest_balance(h)
         if n < 0:
             raise RuntimeError(f"g5_forest_balance failed ({n})")
-        self._set_leaves(self._forest_leaves(lib, h))
+        self._leaves_changed(lib, h)
         return int(n)
 
     # ------------------------------------------------------------ adaptation
@@ -273,8 +301,8 @@ class BlockMesh:
         import ctypes
 
         flags = np.ascontiguousarray(np.asarray(flags).reshape(-1), np.int8)
-        if flags.shape[0] != len(self.leaves):
-            raise ValueError(f"expected {len(self.leaves)} flags, got {flags.shape[0]}")
+        if flags.shape[0] != self._num_leaves():
+            raise ValueError(f"expected {self._num_leaves()} flags, got {flags.shape[0]}")
         nc = 2**self.dim
         cap = max(1, flags.shape[0] * nc)
         kind = np.zeros(cap, np.int8)
@@ -286,7 +314,7 @@ class BlockMesh:
         if n_new < 0:
             self._drop_forest()  # the forest may be half-adapted
             raise RuntimeError(f"g5_forest_adapt failed ({n_new})")
-        self._set_leaves(self._forest_leaves(lib, h))
+        self._leaves_changed(lib, h)
         return RemapTable(dim=self.dim, bsize=self.bsize, n_old=flags.shape[0], kind=kind[:n_new].copy(), src=src[:n_new].copy())
 
     # ------------------------------------------------------------------ tables
