@@ -308,7 +308,9 @@ plan_host_pipe(G5Context * c, const G5Mesh * m, const std::vector<int32_t> & def
       if (s == center)
         continue;
       const int32_t * nb = m->nbr + ((size_t)n * ns + s) * nch;
-      for (int ch = 0; ch < nch; ++ch)
+      // only a finer slot lists more than one block
+      const int       nread = m->nbr_rel[(size_t)n * ns + s] > 0 ? nch : 1;
+      for (int ch = 0; ch < nread; ++ch)
         if (nb[ch] >= 0)
           r = r > arrival(nb[ch]) ? r : arrival(nb[ch]);
     }
