@@ -256,13 +256,7 @@ refine_flags_kernel(const double * U,
 {
   using H = V<DIM>;
   constexpr int NC = (DIM == 2) ? B * B : B * B * B;
-  constexpr int NF = (B + 1) * (DIM == 2 ? B : B * B); // faces per direction
   __shared__ int sflag;
-  // SIMPLE_GRADIENT: the normalised gradient of a face is the same for the
-  // two cells it separates (symmetric in its arguments, to the bit), so it is
-  // evaluated once per face and variable ([DIM][2][NF]) and each cell takes
-  // the maximum over its faces, per variable as the per-cell form does
-  __shared__ double sface[DIM * 2 * NF];
   for (int n = blockIdx.x; n < m.n_owned; n += gridDim.x)
   {
     if (threadIdx.x == 0)
@@ -270,88 +264,6 @@ refine_flags_kernel(const double * U,
     __syncthreads();
     const int lev = m.level[n];
     int       bflag = -1;
-    auto      flag_of = [&](double ind) {
-      if (lev < lmax && ind > eps_r)
-        return 2;
-      if (lev > lmin && ind < eps_c)
-        return 0;
-      return 1;
-    };
-    if (indicator == 0)
-    {
-      const int vars[2] = { H::IAD0, H::IAD1 };
-      for (int w = threadIdx.x; w < DIM * 2 * NF; w += blockDim.x)
-      {
-        const int d = w / (2 * NF), t = (w / NF) % 2, f = w % NF;
-        // face f of direction d: position i (0 .. B) along d, the other
-        // coordinates (x fastest) of the cells it separates
-        const int i = f % (B + 1), r = f / (B + 1);
-        int       cell[3] = { 0, 0, 0 };
-        int       o = 0;
-        for (int e = 0; e < DIM; ++e)
-          if (e != d)
-          {
-            cell[e] = o == 0 ? r % B : r / B;
-            ++o;
-          }
-        const double * Uv = U + ((size_t)n * H::NV + vars[t]) * NC;
-        double         a, b;
-        if (i == 0)
-        {
-          cell[d] = 0;
-          b = Uv[cell[0] + B * (cell[1] + B * cell[2])];
-          a = neighbor_same_level<DIM, B>(U, m, n, cell, d, -1, vars[t]);
-          sface[w] = normalized_gradient(b, a);
-        }
-        else if (i == B)
-        {
-          cell[d] = B - 1;
-          a = Uv[cell[0] + B * (cell[1] + B * cell[2])];
-          b = neighbor_same_level<DIM, B>(U, m, n, cell, d, +1, vars[t]);
-          sface[w] = normalized_gradient(a, b);
-        }
-        else
-        {
-          cell[d] = i - 1;
-          a = Uv[cell[0] + B * (cell[1] + B * cell[2])];
-          cell[d] = i;
-          b = Uv[cell[0] + B * (cell[1] + B * cell[2])];
-          sface[w] = normalized_gradient(a, b);
-        }
-      }
-      __syncthreads();
-      for (int c = threadIdx.x; c < NC; c += blockDim.x)
-      {
-        const int cell[3] = { c % B, (c / B) % B, DIM == 3 ? c / (B * B) : 0 };
-        int       flag = -1;
-        for (int t = 0; t < 2; ++t)
-        {
-          double res = -1.7976931348623157e308;
-          for (int d = 0; d < DIM; ++d)
-          {
-            int r = 0, o = 0;
-            for (int e = 0; e < DIM; ++e)
-              if (e != d)
-              {
-                r += o == 0 ? cell[e] : B * cell[e];
-                ++o;
-              }
-            const double * F = sface + (d * 2 + t) * NF + r * (B + 1);
-            res = fmax(res, F[cell[d]]);     // the face below the cell (its L neighbour)
-            res = fmax(res, F[cell[d] + 1]); // the face above (its R neighbour)
-          }
-          const int fl = flag_of(res);
-          flag = flag > fl ? flag : fl;
-        }
-        bflag = bflag > flag ? bflag : flag;
-      }
-      atomicMax(&sflag, bflag);
-      __syncthreads();
-      if (threadIdx.x == 0)
-        flags[n] = (int8_t)sflag;
-      __syncthreads();
-      continue;
-    }
     for (int c = threadIdx.x; c < NC; c += blockDim.x)
     {
       const int cell[3] = { c % B, (c / B) % B, DIM == 3 ? c / (B * B) : 0 };
