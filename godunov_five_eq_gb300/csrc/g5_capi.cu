@@ -391,11 +391,6 @@ g5_create(const G5Params * params, G5Context ** out_ctx)
     return G5_ERR_UNSUPPORTED;
   if (params->prolongation < G5_PROLONG_SIMPLE_COPY || params->prolongation > G5_PROLONG_CONSERVATIVE_O4)
     return G5_ERR_ARG;
-  // order 4 reaches 3 coarse cells around a block: past the children of a
-  // finer neighbour that touch it (the only ones the block table lists)
-  // unless the blocks have 16 cells per edge
-  if (params->prolongation == G5_PROLONG_CONSERVATIVE_O4 && params->bsize < 16)
-    return G5_ERR_UNSUPPORTED;
   for (int k = 0; k < 2; ++k)
     if (!(params->gamma[k] > 1.0))
       return G5_ERR_ARG;

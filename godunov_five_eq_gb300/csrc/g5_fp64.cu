@@ -138,6 +138,14 @@ static cudaError_t
 prolong_t(const StepArgs & a, cudaStream_t s, int * launches)
 {
   using T = ProlongTraits<DIM, B, MODE>;
+  static bool configured = false;
+  if (!configured)
+  {
+    const cudaError_t e = cudaFuncSetAttribute(prolong_kernel<DIM, B, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::smem_bytes);
+    if (e != cudaSuccess)
+      return e;
+    configured = true;
+  }
   int grid = num_sms() * 8;
   if (grid > step_count(a))
     grid = step_count(a);
@@ -160,9 +168,15 @@ launch_prolong(int dim, int b, const StepArgs & a, cudaStream_t s, int * launche
          : mode == 3 ? prolong_t<2, 16, 3>(a, s, launches)
                      : cudaErrorInvalidValue;
   if (dim == 2 && b == 8)
-    return mode == 1 ? prolong_t<2, 8, 1>(a, s, launches) : mode == 2 ? prolong_t<2, 8, 2>(a, s, launches) : cudaErrorInvalidValue;
+    return mode == 1 ? prolong_t<2, 8, 1>(a, s, launches)
+         : mode == 2 ? prolong_t<2, 8, 2>(a, s, launches)
+         : mode == 3 ? prolong_t<2, 8, 3>(a, s, launches)
+                     : cudaErrorInvalidValue;
   if (dim == 3 && b == 8)
-    return mode == 1 ? prolong_t<3, 8, 1>(a, s, launches) : mode == 2 ? prolong_t<3, 8, 2>(a, s, launches) : cudaErrorInvalidValue;
+    return mode == 1 ? prolong_t<3, 8, 1>(a, s, launches)
+         : mode == 2 ? prolong_t<3, 8, 2>(a, s, launches)
+         : mode == 3 ? prolong_t<3, 8, 3>(a, s, launches)
+                     : cudaErrorInvalidValue;
   return cudaErrorInvalidValue;
 }
 
@@ -200,10 +214,12 @@ launch_remap_prolong(int dim, int b, int mode, const double * Uold, double * Une
   if (dim == 2 && b == 8)
     return mode == 1 ? refine_t<2, 8, 1>(Uold, Unew, m, list, n_ref, status, s)
          : mode == 2 ? refine_t<2, 8, 2>(Uold, Unew, m, list, n_ref, status, s)
+         : mode == 3 ? refine_t<2, 8, 3>(Uold, Unew, m, list, n_ref, status, s)
                      : cudaErrorInvalidValue;
   if (dim == 3 && b == 8)
     return mode == 1 ? refine_t<3, 8, 1>(Uold, Unew, m, list, n_ref, status, s)
          : mode == 2 ? refine_t<3, 8, 2>(Uold, Unew, m, list, n_ref, status, s)
+         : mode == 3 ? refine_t<3, 8, 3>(Uold, Unew, m, list, n_ref, status, s)
                      : cudaErrorInvalidValue;
   return cudaErrorInvalidValue;
 }

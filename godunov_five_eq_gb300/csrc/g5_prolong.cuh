@@ -27,8 +27,11 @@
 // Reach: the patch spans r + 1 coarse cells around the block's footprint
 // (r = 1 for minmod and order 2, 2 for order 4), so every patch cell lies in
 // one of the block's 3^dim neighbour slots; in a finer slot it lies in a
-// child that touches the block when r <= b/4 - 1/2 (order 4 therefore needs
-// 16-cell blocks: the block table lists only the touching children).
+// child that touches the block when r <= b/4 - 1/2.  Order 4 on 8-cell blocks
+// also reads the far children of a finer slot, which the block table does not
+// list: each is found as the same-level neighbour of its touching sibling
+// (owned, with a neighbour table); a far child refined further, or one beyond
+// a domain face (an outside twin), raises the mesh status.
 #pragma once
 
 #include "g5_common.cuh"
@@ -49,7 +52,6 @@ struct ProlongTraits
   static constexpr int NS = DIM == 2 ? 9 : 27, NCH = DIM == 2 ? 4 : 8;
   static constexpr int NT = 128;
   static constexpr size_t smem_bytes = sizeof(double) * (size_t)NVI * NP;
-  static_assert(B >= 4 + 4 * R, "the patch reaches past the children of a finer slot that touch the block");
 };
 
 // where the value of coarse cell q (coarse coordinates relative to block n's
@@ -112,6 +114,22 @@ coarse_cell_ref(const DevMesh & m, int n, const int * c0, const int * q, int & k
     kind = 2;
     src = nb[DIM == 2 ? ch[0] + 2 * ch[1] : ch[0] + 2 * ch[1] + 4 * ch[2]];
     c = cell(l);
+    if (src < 0)
+    {
+      // a child that does not touch the block (order-4 patches of 8-cell
+      // blocks reach it): the same-level neighbour of the touching sibling,
+      // when that sibling is owned and the child is a leaf
+      int ct[3] = { 0, 0, 0 }, dl[3] = { 0, 0, 0 };
+#pragma unroll
+      for (int e = 0; e < DIM; ++e)
+      {
+        ct[e] = s[e] == 0 ? ch[e] : (s[e] < 0 ? 1 : 0);
+        dl[e] = ch[e] - ct[e];
+      }
+      const int T = nb[DIM == 2 ? ct[0] + 2 * ct[1] : ct[0] + 2 * ct[1] + 4 * ct[2]];
+      const int st = DIM == 2 ? (dl[0] + 1) + 3 * (dl[1] + 1) : (dl[0] + 1) + 3 * (dl[1] + 1) + 9 * (dl[2] + 1);
+      src = (T >= 0 && T < m.n_owned && m.nbr_rel[(size_t)T * NS + st] == 0) ? m.nbr[((size_t)T * NS + st) * NCH] : -1;
+    }
   }
   if (src < 0 || src >= m.n_total)
     kind = -1;

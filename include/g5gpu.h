@@ -100,9 +100,10 @@ typedef struct G5Params
  * (scheme/ConvertToPrimitivesVariablesFunctor.cpp:893-917).  SIMPLE_COPY
  * copies the coarse cell; the others are computed by a pass before each step
  * kernel launch (g5_step, g5_step_batched, g5_step_host, g5_advance, g5_run)
- * from the coarse cells around the block.  CONSERVATIVE_O4 needs bsize 16
- * (g5_create returns G5_ERR_UNSUPPORTED otherwise); g5_step_static supports
- * SIMPLE_COPY only. */
+ * from the coarse cells around the block.  CONSERVATIVE_O4 on 8-cell blocks
+ * also reads children of a finer neighbour that do not touch the block; where
+ * such a child is refined further or lies beyond a domain face the device
+ * raises G5_ERR_MESH (g5_status).  g5_step_static supports SIMPLE_COPY only. */
 #define G5_PROLONG_SIMPLE_COPY 0
 #define G5_PROLONG_EXTRAPOLATE_LINEAR_MINMOD 1
 #define G5_PROLONG_CONSERVATIVE_O2 2

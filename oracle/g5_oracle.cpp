@@ -697,8 +697,25 @@ coarse_cell_value(const Ctx & x, const double * U, int n, const int * q, int var
     ch[e] = f[e] >= h ? 1 : 0;
     l[e] = 2 * (f[e] - ch[e] * h);
   }
-  const int F = nb[DIM == 2 ? ch[0] + 2 * ch[1] : ch[0] + 2 * ch[1] + 4 * ch[2]];
-  double    sum = 0.0;
+  int F = nb[DIM == 2 ? ch[0] + 2 * ch[1] : ch[0] + 2 * ch[1] + 4 * ch[2]];
+  if (F < 0)
+  {
+    // a child of the finer neighbour that does not touch the block (order-4
+    // stencils of 8-cell blocks reach it): the same-level neighbour of the
+    // touching sibling, when that sibling is owned and the child is a leaf
+    int ct[3] = { 0, 0, 0 }, dl[3] = { 0, 0, 0 };
+    for (int e = 0; e < DIM; ++e)
+    {
+      ct[e] = s[e] == 0 ? ch[e] : (s[e] < 0 ? 1 : 0);
+      dl[e] = ch[e] - ct[e];
+    }
+    const int T = nb[DIM == 2 ? ct[0] + 2 * ct[1] : ct[0] + 2 * ct[1] + 4 * ct[2]];
+    const int st = slot_index(DIM, dl);
+    if (T < 0 || T >= x.n_owned || x.nbr_rel[(size_t)T * x.ns + st] != 0)
+      return NAN; // unresolvable here: the GPU raises its mesh status
+    F = x.nbr[((size_t)T * x.ns + st) * x.nc];
+  }
+  double sum = 0.0;
   for (int oz = 0; oz < (DIM == 3 ? 2 : 1); ++oz)
     for (int oy = 0; oy < 2; ++oy)
       for (int ox = 0; ox < 2; ++ox)
