@@ -155,6 +155,92 @@ uniform_block_table_2d(int nx, int ny, bool periodic_x, bool periodic_y, int lev
   return t;
 }
 
+// The host block forest of the dynamic AMR cycle (g5_forest_*): the
+// adaptation that p4est performs in the reference, the old -> new block map
+// for remap_block_data and the block table for resize_auxiliary_data.
+class Forest
+{
+public:
+  //! uniform at spec.level_min when `leaves` is empty, else those leaves ((level, x, y, z) rows)
+  explicit Forest(const G5ForestSpec & spec, const std::vector<int32_t> & leaves = {})
+    : m_dim(spec.dim)
+  {
+    check(g5_forest_create(&spec, leaves.empty() ? nullptr : leaves.data(), (int64_t)(leaves.size() / 4), &m_f), "g5_forest_create");
+  }
+  ~Forest()
+  {
+    if (m_f)
+      g5_forest_destroy(m_f);
+  }
+  Forest(const Forest &) = delete;
+  Forest & operator=(const Forest &) = delete;
+
+  int64_t num_leaves() const { return g5_forest_num_leaves(m_f); }
+
+  //! the leaves in table order, 4 int32 each
+  std::vector<int32_t> leaves() const
+  {
+    std::vector<int32_t> out((size_t)num_leaves() * 4);
+    check(g5_forest_leaves(m_f, out.data()), "g5_forest_leaves");
+    return out;
+  }
+
+  int refine(const std::vector<int32_t> & keys) { return check(g5_forest_refine(m_f, keys.data(), (int64_t)(keys.size() / 4)), "g5_forest_refine"); }
+  int balance() { return check(g5_forest_balance(m_f), "g5_forest_balance"); }
+
+  //! one adaptation from ComputeRefineFlags codes (one per leaf, table order);
+  //! fills kind / src (G5Remap's arrays) and returns the map
+  G5Remap adapt(const std::vector<int8_t> & flags, std::vector<int8_t> & kind, std::vector<int32_t> & src)
+  {
+    const int64_t nc = (int64_t)1 << m_dim, cap = (int64_t)flags.size() * nc;
+    kind.assign((size_t)cap, 0);
+    src.assign((size_t)(cap * nc), -1);
+    const int64_t n_new = g5_forest_adapt(m_f, flags.data(), (int64_t)flags.size(), kind.data(), src.data(), cap);
+    if (n_new < 0)
+      throw Error((int)n_new, "g5_forest_adapt");
+    kind.resize((size_t)n_new);
+    src.resize((size_t)(n_new * nc));
+    G5Remap r{};
+    r.n_old = (int32_t)flags.size();
+    r.n_new = (int32_t)n_new;
+    r.kind = kind.data();
+    r.src = src.data();
+    return r;
+  }
+
+  //! the block table of the current leaves
+  BlockTable table()
+  {
+    int32_t no = 0, nt = 0;
+    check(g5_forest_table_sizes(m_f, &no, &nt), "g5_forest_table_sizes");
+    const int  ns = m_dim == 2 ? 9 : 27, nc = 1 << m_dim;
+    BlockTable t;
+    t.n_owned = no;
+    t.n_outside = nt;
+    t.level.resize((size_t)(no + nt));
+    t.coord.resize((size_t)(no + nt) * 3);
+    t.nbr.resize((size_t)no * ns * nc);
+    t.nbr_rel.resize((size_t)no * ns);
+    t.out_src.resize((size_t)nt);
+    t.out_normal.resize((size_t)nt * 3);
+    t.out_border.resize((size_t)nt * 6);
+    check(g5_forest_table(m_f, t.level.data(), t.coord.data(), t.nbr.data(), t.nbr_rel.data(), t.out_src.data(), t.out_normal.data(),
+                          t.out_border.data()),
+          "g5_forest_table");
+    return t;
+  }
+
+private:
+  static int check(int rc, const char * what)
+  {
+    if (rc < 0)
+      throw Error(rc, what);
+    return rc;
+  }
+  int        m_dim;
+  G5Forest * m_f = nullptr;
+};
+
 } // namespace g5
 
 namespace godunov_five_eq
