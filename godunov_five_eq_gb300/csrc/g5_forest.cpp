@@ -359,6 +359,31 @@ g5_forest_create(const G5ForestSpec * spec, const int32_t * leaves, int64_t n_le
       }
       f->add(k);
     }
+    // the leaves must tile the brick: no duplicate, no leaf inside another,
+    // and the covered volume (in cells of the finest level present) that of
+    // the brick
+    int Lm = 0;
+    for (const Key & k : f->leaves)
+      Lm = k.L > Lm ? k.L : Lm;
+    bool               ok = (int64_t)f->leaves.size() == n_leaves;
+    unsigned __int128  vol = 0, full = 1;
+    for (int e = 0; e < f->dim; ++e)
+      full *= (unsigned __int128)f->extent(Lm, e);
+    for (const Key & k : f->leaves)
+    {
+      vol += (unsigned __int128)1 << (f->dim * (Lm - k.L));
+      Key a = k;
+      while (ok && a.L > f->lmin)
+      {
+        a = f->parent(a);
+        ok = !f->has(a);
+      }
+    }
+    if (!ok || vol != full)
+    {
+      delete f;
+      return G5_ERR_MESH;
+    }
   }
   *out = f;
   return G5_OK;

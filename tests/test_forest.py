@@ -75,3 +75,13 @@ def test_native_forest_rejects_bad_input():
     nat.leaves.add((1, 99, 0, 0))  # outside the brick
     with pytest.raises(RuntimeError):
         nat.build()
+    # leaves that do not tile the brick: a parent beside its child, a hole
+    nat = BlockMesh(2, 8, (2, 2), (True, True), 1, 3)
+    nat.refine([(1, 0, 0, 0)])
+    nat.leaves.add((1, 0, 0, 0))
+    with pytest.raises(RuntimeError):
+        nat.build()
+    nat = BlockMesh(2, 8, (2, 2), (True, True), 1, 3)
+    nat.leaves.discard((1, 3, 3, 0))
+    with pytest.raises(RuntimeError):
+        nat.build()
