@@ -76,8 +76,8 @@ def parse():
     return ap.parse_args()
 
 
-def build_workload(name, flag_fn, prolongation=0, with_mesh=False):
-    desc, t, p, U, mesh = _workload(name, flag_fn)
+def build_workload(name, flag_fn, prolongation=0, with_mesh=False, mesh_cls=None):
+    desc, t, p, U, mesh = _workload(name, flag_fn, mesh_cls)
     if prolongation:
         import dataclasses
 
@@ -86,31 +86,34 @@ def build_workload(name, flag_fn, prolongation=0, with_mesh=False):
     return (desc, t, p, U, mesh) if with_mesh else (desc, t, p, U)
 
 
-def _workload(name, flag_fn):
+def _workload(name, flag_fn, mesh_cls=None):
     from godunov_five_eq_gb300 import configs
+    from godunov_five_eq_gb300.mesh import BlockMesh
+
+    kw = {"mesh_cls": mesh_cls or BlockMesh}
 
     if name == "shock_bubble":
-        mesh, t, p, U = configs.shock_bubble("helium", thinc=False, flag_fn=flag_fn)
+        mesh, t, p, U = configs.shock_bubble("helium", thinc=False, flag_fn=flag_fn, **kw)
         desc = "shock_bubble_air_helium_2d_amr_levels4-6_16x16"
     elif name == "shock_bubble_r22_thinc":
-        mesh, t, p, U = configs.shock_bubble("r22", thinc=True, flag_fn=flag_fn)
+        mesh, t, p, U = configs.shock_bubble("r22", thinc=True, flag_fn=flag_fn, **kw)
         desc = "shock_bubble_air_r22_thinc_2d_amr_levels4-6_16x16"
     elif name == "triple_point_3d":
-        mesh, t, p, U = configs.triple_point_3d(flag_fn=flag_fn)
+        mesh, t, p, U = configs.triple_point_3d(flag_fn=flag_fn, **kw)
         desc = "triple_point_3d_thinc_amr_levels0-3_8x8x8"
     elif name == "triple_point_3d_small":
-        mesh, t, p, U = configs.triple_point_3d(level_min=0, level_max=2, flag_fn=flag_fn)
+        mesh, t, p, U = configs.triple_point_3d(level_min=0, level_max=2, flag_fn=flag_fn, **kw)
         desc = "triple_point_3d_thinc_amr_levels0-2_8x8x8"
     elif name == "gas_water":
-        mesh, t, p, U = configs.gas_water_shock_tube()
+        mesh, t, p, U = configs.gas_water_shock_tube(**kw)
         desc = "gas_water_shock_tube_2d_512x32_16x16"
     elif name == "droplets32":
-        _, t, p, U, _ = configs.droplet_instances(n_inst=32)
+        _, t, p, U, _ = configs.droplet_instances(n_inst=32, **kw)
         U = np.ascontiguousarray(U)
         mesh = None
         desc = "droplet_advection_2d_32_instances_16x16"
     else:
-        _, t, p, U, _ = configs.droplet_instances()
+        _, t, p, U, _ = configs.droplet_instances(**kw)
         U = np.ascontiguousarray(U)
         mesh = None
         desc = "droplet_advection_2d_256_instances_16x16"
@@ -236,9 +239,12 @@ def run_reference(args):
 
     if rank_env()[1] != 0:
         return 0
+    from oracle.forest_py import PyBlockMesh
     from oracle.oracle import Oracle, oracle_flag_fn
 
-    desc, t, p, U = build_workload(args.workload, oracle_flag_fn(), args.prolongation)
+    # the mesh comes from the Python forest restatement and the refine flags
+    # from the oracle: this arm loads no library of the GPU product
+    desc, t, p, U = build_workload(args.workload, oracle_flag_fn(), args.prolongation, mesh_cls=PyBlockMesh)
     cores = os.cpu_count() or 1
     o = Oracle(t, p, nthreads=cores)
     A = U.copy()

@@ -155,12 +155,15 @@ def rankine_hugoniot(gamma, rho1, p1, mach):
 # ----------------------------------------------------------------------------
 # config 1: 2D gas-water two-fluid shock tube, 512x32 cells, 32x2 blocks of 16^2
 # ----------------------------------------------------------------------------
-def gas_water_shock_tube(bsize=16, nx_blocks=32, ny_blocks=2):
-    """Water (stiffened gas 4.4 / 6e8) at x<0.5 against air (ideal 1.4) at x>0.5."""
+def gas_water_shock_tube(bsize=16, nx_blocks=32, ny_blocks=2, mesh_cls=BlockMesh):
+    """Water (stiffened gas 4.4 / 6e8) at x<0.5 against air (ideal 1.4) at x>0.5.
+
+    ``mesh_cls`` (every builder below takes it) is the BlockMesh class that
+    holds the forest: a subclass may replace the native forest operations."""
     level = 1
     trees_x = nx_blocks >> level
     trees_y = max(1, ny_blocks >> level)
-    mesh = BlockMesh(2, bsize, (trees_x, trees_y), (False, True), level, level, scaling=1.0 / trees_x)
+    mesh = mesh_cls(2, bsize, (trees_x, trees_y), (False, True), level, level, scaling=1.0 / trees_x)
     table = mesh.build()
     params = HydroParams(
         dim=2,
@@ -264,7 +267,7 @@ def _shock_bubble_prim(params, xc, dxf, bubble_gamma_rho, mach=1.22):
     return a0, ar0, ar1, p, u
 
 
-def shock_bubble(bubble="helium", thinc=False, level_min=4, level_max=6, bsize=16, flag_fn=None, slope_type=1.0, initial_level=None):
+def shock_bubble(bubble="helium", thinc=False, level_min=4, level_max=6, bsize=16, flag_fn=None, slope_type=1.0, initial_level=None, mesh_cls=BlockMesh):
     """Mach 1.22 shock in air hitting a helium (or R22) bubble; domain [0,4]x[0,1].
 
     The mesh is refined from ``level_min`` by the refine flags evaluated on the
@@ -275,7 +278,7 @@ def shock_bubble(bubble="helium", thinc=False, level_min=4, level_max=6, bsize=1
     that level (a mesh that a dynamic AMR cycle then coarsens and refines).
     """
     gb = {"helium": (1.648, 0.138), "r22": (1.249, 3.1538)}[bubble]
-    mesh = BlockMesh(2, bsize, (4, 1), (False, False), level_min, level_max, scaling=1.0)
+    mesh = mesh_cls(2, bsize, (4, 1), (False, False), level_min, level_max, scaling=1.0)
     for _ in range(level_min, initial_level if initial_level is not None else level_min):
         mesh.refine(list(mesh.leaves))
     params = HydroParams(
@@ -350,7 +353,7 @@ class SplitMix64:
         return lo + (hi - lo) * ((self.next_u64() >> 11) * (1.0 / (1 << 53)))
 
 
-def droplet_instances(n_inst=256, sides=(64, 128, 256, 512), bsize=16, seed=0x5EED2026):
+def droplet_instances(n_inst=256, sides=(64, 128, 256, 512), bsize=16, seed=0x5EED2026, mesh_cls=BlockMesh):
     """Independent periodic droplet-advection runs of uneven sizes in one table."""
     rng = SplitMix64(seed)
     tables, meshes, Us = [], [], []
@@ -374,7 +377,7 @@ def droplet_instances(n_inst=256, sides=(64, 128, 256, 512), bsize=16, seed=0x5E
     for side, radius, u, v in specs:
         # one tree of unit length at level log2(side / bsize)
         level = int(round(math.log2(side // bsize)))
-        mesh = BlockMesh(2, bsize, (1, 1), (True, True), level, level, scaling=1.0)
+        mesh = mesh_cls(2, bsize, (1, 1), (True, True), level, level, scaling=1.0)
         t = mesh.build()
         # all instances share the level -> dx table of a unit tree
         xc = cell_centers(mesh, t)
@@ -400,9 +403,9 @@ def droplet_instances(n_inst=256, sides=(64, 128, 256, 512), bsize=16, seed=0x5E
 # ----------------------------------------------------------------------------
 # config 5: 3D triple point
 # ----------------------------------------------------------------------------
-def triple_point_3d(level_min=0, level_max=3, bsize=8, nbrick=(14, 6, 3), scaling=0.5, thinc=True, flag_fn=None):
+def triple_point_3d(level_min=0, level_max=3, bsize=8, nbrick=(14, 6, 3), scaling=0.5, thinc=True, flag_fn=None, mesh_cls=BlockMesh):
     """Three-region triple-point problem on [0,7]x[0,3]x[0,1.5]."""
-    mesh = BlockMesh(3, bsize, nbrick, (False, False, False), level_min, level_max, scaling=scaling)
+    mesh = mesh_cls(3, bsize, nbrick, (False, False, False), level_min, level_max, scaling=scaling)
     params = HydroParams(
         dim=3,
         bsize=bsize,

@@ -466,50 +466,8 @@ g5_set_mesh(G5Context * c, const G5Mesh * m)
   const int n_inst = m->n_inst > 0 ? m->n_inst : 1;
   const int ns = c->ns, nch = c->nch, dim = c->dim;
   // ---- validate the table (the reference asserts these in StencilHelper / hashmap lookups)
-  for (int n = 0; n < n_total; ++n)
-    if (m->level[n] < 0 || m->level[n] > 31)
-      return G5_ERR_MESH;
-  if (m->inst)
-    for (int n = 0; n < n_total; ++n)
-      if (m->inst[n] < 0 || m->inst[n] >= n_inst)
-        return G5_ERR_MESH;
-  for (int n = 0; n < n_owned; ++n)
-    for (int s = 0; s < ns; ++s)
-    {
-      const int center = dim == 2 ? 4 : 13;
-      if (s == center)
-        continue;
-      const int   rel = m->nbr_rel[(size_t)n * ns + s];
-      const int * nb = m->nbr + ((size_t)n * ns + s) * nch;
-      if (rel < -1 || rel > 1)
-        return G5_ERR_MESH;
-      if (rel <= 0)
-      {
-        if (nb[0] < 0 || nb[0] >= n_total)
-          return G5_ERR_MESH;
-      }
-      else
-      {
-        const int d[3] = { s % 3 - 1, (s / 3) % 3 - 1, s / 9 - 1 };
-        for (int ch = 0; ch < nch; ++ch)
-        {
-          bool needed = true;
-          for (int e = 0; e < dim; ++e)
-          {
-            const int ce = (ch >> e) & 1;
-            if ((d[e] == -1 && ce != 1) || (d[e] == 1 && ce != 0))
-              needed = false;
-          }
-          if (needed && (nb[ch] < 0 || nb[ch] >= n_total))
-            return G5_ERR_MESH;
-          if (!needed && nb[ch] >= n_total)
-            return G5_ERR_MESH;
-        }
-      }
-    }
-  for (int o = 0; o < m->n_outside; ++o)
-    if (m->out_src[o] < 0 || m->out_src[o] >= n_owned)
-      return G5_ERR_MESH;
+  if (g5::validate_table(dim, m) != G5_OK)
+    return G5_ERR_MESH;
 
   // ---- coarse/fine face records
   const int            nfaces = 2 * dim;

@@ -26,6 +26,61 @@ eos_params_valid(const G5Params * prm)
   return true;
 }
 
+// Block-table check shared by g5_set_mesh and g5_step_static (the reference
+// asserts the same facts in StencilHelper and its hashmap lookups): levels in
+// range, instance ids below n_inst, relation codes in {-1, 0, 1}, a valid
+// block for every coarser or same-level slot and for every child of a finer
+// slot that touches the block (the other children may be -1), outside blocks
+// mirroring owned ones.  Array presence is the caller's check.  Returns G5_OK
+// or G5_ERR_MESH.
+inline int
+validate_table(int dim, const G5Mesh * m)
+{
+  const int n_owned = m->n_owned, n_total = m->n_owned + m->n_outside;
+  const int n_inst = m->n_inst > 0 ? m->n_inst : 1;
+  const int ns = dim == 2 ? 9 : 27, nch = dim == 2 ? 4 : 8, center = dim == 2 ? 4 : 13;
+  for (int n = 0; n < n_total; ++n)
+    if (m->level[n] < 0 || m->level[n] > 31)
+      return G5_ERR_MESH;
+  if (m->inst)
+    for (int n = 0; n < n_total; ++n)
+      if (m->inst[n] < 0 || m->inst[n] >= n_inst)
+        return G5_ERR_MESH;
+  for (int n = 0; n < n_owned; ++n)
+    for (int s = 0; s < ns; ++s)
+    {
+      if (s == center)
+        continue;
+      const int       rel = m->nbr_rel[(size_t)n * ns + s];
+      const int32_t * nb = m->nbr + ((size_t)n * ns + s) * nch;
+      if (rel < -1 || rel > 1)
+        return G5_ERR_MESH;
+      if (rel <= 0)
+      {
+        if (nb[0] < 0 || nb[0] >= n_total)
+          return G5_ERR_MESH;
+        continue;
+      }
+      const int d[3] = { s % 3 - 1, (s / 3) % 3 - 1, s / 9 - 1 };
+      for (int ch = 0; ch < nch; ++ch)
+      {
+        bool needed = true;
+        for (int e = 0; e < dim; ++e)
+        {
+          const int ce = (ch >> e) & 1;
+          if ((d[e] == -1 && ce != 1) || (d[e] == 1 && ce != 0))
+            needed = false;
+        }
+        if (nb[ch] >= n_total || (needed && nb[ch] < 0))
+          return G5_ERR_MESH;
+      }
+    }
+  for (int o = 0; o < m->n_outside; ++o)
+    if (m->out_src[o] < 0 || m->out_src[o] >= n_owned)
+      return G5_ERR_MESH;
+  return G5_OK;
+}
+
 inline PhysParams
 make_phys(const G5Params * params)
 {

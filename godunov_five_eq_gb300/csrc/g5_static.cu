@@ -60,8 +60,11 @@ align256(size_t x)
   return (x + 255) & ~(size_t)255;
 }
 
-// host -> scratch copy of a caller array (pageable memory: the call returns
-// once the bytes are staged, so the source may be reused immediately)
+// host -> scratch copy of a caller array.  From pageable memory (the stack
+// buffers of the face records, and most callers' tables) cudaMemcpyAsync
+// returns once the bytes are staged, so the source may be reused at once; a
+// page-locked source is read later, when the stream reaches the copy, so the
+// caller must leave it unchanged until then.
 int
 put(unsigned char * base, size_t off, const void * src, size_t bytes, cudaStream_t s)
 {
@@ -102,30 +105,29 @@ g5_step_static(const G5Params * params,
   const int n_total = n_owned + n_outside, n_inst = mesh->n_inst > 0 ? mesh->n_inst : 1;
   if (n_owned <= 0 || n_outside < 0 || !mesh->level || !mesh->coord || !mesh->nbr || !mesh->nbr_rel)
     return G5_ERR_ARG;
-  const int ns = dim == 2 ? 9 : 27, nch = dim == 2 ? 4 : 8, nfaces = 2 * dim, center = dim == 2 ? 4 : 13;
+  const int ns = dim == 2 ? 9 : 27, nch = dim == 2 ? 4 : 8, nfaces = 2 * dim;
   for (int i = 0; i < n_inst; ++i)
     if (!(dt_host[i] > 0.0))
       return G5_ERR_ARG;
-
-  // ---- validate the table and count the coarse/fine face records
-  int n_reflux = 0, n_defer = 0;
-  for (int n = 0; n < n_total; ++n)
-    if (mesh->level[n] < 0 || mesh->level[n] > 31 || (mesh->inst && (mesh->inst[n] < 0 || mesh->inst[n] >= n_inst)))
-      return G5_ERR_MESH;
-  for (int n = 0; n < n_owned; ++n)
+  // the host arrays are staged at call time (copies from host memory, some
+  // from this function's stack): refuse a stream in capture mode rather than
+  // record copies whose sources are gone when the graph runs
   {
-    for (int s = 0; s < ns; ++s)
-    {
-      if (s == center)
-        continue;
-      const int   rel = mesh->nbr_rel[(size_t)n * ns + s];
-      const int * nb = mesh->nbr + ((size_t)n * ns + s) * nch;
-      if (rel < -1 || rel > 1)
-        return G5_ERR_MESH;
-      for (int ch = 0; ch < (rel > 0 ? nch : 1); ++ch)
-        if (nb[ch] >= n_total || (rel <= 0 && nb[ch] < 0))
-          return G5_ERR_MESH;
-    }
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing((cudaStream_t)stream, &cs) != cudaSuccess)
+      return G5_ERR_CUDA;
+    if (cs != cudaStreamCaptureStatusNone)
+      return G5_ERR_UNSUPPORTED;
+  }
+
+  // ---- validate the table (the same check as g5_set_mesh) and count the
+  // coarse/fine face records
+  if (n_outside > 0 && !mesh->out_src)
+    return G5_ERR_ARG;
+  if (g5::validate_table(dim, mesh) != G5_OK)
+    return G5_ERR_MESH;
+  int n_reflux = 0, n_defer = 0;
+  for (int n = 0; n < n_owned; ++n)
     for (int f = 0; f < nfaces; ++f)
     {
       int d[3] = { 0, 0, 0 };
@@ -144,12 +146,6 @@ g5_step_static(const G5Params * params,
         n_defer += owned ? 1 : 0;
       }
     }
-  }
-  if (n_outside > 0 && !mesh->out_src)
-    return G5_ERR_ARG;
-  for (int o = 0; o < n_outside; ++o)
-    if (mesh->out_src[o] < 0 || mesh->out_src[o] >= n_owned)
-      return G5_ERR_MESH;
 
   // ---- scratch layout; refuse meshes that do not fit
   const size_t face_cells = dim == 2 ? (size_t)b : (size_t)b * b;

@@ -316,10 +316,21 @@ int g5_last_launch_count(const G5Context * ctx);
  * loading the library keeps until the process exits.  No cudaMalloc, cudaFree
  * or other allocating routine is called.
  *
- * Same step and arguments meaning as g5_step; d_status_out (device, may be
- * NULL) receives the G5_STATUS_* bits raised by the kernels (the caller zeroes
- * it).  Returns G5_ERR_ARG when the mesh needs more than
- * G5_STATIC_SCRATCH_BYTES of scratch.
+ * Same step and arguments meaning as g5_step; the block table is checked as
+ * g5_set_mesh checks it (G5_ERR_MESH).  d_status_out (device, may be NULL)
+ * receives the G5_STATUS_* bits raised by the kernels (the caller zeroes it);
+ * with NULL the bits go to a word inside the scratch array that no call
+ * reads, so non-physical states are not reported.  Returns G5_ERR_ARG when
+ * the mesh needs more than G5_STATIC_SCRATCH_BYTES of scratch, and
+ * G5_ERR_UNSUPPORTED when `stream` is in capture mode (the host arrays are
+ * staged at call time).
+ *
+ * dt_host and the G5Mesh arrays are copied to the scratch array with
+ * cudaMemcpyAsync on `stream`.  From pageable memory the copy is staged
+ * before the call returns, so the arrays may be reused at once; from
+ * page-locked memory (cudaHostAlloc, registered or pinned buffers) it runs
+ * when the stream reaches it, so the caller must leave those arrays unchanged
+ * until the stream has passed this call.
  *
  * The first call on a device looks up the array's device address with that
  * device current (cudaGetSymbolAddress); make that first call before any

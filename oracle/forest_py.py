@@ -1,7 +1,12 @@
 """Python restatement of the block-forest algorithms (balance, adaptation
-with the old -> new block map, leaf order, block table), kept to check the
-native forest of libg5gpu.so (csrc/g5_forest.cpp) on random meshes: both
-must give the same leaves, remap tables and block tables."""
+with the old -> new block map, leaf order, block table).
+
+Test infrastructure, like the rest of oracle/: it checks the native forest of
+libg5gpu.so (godunov_five_eq_gb300/csrc/g5_forest.cpp) on random meshes (both
+must give the same leaves, remap tables and block tables), and it builds the
+meshes of bench.py's CPU reference arm, which then loads no library of the
+product.  PyBlockMesh never touches the native forest: every BlockMesh
+operation that would call it is overridden here."""
 import itertools
 
 import numpy as np

@@ -1,5 +1,5 @@
 """The native block forest (libg5gpu.so, g5_forest_*) against the Python
-restatement of the same algorithms (tests/forest_py.py): identical leaves,
+restatement of the same algorithms (oracle/forest_py.py): identical leaves,
 leaf order, old -> new block maps and block tables over random refinement,
 balance and adaptation cycles, in 2D and 3D, periodic and bounded.  Host
 code only (no GPU)."""
@@ -7,7 +7,7 @@ import numpy as np
 import pytest
 
 from godunov_five_eq_gb300.mesh import BlockMesh
-from tests.forest_py import PyBlockMesh
+from oracle.forest_py import PyBlockMesh
 
 TABLE_FIELDS = ("level", "coord", "nbr", "nbr_rel", "out_src", "out_normal", "out_border")
 

@@ -150,17 +150,34 @@ def test_refine_flags_exact():
         assert np.array_equal(got, ref), ind
 
 
-def test_nonphysical_input_raises_status_not_fault():
+@pytest.mark.parametrize("mode", ["fp64", "mixed"])
+@pytest.mark.parametrize("var", [1, 2, 7])
+def test_nonphysical_input_raises_status_not_fault(mode, var):
+    """A NaN planted on the host in one cell (energy, momentum or a partial
+    density) raises the status word in both precision forms, and every value
+    the FP64 oracle turns non-finite is non-finite on the GPU too: the mixed
+    path's double -> float conversion must carry the NaN into the neighbours'
+    fluxes, not a finite stand-in."""
     mesh, t = amr_mesh(dim=2, b=8, nref=2)
     p = water_air_params(t)
     U = smooth_state(mesh, t, p)
-    U[0, 1, 5] = np.nan  # a NaN planted in the input on the host
+    U[0, var, 5 * 8 + 5] = np.nan
+    o = Oracle(t, p)
+    o.fill_outside(U)
+    ref = o.step(U, 1e-7)
     impl = GodunovImplemGB300(p, t)
     d_U = torch.from_numpy(U).cuda()
     d_U2 = torch.zeros_like(d_U)
-    impl.do_time_step(d_U, d_U2, 1e-7)
+    impl.do_time_step(d_U, d_U2, 1e-7, mode=mode)
     assert impl.status() & 1
     assert impl.status() == 0  # cleared by the read
+    n = t.n_owned
+    got = d_U2.cpu().numpy()[:n]
+    bad_ref = ~np.isfinite(ref[:n])
+    assert bad_ref.any()
+    assert np.all(~np.isfinite(got[bad_ref]))
+    if mode == "fp64":
+        assert np.array_equal(~np.isfinite(got), bad_ref)
 
 
 def test_bad_mesh_rejected():
