@@ -401,7 +401,11 @@ class GodunovImplemGB300:
         return out
 
     def compute_dt_local(self, U, stream=None):
-        return self.params.cfl / self.compute_inv_dt(U, stream=stream)
+        """dt = cfl / invDt per instance (SolverGodunovFiveEq.cpp:386), as one
+        correctly rounded FP64 division (a scalar divided by a tensor would be
+        evaluated as scalar x reciprocal, one rounding more)."""
+        inv = self.compute_inv_dt(U, stream=stream)
+        return inv.new_full(inv.shape, float(self.params.cfl)) / inv
 
     def fill_outside_quadrants(self, U, stream=None):
         rc = self.lib.g5_fill_outside(self.ctx, ctypes.c_void_p(_dptr(U)), _stream(stream))

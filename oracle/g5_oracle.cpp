@@ -12,6 +12,14 @@
  * reference's operation order; build with -ffp-contract=off so that no
  * multiply-add is fused (results are then identical on x86-64 and aarch64).
  *
+ * Pinned to the reference's own code compiled from its tree (oracle/refpin,
+ * golden vectors in tests/golden/, tests/test_golden.py): riemann_hllc and
+ * computePrimitives per state, and one whole do_time_step of periodic tiles
+ * of same-level blocks through the reference's scheme functors (limited
+ * slopes, MUSCL-Hancock and THINC reconstruction, flux store, read-back
+ * update with both volume-fraction source terms, renormalisation, CFL
+ * reduction), 2D and 3D, bit for bit.
+ *
  * Unpinned restatements (external kalypsso core, absent):
  *   - stiffened-gas mixture EOS (Allaire, Clerc & Kokh 2002);
  *   - Youngs normal (3x3(x3) weighted central differences, unit cell);

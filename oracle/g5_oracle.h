@@ -5,15 +5,20 @@
  * path: only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg
  * may load it.  The product (godunov_five_eq_gb300) never links or calls it.
  *
- * Parity status: partially pinned.  The HLLC solver and the
- * conservative->primitive conversion are pinned against the reference's own
- * header code (models/RiemannSolvers.h, models/utils.h) compiled from the
- * reference tree with shim headers (oracle/refpin/), through golden vectors
- * committed under tests/golden/.  The mixture EOS, the Youngs normal, the
- * AMR stencil semantics (restriction / prolongation / face sibling sums),
- * the cell length and tree ordering live in the external kalypsso core,
- * which is not available; they are restated from published mathematics and
- * are "parity unpinned".
+ * Parity status: the scheme is pinned to the reference's own code, compiled
+ * from the reference tree with shim headers (oracle/refpin/), through golden
+ * vectors committed under tests/golden/: the HLLC solver and the
+ * conservative->primitive conversion per state (models/RiemannSolvers.h,
+ * models/utils.h), and one whole do_time_step of periodic tiles of
+ * same-level blocks through the reference's scheme functors (limited slopes,
+ * MUSCL-Hancock and THINC reconstruction, flux store, read-back update with
+ * the ALLAIRE_KOKH and MILLER_PUCKETT source terms, volume-fraction
+ * renormalisation, CFL reduction), 2D and 3D, bit for bit.  The mixture EOS,
+ * the Youngs normal, the AMR stencil semantics (restriction / prolongation /
+ * face sibling sums), the cell length and tree ordering live in the external
+ * kalypsso core, which is not available; they are restated from published
+ * mathematics and are "parity unpinned" (the pin uses the same restatements
+ * for them).
  *
  * Layout of every conservative array U: [n_blocks][nv][b^dim] (cells x
  * fastest), owned blocks first, then "outside" blocks (the reference's

@@ -2,7 +2,12 @@
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import
 this module; it is the checker, never the measured or shipped path.
-Parity status: partially pinned (see g5_oracle.h).
+Parity status: the scheme arithmetic is pinned to the reference's own code
+(HLLC and primitive conversion per state, and whole block steps of
+same-level tiles through the reference's scheme functors: tests/test_golden.py);
+the AMR stencils (restriction, prolongation, coarse/fine face sums), the
+mixture EOS and the Youngs normal are restatements of the external core
+(see g5_oracle.cpp).
 """
 from __future__ import annotations
 

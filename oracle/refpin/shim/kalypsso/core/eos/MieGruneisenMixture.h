@@ -37,5 +37,12 @@ public:
     const double c2 = (p * (s + 1.0) + PI(a0, a1)) / (rho * s);
     return std::sqrt(std::fmax(c2, 0.0));
   }
+  // bulk moduli of the Miller-Puckett source term: K_k = gamma_k (p + pinf_k),
+  // 1 / Kbar = a0 / K0 + a1 / K1
+  double material_bulk_modulus(int k, double p, double, double) const { return gamma[k] * (p + pinf[k]); }
+  double mixture_bulk_modulus(double, double p, double a0, double a1, double ar0, double ar1) const
+  {
+    return 1.0 / (a0 / material_bulk_modulus(0, p, a0, ar0) + a1 / material_bulk_modulus(1, p, a1, ar1));
+  }
 };
 } } }

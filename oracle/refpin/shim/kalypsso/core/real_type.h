@@ -8,3 +8,4 @@ using kalypsso::real_t;
 #define ZERO_F (0.0)
 #define ONE_F (1.0)
 #define HALF_F (0.5)
+#define TWO_F (2.0)

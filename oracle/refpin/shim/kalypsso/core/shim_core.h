@@ -1,0 +1,428 @@
+// Stand-ins for the parts of the external kalypsso core that the reference's
+// scheme functors name (kalypsso_data_container.h, utils_block.h,
+// orchard keys, AMRMeshInfo, conformal face status, StencilHelper, the time
+// integrator and THINC settings, gravity, the Youngs normal, cell lengths).
+// Test infrastructure: it lets the reference's own scheme code compile and run
+// serially on one block of same-level neighbours, so that its results pin the
+// CPU oracle.  Every arithmetic definition here is a restatement (the core is
+// absent) and is the same as the oracle's:
+//   * compute_cell_length(level, bx) = 1 / (bx 2^level) (scaling applied by
+//     the caller, as in the reference);
+//   * Youngs normal: (1,2,1)-weighted central differences of the volume
+//     fraction, n = -grad / |grad|;
+//   * tanh: the oracle's own g5o_tanh (libm's tanh differs between hosts),
+//     substituted through kalypsso::tanh, which the reference's unqualified
+//     tanh calls find first.
+// What a same-level block never reaches (finer-neighbour face sums through
+// StencilHelper) aborts if called.
+#pragma once
+#include <algorithm>
+#include <array>
+#include <cstdint>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include <../better-enums/enum.h>
+#include <kalypsso/core/kokkos_shared.h>
+#include <kalypsso/core/real_type.h>
+#include <kalypsso/utils/config/ConfigMap.h>
+
+extern "C" double g5o_tanh(double);
+
+// element-wise arithmetic of small state arrays, in namespace Kokkos so that
+// argument-dependent lookup finds it wherever the reference uses it
+namespace Kokkos
+{
+template <typename T, size_t N>
+Kokkos::Array<T, N>
+operator+(Kokkos::Array<T, N> const & a, Kokkos::Array<T, N> const & b)
+{
+  Kokkos::Array<T, N> r;
+  for (size_t i = 0; i < N; ++i)
+    r[i] = a[i] + b[i];
+  return r;
+}
+template <typename T, size_t N>
+Kokkos::Array<T, N>
+operator-(Kokkos::Array<T, N> const & a, Kokkos::Array<T, N> const & b)
+{
+  Kokkos::Array<T, N> r;
+  for (size_t i = 0; i < N; ++i)
+    r[i] = a[i] - b[i];
+  return r;
+}
+template <typename T, size_t N, typename S>
+Kokkos::Array<T, N>
+operator*(Kokkos::Array<T, N> const & a, S s)
+{
+  Kokkos::Array<T, N> r;
+  for (size_t i = 0; i < N; ++i)
+    r[i] = a[i] * s;
+  return r;
+}
+template <typename T, size_t N, typename S>
+Kokkos::Array<T, N>
+operator/(Kokkos::Array<T, N> const & a, S s)
+{
+  Kokkos::Array<T, N> r;
+  for (size_t i = 0; i < N; ++i)
+    r[i] = a[i] / s;
+  return r;
+}
+
+} // namespace Kokkos
+
+namespace kalypsso
+{
+// the oracle's tanh for the reference's unqualified tanh(...) calls
+inline double
+tanh(double x)
+{
+  return g5o_tanh(x);
+}
+
+enum : int
+{
+  IX = 0,
+  IY = 1,
+  IZ = 2
+};
+using iOct_t = int32_t;
+
+template <size_t dim, typename T = int32_t>
+using coord_t = Kokkos::Array<T, dim>;
+template <size_t dim>
+using shift_t = Kokkos::Array<int32_t, dim>;
+template <size_t dim>
+using block_size_t = Kokkos::Array<int32_t, dim>;
+template <size_t dim>
+using brick_size_t = Kokkos::Array<int32_t, dim>;
+
+template <typename T, size_t N>
+constexpr Kokkos::Array<T, N>
+init_kokkos_array(T v)
+{
+  Kokkos::Array<T, N> a{};
+  for (size_t i = 0; i < N; ++i)
+    a[i] = v;
+  return a;
+}
+
+template <typename T>
+KOKKOS_INLINE_FUNCTION void
+my_swap(T & a, T & b)
+{
+  T t = a;
+  a = b;
+  b = t;
+}
+
+#define assertm(exp, msg) ((void)0)
+
+template <size_t dim>
+KOKKOS_INLINE_FUNCTION coord_t<dim>
+cell_index_unravel(int64_t index, block_size_t<dim> const & shape)
+{
+  coord_t<dim> c{};
+  c[IX] = static_cast<int32_t>(index % shape[IX]);
+  c[IY] = static_cast<int32_t>((index / shape[IX]) % shape[IY]);
+  if constexpr (dim == 3)
+    c[IZ] = static_cast<int32_t>(index / (shape[IX] * shape[IY]));
+  return c;
+}
+
+template <size_t dim>
+KOKKOS_INLINE_FUNCTION coord_t<dim>
+cellindex_to_coord(int64_t index, block_size_t<dim> const & ghosted_size, shift_t<dim> const & shift)
+{
+  coord_t<dim> c = cell_index_unravel<dim>(index, ghosted_size);
+  for (size_t e = 0; e < dim; ++e)
+    c[e] -= shift[e];
+  return c;
+}
+
+template <size_t dim>
+KOKKOS_INLINE_FUNCTION coord_t<dim>
+get_unit_vector(int dir)
+{
+  coord_t<dim> u{};
+  for (size_t e = 0; e < dim; ++e)
+    u[e] = (static_cast<int>(e) == dir) ? 1 : 0;
+  return u;
+}
+
+template <size_t dim>
+block_size_t<dim>
+get_flux_block_sizes(block_size_t<dim> bs, int direction)
+{
+  bs[direction] += 1;
+  return bs;
+}
+
+// block array [n_quadrants][n_vars][cells], cell index x fastest
+template <size_t dim, typename T, typename device_t>
+class DataArrayBlock
+{
+public:
+  std::shared_ptr<std::vector<T>> s;
+  block_size_t<dim>               bs{};
+  int32_t                         nvar = 0, nquad = 0;
+  DataArrayBlock() = default;
+  DataArrayBlock(block_size_t<dim> b, int32_t nv, int32_t nq)
+    : s(std::make_shared<std::vector<T>>((size_t)Kokkos::dim_prod(b) * nv * nq))
+    , bs(b)
+    , nvar(nv)
+    , nquad(nq)
+  {}
+  int32_t           num_cells() const { return Kokkos::dim_prod(bs); }
+  int32_t           num_vars() const { return nvar; }
+  int32_t           num_quadrants() const { return nquad; }
+  block_size_t<dim> block_size() const { return bs; }
+  block_size_t<dim> shape() const { return bs; }
+  void              reshape(block_size_t<dim> b) { bs = b; }
+  T *               data() const { return s->data(); }
+  T &               operator()(int64_t cell, int var, int64_t oct) const
+  {
+    return (*s)[((size_t)oct * nvar + var) * num_cells() + cell];
+  }
+  T & operator()(int32_t i, int32_t j, int var, int32_t oct) const { return (*this)(i + (int64_t)bs[IX] * j, var, oct); }
+  T & operator()(int32_t i, int32_t j, int32_t k, int var, int32_t oct) const
+  {
+    return (*this)(i + (int64_t)bs[IX] * (j + (int64_t)bs[IY] * k), var, oct);
+  }
+};
+
+// ghosted block array: cells -g .. b+g-1 along each direction
+template <size_t dim, typename T, typename device_t>
+class DataArrayGhostedBlock
+{
+public:
+  std::shared_ptr<std::vector<T>> s;
+  block_size_t<dim>               bs{}, gbs{};
+  int32_t                         g = 0, nvar = 0, nquad = 0;
+  DataArrayGhostedBlock() = default;
+  DataArrayGhostedBlock(block_size_t<dim> b, int32_t ghost, int32_t nv, int32_t nq)
+    : bs(b)
+    , g(ghost)
+    , nvar(nv)
+    , nquad(nq)
+  {
+    for (size_t e = 0; e < dim; ++e)
+      gbs[e] = b[e] + 2 * ghost;
+    s = std::make_shared<std::vector<T>>((size_t)Kokkos::dim_prod(gbs) * nv * nq);
+  }
+  int32_t           num_cells() const { return Kokkos::dim_prod(gbs); }
+  int32_t           num_vars() const { return nvar; }
+  int32_t           num_quadrants() const { return nquad; }
+  block_size_t<dim> block_size() const { return bs; }
+  block_size_t<dim> ghosted_block_size() const { return gbs; }
+  shift_t<dim>      shift() const { return init_kokkos_array<int32_t, dim>(g); }
+  int32_t           ghost_width() const { return g; }
+  T *               data() const { return s->data(); }
+  T &               operator()(int64_t cell, int var, int64_t oct) const
+  {
+    return (*s)[((size_t)oct * nvar + var) * num_cells() + cell];
+  }
+  T & operator()(int32_t i, int32_t j, int var, int32_t oct) const
+  {
+    return (*this)((i + g) + (int64_t)gbs[IX] * (j + g), var, oct);
+  }
+  T & operator()(int32_t i, int32_t j, int32_t k, int var, int32_t oct) const
+  {
+    return (*this)((i + g) + (int64_t)gbs[IX] * ((j + g) + (int64_t)gbs[IY] * (k + g)), var, oct);
+  }
+};
+
+// orchard keys: the shim's key is the block's AMR level
+template <typename device_t>
+struct orchard_key_base_t
+{
+  using key_t = uint64_t;
+  using view_t = Kokkos::View<uint64_t *, device_t>;
+};
+template <size_t dim>
+struct orchard_key_t
+{
+  static KOKKOS_INLINE_FUNCTION int level(uint64_t key) { return static_cast<int>(key); }
+};
+
+template <typename device_t>
+struct hashmap_base_t
+{
+  struct map_t
+  {};
+};
+
+class AMRMeshInfo
+{
+public:
+  int32_t n_owned = 0, n_ghosts = 0;
+  AMRMeshInfo() = default;
+  AMRMeshInfo(int32_t o, int32_t g)
+    : n_owned(o)
+    , n_ghosts(g)
+  {}
+  int32_t local_num_quadrants() const { return n_owned; }
+  int32_t local_num_ghosts() const { return n_ghosts; }
+};
+
+// conformal face status: 2 bits per face (xmin xmax ymin ymax zmin zmax)
+enum class conformal_neighbor_status : uint8_t
+{
+  NEIGHBOR_IS_SAME_SIZE = 0,
+  NEIGHBOR_IS_LARGER = 1,
+  NEIGHBOR_IS_FINER = 2,
+  NEIGHBOR_IS_OUTSIDE = 3
+};
+template <size_t dim, typename device_t>
+using conformal_status_view_t = Kokkos::View<uint16_t *, device_t>;
+template <size_t dim>
+struct conformal_face_status_t
+{
+  static conformal_neighbor_status face(uint16_t s, int f) { return static_cast<conformal_neighbor_status>((s >> (2 * f)) & 3u); }
+  static conformal_neighbor_status face_xmin(uint16_t s) { return face(s, 0); }
+  static conformal_neighbor_status face_xmax(uint16_t s) { return face(s, 1); }
+  static conformal_neighbor_status face_ymin(uint16_t s) { return face(s, 2); }
+  static conformal_neighbor_status face_ymax(uint16_t s) { return face(s, 3); }
+  static conformal_neighbor_status face_zmin(uint16_t s) { return face(s, 4); }
+  static conformal_neighbor_status face_zmax(uint16_t s) { return face(s, 5); }
+};
+
+template <size_t dim, typename device_t>
+struct AMRContext
+{
+  using amrflags_view_t = Kokkos::View<int8_t *, device_t>;
+};
+
+template <size_t dim>
+struct CellLocation
+{
+  coord_t<dim> coords;
+  uint64_t     key;
+  int32_t      iOct;
+  bool         is_ghost;
+};
+
+// neighbour lookups across levels: not reached by same-level blocks
+template <size_t dim, typename device_t>
+class StencilHelper
+{
+public:
+  StencilHelper() = default;
+  template <typename M, typename K>
+  StencilHelper(M const &, K const &, block_size_t<dim>, brick_size_t<dim>, Kokkos::Array<bool, dim>)
+  {}
+  CellLocation<dim> getNeighLocFinerNearer(CellLocation<dim> const &, shift_t<dim> const &) const
+  {
+    Kokkos::abort("refpin: finer-neighbour lookup is outside the same-level pin");
+    return {};
+  }
+  template <typename A>
+  real_t compute_face_siblings_sum(CellLocation<dim> const &, int, A const &, bool) const
+  {
+    Kokkos::abort("refpin: finer-neighbour face sum is outside the same-level pin");
+    return 0;
+  }
+};
+
+template <size_t dim>
+struct UniformGravityField
+{
+  real_t            g[3] = { 0, 0, 0 };
+  KOKKOS_INLINE_FUNCTION real_t operator[](int e) const { return g[e]; }
+};
+template <size_t dim>
+UniformGravityField<dim>
+get_uniform_gravity_vector(ConfigMap const &)
+{
+  return UniformGravityField<dim>{};
+}
+
+BETTER_ENUM(TimeIntegrator, int, HANCOCK, RK1, RK2_SSP)
+struct TimeIntegratorConfig
+{
+  static TimeIntegrator get_time_integrator(ConfigMap const & c)
+  {
+    const int v = c.getInteger("refpin", "integrator", 0);
+    return v == 1 ? TimeIntegrator(TimeIntegrator::RK1) : (v == 2 ? TimeIntegrator(TimeIntegrator::RK2_SSP) : TimeIntegrator(TimeIntegrator::HANCOCK));
+  }
+};
+
+struct THINCParams
+{
+  bool   enabled = false;
+  real_t beta = 1.6;
+  real_t epsilon = 1e-3;
+  THINCParams() = default;
+  explicit THINCParams(ConfigMap const & c)
+    : enabled(c.getBool("THINC", "enabled", false))
+    , beta(c.getReal("THINC", "beta", 1.6))
+    , epsilon(c.getReal("THINC", "epsilon", 1e-3))
+  {}
+};
+
+inline real_t
+get_scaling_factor(ConfigMap const & c)
+{
+  return c.getReal("refpin", "scaling", 1.0);
+}
+
+template <size_t dim>
+KOKKOS_INLINE_FUNCTION real_t
+compute_cell_length(int level, int32_t bx)
+{
+  return 1.0 / (static_cast<real_t>(bx) * static_cast<real_t>(1LL << level));
+}
+
+namespace core
+{
+BETTER_ENUM(VolFracAdvectionSourceTermType, int, ALLAIRE_KOKH, MILLER_PUCKETT)
+inline VolFracAdvectionSourceTermType
+get_volume_fraction_advection_source_term_type(ConfigMap const & c)
+{
+  return c.getInteger("refpin", "source_term", 0) == 1 ? VolFracAdvectionSourceTermType(VolFracAdvectionSourceTermType::MILLER_PUCKETT)
+                                                       : VolFracAdvectionSourceTermType(VolFracAdvectionSourceTermType::ALLAIRE_KOKH);
+}
+} // namespace core
+
+namespace vof
+{
+// Youngs normal of variable `ivar` at cell ijs of a ghosted block (unit cell
+// size): (1,2,1)-weighted central differences, n = -grad / |grad|
+template <typename A, size_t dim>
+KOKKOS_INLINE_FUNCTION Kokkos::Array<real_t, dim>
+youngs_normal_inplace(A const & q, coord_t<dim> const & c, int ivar, int32_t iOct, Kokkos::Array<real_t, dim> const &)
+{
+  real_t g[3] = { 0, 0, 0 };
+  if constexpr (dim == 2)
+  {
+    auto Q = [&](int a, int b) { return q(c[IX] + a, c[IY] + b, ivar, iOct); };
+    g[0] = (Q(1, -1) + 2.0 * Q(1, 0) + Q(1, 1)) - (Q(-1, -1) + 2.0 * Q(-1, 0) + Q(-1, 1));
+    g[1] = (Q(-1, 1) + 2.0 * Q(0, 1) + Q(1, 1)) - (Q(-1, -1) + 2.0 * Q(0, -1) + Q(1, -1));
+  }
+  else
+  {
+    auto         Q = [&](int a, int b, int cc) { return q(c[IX] + a, c[IY] + b, c[IZ] + cc, ivar, iOct); };
+    const real_t w[3] = { 1.0, 2.0, 1.0 };
+    for (int cc = -1; cc <= 1; ++cc)
+      for (int b = -1; b <= 1; ++b)
+      {
+        const real_t ww = w[b + 1] * w[cc + 1];
+        g[0] += ww * (Q(1, b, cc) - Q(-1, b, cc));
+        g[1] += ww * (Q(b, 1, cc) - Q(b, -1, cc));
+        g[2] += ww * (Q(b, cc, 1) - Q(b, cc, -1));
+      }
+  }
+  real_t nrm = g[0] * g[0] + g[1] * g[1];
+  if constexpr (dim == 3)
+    nrm += g[2] * g[2];
+  nrm = std::sqrt(nrm);
+  Kokkos::Array<real_t, dim> n;
+  for (size_t e = 0; e < dim; ++e)
+    n[e] = (nrm > 0.0) ? -g[e] / nrm : 0.0;
+  return n;
+}
+} // namespace vof
+
+} // namespace kalypsso

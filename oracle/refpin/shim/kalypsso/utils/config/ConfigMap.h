@@ -3,6 +3,7 @@
 #include <map>
 #include <string>
 #include <cstdlib>
+#include <vector>
 namespace kalypsso
 {
 class ConfigMap
@@ -25,6 +26,7 @@ public:
     auto it = kv.find(s + "/" + k);
     return it == kv.end() ? d : std::atoi(it->second.c_str());
   }
+  std::vector<double> getRealVector(const std::string &, const std::string &, std::vector<double> d) const { return d; }
   bool getBool(const std::string & s, const std::string & k, bool d) const
   {
     auto it = kv.find(s + "/" + k);

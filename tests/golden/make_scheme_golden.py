@@ -1,0 +1,145 @@
+"""Generate golden vectors of one whole block timestep from the reference's
+own scheme code.
+
+oracle/refpin compiles, in place from the reference tree, the functors of
+GodunovImplemV0::do_time_step (scheme/GodunovImplemV0.cpp:85-151): limited
+slopes, MUSCL-Hancock and THINC reconstruction with HLLC fluxes and their
+dt/dx scaling, the per-direction read-back update with the volume-fraction
+source term (ALLAIRE_KOKH and MILLER_PUCKETT), the volume-fraction
+renormalisation and the CFL reduction, and runs them serially on a periodic
+tile of same-level blocks (refpin_scheme_step).  This script stores the
+inputs and the reference's outputs for a few parameter sets, 2D and 3D, in
+tests/golden/scheme_step_golden.npz, so that the oracle can be checked against
+them where the reference tree is absent.
+
+Run from the repository root (needs the reference tree and a built oracle):
+
+    python tests/golden/make_scheme_golden.py
+"""
+import ctypes
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+OUT = os.path.join(ROOT, "tests", "golden", "scheme_step_golden.npz")
+LIB = os.path.join(ROOT, "oracle", "_ref", "librefpin.so")
+
+# name: dim, b, nb (blocks per tile edge), materials, thinc, integrator
+# (0 HANCOCK, 1 RK1), source term (0 ALLAIRE_KOKH, 1 MILLER_PUCKETT), slope type, seed
+CASES = {
+    "2d_muscl_hancock_ak_minmod_water_air": (2, 8, 2, "water_air", 0, 0, 0, 1.0, 1),
+    "2d_thinc_hancock_ak_mc_water_air": (2, 8, 2, "water_air", 1, 0, 0, 2.0, 2),
+    "2d_muscl_rk1_mp_minmod_water_air": (2, 8, 2, "water_air", 0, 1, 1, 1.0, 3),
+    "2d_thinc_hancock_mp_minmod_air_helium": (2, 8, 2, "air_helium", 1, 0, 1, 1.0, 4),
+    "3d_muscl_hancock_ak_minmod_water_air": (3, 8, 1, "water_air", 0, 0, 0, 1.0, 5),
+    "3d_thinc_hancock_mp_mc_air_r22": (3, 8, 1, "air_r22", 1, 0, 1, 2.0, 6),
+}
+MATERIALS = {"water_air": ((4.4, 1.4), (6e8, 0.0)), "air_helium": ((1.4, 1.648), (0.0, 0.0)), "air_r22": ((1.4, 1.249), (0.0, 0.0))}
+
+
+def tile_case(dim, b, nb, materials, thinc, integrator, source_term, slope_type, seed):
+    """Mesh, parameters and state of a periodic tile of nb^dim level-0 blocks:
+    smooth velocity and pressure fields and a material interface about one
+    cell wide (THINC reconstructs there)."""
+    from godunov_five_eq_gb300 import configs
+    from godunov_five_eq_gb300.mesh import BlockMesh
+
+    gamma, pinf = MATERIALS[materials]
+    mesh = BlockMesh(dim, b, (nb,) * dim, (True,) * dim, 0, 0, scaling=1.0)
+    t = mesh.build()
+    p = configs.HydroParams(
+        dim=dim,
+        bsize=b,
+        gamma=gamma,
+        pinf=pinf,
+        slope_type=slope_type,
+        cfl=0.4,
+        integrator=integrator,
+        thinc=thinc,
+        thinc_beta=1.6,
+        thinc_eps=1e-3,
+        source_term=source_term,
+        bc=(1,) * 6,
+        level_dx=t.level_dx,
+    )
+    rng = np.random.default_rng(seed)
+    xc = configs.cell_centers(mesh, t)
+    x, y = xc[:, 0], xc[:, 1]
+    z = xc[:, 2] if dim == 3 else 0.0 * x
+    L = float(nb)
+    c0 = rng.uniform(0.3, 0.7, 3) * L
+    r = np.sqrt((x - c0[0]) ** 2 + (y - c0[1]) ** 2 + ((z - c0[2]) ** 2 if dim == 3 else 0.0))
+    dx = 1.0 / b
+    a0 = 1e-6 + (1 - 2e-6) * 0.5 * (1 - np.tanh((r - 0.3 * L) / (0.8 * dx)))
+    rho0, rho1 = (1000.0, 1.2) if materials == "water_air" else (1.0, 0.138 if materials == "air_helium" else 3.15)
+    k = rng.uniform(0.5, 1.5, 4)
+    ar0 = a0 * rho0 * (1 + 0.05 * np.sin(2 * np.pi * k[0] * y / L))
+    ar1 = (1 - a0) * rho1 * (1 + 0.05 * np.cos(2 * np.pi * k[1] * x / L))
+    pbase = 1e5 if materials == "water_air" else 1.0
+    pr = pbase * (1 + 0.3 * np.sin(2 * np.pi * (x + y) / L) + 0.5 * (x < 0.5 * L))
+    s = 10.0 if materials == "water_air" else 0.3
+    vel = [s * np.cos(2 * np.pi * k[2] * y / L), -0.5 * s * np.sin(2 * np.pi * k[3] * x / L)]
+    if dim == 3:
+        vel.append(0.3 * s * np.cos(2 * np.pi * z / L))
+    U = np.zeros((t.n_total, t.nv, t.ncell))
+    U[: t.n_owned] = np.moveaxis(configs.prim_to_cons(dim, p, a0, ar0, ar1, pr, tuple(vel)), 0, 1)
+    return mesh, t, p, U
+
+
+def params_vector(p, thinc, integrator, source_term):
+    return np.array(
+        [p.gamma[0], p.gamma[1], p.pinf[0], p.pinf[1], p.smallr, p.smallc, p.slope_type, thinc, p.thinc_beta, p.thinc_eps, integrator, source_term],
+        dtype=np.float64,
+    )
+
+
+def reference_step(lib, dim, b, nb, prm, U, dt):
+    vp = ctypes.c_void_p
+    U = np.ascontiguousarray(U, np.float64)
+    out = np.zeros_like(U)
+    inv = np.zeros(1)
+    rc = lib.refpin_scheme_step(prm.ctypes.data_as(vp), dim, b, nb, 0, U.ctypes.data_as(vp), float(dt), out.ctypes.data_as(vp), inv.ctypes.data_as(vp))
+    if rc != 0:
+        raise RuntimeError(f"refpin_scheme_step failed ({rc})")
+    return out, float(inv[0])
+
+
+def load():
+    lib = ctypes.CDLL(LIB)
+    vp = ctypes.c_void_p
+    lib.refpin_scheme_step.restype = ctypes.c_int
+    lib.refpin_scheme_step.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, ctypes.c_double, vp, vp]
+    return lib
+
+
+def main():
+    subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "-s"], check=True)
+    subprocess.run(["make", "-C", os.path.join(ROOT, "oracle", "refpin"), "-s", "-j8"], check=True)
+    lib = load()
+    data = {}
+    for name, (dim, b, nb, mats, thinc, integ, st, slope, seed) in CASES.items():
+        mesh, t, p, U = tile_case(dim, b, nb, mats, thinc, integ, st, slope, seed)
+        # dt from the CFL condition of the initial state, written with the case
+        from oracle.oracle import Oracle
+
+        o = Oracle(t, p)
+        dt = float(o.dt(U)[0])
+        o.close()
+        prm = params_vector(p, thinc, integ, st)
+        out, inv = reference_step(lib, dim, b, nb, prm, U[: t.n_owned], dt)
+        data[f"{name}/prm"] = prm
+        data[f"{name}/shape"] = np.array([dim, b, nb])
+        data[f"{name}/dt"] = np.array([dt])
+        data[f"{name}/U"] = U[: t.n_owned]
+        data[f"{name}/U2"] = out
+        data[f"{name}/inv_dt"] = np.array([inv])
+    np.savez_compressed(OUT, **data)
+    print("wrote", OUT, os.path.getsize(OUT), "bytes")
+
+
+if __name__ == "__main__":
+    sys.exit(main())

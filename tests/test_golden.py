@@ -76,3 +76,118 @@ def test_golden_vectors_cover_all_hllc_waves():
         seen |= {"star_left"} if np.any((us > 0) & (us != ul)) else set()
         seen |= {"star_right"} if np.any((us <= 0) & (us != ur)) else set()
     assert seen == {"left", "right", "star_left", "star_right"}
+
+
+# ---------------------------------------------------------------------------
+# One whole block timestep (slopes, MUSCL-Hancock / THINC reconstruction,
+# HLLC fluxes with their dt/dx scaling, per-direction read-back update with
+# the volume-fraction source term, renormalisation, CFL reduction) against the
+# reference's own scheme functors, on periodic tiles of same-level blocks.
+# tests/golden/scheme_step_golden.npz comes from tests/golden/make_scheme_golden.py.
+# ---------------------------------------------------------------------------
+SCHEME_GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "scheme_step_golden.npz")
+REFPIN_LIB = os.path.join(os.path.dirname(os.path.dirname(__file__)), "oracle", "_ref", "librefpin.so")
+
+
+def _scheme_cases():
+    g = np.load(SCHEME_GOLDEN)
+    return sorted({k.split("/")[0] for k in g.keys()})
+
+
+def _tile(dim, b, nb, prm):
+    from godunov_five_eq_gb300 import configs
+    from godunov_five_eq_gb300.mesh import BlockMesh
+
+    mesh = BlockMesh(dim, b, (nb,) * dim, (True,) * dim, 0, 0, scaling=1.0)
+    t = mesh.build()
+    p = configs.HydroParams(
+        dim=dim,
+        bsize=b,
+        gamma=(prm[0], prm[1]),
+        pinf=(prm[2], prm[3]),
+        smallr=prm[4],
+        smallc=prm[5],
+        slope_type=prm[6],
+        cfl=0.4,
+        thinc=int(prm[7]),
+        thinc_beta=prm[8],
+        thinc_eps=prm[9],
+        integrator=int(prm[10]),
+        source_term=int(prm[11]),
+        bc=(1,) * 6,
+        level_dx=t.level_dx,
+    )
+    return mesh, t, p
+
+
+def _oracle_step(t, p, U, dt):
+    from oracle.oracle import Oracle
+
+    o = Oracle(t, p)
+    U = np.ascontiguousarray(U)
+    o.fill_outside(U)
+    out = o.step(U, dt)
+    o.fill_outside(out)
+    inv = float(o.inv_dt(out)[0])
+    o.close()
+    return out[: t.n_owned], inv
+
+
+@pytest.mark.parametrize("name", _scheme_cases())
+def test_oracle_scheme_step_matches_reference_golden(name):
+    import dataclasses
+
+    g = np.load(SCHEME_GOLDEN)
+    prm, (dim, b, nb), dt = g[f"{name}/prm"], g[f"{name}/shape"], float(g[f"{name}/dt"][0])
+    mesh, t, p = _tile(int(dim), int(b), int(nb), prm)
+    U = np.zeros((t.n_total, t.nv, t.ncell))
+    U[: t.n_owned] = g[f"{name}/U"]
+    got, inv = _oracle_step(t, p, U, dt)
+    ref = g[f"{name}/U2"]
+    assert np.array_equal(got, ref), f"{(got != ref).sum()} of {ref.size} values differ"
+    assert inv == float(g[f"{name}/inv_dt"][0])
+    if p.thinc:
+        # the THINC branch was taken: the MUSCL step gives another state
+        plain, _ = _oracle_step(t, dataclasses.replace(p, thinc=0), U, dt)
+        assert not np.array_equal(plain, ref)
+
+
+def test_scheme_golden_cases_cover_the_options():
+    g = np.load(SCHEME_GOLDEN)
+    opts = {(int(g[f"{n}/shape"][0]), int(g[f"{n}/prm"][7]), int(g[f"{n}/prm"][10]), int(g[f"{n}/prm"][11]), float(g[f"{n}/prm"][6])) for n in _scheme_cases()}
+    assert {o[0] for o in opts} == {2, 3}  # 2D and 3D
+    assert {o[1] for o in opts} == {0, 1}  # MUSCL and THINC
+    assert {o[2] for o in opts} == {0, 1}  # HANCOCK and RK1
+    assert {o[3] for o in opts} == {0, 1}  # ALLAIRE_KOKH and MILLER_PUCKETT
+    assert {o[4] for o in opts} == {1.0, 2.0}  # minmod and MC
+
+
+@pytest.mark.skipif(not os.path.exists(REFPIN_LIB), reason="reference-pinning library not built (needs the reference tree)")
+@pytest.mark.parametrize("dim", [2, 3])
+def test_oracle_scheme_step_matches_reference_live(dim):
+    """Fresh states and every option combination against the reference's
+    scheme code compiled in this checkout (oracle/_ref/librefpin.so)."""
+    from tests.golden.make_scheme_golden import load, params_vector, reference_step, tile_case
+
+    lib = load()
+    nb = 2 if dim == 2 else 1
+    bad = []
+    n = 0
+    for mats in ("water_air", "air_helium"):
+        for thinc in (0, 1):
+            for integ in (0, 1):
+                for st in (0, 1):
+                    for slope in (1.0, 2.0):
+                        seed = 100 + n
+                        n += 1
+                        mesh, t, p, U = tile_case(dim, 8, nb, mats, thinc, integ, st, slope, seed)
+                        from oracle.oracle import Oracle
+
+                        o = Oracle(t, p)
+                        dt = float(o.dt(U)[0])
+                        o.close()
+                        ref, inv_ref = reference_step(lib, dim, 8, nb, params_vector(p, thinc, integ, st), U[: t.n_owned], dt)
+                        got, inv = _oracle_step(t, p, U, dt)
+                        if not (np.array_equal(got, ref) and inv == inv_ref):
+                            bad.append((mats, thinc, integ, st, slope, int((got != ref).sum())))
+    assert not bad, bad
