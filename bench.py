@@ -22,6 +22,9 @@ roofline         fused step kernel: 128 B/cell-update (read U + write U2,
                  bandwidth of MEASURED_PEAKS.json
 cpu_baseline     the CPU oracle (FP64 restatement, OpenMP) on the host cores,
                  bounded sample of the same workload
+workloads        the same measurements (value, FP64 value, L1, roofline, CPU
+                 baseline) for further workloads, by default the 256
+                 batched droplet-advection instances (--extra-workloads)
 
 --impl reference times the CPU restatement of the reference method (the
 reference's own Kokkos build cannot be built: its kalypsso core, Kokkos and
@@ -57,6 +60,11 @@ def parse():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--workload", choices=list(L1_STEPS), default="shock_bubble")
     ap.add_argument("--no-l1", action="store_true", help="skip the 500-step accuracy run")
+    ap.add_argument(
+        "--extra-workloads",
+        default="droplets",
+        help="comma-separated workloads measured after the headline and reported under 'workloads' ('none' to skip)",
+    )
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--profile", action="store_true", help="one FP64 and one mixed step kernel launch, for ncu")
     ap.add_argument("--no-clocks", action="store_true", help="skip the nvidia-smi clock sampling (and its bracketing load)")
@@ -423,6 +431,100 @@ def run_amr_case(args):
     return 0 if st == 0 else 1
 
 
+def measure(name, args, world, local, flush, stream, steps, clocks=True, want_l1=True):
+    """Time one workload: K graph-replayed solver steps per precision form (L2
+    flushed before each), the step kernel alone, and the mixed form's L1 error
+    against the FP64 form after the config's step count."""
+    import torch
+    import torch.distributed as dist
+
+    from godunov_five_eq_gb300 import GodunovImplemGB300, gpu_flag_fn
+    from godunov_five_eq_gb300.replicas import max_over_ranks, whole_job_rate
+
+    desc, t, p, U = build_workload(name, gpu_flag_fn(), args.prolongation)
+    cells = t.n_owned * t.ncell
+    res = {}
+    for mode in ("fp64", "mixed"):
+        impl = GodunovImplemGB300(p, t)
+        A = torch.from_numpy(U.copy()).cuda()
+        B = torch.zeros_like(A)
+        impl.begin(A)
+        for _ in range(args.warmup):
+            impl.advance(A, B, mode)
+            A, B = B, A
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        sampler = ClockSampler(local) if (mode == "mixed" and clocks) else None
+        if sampler:
+            # nvidia-smi samples every 200 ms: the same load runs for ~0.5 s
+            # before and after the timed steps so that the samples see it
+            sampler.start()
+            A, B = _load(impl, A, B, mode, 0.5)
+        total_ms, launches, A, B = time_steps(impl, A, B, mode, steps, flush, stream)
+        if sampler:
+            A, B = _load(impl, A, B, mode, 0.4)
+        clk = sampler.stop() if sampler else None
+        total_ms = max_over_ranks(total_ms, device="cuda")
+        d_dt = impl.compute_dt_local(A)
+        kern_ms = time_kernel(impl, A, B, d_dt, mode, max(5, min(steps, 20)), flush, stream)
+        res[mode] = dict(total_ms=total_ms, launches=launches, clocks=clk, kern_ms=kern_ms, impl=impl)
+        del A, B
+    out = dict(desc=desc, t=t, p=p, U=U, cells=cells, res=res)
+    out["value"] = whole_job_rate(world, cells, steps, res["mixed"]["total_ms"])
+    out["value64"] = whole_job_rate(world, cells, steps, res["fp64"]["total_ms"])
+
+    # accuracy of the mixed path: L1 against the FP64 path after the config's step count
+    l1 = None
+    if want_l1:
+        nst = L1_STEPS[name]
+        outs = {}
+        for mode in ("fp64", "mixed"):
+            impl = res[mode]["impl"]
+            A = torch.from_numpy(U.copy()).cuda()
+            B = torch.zeros_like(A)
+            impl.run(A, B, nst, mode)
+            torch.cuda.synchronize()
+            outs[mode] = A.cpu().numpy()
+            del A, B
+        from godunov_five_eq_gb300.metrics import interface_error, l1_relative, linf_relative
+
+        errs = [float(e) for e in l1_relative(t, outs["mixed"], outs["fp64"])]
+        linf = [float(e) for e in linf_relative(t, outs["mixed"], outs["fp64"])]
+        l1 = {
+            "steps": nst,
+            "max": max(errs),
+            "per_variable": errs,
+            "norm": "volume-weighted relative L1 (momentum by |rho u|)",
+            "linf_max": max(linf),
+            "linf_per_variable": linf,
+            "interface": interface_error(t, outs["mixed"], outs["fp64"]) if t.n_inst == 1 else None,
+        }
+    out["l1"] = l1
+
+    peak, peak_kind = measured_peaks()
+    kern_s = res["mixed"]["kern_ms"] * 1e-3
+    bpc = BYTES_PER_CELL_2D if t.dim == 2 else BYTES_PER_CELL_3D
+    achieved = cells * bpc / kern_s / 1e9
+    traffic = ncu_traffic(name, "mixed", cells)
+    out["roofline"] = {
+        "bound": "hbm",
+        "achieved": achieved,
+        "peak": peak,
+        "unit": "GB/s",
+        "frac": achieved / peak,
+        "traffic": traffic,
+        "traffic_source": (f"committed ncu capture profiles/{PROFILE_OF[name][0]} (dram read + write bytes per launch), scaled by cells" if traffic else None),
+        "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback 6.8 TB/s",
+        "kernel": "step2d_kernel<16,mixed> (+reflux2d)" if t.dim == 2 else "step3d_kernel<mixed> (+reflux3d)",
+        "kernel_ms": res["mixed"]["kern_ms"],
+        "algorithmic_bytes_per_launch": cells * bpc,
+        "fp64_kernel_ms": res["fp64"]["kern_ms"],
+        "fp64_frac": cells * bpc / (res["fp64"]["kern_ms"] * 1e-3) / 1e9 / peak,
+    }
+    return out
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -440,66 +542,12 @@ def main():
     torch.cuda.set_device(local)
     if world > 1:
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    from godunov_five_eq_gb300 import GodunovImplemGB300, gpu_flag_fn
 
-    desc, t, p, U = build_workload(args.workload, gpu_flag_fn(), args.prolongation)
-    cells = t.n_owned * t.ncell
     stream = torch.cuda.current_stream()
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float64, device="cuda")  # 512 MB > L2
-    res = {}
-    for mode in ("fp64", "mixed"):
-        impl = GodunovImplemGB300(p, t)
-        A = torch.from_numpy(U.copy()).cuda()
-        B = torch.zeros_like(A)
-        impl.begin(A)
-        for _ in range(args.warmup):
-            impl.advance(A, B, mode)
-            A, B = B, A
-        torch.cuda.synchronize()
-        if world > 1:
-            dist.barrier()
-        sampler = ClockSampler(local) if (mode == "mixed" and not args.no_clocks) else None
-        if sampler:
-            # nvidia-smi samples every 200 ms: the same load runs for ~0.5 s
-            # before and after the timed steps so that the samples see it
-            sampler.start()
-            A, B = _load(impl, A, B, mode, 0.5)
-        total_ms, launches, A, B = time_steps(impl, A, B, mode, args.steps, flush, stream)
-        if sampler:
-            A, B = _load(impl, A, B, mode, 0.4)
-        clocks = sampler.stop() if sampler else None
-        total_ms = max_over_ranks(total_ms, device="cuda")
-        d_dt = impl.compute_dt_local(A)
-        kern_ms = time_kernel(impl, A, B, d_dt, mode, max(5, min(args.steps, 20)), flush, stream)
-        res[mode] = dict(total_ms=total_ms, launches=launches, clocks=clocks, kern_ms=kern_ms, impl=impl)
-    value = whole_job_rate(world, cells, args.steps, res["mixed"]["total_ms"])
-    value64 = whole_job_rate(world, cells, args.steps, res["fp64"]["total_ms"])
-
-    # accuracy of the mixed path: L1 against the FP64 path after the config's step count
-    l1 = None
-    if not args.no_l1:
-        nst = L1_STEPS[args.workload]
-        outs = {}
-        for mode in ("fp64", "mixed"):
-            impl = res[mode]["impl"]
-            A = torch.from_numpy(U.copy()).cuda()
-            B = torch.zeros_like(A)
-            impl.run(A, B, nst, mode)
-            torch.cuda.synchronize()
-            outs[mode] = A.cpu().numpy()
-        from godunov_five_eq_gb300.metrics import interface_error, l1_relative, linf_relative
-
-        errs = [float(e) for e in l1_relative(t, outs["mixed"], outs["fp64"])]
-        linf = [float(e) for e in linf_relative(t, outs["mixed"], outs["fp64"])]
-        l1 = {
-            "steps": nst,
-            "max": max(errs),
-            "per_variable": errs,
-            "norm": "volume-weighted relative L1 (momentum by |rho u|)",
-            "linf_max": max(linf),
-            "linf_per_variable": linf,
-            "interface": interface_error(t, outs["mixed"], outs["fp64"]),
-        }
+    m = measure(args.workload, args, world, local, flush, stream, args.steps, clocks=not args.no_clocks, want_l1=not args.no_l1)
+    desc, t, p, U, cells, res = m["desc"], m["t"], m["p"], m["U"], m["cells"], m["res"]
+    value, value64 = m["value"], m["value64"]
 
     # end to end through the C ABI with host buffers: g5_step_host copies the
     # pinned host U (owned + outside blocks) to the device and the owned blocks
@@ -530,27 +578,37 @@ def main():
         "d2h_bytes_per_step": int(t.n_owned * blk),
         "api": "g5_step_host: pinned host U copied in chunks of about 3.5 MB (8 to 16), chunk steps on 8 streams as neighbours arrive, U2 stored by the kernels into pinned host memory (one CUDA graph)",
     }
-    peak, peak_kind = measured_peaks()
-    kern_s = res["mixed"]["kern_ms"] * 1e-3
-    bpc = BYTES_PER_CELL_2D if t.dim == 2 else BYTES_PER_CELL_3D
-    achieved = cells * bpc / kern_s / 1e9
-    roofline = {
-        "bound": "hbm",
-        "achieved": achieved,
-        "peak": peak,
-        "unit": "GB/s",
-        "frac": achieved / peak,
-        "traffic": ncu_traffic(args.workload, "mixed", cells),
-        "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback 6.8 TB/s",
-        "kernel": "step2d_kernel<16,mixed> (+reflux2d)" if t.dim == 2 else "step3d_kernel<mixed> (+reflux3d)",
-        "kernel_ms": res["mixed"]["kern_ms"],
-        "algorithmic_bytes_per_launch": cells * bpc,
-        "fp64_kernel_ms": res["fp64"]["kern_ms"],
-        "fp64_frac": cells * bpc / (res["fp64"]["kern_ms"] * 1e-3) / 1e9 / peak,
-    }
+    del hU, hO
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(t, p, U)
+    for mode in ("fp64", "mixed"):
+        res[mode]["impl"].close()
+
+    # further workloads on the same line (not the headline): the batched
+    # droplet instances (many uneven instances in one persistent launch)
+    workloads = {}
+    for extra in [w for w in args.extra_workloads.split(",") if w and w != "none" and w != args.workload]:
+        mx = measure(extra, args, world, local, flush, stream, min(args.steps, 10), clocks=False, want_l1=not args.no_l1)
+        tx = mx["t"]
+        workloads[extra] = {
+            "workload": mx["desc"],
+            "instances": int(tx.n_inst),
+            "blocks": int(tx.n_owned),
+            "cells": int(mx["cells"]),
+            "value": mx["value"],
+            "unit": "cell-updates/s",
+            "ms_per_step": mx["res"]["mixed"]["total_ms"] / min(args.steps, 10),
+            "fp64_plain": {"value": mx["value64"], "unit": "cell-updates/s"},
+            "speedup_mixed_vs_fp64": mx["value"] / mx["value64"],
+            "l1_err_vs_fp64": mx["l1"],
+            "roofline": mx["roofline"],
+            "cpu_baseline": cpu_baseline(tx, mx["p"], mx["U"], max_seconds=12.0) if (rank == 0 and not args.no_cpu) else None,
+            "gpu_launches": int(mx["res"]["mixed"]["launches"]),
+        }
+        for mode in ("fp64", "mixed"):
+            mx["res"][mode]["impl"].close()
+        del mx
     if rank == 0:
         line = {
             "metric": METRIC,
@@ -576,12 +634,13 @@ def main():
             },
             "fp64_plain": {"value": value64, "unit": "cell-updates/s", "ms_per_step": res["fp64"]["total_ms"] / args.steps},
             "speedup_mixed_vs_fp64": value / value64,
-            "l1_err_vs_fp64": l1,
-            "roofline": roofline,
+            "l1_err_vs_fp64": m["l1"],
+            "roofline": m["roofline"],
             "cpu_baseline": cpu,
             "e2e": e2e,
             "gpu_launches": int(res["mixed"]["launches"]),
             "clocks": res["mixed"]["clocks"],
+            "workloads": workloads,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -833,21 +833,21 @@ hllc_fp32(const float * ql, const float * qr, float xi0, float xi1, float gp0, f
 // mantissa bits move into float position with one funnel shift, the exponent
 // is rebiased by flipping its top bit (e - 896 mod 256), the mantissa is
 // truncated; magnitudes below FLT_MIN (zeros included) give a signed zero.
-// NaN gives a quiet NaN, and infinities and magnitudes of 2^128 and above give
-// an infinity of the same sign, so a non-finite neighbour reaches the fluxes
-// as non-finite (and the status word) rather than as a finite value.
+// NaN, infinities and magnitudes of 2^128 and above (rare) take the hardware
+// conversion (NaN stays NaN, the others give an infinity of the same sign),
+// so a non-finite neighbour reaches the fluxes as non-finite (and the status
+// word) rather than as a finite value.
 __device__ __forceinline__ float
 d2f_fast(double x)
 {
   const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
   const unsigned ah = hi & 0x7FFFFFFFu, sgn = hi & 0x80000000u;
   const unsigned m = __funnelshift_l(lo, hi, 3); // e[8:0] m[51:29]
-  unsigned       f = (((m & 0x7FFFFFFFu) ^ 0x40000000u)) | sgn;
-  if (ah < (897u << 20))
-    f = sgn;
+  const unsigned f = (((m & 0x7FFFFFFFu) ^ 0x40000000u)) | sgn;
+  float          r = __uint_as_float(ah < (897u << 20) ? sgn : f);
   if (ah >= (1151u << 20))
-    f = sgn | 0x7F800000u | ((ah > 0x7FF00000u || (ah == 0x7FF00000u && lo != 0u)) ? 0x00400000u : 0u);
-  return __uint_as_float(f);
+    r = __double2float_rn(x);
+  return r;
 }
 
 // exact float -> double on the integer pipe (float denormals read as zero,
