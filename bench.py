@@ -66,6 +66,7 @@ def parse():
         help="comma-separated workloads measured after the headline and reported under 'workloads' ('none' to skip)",
     )
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-tune", action="store_true", help="keep the default launch shape (no g5_tune before timing)")
     ap.add_argument("--profile", action="store_true", help="one FP64 and one mixed step kernel launch, for ncu")
     ap.add_argument("--no-clocks", action="store_true", help="skip the nvidia-smi clock sampling (and its bracketing load)")
     ap.add_argument(
@@ -448,6 +449,9 @@ def measure(name, args, world, local, flush, stream, steps, clocks=True, want_l1
         impl = GodunovImplemGB300(p, t)
         A = torch.from_numpy(U.copy()).cuda()
         B = torch.zeros_like(A)
+        # the autotuner picks the launch shape of this mesh (g5_tune, untimed)
+        impl.fill_outside_quadrants(A)
+        shape = impl.tune(A, B, mode) if not args.no_tune else impl.tune_choice(mode)
         impl.begin(A)
         for _ in range(args.warmup):
             impl.advance(A, B, mode)
@@ -468,7 +472,7 @@ def measure(name, args, world, local, flush, stream, steps, clocks=True, want_l1
         total_ms = max_over_ranks(total_ms, device="cuda")
         d_dt = impl.compute_dt_local(A)
         kern_ms = time_kernel(impl, A, B, d_dt, mode, max(5, min(steps, 20)), flush, stream)
-        res[mode] = dict(total_ms=total_ms, launches=launches, clocks=clk, kern_ms=kern_ms, impl=impl)
+        res[mode] = dict(total_ms=total_ms, launches=launches, clocks=clk, kern_ms=kern_ms, impl=impl, shape=shape)
         del A, B
     out = dict(desc=desc, t=t, p=p, U=U, cells=cells, res=res)
     out["value"] = whole_job_rate(world, cells, steps, res["mixed"]["total_ms"])
@@ -605,6 +609,7 @@ def main():
             "roofline": mx["roofline"],
             "cpu_baseline": cpu_baseline(tx, mx["p"], mx["U"], max_seconds=12.0) if (rank == 0 and not args.no_cpu) else None,
             "gpu_launches": int(mx["res"]["mixed"]["launches"]),
+            "launch_shape": {mode: mx["res"][mode]["shape"] for mode in ("fp64", "mixed")},
         }
         for mode in ("fp64", "mixed"):
             mx["res"][mode]["impl"].close()
@@ -631,6 +636,7 @@ def main():
                 "blocks_per_level": {int(k): int(v) for k, v in enumerate(np.bincount(t.level[: t.n_owned])) if v},
                 "l2": "flushed (512 MB write) before every timed step",
                 "parallelism": "replicas" if world > 1 else "single GPU",
+                "launch_shape": {mode: res[mode]["shape"] for mode in ("fp64", "mixed")},
             },
             "fp64_plain": {"value": value64, "unit": "cell-updates/s", "ms_per_step": res["fp64"]["total_ms"] / args.steps},
             "speedup_mixed_vs_fp64": value / value64,

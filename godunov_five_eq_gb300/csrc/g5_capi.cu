@@ -49,7 +49,18 @@ struct G5Context
     size_t cap = 0;
   };
   std::unordered_map<const void *, PoolEntry> pool; // device buffers by field (dev_alloc)
-  int            ctas_per_sm[2] = { 0, 0 };
+  // launch shape of the step per precision mode (g5_tune): CTAs per SM (0:
+  // occupancy maximum), dynamic block claiming, walk order (1: blocks with
+  // coarse/fine neighbours first, 0: table order), reflux-pass layout
+  struct Shape
+  {
+    int ctas_per_sm = 0;
+    int claim = 1;
+    int walk = 1;
+    int reflux = 0;
+  };
+  Shape          shape[2];
+  std::vector<std::pair<int, float>> tune_log[2]; // (packed shape, ms per step) of the last g5_tune
   int            last_launches = 0;
   // cached one-step graphs of g5_advance
   struct GraphSlot
@@ -262,12 +273,14 @@ do_step(G5Context * c, const double * U, double * U2, const double * d_dt, int m
   a.m = dev_mesh(c);
   a.p = c->phys;
   a.fill_twins = fill_twins ? 1 : 0;
-  a.ticket = c->d_ticket;
-  a.work = c->d_walk;
-  a.n_work = c->n_owned;
+  const G5Context::Shape & sh = c->shape[mode];
+  a.ticket = sh.claim ? c->d_ticket : nullptr;
+  a.work = sh.walk ? c->d_walk : nullptr;
+  a.n_work = sh.walk ? c->n_owned : 0;
+  a.reflux_layout = sh.reflux;
   int         launches = 0;
-  cudaError_t e = mode == G5_MODE_FP64 ? g5::launch_step_fp64(c->dim, c->b, a, c->ctas_per_sm[0], s, &launches)
-                                       : g5::launch_step_mixed(c->dim, c->b, a, c->ctas_per_sm[1], s, &launches);
+  cudaError_t e = mode == G5_MODE_FP64 ? g5::launch_step_fp64(c->dim, c->b, a, sh.ctas_per_sm, s, &launches)
+                                       : g5::launch_step_mixed(c->dim, c->b, a, sh.ctas_per_sm, s, &launches);
   c->last_launches = launches;
   return e == cudaSuccess ? G5_OK : G5_ERR_CUDA;
 }
@@ -743,9 +756,10 @@ enqueue_host_step(G5Context * c, const double * h_U, double * h_U2, double * d_U
     a.m.defer_list = nullptr;
     a.m.n_defer = 0;
     a.p = c->phys;
+    a.reflux_layout = c->shape[mode].reflux;
     auto launch = [&](const g5::StepArgs & args) {
-      const cudaError_t e = mode == G5_MODE_FP64 ? g5::launch_step_fp64(c->dim, c->b, args, c->ctas_per_sm[0], q, launches)
-                                                 : g5::launch_step_mixed(c->dim, c->b, args, c->ctas_per_sm[1], q, launches);
+      const cudaError_t e = mode == G5_MODE_FP64 ? g5::launch_step_fp64(c->dim, c->b, args, c->shape[0].ctas_per_sm, q, launches)
+                                                 : g5::launch_step_mixed(c->dim, c->b, args, c->shape[1].ctas_per_sm, q, launches);
       return e == cudaSuccess;
     };
     if (ok && a.n_work > 0)
@@ -830,12 +844,13 @@ g5_step_batched(G5Context * c, const double * d_U, double * d_U2, const double *
   a.work = c->d_batch_work;
   a.n_work = (int)work.size();
   a.inst_active = c->d_inst_active;
-  a.ticket = c->d_ticket;
+  a.ticket = c->shape[mode].claim ? c->d_ticket : nullptr;
+  a.reflux_layout = c->shape[mode].reflux;
   a.m = dev_mesh(c);
   a.p = c->phys;
   int         launches = 0;
-  cudaError_t e = mode == G5_MODE_FP64 ? g5::launch_step_fp64(c->dim, c->b, a, c->ctas_per_sm[0], s, &launches)
-                                       : g5::launch_step_mixed(c->dim, c->b, a, c->ctas_per_sm[1], s, &launches);
+  cudaError_t e = mode == G5_MODE_FP64 ? g5::launch_step_fp64(c->dim, c->b, a, c->shape[0].ctas_per_sm, s, &launches)
+                                       : g5::launch_step_mixed(c->dim, c->b, a, c->shape[1].ctas_per_sm, s, &launches);
   c->last_launches = launches;
   return e == cudaSuccess ? G5_OK : G5_ERR_CUDA;
 }
@@ -1309,6 +1324,33 @@ g5_status(G5Context * ctx, void * stream)
   return (int)h;
 }
 
+namespace
+{
+// packed launch shape: ctas_per_sm + 16 claim + 32 walk + 64 reflux
+int
+pack_shape(const G5Context::Shape & sh)
+{
+  return sh.ctas_per_sm + 16 * sh.claim + 32 * sh.walk + 64 * sh.reflux;
+}
+} // namespace
+
+extern "C" int
+g5_tune_pick(const float * ms, int n, int default_index, float margin)
+{
+  if (!ms || n <= 0 || default_index < 0 || default_index >= n || !(margin >= 0.0f))
+    return G5_ERR_ARG;
+  int best = -1;
+  for (int i = 0; i < n; ++i)
+    if (ms[i] > 0.0f && (best < 0 || ms[i] < ms[best]))
+      best = i;
+  if (best < 0)
+    return G5_ERR_ARG;
+  // the default shape stays unless another one is faster by more than the margin
+  if (ms[default_index] > 0.0f && ms[default_index] <= ms[best] * (1.0f + margin))
+    return default_index;
+  return best;
+}
+
 extern "C" int
 g5_tune(G5Context * c, const double * d_U, double * d_U2, int mode, void * stream)
 {
@@ -1326,35 +1368,117 @@ g5_tune(G5Context * c, const double * d_U, double * d_U2, int mode, void * strea
     return rc;
   if (g5::launch_dt_update(c->d_invdt, c->d_dt, nullptr, c->n_inst, c->phys.cfl, s) != cudaSuccess)
     return G5_ERR_CUDA;
-  cudaEvent_t e0, e1;
-  cudaEventCreate(&e0);
-  cudaEventCreate(&e1);
-  float best = 1e30f;
-  int   best_k = occ;
-  for (int k = 1; k <= occ; ++k)
+  // candidates: CTAs per SM x block claiming x walk order x reflux layout
+  // (the last only where it exists: the FP32-bulk 2D pass with records)
+  std::vector<G5Context::Shape> cand;
+  const int nreflux = (mode == G5_MODE_MIXED && c->dim == 2 && c->n_defer > 0) ? 2 : 1;
+  for (int k = 1; k <= occ && k < 16; ++k)
+    for (int claim = 1; claim >= 0; --claim)
+      for (int walk = 1; walk >= 0; --walk)
+        for (int rf = 0; rf < nreflux; ++rf)
+        {
+          G5Context::Shape sh;
+          sh.ctas_per_sm = k;
+          sh.claim = claim;
+          sh.walk = walk;
+          sh.reflux = rf;
+          cand.push_back(sh);
+        }
+  // the default: the occupancy maximum, claiming, coarse/fine-first walk, lanes
+  int def = 0;
+  for (size_t i = 0; i < cand.size(); ++i)
+    if (cand[i].ctas_per_sm == occ && cand[i].claim == 1 && cand[i].walk == 1 && cand[i].reflux == 0)
+      def = (int)i;
+  const G5Context::Shape saved = c->shape[mode];
+  std::vector<float>     ms(cand.size(), 0.0f);
+  cudaEvent_t            e0, e1;
+  if (cudaEventCreate(&e0) != cudaSuccess)
+    return G5_ERR_CUDA;
+  if (cudaEventCreate(&e1) != cudaSuccess)
   {
-    c->ctas_per_sm[mode] = k;
-    rc = do_step(c, d_U, d_U2, c->d_dt, mode, nullptr, s); // warm-up
-    if (rc)
-      break;
-    cudaEventRecord(e0, s);
-    for (int r = 0; r < 3; ++r)
-      do_step(c, d_U, d_U2, c->d_dt, mode, nullptr, s);
-    cudaEventRecord(e1, s);
-    cudaEventSynchronize(e1);
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, e0, e1);
-    if (ms < best)
-    {
-      best = ms;
-      best_k = k;
-    }
+    cudaEventDestroy(e0);
+    return G5_ERR_CUDA;
   }
+  constexpr int reps = 3;
+  for (int pass = 0; pass < 2 && !rc; ++pass) // two passes, the best of both per candidate
+    for (size_t i = 0; i < cand.size() && !rc; ++i)
+    {
+      c->shape[mode] = cand[i];
+      rc = do_step(c, d_U, d_U2, c->d_dt, mode, nullptr, s); // warm-up
+      if (rc)
+        break;
+      cudaEventRecord(e0, s);
+      for (int r = 0; r < reps && !rc; ++r)
+        rc = do_step(c, d_U, d_U2, c->d_dt, mode, nullptr, s);
+      cudaEventRecord(e1, s);
+      if (cudaEventSynchronize(e1) != cudaSuccess)
+        rc = G5_ERR_CUDA;
+      float t = 0.f;
+      cudaEventElapsedTime(&t, e0, e1);
+      t /= reps;
+      ms[i] = (pass == 0 || t < ms[i]) ? t : ms[i];
+    }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  c->ctas_per_sm[mode] = best_k;
+  if (rc)
+  {
+    c->shape[mode] = saved;
+    return rc;
+  }
+  const int pick = g5_tune_pick(ms.data(), (int)ms.size(), def, 0.02f);
+  c->shape[mode] = cand[pick < 0 ? def : pick];
+  c->tune_log[mode].clear();
+  for (size_t i = 0; i < cand.size(); ++i)
+    c->tune_log[mode].emplace_back(pack_shape(cand[i]), ms[i]);
   drop_graphs(c);
-  return rc ? rc : best_k;
+  return pack_shape(c->shape[mode]);
+}
+
+extern "C" int
+g5_tune_choice(const G5Context * c, int mode, int32_t * out4)
+{
+  if (!c || !out4 || (mode != G5_MODE_FP64 && mode != G5_MODE_MIXED))
+    return G5_ERR_ARG;
+  const G5Context::Shape & sh = c->shape[mode];
+  const int occ = mode == G5_MODE_FP64 ? g5::step_max_ctas_per_sm_fp64(c->dim, c->b) : g5::step_max_ctas_per_sm_mixed(c->dim, c->b);
+  out4[0] = sh.ctas_per_sm > 0 ? sh.ctas_per_sm : occ;
+  out4[1] = sh.claim;
+  out4[2] = sh.walk;
+  out4[3] = sh.reflux;
+  return G5_OK;
+}
+
+extern "C" int
+g5_tune_report(const G5Context * c, int mode, int32_t * shapes, float * ms, int cap)
+{
+  if (!c || (mode != G5_MODE_FP64 && mode != G5_MODE_MIXED) || cap < 0)
+    return G5_ERR_ARG;
+  const auto & log = c->tune_log[mode];
+  for (int i = 0; i < cap && i < (int)log.size(); ++i)
+  {
+    if (shapes)
+      shapes[i] = log[i].first;
+    if (ms)
+      ms[i] = log[i].second;
+  }
+  return (int)log.size();
+}
+
+extern "C" int
+g5_set_shape(G5Context * c, int mode, const int32_t * shape4)
+{
+  if (!c || !shape4 || (mode != G5_MODE_FP64 && mode != G5_MODE_MIXED))
+    return G5_ERR_ARG;
+  if (shape4[0] < 0 || shape4[0] > 15 || (shape4[1] & ~1) || (shape4[2] & ~1) || (shape4[3] & ~1))
+    return G5_ERR_ARG;
+  G5Context::Shape sh;
+  sh.ctas_per_sm = shape4[0];
+  sh.claim = shape4[1];
+  sh.walk = shape4[2];
+  sh.reflux = shape4[3];
+  c->shape[mode] = sh;
+  drop_graphs(c);
+  return G5_OK;
 }
 
 extern "C" int

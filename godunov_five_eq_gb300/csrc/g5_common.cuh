@@ -99,6 +99,9 @@ struct StepArgs
   // steps block b, then claims further blocks with tickets of this counter;
   // the CTA drawing the launch's last ticket resets it to 0.
   unsigned int * ticket = nullptr;
+  // layout of the FP32-bulk 2D reflux pass: 0 eight lanes per deferred cell,
+  // 1 one thread per deferred cell (the FP64 form and 3D: one thread per cell)
+  int            reflux_layout = 0;
   DevMesh        m;
   PhysParams     p;
 };
@@ -833,21 +836,35 @@ hllc_fp32(const float * ql, const float * qr, float xi0, float xi1, float gp0, f
 // mantissa bits move into float position with one funnel shift, the exponent
 // is rebiased by flipping its top bit (e - 896 mod 256), the mantissa is
 // truncated; magnitudes below FLT_MIN (zeros included) give a signed zero.
-// NaN, infinities and magnitudes of 2^128 and above (rare) take the hardware
-// conversion (NaN stays NaN, the others give an infinity of the same sign),
-// so a non-finite neighbour reaches the fluxes as non-finite (and the status
-// word) rather than as a finite value.
+// Only for finite values of the state (far below FLT_MAX): a NaN or an
+// infinity gives a finite float.  It converts the cell's own values, whose
+// non-finiteness the FP64 adds into the new state carry to the status word.
 __device__ __forceinline__ float
 d2f_fast(double x)
 {
   const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+  const unsigned m = __funnelshift_l(lo, hi, 3); // e[8:0] m[51:29]
+  const unsigned f = (((m & 0x7FFFFFFFu) ^ 0x40000000u)) | (hi & 0x80000000u);
+  return __uint_as_float(((hi & 0x7FFFFFFFu) < (897u << 20)) ? (hi & 0x80000000u) : f);
+}
+
+// The same conversion keeping non-finite values non-finite, for states that
+// enter the fluxes (the primitive conversion of the block and its halo): a
+// double of magnitude 2^128 or more, an infinity or a NaN gives a float with
+// an all-ones exponent and the top 23 mantissa bits, i.e. infinity stays
+// infinity and a NaN whose top mantissa bits are not all zero (every NaN that
+// arithmetic produces) stays NaN.  Two integer instructions more than
+// d2f_fast (a compare and a select).
+__device__ __forceinline__ float
+d2f_nan(double x)
+{
+  const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
   const unsigned ah = hi & 0x7FFFFFFFu, sgn = hi & 0x80000000u;
   const unsigned m = __funnelshift_l(lo, hi, 3); // e[8:0] m[51:29]
-  const unsigned f = (((m & 0x7FFFFFFFu) ^ 0x40000000u)) | sgn;
-  float          r = __uint_as_float(ah < (897u << 20) ? sgn : f);
-  if (ah >= (1151u << 20))
-    r = __double2float_rn(x);
-  return r;
+  unsigned       f = (((m & 0x7FFFFFFFu) ^ 0x40000000u)) | sgn;
+  f = ah < (897u << 20) ? sgn : f;
+  f = ah >= (1151u << 20) ? ((m & 0x007FFFFFu) | 0x7F800000u | sgn) : f;
+  return __uint_as_float(f);
 }
 
 // exact float -> double on the integer pipe (float denormals read as zero,
@@ -964,28 +981,28 @@ __device__ __forceinline__ float
 pressure_mixed(const double * u, const PhysParams & P, bool stiff, float & d, float & ux, float & uy, float & uz, float & a0f)
 {
   using H = V<DIM>;
-  d = fmaxf(d2f_fast(u[H::ID]), P.f_smallr);
+  d = fmaxf(d2f_nan(u[H::ID]), P.f_smallr);
   const float inv = __frcp_rn(d);
-  ux = d2f_fast(u[H::IU]) * inv;
-  uy = d2f_fast(u[H::IV]) * inv;
+  ux = d2f_nan(u[H::IU]) * inv;
+  uy = d2f_nan(u[H::IV]) * inv;
   float k2 = ux * ux + uy * uy;
   uz = 0.0f;
   if constexpr (DIM == 3)
   {
-    uz = d2f_fast(u[H::IW]) * inv;
+    uz = d2f_nan(u[H::IW]) * inv;
     k2 += uz * uz;
   }
   const double a0u = u[H::IA0];
-  a0f = d2f_fast(a0u);
+  a0f = d2f_nan(a0u);
   const float K = 0.5f * d * k2;
   float       num;
   if (stiff)
   {
     const double PI = fma(a0u, P.dgpx, P.gpx[1]);
-    num = d2f_fast((u[H::IE] - PI) - f2d_exact(K));
+    num = d2f_nan((u[H::IE] - PI) - f2d_exact(K));
   }
   else
-    num = d2f_fast(u[H::IE]) - K;
+    num = d2f_nan(u[H::IE]) - K;
   const float S = fmaf(a0f, P.f_dxi, P.f_xi[1]);
   return __fdividef(num, S);
 }
@@ -1004,7 +1021,7 @@ source_factors_mixed(const double * u, const PhysParams & P, bool stiff, float &
   const float p = pressure_mixed<DIM>(u, P, stiff, d, ux, uy, uz, a0f);
   const float K0 = (float)P.gamma[0] * (p + (float)P.pinf[0]);
   const float K1 = (float)P.gamma[1] * (p + (float)P.pinf[1]);
-  const float kbar = __frcp_rn(a0f * __frcp_rn(K0) + d2f_fast(u[H::IA1]) * __frcp_rn(K1));
+  const float kbar = __frcp_rn(a0f * __frcp_rn(K0) + d2f_nan(u[H::IA1]) * __frcp_rn(K1));
   st0 = 1.0f - kbar * __frcp_rn(K0);
   st1 = 1.0f - kbar * __frcp_rn(K1);
 }
@@ -1018,7 +1035,7 @@ prim_mixed(const double * u, float * q, const PhysParams & P, bool stiff)
   float       d, ux, uy, uz, a0f;
   const float p = pressure_mixed<DIM>(u, P, stiff, d, ux, uy, uz, a0f);
   float       a0 = fmaxf(0.0f, fminf(1.0f, a0f));
-  float       r0 = d2f_fast(u[H::IAD0]), r1 = d2f_fast(u[H::IAD1]);
+  float       r0 = d2f_nan(u[H::IAD0]), r1 = d2f_nan(u[H::IAD1]);
   const float eps = 1e-12f;
   if (r0 < eps)
     r0 = 0.0f;

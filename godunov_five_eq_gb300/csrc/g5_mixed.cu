@@ -53,10 +53,18 @@ launch_step2d_m(const StepArgs & a, int ctas_per_sm, cudaStream_t s, int * launc
     if (e != cudaSuccess)
       return e;
   }
-  if (a.m.n_defer > 0)
+  if (a.m.n_defer > 0 && a.reflux_layout == 1)
   {
     const int n = a.m.n_defer * B;
     reflux2d_kernel<B, true><<<(n + 31) / 32, 32, 0, s>>>(a);
+    ++*launches;
+    e = cudaGetLastError();
+  }
+  else if (a.m.n_defer > 0)
+  {
+    // 8 lanes per deferred cell
+    const int n = a.m.n_defer * B * 8;
+    reflux2d_mixed_lanes_kernel<B><<<(n + 127) / 128, 128, 0, s>>>(a);
     ++*launches;
     e = cudaGetLastError();
   }

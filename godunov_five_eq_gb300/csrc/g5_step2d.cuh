@@ -1274,4 +1274,259 @@ reflux2d_kernel(StepArgs a)
   }
 }
 
+// ---------------------------------------------------------------------------
+// The FP32-bulk reflux pass with 8 lanes per deferred cell.  One thread per
+// cell ran a serial chain of about a thousand instructions with one warp per
+// SM (latency-bound at ~8 us on the shock-bubble); here lane k of a cell's
+// group of 8 handles face-flux component k (r0 r1 a0 a1 e u v u*) and the
+// state variable it updates (IAD0 IAD1 IA0 IA1 IE IU IV ID), and the lanes
+// exchange what couples them (u* for the volume-fraction source term, the two
+// volume fractions for the renormalisation, the partial densities for ID, the
+// new state for the CFL rate) by shuffles.  Every value is computed with the
+// arithmetic of apply_mixed_2d in the same order, so the pass gives the same
+// bits as the one-thread form.  All lanes of a warp reach every shuffle:
+// inactive cells (past the end, skipped, or of a stopped instance) compute on
+// zeros and write nothing.
+// ---------------------------------------------------------------------------
+template <int B>
+__global__ void __launch_bounds__(128)
+reflux2d_mixed_lanes_kernel(StepArgs a)
+{
+  using H = V<2>;
+  using D = DeferInfo<2>;
+  constexpr int NC = B * B;
+  const int     gid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int     k = gid & 7;                     // flux component of this lane
+  const int     gb = (int)(threadIdx.x & 31u) & ~7; // first lane of the cell's group
+  const int     cslot = gid >> 3;
+  bool          act = cslot < a.m.n_defer * B;
+  const int     rec = act ? cslot / B : 0, pos = cslot % B;
+  int4          r0 = make_int4(0, -1, -1, -1), r1 = make_int4(-1, -1, -1, -1), r2 = make_int4(-1, -1, -1, -1), r3 = make_int4(-1, 0, 0, 0);
+  if (act)
+  {
+    const int4 * row = reinterpret_cast<const int4 *>(a.m.defer_info + (size_t)rec * D::STRIDE);
+    r0 = row[0];
+    r1 = row[1];
+    r2 = row[2];
+    r3 = row[3];
+  }
+  const int code = r0.x;
+  const int dsl[4] = { r0.y, r0.z, r0.w, r1.x };
+  const int rsf[4][2] = { { r1.y, r1.z }, { r1.w, r2.x }, { r2.y, r2.z }, { r2.w, r3.x } };
+  const int n = code >> 3, face = code & 7;
+  const int ins = act ? r3.z : 0;
+  if (act && a.inst_active && !a.inst_active[ins])
+    act = false;
+  const int dirf = face >> 1, sidef = face & 1;
+  const int ci = dirf == 0 ? (sidef ? B - 1 : 0) : pos;
+  const int cj = dirf == 0 ? pos : (sidef ? B - 1 : 0);
+  const int cell = ci + B * cj;
+  // a cell next to two finer faces is handled by the lower face index
+#pragma unroll
+  for (int f2 = 0; f2 < 4; ++f2)
+    if (f2 < face && dsl[f2] >= 0 && (f2 >> 1 == 0 ? ci : cj) == ((f2 & 1) ? B - 1 : 0))
+      act = false;
+  bool fine[4];
+  int  rs[4];
+#pragma unroll
+  for (int f = 0; f < 4; ++f)
+  {
+    const int cd = (f >> 1) == 0 ? ci : cj, ct = (f >> 1) == 0 ? cj : ci;
+    fine[f] = cd == ((f & 1) ? B - 1 : 0) && dsl[f] >= 0;
+    rs[f] = fine[f] ? ((2 * ct) / B ? rsf[f][1] : rsf[f][0]) : -1;
+    if (act && fine[f] && rs[f] < 0)
+    {
+      if (k == 0)
+        raise_status(a.status, STATUS_MESH);
+      act = false;
+    }
+  }
+  // the state variable this lane updates (flux component k -> variable)
+  // (component k -> variable: r0 IAD0, r1 IAD1, a0 IA0, a1 IA1, e IE, u IU,
+  // v IV, u* ID, packed as nibbles)
+  static_assert(H::FR0 == 0 && H::FR1 == 1 && H::FA0 == 2 && H::FA1 == 3 && H::FE == 4 && H::FU == 5 && H::FV == 6 && H::FUS == 7, "2D face record order");
+  static_assert(H::ID == 0 && H::IE == 1 && H::IU == 2 && H::IV == 3 && H::IA0 == 4 && H::IAD0 == 5 && H::IA1 == 6 && H::IAD1 == 7, "2D variable order");
+  const int     var = (int)((0x03216475u >> (4 * k)) & 15u);
+  constexpr int lane_of[8] = { 7, 4, 5, 6, 2, 0, 3, 1 }; // variable -> lane (inverse of the map above)
+  const double  u_own = act ? a.U[((size_t)n * H::NV + var) * NC + cell] : 0.0;
+  // component k of the face fluxes: own faces from the record, fine faces
+  // from the two fine faces' published fluxes
+  const int     dslf = face == 0 ? dsl[0] : face == 1 ? dsl[1] : face == 2 ? dsl[2] : dsl[3];
+  float         F0[4], F1[4];
+#pragma unroll
+  for (int f = 0; f < 4; ++f)
+  {
+    F0[f] = 0.0f;
+    F1[f] = 0.0f;
+    if (act)
+    {
+      const int ct = (f >> 1) == 0 ? cj : ci;
+      const int fl = 2 * ct - ((2 * ct) / B) * B;
+      if (fine[f])
+      {
+        const float * p0 = reinterpret_cast<const float *>(a.reflux_buf) + ((size_t)rs[f] * B + fl) * 8;
+        F0[f] = p0[k];
+        F1[f] = p0[8 + k];
+      }
+      else
+        F0[f] = reinterpret_cast<const float *>(a.defer_buf)[((size_t)dslf * B + pos) * 32 + f * 8 + k];
+    }
+  }
+  // the whole old state in every lane of the group
+  double uin[H::NV];
+#pragma unroll
+  for (int v = 0; v < H::NV; ++v)
+    uin[v] = __shfl_sync(0xffffffffu, u_own, gb + lane_of[v]);
+  const bool stiff = a.p.gpx[0] != 0.0 || a.p.gpx[1] != 0.0;
+  float      a0f = d2f_fast(uin[H::IA0]), a1f = d2f_fast(uin[H::IA1]);
+  {
+    float st0f, st1f;
+    source_factors_mixed<2>(uin, a.p, stiff, st0f, st1f);
+    a0f *= st0f;
+    a1f *= st1f;
+  }
+  // per direction: this component's side values (a fine side is the exact
+  // float-float sum of its two fine faces, / 4)
+  float Fh[2][2], Fl[2][2];
+#pragma unroll
+  for (int dir = 0; dir < 2; ++dir)
+#pragma unroll
+    for (int side = 0; side < 2; ++side)
+    {
+      const int f = 2 * dir + side;
+      if (fine[f])
+      {
+        float sh, sl;
+        two_sum(F0[f], F1[f], sh, sl);
+        Fh[dir][side] = 0.25f * sh;
+        Fl[dir][side] = 0.25f * sl;
+      }
+      else
+      {
+        Fh[dir][side] = F0[f];
+        Fl[dir][side] = 0.0f;
+      }
+    }
+  // u* of both sides (lane FUS) for the volume-fraction source term
+  float usl[2], usr[2];
+#pragma unroll
+  for (int dir = 0; dir < 2; ++dir)
+  {
+    usl[dir] = __shfl_sync(0xffffffffu, Fh[dir][0] + Fl[dir][0], gb + H::FUS);
+    usr[dir] = __shfl_sync(0xffffffffu, Fh[dir][1] + Fl[dir][1], gb + H::FUS);
+  }
+  const double eps = 1e-12, one_m_eps = 1.0 - 1e-12;
+  double       u2v = u_own;
+  if (k == H::FR0 || k == H::FR1 || k == H::FE || k == H::FU || k == H::FV)
+  {
+    float h[2], l[2];
+#pragma unroll
+    for (int dir = 0; dir < 2; ++dir)
+    {
+      float hh, ll;
+      two_diff(Fh[dir][0], Fh[dir][1], hh, ll);
+      h[dir] = hh;
+      l[dir] = ll + (Fl[dir][0] - Fl[dir][1]);
+    }
+    const bool  clamp = k == H::FR0 || k == H::FR1;
+    const float uf = d2f_fast(u2v);
+    if (!clamp || uf > 2.0f * fabsf(h[0]) + 2e-12f)
+    {
+      float s, t;
+      two_sum(h[0], h[1], s, t);
+      two_sum(s, t + (l[0] + l[1]), s, t);
+      u2v += ff_to_d(s, t);
+      if (clamp && dlt_pos(u2v, eps))
+        u2v = 0.0;
+    }
+    else
+    {
+#pragma unroll
+      for (int dir = 0; dir < 2; ++dir)
+      {
+        u2v = (u2v + f2d_exact(h[dir])) + f2d_exact(l[dir]);
+        if (dlt_pos(u2v, eps))
+          u2v = 0.0;
+      }
+    }
+  }
+  else if (k == H::FA0 || k == H::FA1)
+  {
+    const float af_src = k == H::FA0 ? a0f : a1f;
+    float       dA[2];
+#pragma unroll
+    for (int dir = 0; dir < 2; ++dir)
+      dA[dir] = (((Fh[dir][0] + Fl[dir][0]) - usl[dir] * af_src) - (Fh[dir][1] + Fl[dir][1])) + usr[dir] * af_src;
+    const float af = d2f_fast(uin[var]);
+    const float m = 2.0f * fabsf(dA[0]) + 2e-12f;
+    if (af > m && af + m < 1.0f)
+    {
+      u2v += f2d_exact(dA[0] + dA[1]);
+      if (dlt_pos(u2v, eps))
+        u2v = 0.0;
+      if (dgt_pos(u2v, one_m_eps))
+        u2v = 1.0;
+    }
+    else
+    {
+#pragma unroll
+      for (int dir = 0; dir < 2; ++dir)
+      {
+        u2v += f2d_exact(dA[dir]);
+        if (dlt_pos(u2v, eps))
+          u2v = 0.0;
+        if (dgt_pos(u2v, one_m_eps))
+          u2v = 1.0;
+      }
+    }
+  }
+  // renormalisation of the volume fractions (lanes FA0 and FA1)
+  {
+    const double a0n = __shfl_sync(0xffffffffu, u2v, gb + H::FA0);
+    const double a1n = __shfl_sync(0xffffffffu, u2v, gb + H::FA1);
+    const double sa = a0n + a1n;
+    const double d = sa - 1.0;
+    if ((k == H::FA0 || k == H::FA1) && d != 0.0)
+    {
+      if ((__double_as_longlong(d) & 0x7FFFFFFFFFFFFFFFLL) < __double_as_longlong(1e-8))
+        u2v = fma(-u2v, d, u2v);
+      else
+        u2v *= 1.0 / sa;
+    }
+  }
+  // ID = IAD0 + IAD1 (lane FUS)
+  {
+    const double r0n = __shfl_sync(0xffffffffu, u2v, gb + H::FR0);
+    const double r1n = __shfl_sync(0xffffffffu, u2v, gb + H::FR1);
+    if (k == H::FUS)
+      u2v = r0n + r1n;
+  }
+  // the new state in every lane: CFL rate of the cell, twin patches
+  double u2[H::NV];
+#pragma unroll
+  for (int v = 0; v < H::NV; ++v)
+    u2[v] = __shfl_sync(0xffffffffu, u2v, gb + lane_of[v]);
+  if (act)
+  {
+    a.U2[((size_t)n * H::NV + var) * NC + cell] = u2v;
+    if (!finite_bits(u2v))
+      raise_status(a.status, STATUS_NONPHYSICAL);
+    if (a.fill_twins && k == 0)
+      patch_twins_2d<B>(a, n, ci, cj, u2);
+  }
+  if (a.invdt)
+  {
+    float m_inv = 0.0f;
+    if (act && k == 0)
+    {
+      float       df, ux, uy, uz, a0;
+      const float p = pressure_mixed<2>(u2, a.p, stiff, df, ux, uy, uz, a0);
+      const float a0s = fmaxf(0.0f, fminf(1.0f, a0));
+      const float c = sound_speed_f(a.p.f_xi[0], a.p.f_xi[1], a.p.f_gpx[0], a.p.f_gpx[1], df, p, a0s);
+      m_inv = ((c + fabsf(ux)) + (c + fabsf(uy))) * __frcp_rn(d2f_fast(a.p.level_dx[r3.y]));
+    }
+    atomic_max_pos_warp(a.invdt, ins, (double)m_inv);
+  }
+}
+
 } // namespace g5

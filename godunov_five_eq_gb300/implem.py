@@ -126,6 +126,10 @@ EXPORTS = [
     "g5_refine_flags",
     "g5_status",
     "g5_tune",
+    "g5_tune_pick",
+    "g5_tune_choice",
+    "g5_tune_report",
+    "g5_set_shape",
     "g5_last_launch_count",
     "g5_step_static",
     "g5_remap",
@@ -178,6 +182,10 @@ def load_library(build_if_missing: bool = True):
     L.g5_refine_flags.argtypes = [vp, vp, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int, vp, vp]
     L.g5_status.argtypes = [vp, vp]
     L.g5_tune.argtypes = [vp, vp, vp, ctypes.c_int, vp]
+    L.g5_tune_pick.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_float]
+    L.g5_tune_choice.argtypes = [vp, ctypes.c_int, vp]
+    L.g5_tune_report.argtypes = [vp, ctypes.c_int, vp, vp, ctypes.c_int]
+    L.g5_set_shape.argtypes = [vp, ctypes.c_int, vp]
     L.g5_last_launch_count.argtypes = [vp]
     L.g5_remap.argtypes = [vp, ctypes.POINTER(G5Remap), vp, vp, vp]
     L.g5_step_static.argtypes = [ctypes.POINTER(G5Params), ctypes.POINTER(G5Mesh), vp, vp, vp, ctypes.c_int, vp, vp, vp]
@@ -499,14 +507,56 @@ class GodunovImplemGB300:
             raise G5Error(rc, "g5_status")
         return rc
 
-    def tune(self, U, U2, mode="fp64", stream=None) -> int:
+    def tune(self, U, U2, mode="fp64", stream=None) -> dict:
+        """g5_tune: time the candidate launch shapes of `mode` on U -> U2 (U2
+        is overwritten) and keep the fastest; returns the chosen shape."""
         rc = self.lib.g5_tune(self.ctx, ctypes.c_void_p(_dptr(U)), ctypes.c_void_p(_dptr(U2)), MODES[mode], _stream(stream))
         if rc < 0:
             raise G5Error(rc, "g5_tune")
-        return rc
+        return self.tune_choice(mode)
+
+    SHAPE_KEYS = ("ctas_per_sm", "claim", "walk_cf_first", "reflux_one_thread_per_cell")
+
+    def tune_choice(self, mode="fp64") -> dict:
+        out = (ctypes.c_int32 * 4)()
+        rc = self.lib.g5_tune_choice(self.ctx, MODES[mode], out)
+        if rc != 0:
+            raise G5Error(rc, "g5_tune_choice")
+        return dict(zip(self.SHAPE_KEYS, [int(v) for v in out]))
+
+    def tune_report(self, mode="fp64") -> list:
+        """[(shape dict, ms per step)] of the last g5_tune of `mode`."""
+        n = self.lib.g5_tune_report(self.ctx, MODES[mode], None, None, 0)
+        if n < 0:
+            raise G5Error(n, "g5_tune_report")
+        shapes = (ctypes.c_int32 * max(n, 1))()
+        ms = (ctypes.c_float * max(n, 1))()
+        self.lib.g5_tune_report(self.ctx, MODES[mode], shapes, ms, n)
+        return [(unpack_shape(int(shapes[i])), float(ms[i])) for i in range(n)]
+
+    def set_shape(self, mode="fp64", ctas_per_sm=0, claim=1, walk_cf_first=1, reflux_one_thread_per_cell=0):
+        arr = (ctypes.c_int32 * 4)(ctas_per_sm, claim, walk_cf_first, reflux_one_thread_per_cell)
+        rc = self.lib.g5_set_shape(self.ctx, MODES[mode], arr)
+        if rc != 0:
+            raise G5Error(rc, "g5_set_shape")
 
     def last_launch_count(self) -> int:
         return int(self.lib.g5_last_launch_count(self.ctx))
+
+
+def unpack_shape(code: int) -> dict:
+    """A packed launch shape of g5_tune (ctas_per_sm + 16 claim + 32 walk + 64 reflux)."""
+    return {"ctas_per_sm": code & 15, "claim": (code >> 4) & 1, "walk_cf_first": (code >> 5) & 1, "reflux_one_thread_per_cell": (code >> 6) & 1}
+
+
+def tune_pick(ms, default_index, margin=0.02) -> int:
+    """The tuner's selection rule (g5_tune_pick, host only)."""
+    lib = load_library()
+    arr = (ctypes.c_float * len(ms))(*ms)
+    rc = lib.g5_tune_pick(arr, len(ms), int(default_index), float(margin))
+    if rc < 0:
+        raise G5Error(rc, "g5_tune_pick")
+    return rc
 
 
 def gpu_flag_fn(indicator=0, eps_refine=0.1, eps_coarsen=0.0125, eps_lohner=0.02):

@@ -293,10 +293,39 @@ int g5_remap(G5Context * ctx, const G5Remap * remap, const double * d_Uold, doub
  * Returns the G5_STATUS_* bits (>= 0) or a negative error. */
 int g5_status(G5Context * ctx, void * stream);
 
-/* Autotune the launch shape (CTAs per SM of the persistent step kernel) for
- * the current mesh: times each candidate on d_U -> d_U2 and keeps the best.
- * Returns the chosen CTAs per SM (> 0) or a negative error. */
+/* Autotune the launch shape of the step for the current mesh and one
+ * precision mode (no counterpart in the reference, whose Kokkos policies are
+ * fixed).  Candidates: CTAs per SM of the persistent step kernel (1 up to the
+ * occupancy maximum), dynamic block claiming on or off, the block walk order
+ * (blocks with coarse/fine neighbours first, or table order) and, for the
+ * FP32-bulk 2D pass over coarse/fine records, its layout (8 lanes or one
+ * thread per deferred cell).  Every candidate computes the same values bit for
+ * bit.  Each is timed twice on d_U -> d_U2 (3 steps after a warm-up, CUDA
+ * events on `stream`), and g5_tune_pick chooses with a 2 % margin in favour of
+ * the default shape.  The choice is kept by the context for that mode
+ * (across g5_set_mesh) until the next g5_tune or g5_set_shape.  Synchronises
+ * the stream; d_U2 is overwritten.  Returns the packed shape
+ * (ctas_per_sm + 16 claim + 32 walk + 64 reflux layout, > 0) or a negative
+ * error. */
 int g5_tune(G5Context * ctx, const double * d_U, double * d_U2, int mode, void * stream);
+
+/* The tuner's selection rule, host only: the index of the smallest positive
+ * time of ms[n], except that the default index stays chosen while its time is
+ * within (1 + margin) of the smallest.  Negative on bad arguments. */
+int g5_tune_pick(const float * ms, int n, int default_index, float margin);
+
+/* The launch shape a mode uses: out4 = {CTAs per SM, claim, walk order,
+ * reflux layout}. */
+int g5_tune_choice(const G5Context * ctx, int mode, int32_t * out4);
+
+/* The candidates and their times (ms per step) of the last g5_tune of a mode:
+ * up to cap entries (packed shapes as g5_tune returns them); returns the
+ * number of candidates. */
+int g5_tune_report(const G5Context * ctx, int mode, int32_t * shapes, float * ms, int cap);
+
+/* Set the launch shape of a mode by hand (shape4 as g5_tune_choice gives it;
+ * CTAs per SM 0 = the occupancy maximum). */
+int g5_set_shape(G5Context * ctx, int mode, const int32_t * shape4);
 
 /* Number of kernel launches issued by the last g5_step / g5_advance / g5_run call. */
 int g5_last_launch_count(const G5Context * ctx);

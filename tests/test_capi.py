@@ -38,3 +38,21 @@ def test_invalid_params_rejected_without_device():
     assert lib.g5_create(ctypes.byref(p), ctypes.byref(ctx)) == -1
     assert lib.g5_create(None, ctypes.byref(ctx)) == -1
     assert lib.g5_destroy(None) == -1
+
+
+def test_tune_pick_selection_rule():
+    """g5_tune's selection (host only): the fastest candidate, but the default
+    shape stays while it is within the margin of the fastest."""
+    from godunov_five_eq_gb300.implem import G5Error, tune_pick, unpack_shape
+
+    assert tune_pick([3.0, 2.0, 2.5], default_index=0) == 1
+    assert tune_pick([2.03, 2.0, 2.5], default_index=0, margin=0.02) == 0  # within 2 %
+    assert tune_pick([2.05, 2.0, 2.5], default_index=0, margin=0.02) == 1
+    assert tune_pick([0.0, 2.0, 1.0], default_index=1) == 2  # a failed (zero) timing never wins
+    assert tune_pick([5.0], default_index=0) == 0
+    with pytest.raises(G5Error):
+        tune_pick([1.0, 2.0], default_index=2)
+    with pytest.raises(G5Error):
+        tune_pick([0.0, 0.0], default_index=0)
+    assert unpack_shape(4 + 16 + 32) == {"ctas_per_sm": 4, "claim": 1, "walk_cf_first": 1, "reflux_one_thread_per_cell": 0}
+    assert unpack_shape(2 + 64) == {"ctas_per_sm": 2, "claim": 0, "walk_cf_first": 0, "reflux_one_thread_per_cell": 1}
