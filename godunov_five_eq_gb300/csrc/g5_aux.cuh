@@ -112,7 +112,7 @@ rk2_combine_kernel(const double * U, double * U2, DevMesh m, PhysParams P, doubl
   constexpr int NC = (DIM == 2) ? B * B : B * B * B;
   using DtT = typename std::conditional<MIXED, float, double>::type;
   __shared__ DtT sred[32];
-  const bool     stiff = P.gpx[0] != 0.0 || P.gpx[1] != 0.0;
+  const int      eosk = P.mg_any ? 2 : ((P.gpx[0] != 0.0 || P.gpx[1] != 0.0) ? 1 : 0);
   for (int n = blockIdx.x; n < m.n_owned; n += gridDim.x)
   {
     const double dx = P.level_dx[m.level[n]];
@@ -129,8 +129,8 @@ rk2_combine_kernel(const double * U, double * U2, DevMesh m, PhysParams P, doubl
       if constexpr (MIXED)
       {
         float       d, ux, uy, uz, a0;
-        const float p = pressure_mixed<DIM>(u, P, stiff, d, ux, uy, uz, a0);
-        const float cs = sound_speed_f(P.f_xi[0], P.f_xi[1], P.f_gpx[0], P.f_gpx[1], d, p, fmaxf(0.0f, fminf(1.0f, a0)));
+        const float p = pressure_mixed<DIM>(u, P, eosk, d, ux, uy, uz, a0);
+        const float cs = sound_speed_eos(P, eosk, d, p, fmaxf(0.0f, fminf(1.0f, a0)), d2f_fast(u[H::IAD0]), d2f_fast(u[H::IAD1]));
         float       r = (cs + fabsf(ux)) + (cs + fabsf(uy));
         if constexpr (DIM == 3)
           r += cs + fabsf(uz);

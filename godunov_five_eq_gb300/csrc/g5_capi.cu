@@ -258,8 +258,6 @@ do_step(G5Context * c, const double * U, double * U2, const double * d_dt, int m
     return G5_ERR_ARG;
   if (mode != G5_MODE_FP64 && mode != G5_MODE_MIXED)
     return G5_ERR_ARG;
-  if (mode == G5_MODE_MIXED && c->phys.mg_any)
-    return G5_ERR_UNSUPPORTED; // the FP32-bulk form is written for stiffened gases
   if (!g5::step_supported(c->dim, c->b))
     return G5_ERR_UNSUPPORTED;
   g5::StepArgs a;
@@ -810,8 +808,6 @@ g5_step_batched(G5Context * c, const double * d_U, double * d_U2, const double *
     return G5_ERR_ARG;
   if (mode != G5_MODE_FP64 && mode != G5_MODE_MIXED)
     return G5_ERR_ARG;
-  if (mode == G5_MODE_MIXED && c->phys.mg_any)
-    return G5_ERR_UNSUPPORTED; // the FP32-bulk form is written for stiffened gases
   if (!g5::step_supported(c->dim, c->b))
     return G5_ERR_UNSUPPORTED;
   std::vector<uint8_t> active((size_t)c->n_inst, 0);
@@ -862,8 +858,6 @@ g5_step_host(G5Context * c, const double * h_U, double * h_U2, const double * dt
     return G5_ERR_ARG;
   if (mode != G5_MODE_FP64 && mode != G5_MODE_MIXED)
     return G5_ERR_ARG;
-  if (mode == G5_MODE_MIXED && c->phys.mg_any)
-    return G5_ERR_UNSUPPORTED; // the FP32-bulk form is written for stiffened gases
   for (int i = 0; i < c->n_inst; ++i)
     if (!(dt_host[i] > 0.0))
       return G5_ERR_ARG;
@@ -1214,8 +1208,6 @@ g5_advance(G5Context * c, const double * d_U, double * d_U2, int mode, double * 
     return G5_ERR_ARG;
   if (mode != G5_MODE_FP64 && mode != G5_MODE_MIXED)
     return G5_ERR_ARG;
-  if (mode == G5_MODE_MIXED && c->phys.mg_any)
-    return G5_ERR_UNSUPPORTED; // the FP32-bulk form is written for stiffened gases
   cudaStream_t s = (cudaStream_t)stream;
   // cached graph of one loop step for (U, U2, mode, dt_out)
   G5Context::GraphSlot * slot = nullptr;
@@ -1276,8 +1268,6 @@ g5_run(G5Context * c, double * d_U, double * d_U2, int nsteps, int mode, double 
     return G5_ERR_ARG;
   if (mode != G5_MODE_FP64 && mode != G5_MODE_MIXED)
     return G5_ERR_ARG;
-  if (mode == G5_MODE_MIXED && c->phys.mg_any)
-    return G5_ERR_UNSUPPORTED; // the FP32-bulk form is written for stiffened gases
   cudaStream_t s = (cudaStream_t)stream;
   int          rc = g5_begin(c, d_U, stream);
   if (rc)
@@ -1356,8 +1346,6 @@ g5_tune(G5Context * c, const double * d_U, double * d_U2, int mode, void * strea
 {
   if (!c || !c->has_mesh || !d_U || !d_U2 || (mode != G5_MODE_FP64 && mode != G5_MODE_MIXED))
     return G5_ERR_ARG;
-  if (mode == G5_MODE_MIXED && c->phys.mg_any)
-    return G5_ERR_UNSUPPORTED; // the FP32-bulk form is written for stiffened gases
   cudaStream_t s = (cudaStream_t)stream;
   const int    occ = mode == G5_MODE_FP64 ? g5::step_max_ctas_per_sm_fp64(c->dim, c->b) : g5::step_max_ctas_per_sm_mixed(c->dim, c->b);
   if (occ <= 0)

@@ -38,6 +38,9 @@ struct PhysParams
   int    mg_any;
   double mg[2][8];
   double mg_rho0[2];
+  float  f_mg[2][8]; // FP32 copies for the FP32-bulk path
+  float  f_mg_rho0[2];
+  float  f_gm1[2], f_gpinf[2]; // gamma_k - 1 and gamma_k pinf_k (stiffened-gas law in the mixture rules)
   // ghost cells in a coarser neighbour: 0 SIMPLE_COPY, 1 EXTRAPOLATE_LINEAR_MINMOD,
   // 2 / 3 CONSERVATIVE_INTERPOLATION_ORDER_2 / 4
   int prolong;
@@ -729,14 +732,163 @@ hllc_fp64(const double * ql, const double * qr, const PhysParams & P, double * f
 // HLLC in FP32.  The p -> e -> p round trip of the reference is an identity
 // in exact arithmetic and is dropped here (in FP32 it would cancel the
 // stiffened-gas constant against p S).
+// ---------------------------------------------------------------------------
+// FP32 forms of the Mie-Grueneisen laws and mixture rules above (the
+// FP32-bulk path: fast-math exp and log), same formulas and order
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void
+mg_law_f(const PhysParams & P, int k, float rho, float & G, float & dG, float & f, float & df)
+{
+  const float * c = P.f_mg[k];
+  const int     kind = P.eos_kind[k];
+  if (kind == EOS_JWL)
+  {
+    const float rho0 = c[0], w = c[1], A1 = c[2], A2 = c[3], R1 = c[4], R2 = c[5], e0 = c[6];
+    const float irho = __frcp_rn(rho);
+    const float x1 = R1 * rho0 * irho, x2 = R2 * rho0 * irho;
+    const float E1 = __expf(-x1), E2 = __expf(-x2);
+    G = w;
+    dG = 0.0f;
+    f = A1 * (1.0f - __fdividef(w, x1)) * E1 + A2 * (1.0f - __fdividef(w, x2)) * E2 - w * rho * e0;
+    df = (A1 * E1 * (x1 - w - __fdividef(w, x1)) + A2 * E2 * (x2 - w - __fdividef(w, x2))) * irho - w * e0;
+  }
+  else if (kind == EOS_SHOCKWAVE)
+  {
+    const float rho0 = c[0], g0 = c[1], c0 = c[2], s1 = c[3], s2 = c[4], s3 = c[5], b = c[6], e0 = c[7];
+    const float mu = __fdividef(rho, rho0) - 1.0f;
+    const float K = rho0 * c0 * c0;
+    float       pc, dpc;
+    if (mu > 0.0f)
+    {
+      const float m1 = mu + 1.0f;
+      const float im1 = __frcp_rn(m1);
+      const float N = 1.0f + (1.0f - 0.5f * g0) * mu - 0.5f * b * mu * mu;
+      const float Np = (1.0f - 0.5f * g0) - b * mu;
+      const float D = 1.0f - (s1 - 1.0f) * mu - s2 * mu * mu * im1 - s3 * mu * mu * mu * im1 * im1;
+      const float Dp = -(s1 - 1.0f) - s2 * (mu * mu + 2.0f * mu) * im1 * im1 - s3 * (mu * mu * mu + 3.0f * mu * mu) * im1 * im1 * im1;
+      const float iD = __frcp_rn(D);
+      pc = K * mu * N * iD * iD;
+      dpc = K * ((N + mu * Np) * iD * iD - 2.0f * mu * N * Dp * iD * iD * iD);
+    }
+    else
+    {
+      pc = K * mu;
+      dpc = K;
+    }
+    const float gr = (g0 + b * mu) * rho0;
+    const float irho = __frcp_rn(rho);
+    G = gr * irho;
+    dG = (b - G) * irho;
+    f = pc - gr * e0;
+    df = __fdividef(dpc, rho0) - b * e0;
+  }
+  else if (kind == EOS_SHOCKWAVE2)
+  {
+    const float rho0 = c[0], g0 = c[1], c0 = c[2], sl = c[3], al = c[4], e0 = c[5], p0 = c[6];
+    const float irho = __frcp_rn(rho);
+    const float v = rho0 * irho;
+    const float eta = 1.0f - v;
+    const float w = 1.0f - sl * eta;
+    const float iw = __frcp_rn(w);
+    const float K = rho0 * c0 * c0;
+    const float pH = p0 + K * eta * iw * iw;
+    const float eH = e0 + __fdividef((pH + p0) * eta, 2.0f * rho0);
+    const float gp = al == 1.0f ? v : (al == 0.0f ? 1.0f : __expf(al * __logf(v)));
+    G = g0 * gp;
+    dG = -al * G * irho;
+    const float dpH = K * (1.0f + sl * eta) * iw * iw * iw;
+    const float deH = __fdividef(dpH * eta + pH + p0, 2.0f * rho0);
+    const float deta = v * irho;
+    f = pH - G * rho * eH;
+    df = dpH * deta - (dG * rho + G) * eH - G * rho * deH * deta;
+  }
+  else
+  {
+    G = P.f_gm1[k];
+    dG = 0.0f;
+    f = -P.f_gpinf[k];
+    df = 0.0f;
+  }
+}
+
+__device__ __forceinline__ float
+mg_material_density_f(const PhysParams & P, int k, float a, float ar)
+{
+  return a > 0.0f ? fmaxf(__fdividef(ar, a), P.f_smallr) : P.f_mg_rho0[k];
+}
+
+__device__ __forceinline__ void
+mg_mixture_f(const PhysParams & P, float a0, float a1, float ar0, float ar1, float & S, float & PI, float & C1, float & C0)
+{
+  S = 0.0f;
+  PI = 0.0f;
+  C1 = 0.0f;
+  C0 = 0.0f;
+#pragma unroll
+  for (int k = 0; k < 2; ++k)
+  {
+    const float a = k == 0 ? a0 : a1;
+    const float rho = mg_material_density_f(P, k, a, k == 0 ? ar0 : ar1);
+    float       G, dG, f, df;
+    mg_law_f(P, k, rho, G, dG, f, df);
+    const float xi = __frcp_rn(G);
+    const float h = xi * (1.0f + rho * dG * xi);
+    S = S + a * xi;
+    PI = PI - a * xi * f;
+    C1 = C1 + a * (h + 1.0f);
+    C0 = C0 + a * (xi * rho * df - h * f);
+  }
+}
+
+__device__ __forceinline__ float
+mg_bulk_modulus_f(const PhysParams & P, int k, float a, float ar, float p)
+{
+  const float rho = mg_material_density_f(P, k, a, ar);
+  float       G, dG, f, df;
+  mg_law_f(P, k, rho, G, dG, f, df);
+  return (1.0f + __fdividef(rho * dG, G)) * (p - f) + rho * df + G * p;
+}
+
+// FP32 mixture sound speed: eosk 2 takes the Mie-Grueneisen mixture rules
+// from the partial densities, otherwise the stiffened-gas form
+__device__ __forceinline__ float
+sound_speed_eos(const PhysParams & P, int eosk, float rho, float p, float a0, float r0, float r1)
+{
+  if (eosk == 2)
+  {
+    float S, PI, C1, C0;
+    mg_mixture_f(P, a0, 1.0f - a0, r0, r1, S, PI, C1, C0);
+    return sqrtf(fmaxf(__fdividef(p * C1 + C0, rho * S), 0.0f));
+  }
+  return sound_speed_f(P.f_xi[0], P.f_xi[1], P.f_gpx[0], P.f_gpx[1], rho, p, a0);
+}
+
 template <int DIM>
 __device__ __forceinline__ void
-hllc_fp32(const float * ql, const float * qr, float xi0, float xi1, float gp0, float gp1, float smallr, float smallp, float smallc, float * f)
+hllc_fp32(const float * ql, const float * qr, float xi0, float xi1, float gp0, float gp1, float smallr, float smallp, float smallc, float * f,
+          const PhysParams * Pmg = nullptr)
 {
   using H = V<DIM>;
   const float al = ql[H::QA], ar = qr[H::QA];
-  const float Sl = al * xi0 + (1.0f - al) * xi1, PIl = al * gp0 + (1.0f - al) * gp1;
-  const float Sr = ar * xi0 + (1.0f - ar) * xi1, PIr = ar * gp0 + (1.0f - ar) * gp1;
+  // mixture rules of each side: S, PI and the sound-speed coefficients C1, C0
+  // (rho c^2 S = p C1 + C0; stiffened gases: C1 = S + 1, C0 = PI)
+  float Sl, PIl, C1l, C0l, Sr, PIr, C1r, C0r;
+  if (Pmg)
+  {
+    mg_mixture_f(*Pmg, al, 1.0f - al, ql[H::QR0], ql[H::QR1], Sl, PIl, C1l, C0l);
+    mg_mixture_f(*Pmg, ar, 1.0f - ar, qr[H::QR0], qr[H::QR1], Sr, PIr, C1r, C0r);
+  }
+  else
+  {
+    Sl = al * xi0 + (1.0f - al) * xi1;
+    PIl = al * gp0 + (1.0f - al) * gp1;
+    Sr = ar * xi0 + (1.0f - ar) * xi1;
+    PIr = ar * gp0 + (1.0f - ar) * gp1;
+    C1l = Sl + 1.0f;
+    C0l = PIl;
+    C1r = Sr + 1.0f;
+    C0r = PIr;
+  }
 
   const float rl = fmaxf(ql[H::QR0] + ql[H::QR1], smallr);
   const float pl = fmaxf(ql[H::QP], rl * smallp);
@@ -745,7 +897,7 @@ hllc_fp32(const float * ql, const float * qr, float xi0, float xi1, float gp0, f
   if constexpr (DIM == 3)
     k2l += ql[H::QW] * ql[H::QW];
   const float rel = pl * Sl + PIl; // rho e
-  const float cl = sqrtf(fmaxf(__fdividef(pl * (Sl + 1.0f) + PIl, rl * Sl), 0.0f));
+  const float cl = sqrtf(fmaxf(__fdividef(pl * C1l + C0l, rl * Sl), 0.0f));
   const float etotl = rel + 0.5f * rl * k2l;
 
   const float rr = fmaxf(qr[H::QR0] + qr[H::QR1], smallr);
@@ -755,7 +907,7 @@ hllc_fp32(const float * ql, const float * qr, float xi0, float xi1, float gp0, f
   if constexpr (DIM == 3)
     k2r += qr[H::QW] * qr[H::QW];
   const float rer = pr * Sr + PIr;
-  const float cr = sqrtf(fmaxf(__fdividef(pr * (Sr + 1.0f) + PIr, rr * Sr), 0.0f));
+  const float cr = sqrtf(fmaxf(__fdividef(pr * C1r + C0r, rr * Sr), 0.0f));
   const float etotr = rer + 0.5f * rr * k2r;
 
   const float cf = fmaxf(fmaxf(cl, smallc), fmaxf(cr, smallc));
@@ -974,11 +1126,12 @@ finite_bits(double x)
 }
 
 // mixture pressure from a conservative state: FP32 except the numerator
-// rho e - PI when a stiffened-gas constant makes it cancel (FP64 then).
-// Returns p; also the FP32 density and velocities.
+// rho e - PI when it can cancel (FP64 then): eosk 0 ideal gases, 1 a
+// stiffened-gas constant, 2 Mie-Grueneisen laws (S and PI from the partial
+// densities).  Returns p; also the FP32 density and velocities.
 template <int DIM>
 __device__ __forceinline__ float
-pressure_mixed(const double * u, const PhysParams & P, bool stiff, float & d, float & ux, float & uy, float & uz, float & a0f)
+pressure_mixed(const double * u, const PhysParams & P, int eosk, float & d, float & ux, float & uy, float & uz, float & a0f)
 {
   using H = V<DIM>;
   d = fmaxf(d2f_nan(u[H::ID]), P.f_smallr);
@@ -996,7 +1149,14 @@ pressure_mixed(const double * u, const PhysParams & P, bool stiff, float & d, fl
   a0f = d2f_nan(a0u);
   const float K = 0.5f * d * k2;
   float       num;
-  if (stiff)
+  if (eosk == 2)
+  {
+    float S, PI, C1, C0;
+    mg_mixture_f(P, a0f, 1.0f - a0f, d2f_nan(u[H::IAD0]), d2f_nan(u[H::IAD1]), S, PI, C1, C0);
+    num = d2f_nan((u[H::IE] - f2d_exact(PI)) - f2d_exact(K));
+    return __fdividef(num, S);
+  }
+  if (eosk == 1)
   {
     const double PI = fma(a0u, P.dgpx, P.gpx[1]);
     num = d2f_nan((u[H::IE] - PI) - f2d_exact(K));
@@ -1009,7 +1169,7 @@ pressure_mixed(const double * u, const PhysParams & P, bool stiff, float & d, fl
 // FP32 form of the source-term factors (see source_factors_fp64)
 template <int DIM>
 __device__ __forceinline__ void
-source_factors_mixed(const double * u, const PhysParams & P, bool stiff, float & st0, float & st1)
+source_factors_mixed(const double * u, const PhysParams & P, int eosk, float & st0, float & st1)
 {
   using H = V<DIM>;
   if (P.source_term != 1)
@@ -1018,9 +1178,18 @@ source_factors_mixed(const double * u, const PhysParams & P, bool stiff, float &
     return;
   }
   float       d, ux, uy, uz, a0f;
-  const float p = pressure_mixed<DIM>(u, P, stiff, d, ux, uy, uz, a0f);
-  const float K0 = (float)P.gamma[0] * (p + (float)P.pinf[0]);
-  const float K1 = (float)P.gamma[1] * (p + (float)P.pinf[1]);
+  const float p = pressure_mixed<DIM>(u, P, eosk, d, ux, uy, uz, a0f);
+  float       K0, K1;
+  if (eosk == 2)
+  {
+    K0 = mg_bulk_modulus_f(P, 0, a0f, d2f_nan(u[H::IAD0]), p);
+    K1 = mg_bulk_modulus_f(P, 1, d2f_nan(u[H::IA1]), d2f_nan(u[H::IAD1]), p);
+  }
+  else
+  {
+    K0 = (float)P.gamma[0] * (p + (float)P.pinf[0]);
+    K1 = (float)P.gamma[1] * (p + (float)P.pinf[1]);
+  }
   const float kbar = __frcp_rn(a0f * __frcp_rn(K0) + d2f_nan(u[H::IA1]) * __frcp_rn(K1));
   st0 = 1.0f - kbar * __frcp_rn(K0);
   st1 = 1.0f - kbar * __frcp_rn(K1);
@@ -1029,11 +1198,11 @@ source_factors_mixed(const double * u, const PhysParams & P, bool stiff, float &
 // FP32-bulk conservative -> primitive (computePrimitives, models/utils.h:200-250)
 template <int DIM>
 __device__ __forceinline__ void
-prim_mixed(const double * u, float * q, const PhysParams & P, bool stiff)
+prim_mixed(const double * u, float * q, const PhysParams & P, int eosk)
 {
   using H = V<DIM>;
   float       d, ux, uy, uz, a0f;
-  const float p = pressure_mixed<DIM>(u, P, stiff, d, ux, uy, uz, a0f);
+  const float p = pressure_mixed<DIM>(u, P, eosk, d, ux, uy, uz, a0f);
   float       a0 = fmaxf(0.0f, fminf(1.0f, a0f));
   float       r0 = d2f_nan(u[H::IAD0]), r1 = d2f_nan(u[H::IAD1]);
   const float eps = 1e-12f;

@@ -87,6 +87,8 @@ occupancy2d_m()
   one((const void *)step2d_kernel<B, true, false, 1>);
   one((const void *)step2d_kernel<B, true, true, 0>);
   one((const void *)step2d_kernel<B, true, true, 1>);
+  one((const void *)step2d_kernel<B, true, false, 2>);
+  one((const void *)step2d_kernel<B, true, true, 2>);
   return occ;
 }
 
@@ -162,29 +164,45 @@ launch_step_mixed(int dim, int b, const StepArgs & a, int ctas_per_sm, cudaStrea
   const cudaError_t e = launch_prolong(dim, b, a, s, launches);
   if (e != cudaSuccess)
     return e;
+  // one kernel per case: THINC on or off, and the equation of state (0 ideal
+  // gases, 1 a stiffened-gas constant, 2 Mie-Grueneisen laws)
+  const int eosk = a.p.mg_any ? 2 : ((a.p.gpx[0] != 0.0 || a.p.gpx[1] != 0.0) ? 1 : 0);
+  const int v = (a.p.thinc ? 3 : 0) + eosk;
   if (dim == 3 && b == 8)
   {
-    const bool stiff = a.p.gpx[0] != 0.0 || a.p.gpx[1] != 0.0;
-    const int  v = (a.p.thinc ? 2 : 0) + (stiff ? 1 : 0);
-    return v == 0 ? launch_step3d_m<0, 0>(a, ctas_per_sm, s, launches)
-         : v == 1 ? launch_step3d_m<0, 1>(a, ctas_per_sm, s, launches)
-         : v == 2 ? launch_step3d_m<1, 0>(a, ctas_per_sm, s, launches)
-                  : launch_step3d_m<1, 1>(a, ctas_per_sm, s, launches);
+    switch (v)
+    {
+      case 0: return launch_step3d_m<0, 0>(a, ctas_per_sm, s, launches);
+      case 1: return launch_step3d_m<0, 1>(a, ctas_per_sm, s, launches);
+      case 2: return launch_step3d_m<0, 2>(a, ctas_per_sm, s, launches);
+      case 3: return launch_step3d_m<1, 0>(a, ctas_per_sm, s, launches);
+      case 4: return launch_step3d_m<1, 1>(a, ctas_per_sm, s, launches);
+      default: return launch_step3d_m<1, 2>(a, ctas_per_sm, s, launches);
+    }
   }
-  if (dim == 2)
+  if (dim == 2 && b == 16)
   {
-    const bool stiff = a.p.gpx[0] != 0.0 || a.p.gpx[1] != 0.0;
-    const int  v = (a.p.thinc ? 2 : 0) + (stiff ? 1 : 0);
-    if (b == 16)
-      return v == 0 ? launch_step2d_m<16, false, 0>(a, ctas_per_sm, s, launches)
-           : v == 1 ? launch_step2d_m<16, false, 1>(a, ctas_per_sm, s, launches)
-           : v == 2 ? launch_step2d_m<16, true, 0>(a, ctas_per_sm, s, launches)
-                    : launch_step2d_m<16, true, 1>(a, ctas_per_sm, s, launches);
-    if (b == 8)
-      return v == 0 ? launch_step2d_m<8, false, 0>(a, ctas_per_sm, s, launches)
-           : v == 1 ? launch_step2d_m<8, false, 1>(a, ctas_per_sm, s, launches)
-           : v == 2 ? launch_step2d_m<8, true, 0>(a, ctas_per_sm, s, launches)
-                    : launch_step2d_m<8, true, 1>(a, ctas_per_sm, s, launches);
+    switch (v)
+    {
+      case 0: return launch_step2d_m<16, false, 0>(a, ctas_per_sm, s, launches);
+      case 1: return launch_step2d_m<16, false, 1>(a, ctas_per_sm, s, launches);
+      case 2: return launch_step2d_m<16, false, 2>(a, ctas_per_sm, s, launches);
+      case 3: return launch_step2d_m<16, true, 0>(a, ctas_per_sm, s, launches);
+      case 4: return launch_step2d_m<16, true, 1>(a, ctas_per_sm, s, launches);
+      default: return launch_step2d_m<16, true, 2>(a, ctas_per_sm, s, launches);
+    }
+  }
+  if (dim == 2 && b == 8)
+  {
+    switch (v)
+    {
+      case 0: return launch_step2d_m<8, false, 0>(a, ctas_per_sm, s, launches);
+      case 1: return launch_step2d_m<8, false, 1>(a, ctas_per_sm, s, launches);
+      case 2: return launch_step2d_m<8, false, 2>(a, ctas_per_sm, s, launches);
+      case 3: return launch_step2d_m<8, true, 0>(a, ctas_per_sm, s, launches);
+      case 4: return launch_step2d_m<8, true, 1>(a, ctas_per_sm, s, launches);
+      default: return launch_step2d_m<8, true, 2>(a, ctas_per_sm, s, launches);
+    }
   }
   return cudaErrorInvalidValue;
 }
@@ -210,6 +228,8 @@ step_max_ctas_per_sm_mixed(int dim, int b)
     one((const void *)step3d_kernel<true, 0, 1>);
     one((const void *)step3d_kernel<true, 1, 0>);
     one((const void *)step3d_kernel<true, 1, 1>);
+    one((const void *)step3d_kernel<true, 0, 2>);
+    one((const void *)step3d_kernel<true, 1, 2>);
     return occ;
   }
   return 0;

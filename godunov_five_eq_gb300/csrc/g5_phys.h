@@ -126,6 +126,11 @@ make_phys(const G5Params * params)
     for (int j = 0; j < 8; ++j)
       p.mg[k][j] = params->mg[k][j];
     p.mg_rho0[k] = params->eos[k] != G5_EOS_STIFFENED ? params->mg[k][0] : 1.0;
+    for (int j = 0; j < 8; ++j)
+      p.f_mg[k][j] = (float)params->mg[k][j];
+    p.f_mg_rho0[k] = (float)p.mg_rho0[k];
+    p.f_gm1[k] = (float)(params->gamma[k] - 1.0);
+    p.f_gpinf[k] = (float)(params->gamma[k] * params->pinf[k]);
   }
   p.mg_any = params->eos[0] != G5_EOS_STIFFENED || params->eos[1] != G5_EOS_STIFFENED;
   p.prolong = params->prolongation;

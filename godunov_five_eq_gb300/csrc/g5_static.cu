@@ -99,8 +99,6 @@ g5_step_static(const G5Params * params,
     return G5_ERR_UNSUPPORTED;
   if (!(params->gamma[0] > 1.0) || !(params->gamma[1] > 1.0) || !g5::eos_params_valid(params))
     return G5_ERR_ARG;
-  if (mode == G5_MODE_MIXED && (params->eos[0] != G5_EOS_STIFFENED || params->eos[1] != G5_EOS_STIFFENED))
-    return G5_ERR_UNSUPPORTED; // the FP32-bulk form is written for stiffened gases
   const int n_owned = mesh->n_owned, n_outside = mesh->n_outside;
   const int n_total = n_owned + n_outside, n_inst = mesh->n_inst > 0 ? mesh->n_inst : 1;
   if (n_owned <= 0 || n_outside < 0 || !mesh->level || !mesh->coord || !mesh->nbr || !mesh->nbr_rel)

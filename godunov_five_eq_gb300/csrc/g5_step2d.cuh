@@ -143,13 +143,13 @@ gather_ghost_2d(const StepArgs & a, int n, int cx0, int cy0, int gx, int gy, dou
 
 template <int B, bool MIXED>
 __device__ __forceinline__ void
-store_prim(typename Step2DTraits<B, MIXED>::R * sQ, int gidx, const double * u, const PhysParams & P, bool stiff)
+store_prim(typename Step2DTraits<B, MIXED>::R * sQ, int gidx, const double * u, const PhysParams & P, int eosk)
 {
   constexpr int GG = (B + 4) * (B + 4);
   if constexpr (MIXED)
   {
     float q[6];
-    prim_mixed<2>(u, q, P, stiff);
+    prim_mixed<2>(u, q, P, eosk);
 #pragma unroll
     for (int k = 0; k < 6; ++k)
       sQ[k * GG + gidx] = q[k];
@@ -340,7 +340,7 @@ face_state_mixed(const float * sQ, const float * sRec, int ci, int cj, int side,
 
 // HLLC flux of one face of the mixed form, scaled by dt/dx into the shared
 // flux arrays; DIR selects the face set (X faces (B+1) x B, Y faces B x (B+1))
-template <int B, int DIR, bool THINC>
+template <int B, int DIR, bool THINC, bool MG>
 __device__ __forceinline__ void
 face_flux_mixed(const float * sQ, const float * sRec, float * sF, int ff, float dtdx, const PhysParams & P)
 {
@@ -375,7 +375,7 @@ face_flux_mixed(const float * sQ, const float * sRec, float * sF, int ff, float 
     qR[3] = qR[4];
     qR[4] = t;
   }
-  hllc_fp32<2>(qL, qR, P.f_xi[0], P.f_xi[1], P.f_gpx[0], P.f_gpx[1], P.f_smallr, P.f_smallp, P.f_smallc, fl);
+  hllc_fp32<2>(qL, qR, P.f_xi[0], P.f_xi[1], P.f_gpx[0], P.f_gpx[1], P.f_smallr, P.f_smallp, P.f_smallc, fl, MG ? &P : nullptr);
   if (DIR == 1)
   {
     const float t = fl[H::FU];
@@ -469,7 +469,7 @@ update_fp64(const double * uin, double * u2, const double * sFx, const double * 
 // the old state on entry.  Returns the CFL rate of the new state (or 0).
 __device__ __forceinline__ float
 apply_mixed_2d(const double * uin, double * u2, const float (&h)[2][5], const float (&l)[2][5], const float (&dA)[2][2], float dx,
-               const PhysParams & P, bool stiff, bool want_dt)
+               const PhysParams & P, int eosk, bool want_dt)
 {
   using H = V<2>;
   const double eps = 1e-12, one_m_eps = 1.0 - 1e-12;
@@ -561,15 +561,15 @@ apply_mixed_2d(const double * uin, double * u2, const float (&h)[2][5], const fl
   if (!want_dt)
     return 0.0f;
   float       df, ux, uy, uz, a0;
-  const float p = pressure_mixed<2>(u2, P, stiff, df, ux, uy, uz, a0);
+  const float p = pressure_mixed<2>(u2, P, eosk, df, ux, uy, uz, a0);
   const float a0s = fmaxf(0.0f, fminf(1.0f, a0));
-  const float c = sound_speed_f(P.f_xi[0], P.f_xi[1], P.f_gpx[0], P.f_gpx[1], df, p, a0s);
+  const float c = sound_speed_eos(P, eosk, df, p, a0s, d2f_fast(u2[H::IAD0]), d2f_fast(u2[H::IAD1]));
   return ((c + fabsf(ux)) + (c + fabsf(uy))) * __frcp_rn(dx);
 }
 
 template <int B>
 __device__ __forceinline__ float
-update_mixed(const double * uin, double * u2, const float * sFx, const float * sFy, int ci, int cj, float dx, const PhysParams & P, bool stiff, bool want_dt)
+update_mixed(const double * uin, double * u2, const float * sFx, const float * sFy, int ci, int cj, float dx, const PhysParams & P, int eosk, bool want_dt)
 {
   using H = V<2>;
   constexpr int NFF = B * (B + 1);
@@ -579,7 +579,7 @@ update_mixed(const double * uin, double * u2, const float * sFx, const float * s
   float        a0f = d2f_fast(uin[H::IA0]), a1f = d2f_fast(uin[H::IA1]);
   {
     float st0, st1;
-    source_factors_mixed<2>(uin, P, stiff, st0, st1);
+    source_factors_mixed<2>(uin, P, eosk, st0, st1);
     a0f *= st0;
     a1f *= st1;
   }
@@ -604,7 +604,7 @@ update_mixed(const double * uin, double * u2, const float * sFx, const float * s
     dA[1][0] = ((sFy[H::FA0 * NFF + ily] - usly * a0f) - sFy[H::FA0 * NFF + iry]) + usry * a0f;
     dA[1][1] = ((sFy[H::FA1 * NFF + ily] - usly * a1f) - sFy[H::FA1 * NFF + iry]) + usry * a1f;
   }
-  return apply_mixed_2d(uin, u2, h, l, dA, dx, P, stiff, want_dt);
+  return apply_mixed_2d(uin, u2, h, l, dA, dx, P, eosk, want_dt);
 }
 
 
@@ -637,8 +637,9 @@ step2d_kernel(StepArgs a)
   static_assert(T::NREC * T::S * T::S * sizeof(R) >= H::NV * B * B * sizeof(double), "twin staging does not fit the slope area");
   const int         tid = threadIdx.x;
   const PhysParams & P = a.p;
-  // a stiffened-gas constant makes the pressure numerator cancel: FP64 there
-  const bool stiff = STIFF < 0 ? (P.gpx[0] != 0.0 || P.gpx[1] != 0.0) : STIFF == 1;
+  // the equation of state: 0 ideal gases, 1 a stiffened-gas constant (the
+  // pressure numerator cancels: FP64 there), 2 Mie-Grueneisen laws
+  const int eosk = STIFF < 0 ? (P.mg_any ? 2 : ((P.gpx[0] != 0.0 || P.gpx[1] != 0.0) ? 1 : 0)) : STIFF;
 
   const int nwalk = step_count(a);
   for (int iw = blockIdx.x; iw < nwalk;)
@@ -686,9 +687,9 @@ step2d_kernel(StepArgs a)
         for (int v = 0; v < H::NV; ++v)
           u[v] = uin[v];
       }
-      store_prim<B, MIXED>(sQ, (gx + 2) + G * (gy + 2), u, P, stiff);
+      store_prim<B, MIXED>(sQ, (gx + 2) + G * (gy + 2), u, P, eosk);
     }
-    store_prim<B, MIXED>(sQ, (ci + 2) + G * (cj + 2), uin, P, stiff);
+    store_prim<B, MIXED>(sQ, (ci + 2) + G * (cj + 2), uin, P, eosk);
     if (tid < 10)
       sSlot[tid] = slot_v;
     if (tid == 10)
@@ -739,7 +740,7 @@ step2d_kernel(StepArgs a)
         const R rr = r0 + r1;
         R       c;
         if constexpr (MIXED)
-          c = sound_speed_f(P.f_xi[0], P.f_xi[1], P.f_gpx[0], P.f_gpx[1], rr, p, a0);
+          c = sound_speed_eos(P, eosk, rr, p, a0, r0, r1);
         else
           c = sound_speed_mix(P, rr, p, a0, 1 - a0, r0, r1);
         const R drx0 = dqx[0], drx1 = dqx[1], dpx = dqx[2], dux = dqx[3], dvx = dqx[4];
@@ -784,9 +785,9 @@ step2d_kernel(StepArgs a)
       for (int f = tid; f < 2 * NFF; f += NT)
       {
         if (f < NFF)
-          face_flux_mixed<B, 0, THINC>(sQ, sRec, sFx, f, dtdx_r, P);
+          face_flux_mixed<B, 0, THINC, STIFF == 2>(sQ, sRec, sFx, f, dtdx_r, P);
         else
-          face_flux_mixed<B, 1, THINC>(sQ, sRec, sFy, f - NFF, dtdx_r, P);
+          face_flux_mixed<B, 1, THINC, STIFF == 2>(sQ, sRec, sFy, f - NFF, dtdx_r, P);
       }
     }
     else
@@ -893,7 +894,7 @@ step2d_kernel(StepArgs a)
     if (!deferred)
     {
       if constexpr (MIXED)
-        m_inv = update_mixed<B>(uin, u2, sFx, sFy, ci, cj, d2f_fast(dx), P, stiff, a.invdt != nullptr);
+        m_inv = update_mixed<B>(uin, u2, sFx, sFy, ci, cj, d2f_fast(dx), P, eosk, a.invdt != nullptr);
       else
         m_inv = update_fp64<B>(uin, u2, sFx, sFy, ci, cj, dx, P, a.invdt != nullptr);
       double * out = a.U2 + (size_t)n * H::NV * NC + tid;
@@ -1101,11 +1102,11 @@ reflux2d_kernel(StepArgs a)
     // FP32-bulk form: per-direction increments as float pairs (a fine face
     // side is the exact float-float sum of its two fine faces, / 4), applied
     // as in the step kernel
-    const bool stiff = a.p.gpx[0] != 0.0 || a.p.gpx[1] != 0.0;
+    const int  eosk = a.p.mg_any ? 2 : ((a.p.gpx[0] != 0.0 || a.p.gpx[1] != 0.0) ? 1 : 0);
     float      a0f = d2f_fast(uin[H::IA0]), a1f = d2f_fast(uin[H::IA1]);
     {
       float st0f, st1f;
-      source_factors_mixed<2>(uin, a.p, stiff, st0f, st1f);
+      source_factors_mixed<2>(uin, a.p, eosk, st0f, st1f);
       a0f *= st0f;
       a1f *= st1f;
     }
@@ -1148,7 +1149,7 @@ reflux2d_kernel(StepArgs a)
       dA[dir][0] = (((Fh[0][H::FA0] + Fl[0][H::FA0]) - usl * a0f) - (Fh[1][H::FA0] + Fl[1][H::FA0])) + usr * a0f;
       dA[dir][1] = (((Fh[0][H::FA1] + Fl[0][H::FA1]) - usl * a1f) - (Fh[1][H::FA1] + Fl[1][H::FA1])) + usr * a1f;
     }
-    const float m_inv = apply_mixed_2d(uin, u2, h, l, dA, d2f_fast(dx), a.p, stiff, a.invdt != nullptr);
+    const float m_inv = apply_mixed_2d(uin, u2, h, l, dA, d2f_fast(dx), a.p, eosk, a.invdt != nullptr);
     double *    out = a.U2 + (size_t)n * H::NV * NC + cell;
     bool        finite = true;
 #pragma unroll
@@ -1377,11 +1378,11 @@ reflux2d_mixed_lanes_kernel(StepArgs a)
 #pragma unroll
   for (int v = 0; v < H::NV; ++v)
     uin[v] = __shfl_sync(0xffffffffu, u_own, gb + lane_of[v]);
-  const bool stiff = a.p.gpx[0] != 0.0 || a.p.gpx[1] != 0.0;
+  const int  eosk = a.p.mg_any ? 2 : ((a.p.gpx[0] != 0.0 || a.p.gpx[1] != 0.0) ? 1 : 0);
   float      a0f = d2f_fast(uin[H::IA0]), a1f = d2f_fast(uin[H::IA1]);
   {
     float st0f, st1f;
-    source_factors_mixed<2>(uin, a.p, stiff, st0f, st1f);
+    source_factors_mixed<2>(uin, a.p, eosk, st0f, st1f);
     a0f *= st0f;
     a1f *= st1f;
   }
@@ -1520,9 +1521,9 @@ reflux2d_mixed_lanes_kernel(StepArgs a)
     if (act && k == 0)
     {
       float       df, ux, uy, uz, a0;
-      const float p = pressure_mixed<2>(u2, a.p, stiff, df, ux, uy, uz, a0);
+      const float p = pressure_mixed<2>(u2, a.p, eosk, df, ux, uy, uz, a0);
       const float a0s = fmaxf(0.0f, fminf(1.0f, a0));
-      const float c = sound_speed_f(a.p.f_xi[0], a.p.f_xi[1], a.p.f_gpx[0], a.p.f_gpx[1], df, p, a0s);
+      const float c = sound_speed_eos(a.p, eosk, df, p, a0s, d2f_fast(u2[H::IAD0]), d2f_fast(u2[H::IAD1]));
       m_inv = ((c + fabsf(ux)) + (c + fabsf(uy))) * __frcp_rn(d2f_fast(a.p.level_dx[r3.y]));
     }
     atomic_max_pos_warp(a.invdt, ins, (double)m_inv);

@@ -78,7 +78,7 @@ halo_coords_3d(int h, int * g)
 
 // HLLC flux of face f of direction DIR (normal velocity swapped into u and
 // back), scaled by dt/dx into the face buffer sFd ([9][NFF])
-template <bool MIXED, int DIR, int THINC>
+template <bool MIXED, int DIR, int THINC, bool MG = false>
 __device__ __forceinline__ void face_flux3(const typename Step3DTraits<MIXED>::R * sQ, const typename Step3DTraits<MIXED>::R * sHS,
                                            int f, typename Step3DTraits<MIXED>::R * sFd, typename Step3DTraits<MIXED>::R dtdx_r,
                                            const PhysParams & P);
@@ -167,13 +167,13 @@ gather_ghost_3d(const StepArgs & a, int n, const int * c0, const int * g, double
 
 template <bool MIXED>
 __device__ __forceinline__ void
-store_prim3(typename Step3DTraits<MIXED>::R * sQ, int gidx, const double * u, const PhysParams & P, bool stiff)
+store_prim3(typename Step3DTraits<MIXED>::R * sQ, int gidx, const double * u, const PhysParams & P, int eosk)
 {
   constexpr int GGG = Step3DTraits<MIXED>::GGG;
   if constexpr (MIXED)
   {
     float q[7];
-    prim_mixed<3>(u, q, P, stiff);
+    prim_mixed<3>(u, q, P, eosk);
 #pragma unroll
     for (int k = 0; k < 7; ++k)
       sQ[k * GGG + gidx] = q[k];
@@ -331,7 +331,7 @@ face_state3(const typename Step3DTraits<MIXED>::R * sQ,
   }
 }
 
-template <bool MIXED, int DIR, int THINC>
+template <bool MIXED, int DIR, int THINC, bool MG>
 __device__ __forceinline__ void
 face_flux3(const typename Step3DTraits<MIXED>::R * sQ, const typename Step3DTraits<MIXED>::R * sHS, int f,
            typename Step3DTraits<MIXED>::R * sFd, typename Step3DTraits<MIXED>::R dtdx_r, const PhysParams & P)
@@ -373,7 +373,7 @@ face_flux3(const typename Step3DTraits<MIXED>::R * sQ, const typename Step3DTrai
     qR[iw] = t;
   }
   if constexpr (MIXED)
-    hllc_fp32<3>(qL, qR, P.f_xi[0], P.f_xi[1], P.f_gpx[0], P.f_gpx[1], P.f_smallr, P.f_smallp, P.f_smallc, fl);
+    hllc_fp32<3>(qL, qR, P.f_xi[0], P.f_xi[1], P.f_gpx[0], P.f_gpx[1], P.f_smallr, P.f_smallp, P.f_smallc, fl, MG ? &P : nullptr);
   else
     hllc_fp64<3>(qL, qR, P, fl);
   if (DIR > 0)
@@ -437,7 +437,7 @@ step3d_kernel(StepArgs a)
   __shared__ int     sNext;     // the CTA's next block
   const int          tid = threadIdx.x;
   const PhysParams & P = a.p;
-  const bool         stiff = STIFF < 0 ? (P.gpx[0] != 0.0 || P.gpx[1] != 0.0) : STIFF == 1;
+  const int          eosk = STIFF < 0 ? (P.mg_any ? 2 : ((P.gpx[0] != 0.0 || P.gpx[1] != 0.0) ? 1 : 0)) : STIFF;
   const int          ci = tid % B, cj = (tid / B) % B, ck = tid / (B * B);
 
   const int nwalk = step_count(a);
@@ -481,9 +481,9 @@ step3d_kernel(StepArgs a)
         for (int v = 0; v < H::NV; ++v)
           u[v] = uin[v];
       }
-      store_prim3<MIXED>(sQ, (g[0] + 2) + G * (g[1] + 2) + GG * (g[2] + 2), u, P, stiff);
+      store_prim3<MIXED>(sQ, (g[0] + 2) + G * (g[1] + 2) + GG * (g[2] + 2), u, P, eosk);
     }
-    store_prim3<MIXED>(sQ, (ci + 2) + G * (cj + 2) + GG * (ck + 2), uin, P, stiff);
+    store_prim3<MIXED>(sQ, (ci + 2) + G * (cj + 2) + GG * (ck + 2), uin, P, eosk);
     if (tid < 12)
       sSlot[tid] = slot_v;
     if (tid == 12)
@@ -545,7 +545,7 @@ step3d_kernel(StepArgs a)
         const R rr = r0 + r1;
         R       c;
         if constexpr (MIXED)
-          c = sound_speed_f(P.f_xi[0], P.f_xi[1], P.f_gpx[0], P.f_gpx[1], rr, p, a0);
+          c = sound_speed_eos(P, eosk, rr, p, a0, r0, r1);
         else
           c = sound_speed_mix(P, rr, p, a0, 1 - a0, r0, r1);
         const R drx0 = dq[0][0], drx1 = dq[0][1], dpx = dq[0][2], dux = dq[0][3], dvx = dq[0][4], dwx = dq[0][5];
@@ -588,7 +588,7 @@ step3d_kernel(StepArgs a)
     double st0 = 1.0, st1 = 1.0;
     float  fst0 = 1.0f, fst1 = 1.0f;
     if constexpr (MIXED)
-      source_factors_mixed<3>(uin, P, stiff, fst0, fst1);
+      source_factors_mixed<3>(uin, P, eosk, fst0, fst1);
     else
       source_factors_fp64<3>(uin, P, st0, st1);
     // running state of the owned cell
@@ -620,20 +620,20 @@ step3d_kernel(StepArgs a)
         R *           sF1 = sF + T::NF * NFF;
         if (pass == 0)
         {
-          face_flux3<MIXED, 0, THINC>(sQ, sHS, tid, sF, dtdx_r, P);
+          face_flux3<MIXED, 0, THINC, STIFF == 2>(sQ, sHS, tid, sF, dtdx_r, P);
           if (tid < XR)
-            face_flux3<MIXED, 0, THINC>(sQ, sHS, tid + NT, sF, dtdx_r, P);
+            face_flux3<MIXED, 0, THINC, STIFF == 2>(sQ, sHS, tid + NT, sF, dtdx_r, P);
           else
-            face_flux3<MIXED, 1, THINC>(sQ, sHS, tid - XR, sF1, dtdx_r, P);
+            face_flux3<MIXED, 1, THINC, STIFF == 2>(sQ, sHS, tid - XR, sF1, dtdx_r, P);
         }
         else
         {
           if (tid < YB)
-            face_flux3<MIXED, 1, THINC>(sQ, sHS, tid + YA, sF1, dtdx_r, P);
+            face_flux3<MIXED, 1, THINC, STIFF == 2>(sQ, sHS, tid + YA, sF1, dtdx_r, P);
           else
-            face_flux3<MIXED, 2, THINC>(sQ, sHS, tid - YB, sF, dtdx_r, P);
+            face_flux3<MIXED, 2, THINC, STIFF == 2>(sQ, sHS, tid - YB, sF, dtdx_r, P);
           if (tid < NFF - (NT - YB))
-            face_flux3<MIXED, 2, THINC>(sQ, sHS, tid + NT - YB, sF, dtdx_r, P);
+            face_flux3<MIXED, 2, THINC, STIFF == 2>(sQ, sHS, tid + NT - YB, sF, dtdx_r, P);
         }
       }
       else
@@ -641,11 +641,11 @@ step3d_kernel(StepArgs a)
         for (int f = tid; f < NFF; f += NT)
         {
           if (pass == 0)
-            face_flux3<MIXED, 0, THINC>(sQ, sHS, f, sF, dtdx_r, P);
+            face_flux3<MIXED, 0, THINC, STIFF == 2>(sQ, sHS, f, sF, dtdx_r, P);
           else if (pass == 1)
-            face_flux3<MIXED, 1, THINC>(sQ, sHS, f, sF, dtdx_r, P);
+            face_flux3<MIXED, 1, THINC, STIFF == 2>(sQ, sHS, f, sF, dtdx_r, P);
           else
-            face_flux3<MIXED, 2, THINC>(sQ, sHS, f, sF, dtdx_r, P);
+            face_flux3<MIXED, 2, THINC, STIFF == 2>(sQ, sHS, f, sF, dtdx_r, P);
         }
       }
       __syncthreads();
@@ -861,8 +861,8 @@ step3d_kernel(StepArgs a)
         if constexpr (MIXED)
         {
           float       df, ux, uy, uz, a0;
-          const float p = pressure_mixed<3>(u2, P, stiff, df, ux, uy, uz, a0);
-          const float c = sound_speed_f(P.f_xi[0], P.f_xi[1], P.f_gpx[0], P.f_gpx[1], df, p, fmaxf(0.0f, fminf(1.0f, a0)));
+          const float p = pressure_mixed<3>(u2, P, eosk, df, ux, uy, uz, a0);
+          const float c = sound_speed_eos(P, eosk, df, p, fmaxf(0.0f, fminf(1.0f, a0)), d2f_fast(u2[H::IAD0]), d2f_fast(u2[H::IAD1]));
           m_inv = (((c + fabsf(ux)) + (c + fabsf(uy))) + (c + fabsf(uz))) * __frcp_rn(d2f_fast(dx));
         }
         else
@@ -1041,9 +1041,9 @@ reflux3d_kernel(StepArgs a)
     if constexpr (MIXED)
     {
       float       df, ux, uy, uz, a0;
-      const bool  stiff = a.p.gpx[0] != 0.0 || a.p.gpx[1] != 0.0;
-      const float p = pressure_mixed<3>(u2, a.p, stiff, df, ux, uy, uz, a0);
-      const float c = sound_speed_f(a.p.f_xi[0], a.p.f_xi[1], a.p.f_gpx[0], a.p.f_gpx[1], df, p, fmaxf(0.0f, fminf(1.0f, a0)));
+      const int   eosk = a.p.mg_any ? 2 : ((a.p.gpx[0] != 0.0 || a.p.gpx[1] != 0.0) ? 1 : 0);
+      const float p = pressure_mixed<3>(u2, a.p, eosk, df, ux, uy, uz, a0);
+      const float c = sound_speed_eos(a.p, eosk, df, p, fmaxf(0.0f, fminf(1.0f, a0)), d2f_fast(u2[V<3>::IAD0]), d2f_fast(u2[V<3>::IAD1]));
       atomic_max_pos_warp(a.invdt, ins, (double)((((c + fabsf(ux)) + (c + fabsf(uy))) + (c + fabsf(uz))) * __frcp_rn(d2f_fast(dx))));
     }
     else

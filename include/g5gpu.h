@@ -85,8 +85,9 @@ typedef struct G5Params
    *   G5_EOS_SHOCKWAVE   {rho0, Gamma0, c0, s1, s2, s3, b, e0}
    *   G5_EOS_SHOCKWAVE2  {rho0, Gamma0, c0, s, alpha, e0, p0}
    * (the [material<k>_mie_gruneisen_jwl/_sw/_sw2] sections of the decks).
-   * A non-stiffened law is stepped in G5_MODE_FP64 only; gamma[k] must still
-   * be > 1 (unused by those laws). */
+   * Both precision modes step every law (G5_MODE_MIXED evaluates the laws and
+   * the mixture rules in FP32 and the pressure numerator rho e - PI in FP64);
+   * gamma[k] must still be > 1 (unused by those laws). */
   int32_t eos[2];
   double  mg[2][8];
 } G5Params;
