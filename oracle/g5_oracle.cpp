@@ -18,7 +18,8 @@
  * of same-level blocks through the reference's scheme functors (limited
  * slopes, MUSCL-Hancock and THINC reconstruction, flux store, read-back
  * update with both volume-fraction source terms, renormalisation, CFL
- * reduction), 2D and 3D, bit for bit.
+ * reduction), 2D and 3D, bit for bit; the refinement flags of the
+ * reference's ComputeRefineFlags over threshold sweeps.
  *
  * Unpinned restatements (external kalypsso core, absent):
  *   - stiffened-gas mixture EOS (Allaire, Clerc & Kokh 2002);

@@ -13,7 +13,8 @@
  * same-level blocks through the reference's scheme functors (limited slopes,
  * MUSCL-Hancock and THINC reconstruction, flux store, read-back update with
  * the ALLAIRE_KOKH and MILLER_PUCKETT source terms, volume-fraction
- * renormalisation, CFL reduction), 2D and 3D, bit for bit.  The mixture EOS,
+ * renormalisation, CFL reduction), 2D and 3D, bit for bit, and the
+ * refinement flags of ComputeRefineFlags over threshold sweeps.  The mixture EOS,
  * the Youngs normal, the AMR stencil semantics (restriction / prolongation /
  * face sibling sums), the cell length and tree ordering live in the external
  * kalypsso core, which is not available; they are restated from published

@@ -141,6 +141,19 @@ deep_copy(A const & a, B const & b)
     *a.s = *b.s;
 }
 
+template <typename T>
+struct reduction_identity
+{
+  static constexpr T max() { return -DBL_MAX; }
+};
+template <typename T>
+KOKKOS_INLINE_FUNCTION void
+atomic_max(T * p, T v)
+{
+  if (v > *p)
+    *p = v;
+}
+
 template <typename T, std::size_t N>
 constexpr T
 dim_prod(Array<T, N> const & a)

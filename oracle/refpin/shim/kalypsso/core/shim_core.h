@@ -13,8 +13,10 @@
 //   * tanh: the oracle's own g5o_tanh (libm's tanh differs between hosts),
 //     substituted through kalypsso::tanh, which the reference's unqualified
 //     tanh calls find first.
-// What a same-level block never reaches (finer-neighbour face sums through
-// StencilHelper) aborts if called.
+//   * StencilHelper's neighbour lookup on a periodic tile of same-level
+//     blocks (the refinement indicators read their neighbours through it).
+// What a same-level block never reaches (finer-neighbour face sums and
+// averages through StencilHelper) aborts if called.
 #pragma once
 #include <algorithm>
 #include <array>
@@ -27,6 +29,7 @@
 #include <kalypsso/core/kokkos_shared.h>
 #include <kalypsso/core/real_type.h>
 #include <kalypsso/utils/config/ConfigMap.h>
+#include <kalypsso/utils/log/kalypsso_log.h>
 
 extern "C" double g5o_tanh(double);
 
@@ -140,6 +143,13 @@ cellindex_to_coord(int64_t index, block_size_t<dim> const & ghosted_size, shift_
   for (size_t e = 0; e < dim; ++e)
     c[e] -= shift[e];
   return c;
+}
+
+template <size_t dim>
+KOKKOS_INLINE_FUNCTION coord_t<dim>
+cellindex_to_coord(int64_t index, block_size_t<dim> const & block_size)
+{
+  return cell_index_unravel<dim>(index, block_size);
 }
 
 template <size_t dim>
@@ -298,21 +308,140 @@ struct AMRContext
 template <size_t dim>
 struct CellLocation
 {
-  coord_t<dim> coords;
+  coord_t<dim> ijk;
   uint64_t     key;
   int32_t      iOct;
   bool         is_ghost;
+  bool         is_outside_domain = false;
+  int          level() const { return static_cast<int>(key); }
 };
 
-// neighbour lookups across levels: not reached by same-level blocks
+template <size_t dim>
+KOKKOS_INLINE_FUNCTION int32_t
+coord_to_cellindex(coord_t<dim> const & c, block_size_t<dim> const & bs)
+{
+  int32_t i = c[IX] + bs[IX] * c[IY];
+  if constexpr (dim == 3)
+    i += bs[IX] * bs[IY] * c[IZ];
+  return i;
+}
+
+template <size_t dim, int dir>
+constexpr shift_t<dim>
+get_shift_left()
+{
+  shift_t<dim> s{};
+  s[dir] = -1;
+  return s;
+}
+template <size_t dim, int dir>
+constexpr shift_t<dim>
+get_shift_right()
+{
+  shift_t<dim> s{};
+  s[dir] = 1;
+  return s;
+}
+
+// refinement flags of the AMR context (-1 init, 0 coarsen, 1 nothing, 2 refine)
+struct AMRContextBase
+{
+  using amrflag_t = int8_t;
+  static constexpr amrflag_t KALYPSSO_FLAG_INIT = -1;
+  static constexpr amrflag_t KALYPSSO_DO_COARSEN = 0;
+  static constexpr amrflag_t KALYPSSO_DO_NOTHING = 1;
+  static constexpr amrflag_t KALYPSSO_DO_REFINE = 2;
+};
+
+BETTER_ENUM(Indicator, int, LOHNER_SPLIT, LOHNER_UNSPLIT, SIMPLE_GRADIENT)
+struct RefineIndicatorData
+{
+  Indicator indicator = Indicator::SIMPLE_GRADIENT;
+  real_t    epsilon = 0.02;
+  real_t    refine_th = 0.1;
+  real_t    coarsen_th = 0.0125;
+  int       level_min = 0;
+  int       level_max = 30;
+};
+
+namespace KokkosExt
+{
+template <typename T>
+KOKKOS_INLINE_FUNCTION T
+max_val(T a, T b)
+{
+  return a > b ? a : b;
+}
+} // namespace KokkosExt
+
+template <typename T, typename device_t>
+using DataArrayLeaf = Kokkos::View<T *, device_t>;
+
+struct ParallelEnv
+{};
+
+// |x| of the reference's unqualified abs(...) on reals
+inline double
+abs(double x)
+{
+  return std::fabs(x);
+}
+
+// Neighbour lookup on a periodic tile of same-level blocks (blocks numbered x
+// fastest over the brick of the constructor, level in the key): the cell at
+// ijk + shift, in this block or in the neighbour block it falls in.  The
+// lookups across levels (finer neighbours' face sums and averages) are not
+// reached by such tiles and abort if called.
 template <size_t dim, typename device_t>
 class StencilHelper
 {
 public:
+  typename orchard_key_base_t<device_t>::view_t keys;
+  block_size_t<dim>                             bs{};
+  brick_size_t<dim>                             nb{};
   StencilHelper() = default;
-  template <typename M, typename K>
-  StencilHelper(M const &, K const &, block_size_t<dim>, brick_size_t<dim>, Kokkos::Array<bool, dim>)
+  template <typename M>
+  StencilHelper(M const &, typename orchard_key_base_t<device_t>::view_t const & k, block_size_t<dim> b, brick_size_t<dim> n,
+                Kokkos::Array<bool, dim>)
+    : keys(k)
+    , bs(b)
+    , nb(n)
   {}
+  uint64_t          key(int32_t iOct) const { return keys(iOct); }
+  CellLocation<dim> getNeighLoc(CellLocation<dim> const & loc, shift_t<dim> const & shift) const
+  {
+    CellLocation<dim> out = loc;
+    int32_t           bc[3] = { 0, 0, 0 }, o = loc.iOct;
+    for (size_t e = 0; e < dim; ++e)
+    {
+      bc[e] = o % nb[e];
+      o /= nb[e];
+    }
+    int32_t oct = 0, mul = 1;
+    for (size_t e = 0; e < dim; ++e)
+    {
+      int32_t c = loc.ijk[e] + shift[e];
+      int32_t b = bc[e];
+      while (c < 0)
+      {
+        c += bs[e];
+        b -= 1;
+      }
+      while (c >= bs[e])
+      {
+        c -= bs[e];
+        b += 1;
+      }
+      b = ((b % nb[e]) + nb[e]) % nb[e];
+      out.ijk[e] = c;
+      oct += b * mul;
+      mul *= nb[e];
+    }
+    out.iOct = oct;
+    out.key = keys(oct);
+    out.is_outside_domain = false;
+    return out;
+  }
   CellLocation<dim> getNeighLocFinerNearer(CellLocation<dim> const &, shift_t<dim> const &) const
   {
     Kokkos::abort("refpin: finer-neighbour lookup is outside the same-level pin");
@@ -322,6 +451,12 @@ public:
   real_t compute_face_siblings_sum(CellLocation<dim> const &, int, A const &, bool) const
   {
     Kokkos::abort("refpin: finer-neighbour face sum is outside the same-level pin");
+    return 0;
+  }
+  template <typename A>
+  real_t compute_siblings_average(CellLocation<dim> const &, block_size_t<dim> const &, int, A const &) const
+  {
+    Kokkos::abort("refpin: finer-neighbour average is outside the same-level pin");
     return 0;
   }
 };

@@ -14,7 +14,8 @@ them where the reference tree is absent.
 
 Run from the repository root (needs the reference tree and a built oracle):
 
-    python tests/golden/make_scheme_golden.py
+    python tests/golden/make_scheme_golden.py           # block steps
+    python tests/golden/make_scheme_golden.py --flags   # refinement flags
 """
 import ctypes
 import os
@@ -141,5 +142,70 @@ def main():
     print("wrote", OUT, os.path.getsize(OUT), "bytes")
 
 
-if __name__ == "__main__":
+if __name__ == "__main__" and "--flags" not in sys.argv:
     sys.exit(main())
+
+
+# ---------------------------------------------------------------------------
+# Refinement flags (ComputeRefineFlags::run, scheme/ComputeRefineFlags.cpp:18-368)
+# of the reference's own code on periodic tiles of same-level blocks
+# (refpin_refine_flags), swept over the thresholds so that each block's
+# largest indicator is pinned to an interval: tests/golden/refine_flags_golden.npz
+# ---------------------------------------------------------------------------
+FLAG_OUT = os.path.join(ROOT, "tests", "golden", "refine_flags_golden.npz")
+EPS_REFINE = (0.005, 0.01, 0.02, 0.05, 0.1, 0.2, 0.4, 0.7, 0.95)
+EPS_COARSEN = (0.001, 0.003, 0.0125, 0.05, 0.2)
+EPS_LOHNER = (0.01, 0.02, 0.1)
+
+
+def flag_tile(dim, seed):
+    """A tile of 4x4 (2D) or 2x2x2 (3D) level-0 blocks of 8^dim cells with a
+    material interface over part of it and smooth fields elsewhere."""
+    nb = 4 if dim == 2 else 2
+    return tile_case(dim, 8, nb, "water_air" if seed % 2 else "air_helium", 0, 0, 0, 1.0, seed), nb
+
+
+def reference_flags(lib, dim, b, nb, U, indicator, eps_lohner, eps_refine, eps_coarsen, lmin, lmax):
+    vp = ctypes.c_void_p
+    U = np.ascontiguousarray(U, np.float64)
+    nblocks = nb**dim
+    out = np.zeros(nblocks, np.int8)
+    rc = lib.refpin_refine_flags(dim, b, nb, 0, U.ctypes.data_as(vp), indicator, eps_lohner, eps_refine, eps_coarsen, lmin, lmax, out.ctypes.data_as(vp))
+    if rc != 0:
+        raise RuntimeError(f"refpin_refine_flags failed ({rc})")
+    return out
+
+
+def load_flags():
+    lib = load()
+    vp = ctypes.c_void_p
+    lib.refpin_refine_flags.restype = ctypes.c_int
+    lib.refpin_refine_flags.argtypes = [ctypes.c_int] * 4 + [vp, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int, vp]
+    return lib
+
+
+def sweep(lib, dim, nb, U):
+    """flags[indicator, lohner eps, refine eps, coarsen eps, block] with level 0,
+    level_min -1 (coarsening allowed) and level_max 2."""
+    out = np.zeros((3, len(EPS_LOHNER), len(EPS_REFINE), len(EPS_COARSEN), nb**dim), np.int8)
+    for ind in range(3):
+        for a, el in enumerate(EPS_LOHNER):
+            for i, er in enumerate(EPS_REFINE):
+                for j, ec in enumerate(EPS_COARSEN):
+                    out[ind, a, i, j] = reference_flags(lib, dim, 8, nb, U, ind, el, er, ec, -1, 2)
+    return out
+
+
+def main_flags():
+    lib = load_flags()
+    data = {}
+    for seed in (11, 12):
+        (mesh, t, p, U), nb = flag_tile(2, seed)
+        data[f"seed{seed}/U"] = U[: t.n_owned]
+        data[f"seed{seed}/flags"] = sweep(lib, 2, nb, U[: t.n_owned])
+    np.savez_compressed(FLAG_OUT, **data)
+    print("wrote", FLAG_OUT, os.path.getsize(FLAG_OUT), "bytes")
+
+
+if __name__ == "__main__" and "--flags" in sys.argv:
+    main_flags()

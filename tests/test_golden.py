@@ -191,3 +191,56 @@ def test_oracle_scheme_step_matches_reference_live(dim):
                         if not (np.array_equal(got, ref) and inv == inv_ref):
                             bad.append((mats, thinc, integ, st, slope, int((got != ref).sum())))
     assert not bad, bad
+
+
+# ---------------------------------------------------------------------------
+# Refinement flags against the reference's own ComputeRefineFlags (all three
+# indicators, swept over the refine / coarsen / Loehner thresholds so that
+# every block's largest indicator is pinned to an interval; coarsening allowed
+# with level_min -1).  tests/golden/refine_flags_golden.npz comes from
+# `python tests/golden/make_scheme_golden.py --flags`.
+# ---------------------------------------------------------------------------
+FLAGS_GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "refine_flags_golden.npz")
+
+
+def _oracle_flag_sweep(t, p, U, eps_lohner, eps_refine, eps_coarsen):
+    from oracle.oracle import Oracle
+
+    o = Oracle(t, p)
+    U = np.ascontiguousarray(U)
+    o.fill_outside(U)
+    out = np.zeros((3, len(eps_lohner), len(eps_refine), len(eps_coarsen), t.n_owned), np.int8)
+    for ind in range(3):
+        for a, el in enumerate(eps_lohner):
+            for i, er in enumerate(eps_refine):
+                for j, ec in enumerate(eps_coarsen):
+                    out[ind, a, i, j] = o.refine_flags(U, ind, er, ec, el, -1, 2)
+    o.close()
+    return out
+
+
+@pytest.mark.parametrize("seed", [11, 12])
+def test_oracle_refine_flags_match_reference_golden(seed):
+    from tests.golden.make_scheme_golden import EPS_COARSEN, EPS_LOHNER, EPS_REFINE, flag_tile
+
+    g = np.load(FLAGS_GOLDEN)
+    (mesh, t, p, _), nb = flag_tile(2, seed)
+    U = np.zeros((t.n_total, t.nv, t.ncell))
+    U[: t.n_owned] = g[f"seed{seed}/U"]
+    ref = g[f"seed{seed}/flags"]
+    got = _oracle_flag_sweep(t, p, U, EPS_LOHNER, EPS_REFINE, EPS_COARSEN)
+    assert np.array_equal(got, ref), f"{(got != ref).sum()} of {ref.size} flags differ"
+    assert {0, 1, 2} <= set(np.unique(np.concatenate([np.load(FLAGS_GOLDEN)[f"seed{s}/flags"].ravel() for s in (11, 12)])))
+
+
+@pytest.mark.skipif(not os.path.exists(REFPIN_LIB), reason="reference-pinning library not built (needs the reference tree)")
+@pytest.mark.parametrize("dim", [2, 3])
+def test_oracle_refine_flags_match_reference_live(dim):
+    from tests.golden.make_scheme_golden import EPS_COARSEN, EPS_LOHNER, EPS_REFINE, flag_tile, load_flags, sweep
+
+    lib = load_flags()
+    for seed in (21, 22, 23):
+        (mesh, t, p, U), nb = flag_tile(dim, seed)
+        ref = sweep(lib, dim, nb, U[: t.n_owned])
+        got = _oracle_flag_sweep(t, p, U, EPS_LOHNER, EPS_REFINE, EPS_COARSEN)
+        assert np.array_equal(got, ref), (seed, int((got != ref).sum()))
