@@ -461,10 +461,75 @@ defer_info_kernel(DevMesh m, const int32_t * codes, int n, int32_t * info)
 }
 
 // ComputeDerivedQuantities::run (utils/ComputeDerivedQuantities.h:96-180):
-// one derived quantity per cell of blocks [oct_begin, oct_begin + num_octs),
-// FP64 in the reference's operation order.  quantity: 0 RHO_MIX,
-// 1 THERMAL_PRESSURE, 2 SPEED_OF_SOUND, 3 SPECIFIC_EKIN, 4 LOCAL_MACH_NUMBER,
-// 5 VX, 6 VY, 7 VZ (the DERIVED_QUANTITY enum order).
+// one derived quantity of a cell's conservative state, FP64 in the
+// reference's operation order.  quantity: 0 RHO_MIX, 1 THERMAL_PRESSURE,
+// 2 SPEED_OF_SOUND, 3 SPECIFIC_EKIN, 4 LOCAL_MACH_NUMBER, 5 VX, 6 VY, 7 VZ
+// (the DERIVED_QUANTITY enum order).
+template <int DIM>
+__device__ __forceinline__ double
+derived_value(const double * u, int quantity, const PhysParams & P)
+{
+  using H = V<DIM>;
+  double r = 0.0;
+  if (quantity == 0)
+    r = u[H::ID];
+  else if (quantity == 1 || quantity == 3)
+  {
+    // compute_mixture_ekin (models/utils.h:124-151): density from ID
+    const double d = fmax(u[H::ID], P.smallr);
+    const double ux = u[H::IU] / d, uy = u[H::IV] / d;
+    double       ekin;
+    if constexpr (DIM == 2)
+      ekin = 0.5 * (ux * ux + uy * uy);
+    else
+    {
+      const double uz = u[H::IW] / d;
+      ekin = 0.5 * (ux * ux + uy * uy + uz * uz);
+    }
+    if (quantity == 3)
+      r = ekin;
+    else
+    {
+      // compute_mixture_pressure (models/utils.h:160-185): density from the partial densities
+      const double dm = fmax(u[H::IAD0] + u[H::IAD1], P.smallr);
+      const double eint = u[H::IE] / dm - ekin;
+      const double a0 = u[H::IA0];
+      if (!P.mg_any)
+        r = (dm * eint - eosPI(P, a0, 1 - a0)) / eosS(P, a0, 1 - a0);
+      else
+      {
+        double S, PI, C1, C0;
+        mg_mixture(P, a0, 1 - a0, u[H::IAD0], u[H::IAD1], S, PI, C1, C0);
+        r = (dm * eint - PI) / S;
+      }
+    }
+  }
+  else
+  {
+    double       q[7];
+    const double cs = prim_fp64<DIM>(u, q, P);
+    if (quantity == 2)
+      r = cs;
+    else if (quantity == 4)
+    {
+      double un = q[H::QU] * q[H::QU] + q[H::QV] * q[H::QV];
+      if constexpr (DIM == 3)
+        un += q[H::QW] * q[H::QW];
+      un = sqrt(un);
+      r = un / cs;
+    }
+    else if (quantity == 5)
+      r = q[H::QU];
+    else if (quantity == 6)
+      r = q[H::QV];
+    else if constexpr (DIM == 3)
+      r = q[H::QW];
+  }
+  return r;
+}
+
+// one derived quantity per cell of blocks [oct_begin, oct_begin + num_octs)
+// into out[oct][cell]
 template <int DIM, int B>
 __global__ void
 derived_kernel(const double * __restrict__ U, double * __restrict__ out, int quantity, long long oct_begin, long long num_octs,
@@ -481,62 +546,43 @@ derived_kernel(const double * __restrict__ U, double * __restrict__ out, int qua
 #pragma unroll
     for (int v = 0; v < H::NV; ++v)
       u[v] = U[(oct * H::NV + v) * NC + cell];
-    double r = 0.0;
-    if (quantity == 0)
-      r = u[H::ID];
-    else if (quantity == 1 || quantity == 3)
+    out[oct * NC + cell] = derived_value<DIM>(u, quantity, P);
+  }
+}
+
+// The fields of one output file (SolverGodunovFiveEq::save_solution_hdf5,
+// SolverGodunovFiveEq.cpp:809-886: each a per-quadrant dataset of the state's
+// variables or of a derived quantity) for blocks [oct_begin, oct_begin +
+// num_octs), in one pass over U: field k to out[k][oct - oct_begin][cell].
+// (FieldList codes: a variable of U, or FIELD_DERIVED + a derived quantity).
+
+template <int DIM, int B>
+__global__ void
+pack_fields_kernel(const double * __restrict__ U, double * __restrict__ out, FieldList fl, long long oct_begin, long long num_octs,
+                   PhysParams P)
+{
+  using H = V<DIM>;
+  constexpr int NC = DIM == 2 ? B * B : B * B * B;
+  const long long total = num_octs * NC;
+  for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (long long)gridDim.x * blockDim.x)
+  {
+    const long long oct = oct_begin + g / NC;
+    const int       cell = (int)(g % NC);
+    double          u[H::NV];
+#pragma unroll
+    for (int v = 0; v < H::NV; ++v)
+      u[v] = U[(oct * H::NV + v) * NC + cell];
+    for (int k = 0; k < fl.n; ++k)
     {
-      // compute_mixture_ekin (models/utils.h:124-151): density from ID
-      const double d = fmax(u[H::ID], P.smallr);
-      const double ux = u[H::IU] / d, uy = u[H::IV] / d;
-      double       ekin;
-      if constexpr (DIM == 2)
-        ekin = 0.5 * (ux * ux + uy * uy);
-      else
-      {
-        const double uz = u[H::IW] / d;
-        ekin = 0.5 * (ux * ux + uy * uy + uz * uz);
-      }
-      if (quantity == 3)
-        r = ekin;
-      else
-      {
-        // compute_mixture_pressure (models/utils.h:160-185): density from the partial densities
-        const double dm = fmax(u[H::IAD0] + u[H::IAD1], P.smallr);
-        const double eint = u[H::IE] / dm - ekin;
-        const double a0 = u[H::IA0];
-        if (!P.mg_any)
-          r = (dm * eint - eosPI(P, a0, 1 - a0)) / eosS(P, a0, 1 - a0);
-        else
-        {
-          double S, PI, C1, C0;
-          mg_mixture(P, a0, 1 - a0, u[H::IAD0], u[H::IAD1], S, PI, C1, C0);
-          r = (dm * eint - PI) / S;
-        }
-      }
+      const int c = fl.code[k];
+      double    r = 0.0;
+#pragma unroll
+      for (int v = 0; v < H::NV; ++v)
+        r = c == v ? u[v] : r;
+      if (c >= FIELD_DERIVED)
+        r = derived_value<DIM>(u, c - FIELD_DERIVED, P);
+      out[(size_t)k * total + g] = r;
     }
-    else
-    {
-      double       q[7];
-      const double cs = prim_fp64<DIM>(u, q, P);
-      if (quantity == 2)
-        r = cs;
-      else if (quantity == 4)
-      {
-        double un = q[H::QU] * q[H::QU] + q[H::QV] * q[H::QV];
-        if constexpr (DIM == 3)
-          un += q[H::QW] * q[H::QW];
-        un = sqrt(un);
-        r = un / cs;
-      }
-      else if (quantity == 5)
-        r = q[H::QU];
-      else if (quantity == 6)
-        r = q[H::QV];
-      else if constexpr (DIM == 3)
-        r = q[H::QW];
-    }
-    out[oct * NC + cell] = r;
   }
 }
 

@@ -426,4 +426,39 @@ launch_derived(int dim, int b, const double * U, double * out, int quantity, lon
   return cudaErrorInvalidValue;
 }
 
+template <int DIM, int B>
+static cudaError_t
+pack_fields_t(const double * U, double * out, const FieldList & fl, long long oct_begin, long long num_octs, const PhysParams & p,
+              cudaStream_t s)
+{
+  constexpr int   NC = DIM == 2 ? B * B : B * B * B;
+  const long long total = num_octs * NC;
+  if (total <= 0)
+    return cudaSuccess;
+  long long grid = (total + 255) / 256;
+  if (grid > (long long)num_sms() * 16)
+    grid = (long long)num_sms() * 16;
+  pack_fields_kernel<DIM, B><<<(unsigned)grid, 256, 0, s>>>(U, out, fl, oct_begin, num_octs, p);
+  return cudaGetLastError();
+}
+
+cudaError_t
+launch_pack_fields(int dim, int b, const double * U, double * out, const int * codes, int n, long long oct_begin, long long num_octs,
+                   const PhysParams & p, cudaStream_t s)
+{
+  if (n < 1 || n > MAX_PACK_FIELDS)
+    return cudaErrorInvalidValue;
+  FieldList fl;
+  fl.n = n;
+  for (int k = 0; k < MAX_PACK_FIELDS; ++k)
+    fl.code[k] = k < n ? codes[k] : 0;
+  if (dim == 2 && b == 16)
+    return pack_fields_t<2, 16>(U, out, fl, oct_begin, num_octs, p, s);
+  if (dim == 2 && b == 8)
+    return pack_fields_t<2, 8>(U, out, fl, oct_begin, num_octs, p, s);
+  if (dim == 3 && b == 8)
+    return pack_fields_t<3, 8>(U, out, fl, oct_begin, num_octs, p, s);
+  return cudaErrorInvalidValue;
+}
+
 } // namespace g5

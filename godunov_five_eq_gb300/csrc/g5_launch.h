@@ -43,5 +43,9 @@ cudaError_t launch_defer_info(int dim, const DevMesh & m, const int32_t * codes,
 // derived quantity per cell (ComputeDerivedQuantities)
 cudaError_t launch_derived(int dim, int b, const double * U, double * out, int quantity, long long oct_begin, long long num_octs,
                            const PhysParams & p, cudaStream_t s);
+// the fields of one output file in one pass (pack_fields_kernel): codes[k] a
+// variable of U or FIELD_DERIVED + a derived quantity, 1 <= n <= 16
+cudaError_t launch_pack_fields(int dim, int b, const double * U, double * out, const int * codes, int n, long long oct_begin,
+                               long long num_octs, const PhysParams & p, cudaStream_t s);
 
 } // namespace g5

@@ -459,14 +459,29 @@ step3d_kernel(StepArgs a)
       dtdx_r = a.dt[ins] / dx;
 
     // ---------------- phase 1: own cell (coalesced) + halo -> primitives
-    // (the own cell's loads are in flight while the halo gather runs; its
-    // primitives are stored last)
+    // (the own cell first, so that its nine doubles are dead before the halo
+    // gather: at 64 registers a live own cell spilled)
     double uin[H::NV];
     {
       const double * base = a.U + (size_t)n * H::NV * NC + tid;
 #pragma unroll
       for (int v = 0; v < H::NV; ++v)
         uin[v] = base[v * NC];
+    }
+    store_prim3<MIXED>(sQ, (ci + 2) + G * (cj + 2) + GG * (ck + 2), uin, P, eosk);
+    // FP32-bulk form: the owned cell's volume-fraction source-term factors
+    // and its volume fractions as floats, taken now so that the nine doubles
+    // of the cell do not stay live through the gather, slope and face phases;
+    // the final update reads the cell from U again
+    float a0f = 0.0f, a1f = 0.0f, af0 = 0.0f, af1 = 0.0f;
+    if constexpr (MIXED)
+    {
+      float fst0, fst1;
+      source_factors_mixed<3>(uin, P, eosk, fst0, fst1);
+      af0 = d2f_fast(uin[H::IA0]);
+      af1 = d2f_fast(uin[H::IA1]);
+      a0f = af0 * fst0;
+      a1f = af1 * fst1;
     }
     constexpr int NHALO = GGG - NC;
     for (int h = tid; h < NHALO; h += NT)
@@ -477,13 +492,13 @@ step3d_kernel(StepArgs a)
       if (!gather_ghost_3d(a, n, c0, g, u))
       {
         raise_status(a.status, STATUS_MESH);
+        const double * own = a.U + (size_t)n * H::NV * NC + tid;
 #pragma unroll
         for (int v = 0; v < H::NV; ++v)
-          u[v] = uin[v];
+          u[v] = own[v * NC];
       }
       store_prim3<MIXED>(sQ, (g[0] + 2) + G * (g[1] + 2) + GG * (g[2] + 2), u, P, eosk);
     }
-    store_prim3<MIXED>(sQ, (ci + 2) + G * (cj + 2) + GG * (ck + 2), uin, P, eosk);
     if (tid < 12)
       sSlot[tid] = slot_v;
     if (tid == 12)
@@ -584,18 +599,17 @@ step3d_kernel(StepArgs a)
         deferred = deferred || (dsl[f] >= 0 && cc[f >> 1] == ((f & 1) ? B - 1 : 0));
     }
 
-    // volume-fraction source-term factors of the owned cell
+    // FP64 form: volume-fraction source-term factors and the running state
+    // of the owned cell
     double st0 = 1.0, st1 = 1.0;
-    float  fst0 = 1.0f, fst1 = 1.0f;
-    if constexpr (MIXED)
-      source_factors_mixed<3>(uin, P, eosk, fst0, fst1);
-    else
-      source_factors_fp64<3>(uin, P, st0, st1);
-    // running state of the owned cell
     double u2[H::NV];
+    if constexpr (!MIXED)
+    {
+      source_factors_fp64<3>(uin, P, st0, st1);
 #pragma unroll
-    for (int v = 0; v < H::NV; ++v)
-      u2[v] = uin[v];
+      for (int v = 0; v < H::NV; ++v)
+        u2[v] = uin[v];
+    }
     // mixed form: per-direction increments of the clamped quantities (exact
     // float pairs) and running float-float sums of energy and momentum
     float hh[3][2], ll[3][2], dA[3][2];
@@ -726,7 +740,6 @@ step3d_kernel(StepArgs a)
         }
         else
         {
-          const float a0f = d2f_fast(uin[H::IA0]) * fst0, a1f = d2f_fast(uin[H::IA1]) * fst1;
           two_diff(sFd[H::FR0 * NFF + il], sFd[H::FR0 * NFF + ir], hh[dir][0], ll[dir][0]);
           two_diff(sFd[H::FR1 * NFF + il], sFd[H::FR1 * NFF + ir], hh[dir][1], ll[dir][1]);
           const int ke[4] = { H::FE, H::FU, H::FV, H::FW };
@@ -753,6 +766,12 @@ step3d_kernel(StepArgs a)
       // otherwise applied direction by direction; energy and momentum in one
       // exact float-float sum
       const double eps = 1e-12, one_m_eps = 1.0 - 1e-12;
+      {
+        const double * base = a.U + (size_t)n * H::NV * NC + tid;
+#pragma unroll
+        for (int v = 0; v < H::NV; ++v)
+          u2[v] = base[v * NC];
+      }
 #pragma unroll
       for (int k = 0; k < 2; ++k)
       {
@@ -783,7 +802,7 @@ step3d_kernel(StepArgs a)
       for (int k = 0; k < 2; ++k)
       {
         const int   iv = k == 0 ? H::IA0 : H::IA1;
-        const float af = d2f_fast(uin[iv]);
+        const float af = k == 0 ? af0 : af1;
         const float m = 2.0f * (fabsf(dA[0][k]) + fabsf(dA[1][k])) + 2e-12f;
         if (af > m && af + m < 1.0f)
         {

@@ -118,6 +118,7 @@ EXPORTS = [
     "g5_step_host",
     "g5_step_batched",
     "g5_derived_quantity",
+    "g5_pack_fields",
     "g5_compute_inv_dt",
     "g5_fill_outside",
     "g5_begin",
@@ -174,6 +175,7 @@ def load_library(build_if_missing: bool = True):
     L.g5_step_host.argtypes = [vp, vp, vp, vp, ctypes.c_int, vp, vp]
     L.g5_step_batched.argtypes = [vp, vp, vp, vp, ctypes.c_int, vp, ctypes.c_int, vp, vp]
     L.g5_derived_quantity.argtypes = [vp, vp, ctypes.c_int, ctypes.c_int64, ctypes.c_int64, vp, vp]
+    L.g5_pack_fields.argtypes = [vp, vp, vp, ctypes.c_int, ctypes.c_int64, ctypes.c_int64, vp, vp]
     L.g5_compute_inv_dt.argtypes = [vp, vp, vp, vp]
     L.g5_fill_outside.argtypes = [vp, vp, vp]
     L.g5_run.argtypes = [vp, vp, vp, ctypes.c_int, ctypes.c_int, vp, vp]
@@ -398,6 +400,27 @@ class GodunovImplemGB300:
             raise G5Error(rc, "g5_derived_quantity")
         return out
 
+    FIELD_DERIVED = 64
+    MAX_PACK_FIELDS = 16
+
+    def pack_fields(self, U, fields, oct_begin=0, num_octs=None, out=None, stream=None):
+        """g5_pack_fields: the datasets of one output file in one pass over U:
+        fields[k] a variable of U (the reference's VarId) or FIELD_DERIVED + a
+        derived quantity; returns out[len(fields), num_octs, ncell] (device)."""
+        import torch
+
+        fields = [int(f) for f in fields]
+        n = self.table.n_owned if num_octs is None else int(num_octs)
+        if out is None:
+            out = torch.empty((len(fields), n, self.table.ncell), dtype=torch.float64, device=U.device)
+        arr = (ctypes.c_int32 * max(len(fields), 1))(*fields)
+        rc = self.lib.g5_pack_fields(
+            self.ctx, ctypes.c_void_p(_dptr(U)), arr, len(fields), int(oct_begin), n, ctypes.c_void_p(_dptr(out)), _stream(stream)
+        )
+        if rc != 0:
+            raise G5Error(rc, "g5_pack_fields")
+        return out
+
     def compute_inv_dt(self, U, out=None, stream=None):
         import torch
 
@@ -515,7 +538,9 @@ class GodunovImplemGB300:
             raise G5Error(rc, "g5_tune")
         return self.tune_choice(mode)
 
-    SHAPE_KEYS = ("ctas_per_sm", "claim", "walk_cf_first", "reflux_one_thread_per_cell")
+    # reflux_layout: 0 separate pass with 8 lanes per deferred cell, 1 separate
+    # pass with one thread per cell, 2 fused into the step
+    SHAPE_KEYS = ("ctas_per_sm", "claim", "walk_cf_first", "reflux_layout")
 
     def tune_choice(self, mode="fp64") -> dict:
         out = (ctypes.c_int32 * 4)()
@@ -534,8 +559,8 @@ class GodunovImplemGB300:
         self.lib.g5_tune_report(self.ctx, MODES[mode], shapes, ms, n)
         return [(unpack_shape(int(shapes[i])), float(ms[i])) for i in range(n)]
 
-    def set_shape(self, mode="fp64", ctas_per_sm=0, claim=1, walk_cf_first=1, reflux_one_thread_per_cell=0):
-        arr = (ctypes.c_int32 * 4)(ctas_per_sm, claim, walk_cf_first, reflux_one_thread_per_cell)
+    def set_shape(self, mode="fp64", ctas_per_sm=0, claim=1, walk_cf_first=1, reflux_layout=0):
+        arr = (ctypes.c_int32 * 4)(ctas_per_sm, claim, walk_cf_first, reflux_layout)
         rc = self.lib.g5_set_shape(self.ctx, MODES[mode], arr)
         if rc != 0:
             raise G5Error(rc, "g5_set_shape")
@@ -546,7 +571,7 @@ class GodunovImplemGB300:
 
 def unpack_shape(code: int) -> dict:
     """A packed launch shape of g5_tune (ctas_per_sm + 16 claim + 32 walk + 64 reflux)."""
-    return {"ctas_per_sm": code & 15, "claim": (code >> 4) & 1, "walk_cf_first": (code >> 5) & 1, "reflux_one_thread_per_cell": (code >> 6) & 1}
+    return {"ctas_per_sm": code & 15, "claim": (code >> 4) & 1, "walk_cf_first": (code >> 5) & 1, "reflux_layout": (code >> 6) & 3}
 
 
 def tune_pick(ms, default_index, margin=0.02) -> int:

@@ -217,6 +217,22 @@ int g5_step_host(G5Context * ctx, const double * h_U, double * h_U2, const doubl
  * (owned + outside blocks), as check_args_validity requires. */
 int g5_derived_quantity(G5Context * ctx, const double * d_U, int quantity, int64_t oct_begin, int64_t num_octs, double * d_out, void * stream);
 
+/* The datasets of one output file of SolverGodunovFiveEq::save_solution_hdf5
+ * (SolverGodunovFiveEq.cpp:809-886: a per-quadrant array per state variable
+ * and per derived quantity), packed on the device in one pass over d_U so that
+ * a single device-to-host copy carries them: fields[k] (host, 1 <= nfields <=
+ * G5_MAX_PACK_FIELDS) is a variable of the state (0 .. nv - 1, the reference's
+ * VarId numbering: rho_mix, e_tot, rho_vx, rho_vy[, rho_vz], alpha_0,
+ * alpha_rho_0, alpha_1, alpha_rho_1) or G5_FIELD_DERIVED + a G5_DQ_*
+ * quantity (the values of g5_derived_quantity).  Blocks [oct_begin, oct_begin
+ * + num_octs) of the table go to d_out[k][num_octs][bsize^dim].  No
+ * counterpart of the packing in the reference, which copies the whole state
+ * to the host and writes each dataset from there. */
+#define G5_FIELD_DERIVED 64
+#define G5_MAX_PACK_FIELDS 16
+int g5_pack_fields(G5Context * ctx, const double * d_U, const int32_t * fields, int nfields, int64_t oct_begin, int64_t num_octs,
+                   double * d_out, void * stream);
+
 /* ComputeDtFiveEqFunctor::apply (scheme/ComputeDtFiveEqFunctor.h:113-121):
  * d_inv_dt[n_inst] <- max over owned cells of sum_d (c+|u_d|)/dx. */
 int g5_compute_inv_dt(G5Context * ctx, const double * d_U, double * d_inv_dt, void * stream);
@@ -299,9 +315,10 @@ int g5_status(G5Context * ctx, void * stream);
  * fixed).  Candidates: CTAs per SM of the persistent step kernel (1 up to the
  * occupancy maximum), dynamic block claiming on or off, the block walk order
  * (blocks with coarse/fine neighbours first, or table order) and, for the
- * FP32-bulk 2D pass over coarse/fine records, its layout (8 lanes or one
- * thread per deferred cell).  Every candidate computes the same values bit for
- * bit.  Each is timed twice on d_U -> d_U2 (3 steps after a warm-up, CUDA
+ * FP32-bulk 2D pass over coarse/fine records, its layout (a separate pass
+ * with 8 lanes or one thread per deferred cell, or fused into the step: the
+ * CTA that writes the last input of a block's deferred cells finishes them).
+ * Every candidate computes the same values bit for bit.  Each is timed twice on d_U -> d_U2 (3 steps after a warm-up, CUDA
  * events on `stream`), and g5_tune_pick chooses with a 2 % margin in favour of
  * the default shape.  The choice is kept by the context for that mode
  * (across g5_set_mesh) until the next g5_tune or g5_set_shape.  Synchronises
@@ -316,7 +333,9 @@ int g5_tune(G5Context * ctx, const double * d_U, double * d_U2, int mode, void *
 int g5_tune_pick(const float * ms, int n, int default_index, float margin);
 
 /* The launch shape a mode uses: out4 = {CTAs per SM, claim, walk order,
- * reflux layout}. */
+ * reflux layout (0 separate pass, 8 lanes per cell; 1 separate pass, one
+ * thread per cell; 2 fused into the step)}.  Layouts 1 and 2 apply to the
+ * FP32-bulk 2D full-mesh step; elsewhere the separate pass runs. */
 int g5_tune_choice(const G5Context * ctx, int mode, int32_t * out4);
 
 /* The candidates and their times (ms per step) of the last g5_tune of a mode:

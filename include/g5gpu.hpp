@@ -14,6 +14,7 @@
 //   fill_outside_quadrants(U)          FillOutsideCellFunctor
 //   remap_block_data(map, Uold, Unew)  UserDataRemapper after a mesh adaptation
 //   compute_derived_quantity(U, q, o)  ComputeDerivedQuantities (output path)
+//   pack_output_fields(U, f, n, out)   the datasets of one output, packed in one pass
 //   do_time_step_host(hU, hU2, dt)     do_time_step on host-resident arrays
 // Errors from the C ABI are thrown as g5::Error (the reference aborts).
 #pragma once
@@ -323,6 +324,15 @@ public:
   void compute_derived_quantity(const g5::BlockArray & U, int quantity, const g5::BlockArray & out)
   {
     g5::check(g5_derived_quantity(m_ctx, U.data, quantity, 0, U.n_blocks, out.data, m_stream), "g5_derived_quantity");
+  }
+
+  //! the datasets of one output of SolverGodunovFiveEq::save_solution_hdf5
+  //! (SolverGodunovFiveEq.cpp:809-886) for blocks [0, n_blocks) of U: fields
+  //! are state variable ids or G5_FIELD_DERIVED + G5_DQ_*, out holds
+  //! fields.size() x n_blocks x bsize^dim doubles on the device
+  void pack_output_fields(const g5::BlockArray & U, const std::vector<int32_t> & fields, int64_t n_blocks, double * d_out)
+  {
+    g5::check(g5_pack_fields(m_ctx, U.data, fields.data(), (int)fields.size(), 0, n_blocks, d_out, m_stream), "g5_pack_fields");
   }
 
   //! SolverGodunovFiveEq::fill_outside_quadrants
