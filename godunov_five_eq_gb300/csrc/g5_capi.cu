@@ -36,12 +36,6 @@ struct G5Context
   double *       d_dt = nullptr, *d_invdt = nullptr;
   double *       d_urk = nullptr; // RK2_SSP intermediate stage (SolverGodunovFiveEq.h:349-358 m_U_RK)
   unsigned int * d_ticket = nullptr; // block claiming counter of the step kernels (zero between launches)
-  // fused reflux of the full-mesh step (DevMesh::fin_*): per owned block the
-  // finishing counters it counts itself off, per deferred block its counter
-  // (at its initial value between launches), that value and its records
-  int32_t *      d_fin_tgt = nullptr, *d_fin_rec = nullptr;
-  unsigned int * d_fin_cnt = nullptr, *d_fin_init = nullptr;
-  int            n_fin = 0;
   // g5_step_batched: owned blocks grouped by instance (host), the call's work
   // list and instance mask (device)
   std::vector<int32_t> inst_blocks, inst_off;
@@ -207,9 +201,6 @@ free_mesh(G5Context * c)
   c->d_nbr_rel = c->d_out_normal = c->d_out_border = nullptr;
   c->d_reflux_buf = c->d_defer_buf = c->d_dt = c->d_invdt = nullptr;
   c->d_ticket = nullptr;
-  c->d_fin_tgt = c->d_fin_rec = nullptr;
-  c->d_fin_cnt = c->d_fin_init = nullptr;
-  c->n_fin = 0;
   c->d_batch_work = nullptr;
   c->d_inst_active = nullptr;
   c->inst_blocks.clear();
@@ -285,13 +276,6 @@ do_step(G5Context * c, const double * U, double * U2, const double * d_dt, int m
   a.work = sh.walk ? c->d_walk : nullptr;
   a.n_work = sh.walk ? c->n_owned : 0;
   a.reflux_layout = sh.reflux;
-  if (mode == G5_MODE_MIXED && sh.reflux == 2 && c->dim == 2 && c->n_fin > 0)
-  {
-    a.m.fin_tgt = c->d_fin_tgt;
-    a.m.fin_cnt = c->d_fin_cnt;
-    a.m.fin_init = c->d_fin_init;
-    a.m.fin_rec = c->d_fin_rec;
-  }
   int         launches = 0;
   cudaError_t e = mode == G5_MODE_FP64 ? g5::launch_step_fp64(c->dim, c->b, a, sh.ctas_per_sm, s, &launches)
                                        : g5::launch_step_mixed(c->dim, c->b, a, sh.ctas_per_sm, s, &launches);
@@ -671,69 +655,6 @@ g5_set_mesh(G5Context * c, const G5Mesh * m)
     if (!rc && (g5::launch_defer_info(dim, dev_mesh(c), c->d_defer_list, (int)recs.size(), c->d_defer_info, nullptr) != cudaSuccess ||
                 cudaStreamSynchronize(nullptr) != cudaSuccess))
       rc = 1;
-    // fused reflux: a deferred block's cells are finished by the CTA that
-    // makes the last of its inputs final, i.e. that counts the block's
-    // counter down to zero: the block itself and each fine block face that
-    // publishes into one of its records (the pairs the reflux pass reads,
-    // found as in the DeferInfo rows)
-    if (!rc)
-    {
-      const int            ntg = nfaces + 1;
-      std::vector<int32_t> fin_of(n_owned, -1), tgt((size_t)n_owned * ntg, -1), frec;
-      std::vector<uint32_t> init;
-      auto add_tgt = [&](int blk, int j) {
-        int32_t * row = &tgt[(size_t)blk * ntg];
-        int       k = 0;
-        while (k < ntg && row[k] >= 0)
-          ++k;
-        if (k == ntg)
-          return false;
-        row[k] = j;
-        ++init[j];
-        return true;
-      };
-      bool ok = true;
-      for (size_t r = 0; r < recs.size() && ok; ++r)
-      {
-        const int nb = recs[r] >> 3, f = recs[r] & 7;
-        if (fin_of[nb] < 0)
-        {
-          fin_of[nb] = (int)init.size();
-          init.push_back(0);
-          frec.insert(frec.end(), (size_t)nfaces, -1);
-          ok = add_tgt(nb, fin_of[nb]);
-        }
-        const int j = fin_of[nb];
-        int       k = 0;
-        while (frec[(size_t)j * nfaces + k] >= 0)
-          ++k;
-        frec[(size_t)j * nfaces + k] = (int32_t)r;
-        const int dir = f >> 1, side = f & 1;
-        int       d[3] = { 0, 0, 0 };
-        d[dir] = side ? 1 : -1;
-        const int s = (d[0] + 1) + 3 * (d[1] + 1) + (dim == 3 ? 9 * (d[2] + 1) : 0);
-        for (int cc = 0; cc < (dim == 2 ? 2 : 4) && ok; ++cc)
-        {
-          int ch[3] = { 0, 0, 0 };
-          ch[dir] = side ? 0 : 1;
-          ch[dir == 0 ? 1 : 0] = cc & 1;
-          if (dim == 3)
-            ch[dir == 2 ? 1 : 2] = cc >> 1;
-          const int F = m->nbr[((size_t)nb * ns + s) * nch + ch[0] + 2 * ch[1] + 4 * ch[2]];
-          if (F >= 0 && F < n_owned && reflux_slot[(size_t)F * nfaces + (f ^ 1)] >= 0)
-            ok = add_tgt(F, j);
-        }
-      }
-      rc = ok ? 0 : 1;
-      c->n_fin = (int)init.size();
-      if (!rc)
-      {
-        rc |= dev_upload(c, &c->d_fin_tgt, tgt.data(), tgt.size());
-        rc |= dev_upload(c, &c->d_fin_rec, frec.data(), frec.size());
-        rc |= dev_upload(c, &c->d_fin_init, init.data(), init.size());
-        rc |= dev_upload(c, &c->d_fin_cnt, init.data(), init.size());
-      }
-    }
     if (rc)
     {
       free_mesh(c);
@@ -1459,10 +1380,9 @@ g5_tune(G5Context * c, const double * d_U, double * d_U2, int mode, void * strea
   if (g5::launch_dt_update(c->d_invdt, c->d_dt, nullptr, c->n_inst, c->phys.cfl, s) != cudaSuccess)
     return G5_ERR_CUDA;
   // candidates: CTAs per SM x block claiming x walk order x reflux layout
-  // (the last only where it exists: the FP32-bulk 2D pass with records, as a
-  // separate pass in two layouts or fused into the step)
+  // (the last only where it exists: the FP32-bulk 2D pass with records)
   std::vector<G5Context::Shape> cand;
-  const int nreflux = (mode == G5_MODE_MIXED && c->dim == 2 && c->n_defer > 0) ? (c->n_fin > 0 ? 3 : 2) : 1;
+  const int nreflux = (mode == G5_MODE_MIXED && c->dim == 2 && c->n_defer > 0) ? 2 : 1;
   for (int k = 1; k <= occ && k < 16; ++k)
     for (int claim = 1; claim >= 0; --claim)
       for (int walk = 1; walk >= 0; --walk)
@@ -1560,7 +1480,7 @@ g5_set_shape(G5Context * c, int mode, const int32_t * shape4)
 {
   if (!c || !shape4 || (mode != G5_MODE_FP64 && mode != G5_MODE_MIXED))
     return G5_ERR_ARG;
-  if (shape4[0] < 0 || shape4[0] > 15 || (shape4[1] & ~1) || (shape4[2] & ~1) || shape4[3] < 0 || shape4[3] > 2)
+  if (shape4[0] < 0 || shape4[0] > 15 || (shape4[1] & ~1) || (shape4[2] & ~1) || (shape4[3] & ~1))
     return G5_ERR_ARG;
   G5Context::Shape sh;
   sh.ctas_per_sm = shape4[0];

@@ -70,17 +70,6 @@ struct DevMesh
   // neighbour is coarser; pg = [slot][NV][(b+4)^dim ghosted cells]
   const int32_t * pg_slot = nullptr;
   double *        pg = nullptr;
-  // fused reflux (null: a separate reflux pass finishes the deferred cells).
-  // fin_tgt[n * (2*dim + 1) + k]: the finishing counters owned block n counts
-  // itself off once its step is written (its own, when it has deferred cells,
-  // and those of the coarser blocks it publishes fine-face fluxes to), -1
-  // past the last; per deferred block j: its counter fin_cnt[j] (fin_init[j]
-  // between launches) and its records fin_rec[j * 2*dim + k] (rows of
-  // defer_info, -1 past the last)
-  const int32_t *      fin_tgt = nullptr;
-  unsigned int *       fin_cnt = nullptr;
-  const unsigned int * fin_init = nullptr;
-  const int32_t *      fin_rec = nullptr;
 };
 
 // row of the per-record table read by the reflux pass in one wave:
@@ -123,9 +112,7 @@ struct StepArgs
   // the CTA drawing the launch's last ticket resets it to 0.
   unsigned int * ticket = nullptr;
   // layout of the FP32-bulk 2D reflux pass: 0 eight lanes per deferred cell,
-  // 1 one thread per deferred cell (the FP64 form and 3D: one thread per
-  // cell), 2 fused into the FP32-bulk 2D full-mesh step (m.fin_tgt set; eight
-  // lanes per cell)
+  // 1 one thread per deferred cell (the FP64 form and 3D: one thread per cell)
   int            reflux_layout = 0;
   DevMesh        m;
   PhysParams     p;

@@ -53,16 +53,14 @@ launch_step2d_m(const StepArgs & a, int ctas_per_sm, cudaStream_t s, int * launc
     if (e != cudaSuccess)
       return e;
   }
-  if (a.m.n_defer == 0 || a.m.fin_tgt)
-    return e;
-  if (a.reflux_layout == 1)
+  if (a.m.n_defer > 0 && a.reflux_layout == 1)
   {
     const int n = a.m.n_defer * B;
     reflux2d_kernel<B, true><<<(n + 31) / 32, 32, 0, s>>>(a);
     ++*launches;
     e = cudaGetLastError();
   }
-  else
+  else if (a.m.n_defer > 0)
   {
     // 8 lanes per deferred cell
     const int n = a.m.n_defer * B * 8;

@@ -608,30 +608,6 @@ update_mixed(const double * uin, double * u2, const float * sFx, const float * s
 }
 
 
-template <int B>
-__device__ __forceinline__ void reflux2d_lanes(const StepArgs & a, int rec, int pos, bool act);
-
-// Fused reflux (FP32-bulk form): the deferred cells of deferred block j (its
-// records fin_rec[j * 4 ..]) on the NT threads of the calling CTA, eight
-// lanes per cell (whole warps: B * 8 lanes per record)
-template <int B, int NT>
-__device__ __forceinline__ void
-finish_deferred_2d(const StepArgs & a, int j)
-{
-  constexpr int PER = B * 8;
-  static_assert(PER % 32 == 0 && NT % 32 == 0, "whole warps per record");
-  const int4 rr = *reinterpret_cast<const int4 *>(a.m.fin_rec + (size_t)j * 4);
-  const int  nrec = (rr.x >= 0) + (rr.y >= 0) + (rr.z >= 0) + (rr.w >= 0);
-  for (int base = 0; base < nrec * PER; base += NT)
-  {
-    const int  item = base + (int)threadIdx.x;
-    const bool act = item < nrec * PER;
-    const int  slot = act ? item / PER : 0;
-    const int  rec = slot == 0 ? rr.x : (slot == 1 ? rr.y : (slot == 2 ? rr.z : rr.w));
-    reflux2d_lanes<B>(a, rec, (item >> 3) % B, act);
-  }
-}
-
 // 4 CTAs per SM in the FP32-bulk form (64 registers), so that CTAs in the
 // FP64-heavy update overlap with CTAs in the FP32 face phase; 2 CTAs per SM
 // (128 registers) in the FP64 form
@@ -658,7 +634,6 @@ step2d_kernel(StepArgs a)
   __shared__ DtT sRed[NT / 32];
   __shared__ int sSlot[10]; // the block's reflux slots (faces 0-3), its defer slots, its outside-twin range
   __shared__ int sNext;     // the CTA's next block
-  __shared__ int sFin[5];   // fused reflux: deferred blocks this CTA finishes
   static_assert(T::NREC * T::S * T::S * sizeof(R) >= H::NV * B * B * sizeof(double), "twin staging does not fit the slope area");
   const int         tid = threadIdx.x;
   const PhysParams & P = a.p;
@@ -681,8 +656,6 @@ step2d_kernel(StepArgs a)
       slot_v = tid < 4 ? a.m.reflux_slot[n * 4 + tid] : a.m.defer_slot[n * 4 + tid - 4];
     if (tid == 8 || tid == 9)
       slot_v = a.fill_twins ? a.m.twin_first[n + tid - 8] : 0;
-    // fused reflux: the finishing counters of this block (see below)
-    const int fin_v = (MIXED && a.m.fin_tgt && tid >= 16 && tid < 21) ? a.m.fin_tgt[n * 5 + tid - 16] : -1;
     const int    ins = a.m.inst ? a.m.inst[n] : 0;
     const double dx = P.level_dx[lev];
     R            dtdx_r;
@@ -984,45 +957,6 @@ step2d_kernel(StepArgs a)
         atomic_max_pos(a.invdt + ins, (double)mm);
       }
     }
-    if (MIXED && a.m.fin_tgt)
-    {
-      // fused reflux (FP32-bulk form): every output of this block is written (U2, its deferred
-      // cells' own face fluxes, its published fine-face fluxes, its twin
-      // cells); it counts itself off its finishing counters, and the CTA that
-      // brings one to zero finishes that block's deferred cells and resets
-      // the counter for the next launch.  Release: the barrier orders the
-      // CTA's writes before the counting thread's device-scope fence and
-      // atomic; acquire: that thread's fence after the atomic, then the
-      // barrier (the finishing reads bypass L1).
-      __syncthreads();
-      if (tid >= 16 && tid < 21)
-      {
-        int last = -1;
-        if (fin_v >= 0)
-        {
-          __threadfence();
-          if (atomicSub(a.m.fin_cnt + fin_v, 1u) == 1u)
-          {
-            __threadfence();
-            last = fin_v;
-          }
-        }
-        sFin[tid - 16] = last;
-      }
-      __syncthreads();
-#pragma unroll 1
-      for (int t = 0; t < 5; ++t)
-      {
-        const int j = sFin[t];
-        if (j >= 0)
-        {
-          if constexpr (MIXED)
-            finish_deferred_2d<B, NT>(a, j);
-          if (tid == 0)
-            a.m.fin_cnt[j] = a.m.fin_init[j];
-        }
-      }
-    }
     const int next = sNext; // read before the barrier: the next block's claim overwrites it
     __syncthreads();
     iw = next;
@@ -1072,20 +1006,48 @@ patch_twins_2d(const StepArgs & a, int n, int ci, int cj, const double * u2)
   }
 }
 
+// The same patches for one state variable (the value `val` of variable `var`
+// of the cell), so that the lanes of a cell's group each write their own
+template <int B>
+__device__ __forceinline__ void
+patch_twins_2d_var(const StepArgs & a, int n, int ci, int cj, int var, double val)
+{
+  using H = V<2>;
+  constexpr int NC = B * B;
+  const int     t0 = a.m.twin_first[n], t1 = a.m.twin_first[n + 1];
+  for (int t = t0; t < t1; ++t)
+  {
+    const int e = a.m.twin_list[t];
+    const int o = e >> 3, face = e & 7, dir = face >> 1, bc = a.p.bc[face];
+    double *  base = a.U2 + ((size_t)o * H::NV + var) * NC;
+    if (bc == 2)
+    {
+      if ((dir == 0 ? ci : cj) != ((face & 1) ? B - 1 : 0))
+        continue;
+      for (int k = 0; k < B; ++k)
+        base[dir == 0 ? k + B * cj : ci + B * k] = val;
+    }
+    else
+      base[dir == 0 ? (B - 1 - ci) + B * cj : ci + B * (B - 1 - cj)] = var == H::IU + dir ? -val : val;
+  }
+}
+
 // MIXED selects the FP32-bulk form of the mixed mode (float-pair increments
 // applied by apply_mixed_2d); the FP64 form replays the reference arithmetic.
 // A thread of this pass is latency-bound, so its loads come in two waves: the
 // record's DeferInfo row (slots, fine-face reflux slots, level, instance),
-// then the cell's old state and all face fluxes it needs.  The face fluxes
-// are read past L1 (ld.global.cg): in the step kernel's fused form other CTAs
-// of the same launch wrote them.
+// then the cell's old state and all face fluxes it needs.
 template <int B, bool MIXED>
-__device__ __forceinline__ void
-reflux2d_cell(const StepArgs & a, int rec, int pos)
+__global__ void
+reflux2d_kernel(StepArgs a)
 {
   using H = V<2>;
   using D = DeferInfo<2>;
   constexpr int NC = B * B;
+  const int     gid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= a.m.n_defer * B)
+    return;
+  const int   rec = gid / B, pos = gid % B;
   const int4 * row = reinterpret_cast<const int4 *>(a.m.defer_info + (size_t)rec * D::STRIDE);
   const int4  r0 = row[0], r1 = row[1], r2 = row[2], r3 = row[3];
   const int   code = r0.x;
@@ -1146,8 +1108,8 @@ reflux2d_cell(const StepArgs & a, int rec, int pos)
 #pragma unroll
     for (int k = 0; k < 8 / RV; ++k)
     {
-      const R2 x = __ldcg(q + k);
-      const R2 y = fine[f] ? __ldcg(q + 8 / RV + k) : R2{};
+      const R2 x = q[k];
+      const R2 y = fine[f] ? q[8 / RV + k] : R2{};
       F0[f][RV * k] = x.x;
       F0[f][RV * k + 1] = x.y;
       F1[f][RV * k] = y.x;
@@ -1339,16 +1301,6 @@ reflux2d_cell(const StepArgs & a, int rec, int pos)
   }
 }
 
-template <int B, bool MIXED>
-__global__ void
-reflux2d_kernel(StepArgs a)
-{
-  const int gid = blockIdx.x * blockDim.x + threadIdx.x;
-  if (gid >= a.m.n_defer * B)
-    return;
-  reflux2d_cell<B, MIXED>(a, gid / B, gid % B);
-}
-
 // ---------------------------------------------------------------------------
 // The FP32-bulk reflux pass with 8 lanes per deferred cell.  One thread per
 // cell ran a serial chain of about a thousand instructions with one warp per
@@ -1357,23 +1309,26 @@ reflux2d_kernel(StepArgs a)
 // state variable it updates (IAD0 IAD1 IA0 IA1 IE IU IV ID), and the lanes
 // exchange what couples them (u* for the volume-fraction source term, the two
 // volume fractions for the renormalisation, the partial densities for ID, the
-// new state for the CFL rate) by shuffles.  Every value is computed with the
+// new state for the CFL rate) by shuffles; each lane writes its variable to
+// the cell and to the cell's outside twins.  Every value is computed with the
 // arithmetic of apply_mixed_2d in the same order, so the pass gives the same
 // bits as the one-thread form.  All lanes of a warp reach every shuffle:
 // inactive cells (past the end, skipped, or of a stopped instance) compute on
 // zeros and write nothing.
 // ---------------------------------------------------------------------------
-// reflux2d_lanes: cell `pos` of record `rec` on the 8 lanes of the calling
-// thread's group (lane k = threadIdx.x % 8); every lane of the warp calls it.
 template <int B>
-__device__ __forceinline__ void
-reflux2d_lanes(const StepArgs & a, int rec, int pos, bool act)
+__global__ void __launch_bounds__(128)
+reflux2d_mixed_lanes_kernel(StepArgs a)
 {
   using H = V<2>;
   using D = DeferInfo<2>;
   constexpr int NC = B * B;
-  const int     k = (int)(threadIdx.x & 7u);       // flux component of this lane
+  const int     gid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int     k = gid & 7;                     // flux component of this lane
   const int     gb = (int)(threadIdx.x & 31u) & ~7; // first lane of the cell's group
+  const int     cslot = gid >> 3;
+  bool          act = cslot < a.m.n_defer * B;
+  const int     rec = act ? cslot / B : 0, pos = cslot % B;
   int4          r0 = make_int4(0, -1, -1, -1), r1 = make_int4(-1, -1, -1, -1), r2 = make_int4(-1, -1, -1, -1), r3 = make_int4(-1, 0, 0, 0);
   if (act)
   {
@@ -1438,11 +1393,11 @@ reflux2d_lanes(const StepArgs & a, int rec, int pos, bool act)
       if (fine[f])
       {
         const float * p0 = reinterpret_cast<const float *>(a.reflux_buf) + ((size_t)rs[f] * B + fl) * 8;
-        F0[f] = __ldcg(p0 + k);
-        F1[f] = __ldcg(p0 + 8 + k);
+        F0[f] = p0[k];
+        F1[f] = p0[8 + k];
       }
       else
-        F0[f] = __ldcg(reinterpret_cast<const float *>(a.defer_buf) + ((size_t)dslf * B + pos) * 32 + f * 8 + k);
+        F0[f] = reinterpret_cast<const float *>(a.defer_buf)[((size_t)dslf * B + pos) * 32 + f * 8 + k];
     }
   }
   // the whole old state in every lane of the group
@@ -1574,7 +1529,7 @@ reflux2d_lanes(const StepArgs & a, int rec, int pos, bool act)
     if (k == H::FUS)
       u2v = r0n + r1n;
   }
-  // the new state in every lane: CFL rate of the cell, twin patches
+  // the new state in every lane: CFL rate of the cell
   double u2[H::NV];
 #pragma unroll
   for (int v = 0; v < H::NV; ++v)
@@ -1584,8 +1539,8 @@ reflux2d_lanes(const StepArgs & a, int rec, int pos, bool act)
     a.U2[((size_t)n * H::NV + var) * NC + cell] = u2v;
     if (!finite_bits(u2v))
       raise_status(a.status, STATUS_NONPHYSICAL);
-    if (a.fill_twins && k == 0)
-      patch_twins_2d<B>(a, n, ci, cj, u2);
+    if (a.fill_twins)
+      patch_twins_2d_var<B>(a, n, ci, cj, var, u2v);
   }
   if (a.invdt)
   {
@@ -1600,15 +1555,6 @@ reflux2d_lanes(const StepArgs & a, int rec, int pos, bool act)
     }
     atomic_max_pos_warp(a.invdt, ins, (double)m_inv);
   }
-}
-
-template <int B>
-__global__ void __launch_bounds__(128)
-reflux2d_mixed_lanes_kernel(StepArgs a)
-{
-  const int  cslot = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 3);
-  const bool act = cslot < a.m.n_defer * B;
-  reflux2d_lanes<B>(a, act ? cslot / B : 0, cslot % B, act);
 }
 
 } // namespace g5

@@ -46,33 +46,70 @@ neg_zero(float x)
   return __float_as_uint(x) == 0x80000000u;
 }
 
-// halo cell h (0 .. 1215) of an 8^3 block -> ghosted offsets (-2 .. 9): the
-// four z layers outside the block, then the four y rows outside it in each
-// inner z layer, then the four x cells outside it in each inner row (x
-// fastest everywhere, so a warp reads consecutive cells of a neighbour)
+// The halo cells of an 8^3 block that the step reads, as ghosted offsets
+// (-2 .. 9); the other 128 cells of the 12^3 ghosted cube (two coordinates
+// two cells out) are never read.  h < HALO3_FULL: cells whose primitive state
+// the slopes read: the two layers beyond each face (z faces, then y, then x;
+// x fastest, the x layers as pairs of adjacent cells, so that a warp reads
+// contiguous runs of a neighbour), then the 96 cells along the block's edges
+// (one cell out in two coordinates).  HALO3_FULL <= h < HALO3_FULL +
+// HALO3_ALPHA (THINC only): cells whose volume fraction only the Youngs
+// normal of a face-neighbour cell reads: two coordinates out (one by two
+// cells), then three coordinates out (at most one by two cells).
+constexpr int HALO3_FULL = 864, HALO3_ALPHA = 224;
+
 __device__ __forceinline__ void
 halo_coords_3d(int h, int * g)
 {
-  if (h < 576)
+  if (h < 768)
   {
-    const int layer = h / 144, rem = h - layer * 144;
-    g[2] = layer < 2 ? layer - 2 : layer + 6;
-    g[1] = rem / 12 - 2;
-    g[0] = rem % 12 - 2;
+    if (h < 256)
+    {
+      const int zi = h >> 6;
+      g[2] = zi < 2 ? zi - 2 : zi + 6;
+      g[1] = (h >> 3) & 7;
+      g[0] = h & 7;
+    }
+    else if (h < 512)
+    {
+      const int i = h - 256, yi = i >> 6;
+      g[2] = (i >> 3) & 7;
+      g[1] = yi < 2 ? yi - 2 : yi + 6;
+      g[0] = i & 7;
+    }
+    else
+    {
+      const int i = h - 512, xs = i & 3;
+      g[2] = i >> 5;
+      g[1] = (i >> 2) & 7;
+      g[0] = xs < 2 ? xs - 2 : xs + 6;
+    }
+    return;
   }
-  else if (h < 960)
+  if (h < HALO3_FULL + 192)
   {
-    const int i = h - 576, z = i / 48, rem = i - z * 48, row = rem / 12;
-    g[2] = z;
-    g[1] = row < 2 ? row - 2 : row + 6;
-    g[0] = rem % 12 - 2;
+    // 12 lines along axis A (line >> 2) at one cell (h < HALO3_FULL) or at
+    // one and two cells (in either order) out in the two other axes
+    // (selects, not g[A] = ...: a run-time index would put g in local memory)
+    const bool full = h < HALO3_FULL;
+    const int  i = full ? h - 768 : h - HALO3_FULL;
+    const int  line = full ? i >> 3 : i >> 4;
+    const int  A = line >> 2;
+    const int  e1 = full ? 1 : (((i >> 3) & 1) ? 1 : 2), e2 = full ? 1 : 3 - e1;
+    const int  vA = i & 7, v1 = (line & 1) ? 7 + e1 : -e1, v2 = (line & 2) ? 7 + e2 : -e2;
+    // the first other axis is 1 for A = 0, else 0; the second is 1 for A = 2, else 2
+    g[0] = A == 0 ? vA : v1;
+    g[1] = A == 1 ? vA : (A == 0 ? v1 : v2);
+    g[2] = A == 2 ? vA : v2;
+    return;
   }
-  else
+  // 8 corners x (all one cell out, or one axis two cells out)
+  const int j = h - (HALO3_FULL + 192), corner = j >> 2, combo = j & 3;
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
   {
-    const int i = h - 960, z = i >> 5, rem = i & 31, xs = rem & 3;
-    g[2] = z;
-    g[1] = rem >> 2;
-    g[0] = xs < 2 ? xs - 2 : xs + 6;
+    const int e = combo == k + 1 ? 2 : 1;
+    g[k] = ((corner >> k) & 1) ? 7 + e : -e;
   }
 }
 
@@ -83,7 +120,9 @@ __device__ __forceinline__ void face_flux3(const typename Step3DTraits<MIXED>::R
                                            int f, typename Step3DTraits<MIXED>::R * sFd, typename Step3DTraits<MIXED>::R dtdx_r,
                                            const PhysParams & P);
 
-// conservative state seen by ghost cell g of block n (3D); false on a bad index
+// conservative state seen by ghost cell g of block n (3D); false on a bad
+// index.  ALPHA_ONLY: u[IA0] only (the same loads and sums for that variable)
+template <bool ALPHA_ONLY = false>
 __device__ __forceinline__ bool
 gather_ghost_3d(const StepArgs & a, int n, const int * c0, const int * g, double * u)
 {
@@ -112,7 +151,8 @@ gather_ghost_3d(const StepArgs & a, int n, const int * c0, const int * g, double
     const double * base = a.m.pg + (size_t)ps * H::NV * GGG + (g[0] + 2) + G * ((g[1] + 2) + G * (g[2] + 2));
 #pragma unroll
     for (int k = 0; k < H::NV; ++k)
-      u[k] = base[k * GGG];
+      if (!ALPHA_ONLY || k == H::IA0)
+        u[k] = base[k * GGG];
     return true;
   }
   if (rel <= 0)
@@ -127,7 +167,8 @@ gather_ghost_3d(const StepArgs & a, int n, const int * c0, const int * g, double
     const double * base = a.U + (size_t)src * H::NV * NC + c[0] + B * (c[1] + B * c[2]);
 #pragma unroll
     for (int k = 0; k < H::NV; ++k)
-      u[k] = base[k * NC];
+      if (!ALPHA_ONLY || k == H::IA0)
+        u[k] = base[k * NC];
     return true;
   }
   int ch[3], f0[3];
@@ -147,6 +188,8 @@ gather_ghost_3d(const StepArgs & a, int n, const int * c0, const int * g, double
 #pragma unroll
   for (int t = 0; t < 7; ++t)
   {
+    if (ALPHA_ONLY && vars[t] != H::IA0)
+      continue;
     const double * p = base + vars[t] * NC;
     double         sum = 0.0;
 #pragma unroll
@@ -160,9 +203,38 @@ gather_ghost_3d(const StepArgs & a, int n, const int * c0, const int * g, double
       }
     u[vars[t]] = sum / 8.0;
   }
-  u[H::IA1] = 1.0 - u[H::IA0];
-  u[H::ID] = u[H::IAD0] + u[H::IAD1];
+  if (!ALPHA_ONLY)
+  {
+    u[H::IA1] = 1.0 - u[H::IA0];
+    u[H::ID] = u[H::IAD0] + u[H::IAD1];
+  }
   return true;
+}
+
+// the volume-fraction primitive of store_prim3 (prim_mixed / prim_fp64) from
+// the conservative volume fraction alone
+template <bool MIXED>
+__device__ __forceinline__ typename Step3DTraits<MIXED>::R
+alpha_prim(double ia0)
+{
+  if constexpr (MIXED)
+  {
+    float a0 = fmaxf(0.0f, fminf(1.0f, d2f_nan(ia0)));
+    if (a0 < 1e-12f)
+      a0 = 0.0f;
+    if (a0 > 1.0f - 1e-12f)
+      a0 = 1.0f;
+    return a0;
+  }
+  else
+  {
+    double a0 = fmax(0.0, fmin(1.0, ia0));
+    if (a0 < 1e-12)
+      a0 = 0.0;
+    if (a0 > 1.0 - 1e-12)
+      a0 = 1.0;
+    return a0;
+  }
 }
 
 template <bool MIXED>
@@ -483,21 +555,34 @@ step3d_kernel(StepArgs a)
       a0f = af0 * fst0;
       a1f = af1 * fst1;
     }
-    constexpr int NHALO = GGG - NC;
-    for (int h = tid; h < NHALO; h += NT)
+    const int nhalo = HALO3_FULL + ((THINC < 0 ? P.thinc != 0 : THINC == 1) ? HALO3_ALPHA : 0);
+    for (int h = tid; h < nhalo; h += NT)
     {
       int g[3];
       halo_coords_3d(h, g);
-      double u[H::NV];
-      if (!gather_ghost_3d(a, n, c0, g, u))
+      const int gidx = (g[0] + 2) + G * (g[1] + 2) + GG * (g[2] + 2);
+      double    u[H::NV];
+      if (h < HALO3_FULL)
       {
-        raise_status(a.status, STATUS_MESH);
-        const double * own = a.U + (size_t)n * H::NV * NC + tid;
+        if (!gather_ghost_3d(a, n, c0, g, u))
+        {
+          raise_status(a.status, STATUS_MESH);
+          const double * own = a.U + (size_t)n * H::NV * NC + tid;
 #pragma unroll
-        for (int v = 0; v < H::NV; ++v)
-          u[v] = own[v * NC];
+          for (int v = 0; v < H::NV; ++v)
+            u[v] = own[v * NC];
+        }
+        store_prim3<MIXED>(sQ, gidx, u, P, eosk);
       }
-      store_prim3<MIXED>(sQ, (g[0] + 2) + G * (g[1] + 2) + GG * (g[2] + 2), u, P, eosk);
+      else
+      {
+        if (!gather_ghost_3d<true>(a, n, c0, g, u))
+        {
+          raise_status(a.status, STATUS_MESH);
+          u[H::IA0] = a.U[((size_t)n * H::NV + H::IA0) * NC + tid];
+        }
+        sQ[6 * GGG + gidx] = alpha_prim<MIXED>(u[H::IA0]);
+      }
     }
     if (tid < 12)
       sSlot[tid] = slot_v;

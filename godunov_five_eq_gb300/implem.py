@@ -538,8 +538,8 @@ class GodunovImplemGB300:
             raise G5Error(rc, "g5_tune")
         return self.tune_choice(mode)
 
-    # reflux_layout: 0 separate pass with 8 lanes per deferred cell, 1 separate
-    # pass with one thread per cell, 2 fused into the step
+    # reflux_layout (FP32-bulk 2D reflux pass): 0 eight lanes per deferred
+    # cell, 1 one thread per cell
     SHAPE_KEYS = ("ctas_per_sm", "claim", "walk_cf_first", "reflux_layout")
 
     def tune_choice(self, mode="fp64") -> dict:
@@ -571,7 +571,7 @@ class GodunovImplemGB300:
 
 def unpack_shape(code: int) -> dict:
     """A packed launch shape of g5_tune (ctas_per_sm + 16 claim + 32 walk + 64 reflux)."""
-    return {"ctas_per_sm": code & 15, "claim": (code >> 4) & 1, "walk_cf_first": (code >> 5) & 1, "reflux_layout": (code >> 6) & 3}
+    return {"ctas_per_sm": code & 15, "claim": (code >> 4) & 1, "walk_cf_first": (code >> 5) & 1, "reflux_layout": (code >> 6) & 1}
 
 
 def tune_pick(ms, default_index, margin=0.02) -> int:
