@@ -708,13 +708,26 @@ step2d_kernel(StepArgs a)
         prefetch_l2_line(a.m.nbr_rel + (size_t)nn * 9);
     }
 
-    // ---------------- phase 2: per ring cell slopes + Hancock source
-    for (int r = tid; r < SS; r += NT)
+    // ---------------- phase 2: per face-neighbour cell slopes + Hancock source
+    // (the block, then the row or column beyond each face, without gaps: the
+    // ring's corners are never a face neighbour; r: the cell's index in the
+    // ring layout)
+    for (int h = tid; h < NC + 4 * B; h += NT)
     {
-      const int ri = r % S - 1, rj = r / S - 1;
-      const bool corner = (ri < 0 || ri >= B) && (rj < 0 || rj >= B);
-      if (corner)
-        continue;
+      int ri, rj;
+      if (h < NC)
+      {
+        ri = h % B;
+        rj = h / B;
+      }
+      else
+      {
+        const int i = h - NC, f = i / B, pa = i % B;
+        const int side = (f & 1) ? B : -1;
+        ri = f < 2 ? side : pa;
+        rj = f < 2 ? pa : side;
+      }
+      const int r = (ri + 1) + S * (rj + 1);
       const int gi = (ri + 2) + G * (rj + 2);
       R         q[5], dqx[5], dqy[5];
       R st;

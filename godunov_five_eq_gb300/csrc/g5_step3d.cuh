@@ -615,13 +615,29 @@ step3d_kernel(StepArgs a)
       }
     }
 
-    // ---------------- phase 2: ring cells: Hancock source (and THINC |n|)
-    for (int r = tid; r < SSS; r += NT)
+    // ---------------- phase 2: face-neighbour cells: Hancock source
+    // The 896 cells of the ring that neighbour a face (the block, then the
+    // layer beyond each face; the ring's edges and corners are never a face
+    // neighbour), enumerated without gaps: two rounds of 512 threads, the
+    // second with 12 full warps.  r: the cell's index in the ring (S^3) layout.
+    for (int h = tid; h < NC + 6 * B * B; h += NT)
     {
-      const int ri = r % S - 1, rj = (r / S) % S - 1, rk = r / SS - 1;
-      const int outside = (ri < 0 || ri >= B) + (rj < 0 || rj >= B) + (rk < 0 || rk >= B);
-      if (outside > 1)
-        continue; // edges and corners of the ring are never a face neighbour
+      int ri, rj, rk;
+      if (h < NC)
+      {
+        ri = h & 7;
+        rj = (h >> 3) & 7;
+        rk = h >> 6;
+      }
+      else
+      {
+        const int i = h - NC, f = i >> 6, pa = i & 7, pb = (i >> 3) & 7;
+        const int side = (f & 1) ? B : -1;
+        ri = f < 2 ? side : pa;
+        rj = f < 2 ? pa : (f < 4 ? side : pb);
+        rk = f < 4 ? pb : side;
+      }
+      const int r = (ri + 1) + S * (rj + 1) + SS * (rk + 1);
       const int gi = (ri + 2) + G * (rj + 2) + GG * (rk + 2);
       if (P.integrator == 0)
       {
