@@ -19,7 +19,8 @@
  * slopes, MUSCL-Hancock and THINC reconstruction, flux store, read-back
  * update with both volume-fraction source terms, renormalisation, CFL
  * reduction), 2D and 3D, bit for bit; the refinement flags of the
- * reference's ComputeRefineFlags over threshold sweeps.
+ * reference's ComputeRefineFlags over threshold sweeps; the boundary fill of
+ * the reference's FillOutsideCellFunctor (ZERO_GRADIENT and WALL faces).
  *
  * Unpinned restatements (external kalypsso core, absent):
  *   - stiffened-gas mixture EOS (Allaire, Clerc & Kokh 2002);

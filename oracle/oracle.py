@@ -3,8 +3,9 @@
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import
 this module; it is the checker, never the measured or shipped path.
 Parity status: the scheme arithmetic is pinned to the reference's own code
-(HLLC and primitive conversion per state, and whole block steps of
-same-level tiles through the reference's scheme functors: tests/test_golden.py);
+(HLLC and primitive conversion per state, whole block steps of same-level
+tiles through the reference's scheme functors, the refinement flags and the
+boundary fill: tests/test_golden.py);
 the AMR stencils (restriction, prolongation, coarse/fine face sums), the
 mixture EOS and the Youngs normal are restatements of the external core
 (see g5_oracle.cpp).

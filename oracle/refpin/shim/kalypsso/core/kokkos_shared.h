@@ -28,6 +28,10 @@ struct Array
   static constexpr std::size_t size() { return N; }
   T *                          data() { return data_; }
   const T *                    data() const { return data_; }
+  T *                          begin() { return data_; }
+  T *                          end() { return data_ + N; }
+  const T *                    begin() const { return data_; }
+  const T *                    end() const { return data_ + N; }
 };
 template <typename T, std::size_t N>
 constexpr bool

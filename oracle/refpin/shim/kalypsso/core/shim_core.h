@@ -251,10 +251,62 @@ struct orchard_key_base_t
   using key_t = uint64_t;
   using view_t = Kokkos::View<uint64_t *, device_t>;
 };
+// The boundary fill's view of the block table (FillOutside pin, set by the
+// refpin driver): keys are block indices (owned blocks first, then the outside
+// quadrants); per outside quadrant o its inside source block, its outside
+// normal and the domain-border faces of that source block, as the block table
+// of the GPU path describes them.
+namespace refpin_fill
+{
+struct Table
+{
+  int32_t         n_owned = 0, n_outside = 0;
+  const int32_t * out_src = nullptr;    // [n_outside]
+  const int8_t *  out_normal = nullptr; // [n_outside * 3]
+  const int8_t *  out_border = nullptr; // [n_outside * 6]
+  std::vector<int8_t> border_of;        // [n_owned * 6] from out_border by source block
+};
+inline Table &
+table()
+{
+  static Table t;
+  return t;
+}
+} // namespace refpin_fill
+
 template <size_t dim>
 struct orchard_key_t
 {
   static KOKKOS_INLINE_FUNCTION int level(uint64_t key) { return static_cast<int>(key); }
+  // FillOutside pin (refpin_fill keys)
+  static Kokkos::Array<int32_t, dim> get_outside_normal(uint64_t key, brick_size_t<dim> const &, Kokkos::Array<bool, dim> const &)
+  {
+    const auto &                tb = refpin_fill::table();
+    Kokkos::Array<int32_t, dim> nrm{};
+    for (size_t e = 0; e < dim; ++e)
+      nrm[e] = tb.out_normal[(size_t)(key - tb.n_owned) * 3 + e];
+    return nrm;
+  }
+  static int32_t is_touching_face(uint64_t key, int dir)
+  {
+    const auto & tb = refpin_fill::table();
+    return tb.out_normal[(size_t)(key - tb.n_owned) * 3 + dir] != 0 ? 1 : 0;
+  }
+  static int32_t is_touching_face_X(uint64_t key) { return is_touching_face(key, 0); }
+  static int32_t is_touching_face_Y(uint64_t key) { return is_touching_face(key, 1); }
+  static int32_t is_touching_face_Z(uint64_t key) { return is_touching_face(key, 2); }
+  static uint64_t get_neighbor_key_same_level(uint64_t key, Kokkos::Array<int32_t, dim> const &, brick_size_t<dim> const &,
+                                              Kokkos::Array<bool, dim> const &)
+  {
+    const auto & tb = refpin_fill::table();
+    return (uint64_t)tb.out_src[key - tb.n_owned];
+  }
+  static void reset_outside_bits(uint64_t &) {}
+  static bool is_at_domain_border(uint64_t key_inside, int face, brick_size_t<dim> const &)
+  {
+    return refpin_fill::table().border_of[(size_t)key_inside * 6 + face] != 0;
+  }
+  static bool is_outside_dir(uint64_t key_outside, int dir) { return is_touching_face(key_outside, dir) != 0; }
 };
 
 template <typename device_t>
@@ -267,15 +319,100 @@ struct hashmap_base_t
 class AMRMeshInfo
 {
 public:
-  int32_t n_owned = 0, n_ghosts = 0;
+  int32_t n_owned = 0, n_ghosts = 0, n_outside = 0;
   AMRMeshInfo() = default;
-  AMRMeshInfo(int32_t o, int32_t g)
+  AMRMeshInfo(int32_t o, int32_t g, int32_t out = 0)
     : n_owned(o)
     , n_ghosts(g)
+    , n_outside(out)
   {}
   int32_t local_num_quadrants() const { return n_owned; }
   int32_t local_num_ghosts() const { return n_ghosts; }
+  // outside quadrants follow the owned ones (no ghosts in a one-rank pin)
+  int32_t first_outside_quad_local_id() const { return n_owned + n_ghosts; }
+  int32_t total_local_number_of_outside_quads() const { return n_outside; }
 };
+
+// faces xmin xmax ymin ymax zmin zmax and directions
+namespace Face
+{
+using face_t = int;
+template <size_t dim>
+constexpr Kokkos::Array<int, 2 * dim>
+get_all_faces()
+{
+  Kokkos::Array<int, 2 * dim> f{};
+  for (size_t i = 0; i < 2 * dim; ++i)
+    f[i] = (int)i;
+  return f;
+}
+KOKKOS_INLINE_FUNCTION constexpr bool
+is_left_face(int face)
+{
+  return (face & 1) == 0;
+}
+} // namespace Face
+namespace Dir
+{
+using dir_t = int;
+}
+
+template <size_t dim>
+constexpr Kokkos::Array<bool, dim>
+get_bool_array(bool v)
+{
+  Kokkos::Array<bool, dim> a{};
+  for (size_t i = 0; i < dim; ++i)
+    a[i] = v;
+  return a;
+}
+
+// brick settings read by functor constructors (unused by the pin's keys)
+template <size_t dim>
+brick_size_t<dim>
+get_brick_sizes(ConfigMap const & cm)
+{
+  brick_size_t<dim> b{};
+  for (size_t e = 0; e < dim; ++e)
+    b[e] = cm.getInteger("refpin", "brick" + std::to_string(e), 1);
+  return b;
+}
+template <size_t dim>
+Kokkos::Array<bool, dim>
+get_brick_periodicity(ConfigMap const & cm)
+{
+  Kokkos::Array<bool, dim> p{};
+  for (size_t e = 0; e < dim; ++e)
+    p[e] = cm.getBool("refpin", "periodic" + std::to_string(e), false);
+  return p;
+}
+
+// border conditions per face from the config ("refpin/bc<face>" integers,
+// the enum's integral values), as BorderConditionsConfig hands them over
+template <typename BC>
+struct BorderConditionsConfig
+{
+  template <size_t dim>
+  using bc_array_t = Kokkos::Array<BC, 2 * dim>;
+  template <size_t dim, size_t... I>
+  static bc_array_t<dim> read_faces(ConfigMap const & cm, std::index_sequence<I...>)
+  {
+    return bc_array_t<dim>{ { BC(static_cast<typename BC::_enumerated>(cm.getInteger("refpin", "bc" + std::to_string(I), 0)))... } };
+  }
+  template <size_t dim, typename PE>
+  static bc_array_t<dim> read_border_condition(ConfigMap const & cm, PE const &)
+  {
+    return read_faces<dim>(cm, std::make_index_sequence<2 * dim>{});
+  }
+};
+
+// the block index of a key (refpin_fill keys are block indices)
+template <typename M>
+std::pair<bool, int32_t>
+key_to_value(uint64_t key, M const &)
+{
+  return { true, static_cast<int32_t>(key) };
+}
 
 // conformal face status: 2 bits per face (xmin xmax ymin ymax zmin zmax)
 enum class conformal_neighbor_status : uint8_t

@@ -16,6 +16,7 @@ Run from the repository root (needs the reference tree and a built oracle):
 
     python tests/golden/make_scheme_golden.py           # block steps
     python tests/golden/make_scheme_golden.py --flags   # refinement flags
+    python tests/golden/make_scheme_golden.py --fill    # boundary fill
 """
 import ctypes
 import os
@@ -142,7 +143,7 @@ def main():
     print("wrote", OUT, os.path.getsize(OUT), "bytes")
 
 
-if __name__ == "__main__" and "--flags" not in sys.argv:
+if __name__ == "__main__" and "--flags" not in sys.argv and "--fill" not in sys.argv:
     sys.exit(main())
 
 
@@ -209,3 +210,74 @@ def main_flags():
 
 if __name__ == "__main__" and "--flags" in sys.argv:
     main_flags()
+
+
+# ---------------------------------------------------------------------------
+# Boundary fill (FillOutsideCellFunctor::apply, border_conditions/FillOutside.cpp:
+# 44-172) of the reference's own code on non-periodic AMR meshes with
+# ZERO_GRADIENT and WALL faces (refpin_fill_outside):
+# tests/golden/fill_outside_golden.npz
+# ---------------------------------------------------------------------------
+FILL_OUT = os.path.join(ROOT, "tests", "golden", "fill_outside_golden.npz")
+ZG, WALL = 2, 3
+# name: dim, seed, border condition of each face (xmin xmax ymin ymax zmin zmax)
+FILL_CASES = {
+    "2d_zero_gradient": (2, 1, (ZG,) * 6),
+    "2d_wall": (2, 2, (WALL,) * 6),
+    "2d_mixed": (2, 3, (ZG, WALL, WALL, ZG, ZG, ZG)),
+    "3d_mixed": (3, 4, (WALL, ZG, ZG, WALL, WALL, ZG)),
+}
+
+
+def fill_case(dim, seed):
+    """A non-periodic 2:1-balanced AMR mesh (outside quadrants on every face)
+    and a state whose every owned value is distinct (1 + its flat index), so
+    that each filled value names the value it was copied from."""
+    from tests.helpers import amr_mesh
+
+    if dim == 2:
+        mesh, t = amr_mesh(dim=2, b=8, nref=3, seed=seed, periodic=False)
+    else:
+        mesh, t = amr_mesh(dim=3, b=8, nref=2, seed=seed, periodic=False, nbrick=(2, 1, 1), lmin=1, lmax=2)
+    U = np.zeros((t.n_total, t.nv, t.ncell))
+    U[: t.n_owned] = 1.0 + np.arange(t.n_owned * t.nv * t.ncell, dtype=np.float64).reshape(t.n_owned, t.nv, t.ncell)
+    return mesh, t, U
+
+
+def load_fill():
+    lib = load()
+    vp = ctypes.c_void_p
+    lib.refpin_fill_outside.restype = ctypes.c_int
+    lib.refpin_fill_outside.argtypes = [ctypes.c_int] * 4 + [vp] * 5
+    return lib
+
+
+def reference_fill(lib, t, U, bc):
+    vp = ctypes.c_void_p
+    U = np.ascontiguousarray(U, np.float64).copy()
+    src = np.ascontiguousarray(t.out_src, np.int32)
+    nrm = np.ascontiguousarray(t.out_normal, np.int8)
+    brd = np.ascontiguousarray(t.out_border, np.int8)
+    bca = np.ascontiguousarray(bc, np.int32)
+    rc = lib.refpin_fill_outside(t.dim, t.bsize, t.n_owned, t.n_outside, src.ctypes.data_as(vp), nrm.ctypes.data_as(vp),
+                                 brd.ctypes.data_as(vp), bca.ctypes.data_as(vp), U.ctypes.data_as(vp))
+    if rc != 0:
+        raise RuntimeError(f"refpin_fill_outside failed ({rc})")
+    return U
+
+
+def main_fill():
+    lib = load_fill()
+    data = {}
+    for name, (dim, seed, bc) in FILL_CASES.items():
+        mesh, t, U = fill_case(dim, seed)
+        ref = reference_fill(lib, t, U, bc)
+        out = ref[t.n_owned :]
+        assert np.array_equal(out, np.rint(out)) and np.abs(out).max() < 2**31
+        data[f"{name}/outside"] = out.astype(np.int32)  # exact: the values are integers
+    np.savez_compressed(FILL_OUT, **data)
+    print("wrote", FILL_OUT, os.path.getsize(FILL_OUT), "bytes")
+
+
+if __name__ == "__main__" and "--fill" in sys.argv:
+    main_fill()

@@ -244,3 +244,70 @@ def test_oracle_refine_flags_match_reference_live(dim):
         ref = sweep(lib, dim, nb, U[: t.n_owned])
         got = _oracle_flag_sweep(t, p, U, EPS_LOHNER, EPS_REFINE, EPS_COARSEN)
         assert np.array_equal(got, ref), (seed, int((got != ref).sum()))
+
+
+# ---------------------------------------------------------------------------
+# Boundary fill against the reference's own FillOutsideCellFunctor
+# (border_conditions/FillOutside.cpp:44-172) on non-periodic AMR meshes with
+# ZERO_GRADIENT and WALL faces.  tests/golden/fill_outside_golden.npz comes from
+# `python tests/golden/make_scheme_golden.py --fill`.
+# ---------------------------------------------------------------------------
+FILL_GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "fill_outside_golden.npz")
+
+
+def _oracle_fill(t, U, bc):
+    from oracle.oracle import Oracle
+    from tests.helpers import water_air_params
+
+    p = water_air_params(t, dim=t.dim, b=t.bsize, bc=tuple(bc) + (2,) * (6 - len(bc)))
+    o = Oracle(t, p)
+    U = np.ascontiguousarray(U).copy()
+    o.fill_outside(U)
+    o.close()
+    return U
+
+
+def _fill_cases():
+    from tests.golden.make_scheme_golden import FILL_CASES
+
+    return sorted(FILL_CASES)
+
+
+@pytest.mark.parametrize("name", _fill_cases())
+def test_oracle_fill_outside_matches_reference_golden(name):
+    from tests.golden.make_scheme_golden import FILL_CASES, fill_case
+
+    dim, seed, bc = FILL_CASES[name]
+    mesh, t, U = fill_case(dim, seed)
+    assert t.n_outside > 0
+    ref = np.load(FILL_GOLDEN)[f"{name}/outside"].astype(np.float64)
+    got = _oracle_fill(t, U, bc)[t.n_owned :]
+    assert np.array_equal(got, ref), f"{(got != ref).sum()} of {ref.size} values differ"
+    # every outside value is a copy of an owned value, negated only by a WALL face
+    assert np.all(np.abs(ref) >= 1)
+    assert (ref < 0).any() == (3 in bc[: 2 * dim])
+
+
+@pytest.mark.skipif(not os.path.exists(REFPIN_LIB), reason="reference-pinning library not built (needs the reference tree)")
+@pytest.mark.parametrize("dim", [2, 3])
+def test_oracle_fill_outside_matches_reference_live(dim):
+    """Every ZERO_GRADIENT / WALL combination of the faces (2D; a sample in
+    3D) on fresh meshes and states against the reference's FillOutside
+    compiled in this checkout."""
+    import itertools
+
+    from tests.golden.make_scheme_golden import fill_case, load_fill, reference_fill
+
+    lib = load_fill()
+    combos = list(itertools.product((2, 3), repeat=2 * dim))
+    if dim == 3:
+        combos = combos[::7]
+    bad = []
+    for k, bc in enumerate(combos):
+        mesh, t, U = fill_case(dim, 20 + k % 3)
+        U[: t.n_owned] = np.random.default_rng(k).standard_normal(U[: t.n_owned].shape)
+        ref = reference_fill(lib, t, U, bc)[t.n_owned :]
+        got = _oracle_fill(t, U, bc)[t.n_owned :]
+        if not np.array_equal(got, ref):
+            bad.append((bc, int((got != ref).sum())))
+    assert not bad, bad
