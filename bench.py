@@ -23,9 +23,10 @@ roofline         fused step kernel: 128 B/cell-update (read U + write U2,
 cpu_baseline     the CPU oracle (FP64 restatement, OpenMP) on the host cores,
                  bounded sample of the same workload
 workloads        the same measurements (value, FP64 value, L1, roofline, CPU
-                 baseline) for further workloads, by default the 256
-                 batched droplet-advection instances and the 3D triple point
-                 (--extra-workloads)
+                 baseline) for the other benchmark configurations, by
+                 default the 256 batched droplet-advection instances, the 3D
+                 triple point, the air-R22 THINC shock-bubble and the
+                 gas-water shock tube (--extra-workloads)
 
 --impl reference times the CPU restatement of the reference method (the
 reference's own Kokkos build cannot be built: its kalypsso core, Kokkos and
@@ -63,7 +64,7 @@ def parse():
     ap.add_argument("--no-l1", action="store_true", help="skip the 500-step accuracy run")
     ap.add_argument(
         "--extra-workloads",
-        default="droplets,triple_point_3d",
+        default="droplets,triple_point_3d,shock_bubble_r22_thinc,gas_water",
         help="comma-separated workloads measured after the headline and reported under 'workloads' ('none' to skip)",
     )
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
@@ -591,8 +592,9 @@ def main():
         res[mode]["impl"].close()
 
     # further workloads on the same line (not the headline): the batched
-    # droplet instances (many uneven instances in one persistent launch) and
-    # the 3D triple point (8^3 blocks, THINC, levels 0..3)
+    # droplet instances (many uneven instances in one persistent launch), the
+    # 3D triple point (8^3 blocks, THINC, levels 0..3), the air-R22 THINC
+    # shock-bubble and the gas-water shock tube
     workloads = {}
     for extra in [w for w in args.extra_workloads.split(",") if w and w != "none" and w != args.workload]:
         mx = measure(extra, args, world, local, flush, stream, min(args.steps, 10), clocks=False, want_l1=not args.no_l1)

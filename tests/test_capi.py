@@ -38,6 +38,11 @@ def test_invalid_params_rejected_without_device():
     assert lib.g5_create(ctypes.byref(p), ctypes.byref(ctx)) == -1
     assert lib.g5_create(None, ctypes.byref(ctx)) == -1
     assert lib.g5_destroy(None) == -1
+    # calls on no context are refused before any device work
+    fields = (ctypes.c_int32 * 2)(0, 64)
+    assert lib.g5_pack_fields(None, None, fields, 2, 0, 1, None, None) == -1
+    assert lib.g5_derived_quantity(None, None, 0, 0, 1, None, None) == -1
+    assert lib.g5_set_shape(None, 0, (ctypes.c_int32 * 4)(0, 1, 1, 0)) == -1
 
 
 def test_tune_pick_selection_rule():
