@@ -69,6 +69,13 @@ def parse():
     )
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch shape (no g5_tune before timing)")
+    ap.add_argument(
+        "--reflux-layout",
+        type=int,
+        choices=[0, 1, 2],
+        default=None,
+        help="FP32-bulk 2D reflux layout of --profile and --no-tune runs (0 separate pass, 8 lanes per cell; 1 separate pass, one thread per cell; 2 the step kernel's tail; default: the library's)",
+    )
     ap.add_argument("--profile", action="store_true", help="one FP64 and one mixed step kernel launch, for ncu")
     ap.add_argument("--no-clocks", action="store_true", help="skip the nvidia-smi clock sampling (and its bracketing load)")
     ap.add_argument(
@@ -354,6 +361,8 @@ def run_profile_case(args):
 
     desc, t, p, U = build_workload(args.workload, gpu_flag_fn(), args.prolongation)
     impl = GodunovImplemGB300(p, t)
+    if args.reflux_layout is not None:
+        impl.set_shape("mixed", reflux_layout=args.reflux_layout)
     A = torch.from_numpy(U.copy()).cuda()
     B = torch.zeros_like(A)
     impl.fill_outside_quadrants(A)
@@ -453,6 +462,8 @@ def measure(name, args, world, local, flush, stream, steps, clocks=True, want_l1
         B = torch.zeros_like(A)
         # the autotuner picks the launch shape of this mesh (g5_tune, untimed)
         impl.fill_outside_quadrants(A)
+        if args.no_tune and args.reflux_layout is not None:
+            impl.set_shape(mode, reflux_layout=args.reflux_layout)
         shape = impl.tune(A, B, mode) if not args.no_tune else impl.tune_choice(mode)
         impl.begin(A)
         for _ in range(args.warmup):
@@ -522,7 +533,9 @@ def measure(name, args, world, local, flush, stream, steps, clocks=True, want_l1
         "traffic": traffic,
         "traffic_source": (f"committed ncu capture profiles/{PROFILE_OF[name][0]} (dram read + write bytes per launch), scaled by cells" if traffic else None),
         "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback 6.8 TB/s",
-        "kernel": "step2d_kernel<16,mixed> (+reflux2d)" if t.dim == 2 else "step3d_kernel<mixed> (+reflux3d)",
+        "kernel": ("step2d_kernel<16,mixed> (+reflux in its tail)" if res["mixed"]["shape"].get("reflux_layout") == 2 else "step2d_kernel<16,mixed> (+reflux2d)")
+        if t.dim == 2
+        else "step3d_kernel<mixed> (+reflux3d)",
         "kernel_ms": res["mixed"]["kern_ms"],
         "algorithmic_bytes_per_launch": cells * bpc,
         "fp64_kernel_ms": res["fp64"]["kern_ms"],

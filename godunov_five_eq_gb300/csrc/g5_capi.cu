@@ -36,6 +36,10 @@ struct G5Context
   double *       d_dt = nullptr, *d_invdt = nullptr;
   double *       d_urk = nullptr; // RK2_SSP intermediate stage (SolverGodunovFiveEq.h:349-358 m_U_RK)
   unsigned int * d_ticket = nullptr; // block claiming counter of the step kernels (zero between launches)
+  // reflux in the tail of the FP32-bulk 2D full-mesh step (DevMesh::fin_*)
+  int32_t *      d_fin_tgt = nullptr, *d_fin_rec = nullptr;
+  unsigned int * d_fin_cnt = nullptr, *d_fin_init = nullptr, *d_fin_ticket = nullptr;
+  int            n_fin = 0;
   // g5_step_batched: owned blocks grouped by instance (host), the call's work
   // list and instance mask (device)
   std::vector<int32_t> inst_blocks, inst_off;
@@ -51,13 +55,15 @@ struct G5Context
   std::unordered_map<const void *, PoolEntry> pool; // device buffers by field (dev_alloc)
   // launch shape of the step per precision mode (g5_tune): CTAs per SM (0:
   // occupancy maximum), dynamic block claiming, walk order (1: blocks with
-  // coarse/fine neighbours first, 0: table order), reflux-pass layout
+  // coarse/fine neighbours first, 0: table order), reflux layout (2: the
+  // step kernel's tail where the FP32-bulk 2D full-mesh step has records,
+  // otherwise the separate pass with 8 lanes per cell)
   struct Shape
   {
     int ctas_per_sm = 0;
     int claim = 1;
     int walk = 1;
-    int reflux = 0;
+    int reflux = 2;
   };
   Shape          shape[2];
   std::vector<std::pair<int, float>> tune_log[2]; // (packed shape, ms per step) of the last g5_tune
@@ -201,6 +207,9 @@ free_mesh(G5Context * c)
   c->d_nbr_rel = c->d_out_normal = c->d_out_border = nullptr;
   c->d_reflux_buf = c->d_defer_buf = c->d_dt = c->d_invdt = nullptr;
   c->d_ticket = nullptr;
+  c->d_fin_tgt = c->d_fin_rec = nullptr;
+  c->d_fin_cnt = c->d_fin_init = c->d_fin_ticket = nullptr;
+  c->n_fin = 0;
   c->d_batch_work = nullptr;
   c->d_inst_active = nullptr;
   c->inst_blocks.clear();
@@ -276,6 +285,15 @@ do_step(G5Context * c, const double * U, double * U2, const double * d_dt, int m
   a.work = sh.walk ? c->d_walk : nullptr;
   a.n_work = sh.walk ? c->n_owned : 0;
   a.reflux_layout = sh.reflux;
+  if (mode == G5_MODE_MIXED && sh.reflux == 2 && c->n_fin > 0)
+  {
+    a.m.fin_tgt = c->d_fin_tgt;
+    a.m.fin_cnt = c->d_fin_cnt;
+    a.m.fin_init = c->d_fin_init;
+    a.m.fin_rec = c->d_fin_rec;
+    a.m.fin_ticket = c->d_fin_ticket;
+    a.m.n_fin = c->n_fin;
+  }
   int         launches = 0;
   cudaError_t e = mode == G5_MODE_FP64 ? g5::launch_step_fp64(c->dim, c->b, a, sh.ctas_per_sm, s, &launches)
                                        : g5::launch_step_mixed(c->dim, c->b, a, sh.ctas_per_sm, s, &launches);
@@ -655,6 +673,71 @@ g5_set_mesh(G5Context * c, const G5Mesh * m)
     if (!rc && (g5::launch_defer_info(dim, dev_mesh(c), c->d_defer_list, (int)recs.size(), c->d_defer_info, nullptr) != cudaSuccess ||
                 cudaStreamSynchronize(nullptr) != cudaSuccess))
       rc = 1;
+    // reflux in the step's tail (2D): per deferred block (a coarse block with
+    // records) a counter of the arrivals that make its records final: the
+    // block itself, each fine block face publishing into one of its records
+    // (the pairs the reflux pass reads, found as in the DeferInfo rows), and
+    // one claim by a CTA out of blocks.  Whoever brings it to zero finishes
+    // the block's deferred cells, so nothing waits.
+    if (!rc && dim == 2)
+    {
+      const int             ntg = nfaces + 1;
+      std::vector<int32_t>  fin_of(n_owned, -1), tgt((size_t)n_owned * ntg, -1), frec;
+      std::vector<uint32_t> init;
+      auto                  add_tgt = [&](int blk, int j) {
+        int32_t * row = &tgt[(size_t)blk * ntg];
+        int       k = 0;
+        while (k < ntg && row[k] >= 0)
+          ++k;
+        if (k == ntg)
+          return false;
+        row[k] = j;
+        ++init[j];
+        return true;
+      };
+      bool ok = true;
+      for (size_t r = 0; r < recs.size() && ok; ++r)
+      {
+        const int nb = recs[r] >> 3, f = recs[r] & 7;
+        if (fin_of[nb] < 0)
+        {
+          fin_of[nb] = (int)init.size();
+          init.push_back(1); // the tail claim
+          frec.insert(frec.end(), (size_t)nfaces, -1);
+          ok = add_tgt(nb, fin_of[nb]);
+        }
+        const int j = fin_of[nb];
+        int       k = 0;
+        while (frec[(size_t)j * nfaces + k] >= 0)
+          ++k;
+        frec[(size_t)j * nfaces + k] = (int32_t)r;
+        const int dir = f >> 1, side = f & 1;
+        int       d[3] = { 0, 0, 0 };
+        d[dir] = side ? 1 : -1;
+        const int s = (d[0] + 1) + 3 * (d[1] + 1);
+        for (int cc = 0; cc < 2 && ok; ++cc)
+        {
+          int ch[2] = { 0, 0 };
+          ch[dir] = side ? 0 : 1;
+          ch[dir == 0 ? 1 : 0] = cc & 1;
+          const int F = m->nbr[((size_t)nb * ns + s) * nch + ch[0] + 2 * ch[1]];
+          if (F >= 0 && F < n_owned && reflux_slot[(size_t)F * nfaces + (f ^ 1)] >= 0)
+            ok = add_tgt(F, j);
+        }
+      }
+      rc = ok ? 0 : 1;
+      c->n_fin = ok ? (int)init.size() : 0;
+      if (!rc)
+      {
+        rc |= dev_upload(c, &c->d_fin_tgt, tgt.data(), tgt.size());
+        rc |= dev_upload(c, &c->d_fin_rec, frec.data(), frec.size());
+        rc |= dev_upload(c, &c->d_fin_init, init.data(), init.size());
+        rc |= dev_upload(c, &c->d_fin_cnt, init.data(), init.size());
+        rc |= dev_alloc(c, &c->d_fin_ticket, 1);
+        if (!rc && cudaMemset(c->d_fin_ticket, 0, sizeof(unsigned int)) != cudaSuccess)
+          rc = 1;
+      }
+    }
     if (rc)
     {
       free_mesh(c);
@@ -1382,7 +1465,7 @@ g5_tune(G5Context * c, const double * d_U, double * d_U2, int mode, void * strea
   // candidates: CTAs per SM x block claiming x walk order x reflux layout
   // (the last only where it exists: the FP32-bulk 2D pass with records)
   std::vector<G5Context::Shape> cand;
-  const int nreflux = (mode == G5_MODE_MIXED && c->dim == 2 && c->n_defer > 0) ? 2 : 1;
+  const int nreflux = (mode == G5_MODE_MIXED && c->dim == 2 && c->n_defer > 0) ? (c->n_fin > 0 ? 3 : 2) : 1;
   for (int k = 1; k <= occ && k < 16; ++k)
     for (int claim = 1; claim >= 0; --claim)
       for (int walk = 1; walk >= 0; --walk)
@@ -1395,10 +1478,12 @@ g5_tune(G5Context * c, const double * d_U, double * d_U2, int mode, void * strea
           sh.reflux = rf;
           cand.push_back(sh);
         }
-  // the default: the occupancy maximum, claiming, coarse/fine-first walk, lanes
-  int def = 0;
+  // the default: the occupancy maximum, claiming, coarse/fine-first walk,
+  // records finished in the step's tail where that layout exists, else lanes
+  const int def_reflux = nreflux == 3 ? 2 : 0;
+  int       def = 0;
   for (size_t i = 0; i < cand.size(); ++i)
-    if (cand[i].ctas_per_sm == occ && cand[i].claim == 1 && cand[i].walk == 1 && cand[i].reflux == 0)
+    if (cand[i].ctas_per_sm == occ && cand[i].claim == 1 && cand[i].walk == 1 && cand[i].reflux == def_reflux)
       def = (int)i;
   const G5Context::Shape saved = c->shape[mode];
   std::vector<float>     ms(cand.size(), 0.0f);
@@ -1480,7 +1565,7 @@ g5_set_shape(G5Context * c, int mode, const int32_t * shape4)
 {
   if (!c || !shape4 || (mode != G5_MODE_FP64 && mode != G5_MODE_MIXED))
     return G5_ERR_ARG;
-  if (shape4[0] < 0 || shape4[0] > 15 || (shape4[1] & ~1) || (shape4[2] & ~1) || (shape4[3] & ~1))
+  if (shape4[0] < 0 || shape4[0] > 15 || (shape4[1] & ~1) || (shape4[2] & ~1) || shape4[3] < 0 || shape4[3] > 2)
     return G5_ERR_ARG;
   G5Context::Shape sh;
   sh.ctas_per_sm = shape4[0];

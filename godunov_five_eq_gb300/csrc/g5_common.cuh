@@ -70,6 +70,20 @@ struct DevMesh
   // neighbour is coarser; pg = [slot][NV][(b+4)^dim ghosted cells]
   const int32_t * pg_slot = nullptr;
   double *        pg = nullptr;
+  // reflux in the tail of the FP32-bulk 2D full-mesh step (null: the separate
+  // pass).  fin_tgt[n * 5 + k]: the counters owned block n counts off once
+  // its step is written (its own, when it has deferred cells, and those of
+  // the coarser blocks it publishes fine-face fluxes to), -1 past the last;
+  // per deferred block j: fin_cnt[j] (fin_init[j] between launches: its
+  // arrivals plus one tail claim) and its records fin_rec[j * 4 + k] (rows of
+  // defer_info, -1 past the last); fin_ticket: the tail claims of a launch
+  // (0 between launches)
+  const int32_t *      fin_tgt = nullptr;
+  unsigned int *       fin_cnt = nullptr;
+  const unsigned int * fin_init = nullptr;
+  const int32_t *      fin_rec = nullptr;
+  unsigned int *       fin_ticket = nullptr;
+  int                  n_fin = 0;
 };
 
 // row of the per-record table read by the reflux pass in one wave:
@@ -112,7 +126,9 @@ struct StepArgs
   // the CTA drawing the launch's last ticket resets it to 0.
   unsigned int * ticket = nullptr;
   // layout of the FP32-bulk 2D reflux pass: 0 eight lanes per deferred cell,
-  // 1 one thread per deferred cell (the FP64 form and 3D: one thread per cell)
+  // 1 one thread per deferred cell (the FP64 form and 3D: one thread per
+  // cell), 2 eight lanes per cell in the step kernel's tail when m.fin_tgt is
+  // set (the full-mesh step), else as 0
   int            reflux_layout = 0;
   DevMesh        m;
   PhysParams     p;

@@ -53,6 +53,8 @@ launch_step2d_m(const StepArgs & a, int ctas_per_sm, cudaStream_t s, int * launc
     if (e != cudaSuccess)
       return e;
   }
+  if (a.m.fin_tgt)
+    return e; // the step kernel's tail finished the deferred cells
   if (a.m.n_defer > 0 && a.reflux_layout == 1)
   {
     const int n = a.m.n_defer * B;

@@ -608,6 +608,30 @@ update_mixed(const double * uin, double * u2, const float * sFx, const float * s
 }
 
 
+template <int B>
+__device__ __forceinline__ void reflux2d_lanes(const StepArgs & a, int rec, int pos, bool act);
+
+// Reflux in the step kernel's tail (FP32-bulk form): the deferred cells of
+// deferred block j (its records fin_rec[j * 4 ..]) on the NT threads of the
+// calling CTA, eight lanes per cell (whole warps: B * 8 lanes per record)
+template <int B, int NT>
+__device__ __forceinline__ void
+finish_deferred_2d(const StepArgs & a, int j)
+{
+  constexpr int PER = B * 8;
+  static_assert(PER % 32 == 0 && NT % 32 == 0, "whole warps per record");
+  const int4 rr = *reinterpret_cast<const int4 *>(a.m.fin_rec + (size_t)j * 4);
+  const int  nrec = (rr.x >= 0) + (rr.y >= 0) + (rr.z >= 0) + (rr.w >= 0);
+  for (int base = 0; base < nrec * PER; base += NT)
+  {
+    const int  item = base + (int)threadIdx.x;
+    const bool act = item < nrec * PER;
+    const int  slot = act ? item / PER : 0;
+    const int  rec = slot == 0 ? rr.x : (slot == 1 ? rr.y : (slot == 2 ? rr.z : rr.w));
+    reflux2d_lanes<B>(a, rec, (item >> 3) % B, act);
+  }
+}
+
 // 4 CTAs per SM in the FP32-bulk form (64 registers), so that CTAs in the
 // FP64-heavy update overlap with CTAs in the FP32 face phase; 2 CTAs per SM
 // (128 registers) in the FP64 form
@@ -634,6 +658,7 @@ step2d_kernel(StepArgs a)
   __shared__ DtT sRed[NT / 32];
   __shared__ int sSlot[10]; // the block's reflux slots (faces 0-3), its defer slots, its outside-twin range
   __shared__ int sNext;     // the CTA's next block
+  __shared__ int sFin[6];   // reflux in the tail: deferred blocks to finish, end of the claims
   static_assert(T::NREC * T::S * T::S * sizeof(R) >= H::NV * B * B * sizeof(double), "twin staging does not fit the slope area");
   const int         tid = threadIdx.x;
   const PhysParams & P = a.p;
@@ -642,9 +667,24 @@ step2d_kernel(StepArgs a)
   const int eosk = STIFF < 0 ? (P.mg_any ? 2 : ((P.gpx[0] != 0.0 || P.gpx[1] != 0.0) ? 1 : 0)) : STIFF;
 
   const int nwalk = step_count(a);
-  for (int iw = blockIdx.x; iw < nwalk;)
+  // reflux in the tail (FP32-bulk form, m.fin_tgt set): after its step a
+  // block counts itself off the counters of the deferred blocks whose records
+  // it completes (its own and those of the coarser blocks it publishes to);
+  // a CTA out of blocks claims deferred blocks by ticket and counts a claim
+  // off; whoever brings a counter to zero finishes that block's deferred
+  // cells.  Release: the barrier orders the CTA's writes before the counting
+  // thread's device-scope fence and atomic; acquire: that thread's fence
+  // after the atomic, then the barrier.
+  const bool fused = MIXED && a.m.fin_tgt != nullptr;
+  for (int iw = blockIdx.x;;)
   {
+    int next = iw;
+    if (iw < nwalk)
+    {
     const int    n = a.work ? a.work[iw] : iw;
+    const int    fin_v = (fused && tid >= 16 && tid < 21) ? a.m.fin_tgt[n * 5 + tid - 16] : -1;
+    // (a block with no counter to count off skips the tail's barriers)
+    const bool   counts = fused && a.m.fin_tgt[n * 5] >= 0;
     const int    lev = a.m.level[n];
     const int    cx0 = a.m.coord[n * 3 + 0], cy0 = a.m.coord[n * 3 + 1];
     // the next block is claimed now (the ticket's latency hides behind the gather)
@@ -970,7 +1010,79 @@ step2d_kernel(StepArgs a)
         atomic_max_pos(a.invdt + ins, (double)mm);
       }
     }
-    const int next = sNext; // read before the barrier: the next block's claim overwrites it
+    if (counts)
+    {
+      __syncthreads(); // every output of the block is written
+      if (tid >= 16 && tid < 21)
+      {
+        int ready = -1;
+        if (fin_v >= 0)
+        {
+          __threadfence();
+          if (atomicSub(a.m.fin_cnt + fin_v, 1u) == 1u)
+          {
+            __threadfence();
+            ready = fin_v;
+          }
+        }
+        sFin[tid - 16] = ready;
+      }
+      if (tid == 0)
+        sFin[5] = 0;
+    }
+    next = sNext; // read before the barrier: the next block's claim overwrites it
+    if (!counts)
+    {
+      __syncthreads();
+      iw = next;
+      continue;
+    }
+    }
+    else
+    {
+      if (!fused)
+        break;
+      if (tid == 0)
+      {
+        // claim the next deferred block; the launch's last draw resets the ticket
+        const unsigned d = atomicAdd(a.m.fin_ticket, 1u);
+        int            ready = -1;
+        if (d < (unsigned)a.m.n_fin)
+        {
+          __threadfence();
+          if (atomicSub(a.m.fin_cnt + d, 1u) == 1u)
+          {
+            __threadfence();
+            ready = (int)d;
+          }
+        }
+        else if (d == (unsigned)a.m.n_fin + gridDim.x - 1u)
+          *a.m.fin_ticket = 0u;
+        sFin[0] = ready;
+        sFin[1] = sFin[2] = sFin[3] = sFin[4] = -1;
+        sFin[5] = d >= (unsigned)a.m.n_fin;
+      }
+    }
+    if (fused)
+    {
+      __syncthreads();
+      if constexpr (MIXED)
+      {
+#pragma unroll 1
+        for (int t = 0; t < 5; ++t)
+        {
+          const int j = sFin[t];
+          if (j >= 0)
+          {
+            finish_deferred_2d<B, NT>(a, j);
+            if (tid == 0)
+              a.m.fin_cnt[j] = a.m.fin_init[j];
+          }
+        }
+      }
+      if (iw >= nwalk && sFin[5])
+        break;
+    }
     __syncthreads();
     iw = next;
   }
@@ -1329,19 +1441,19 @@ reflux2d_kernel(StepArgs a)
 // inactive cells (past the end, skipped, or of a stopped instance) compute on
 // zeros and write nothing.
 // ---------------------------------------------------------------------------
+// cell `pos` of record `rec` on the 8 lanes of the calling thread's group
+// (lane k = threadIdx.x % 8); every lane of the warp calls it.  The face
+// fluxes are read past L1 (ld.global.cg): in the step kernel's tail other CTAs
+// of the same launch wrote them.
 template <int B>
-__global__ void __launch_bounds__(128)
-reflux2d_mixed_lanes_kernel(StepArgs a)
+__device__ __forceinline__ void
+reflux2d_lanes(const StepArgs & a, int rec, int pos, bool act)
 {
   using H = V<2>;
   using D = DeferInfo<2>;
   constexpr int NC = B * B;
-  const int     gid = blockIdx.x * blockDim.x + threadIdx.x;
-  const int     k = gid & 7;                     // flux component of this lane
+  const int     k = (int)(threadIdx.x & 7u);       // flux component of this lane
   const int     gb = (int)(threadIdx.x & 31u) & ~7; // first lane of the cell's group
-  const int     cslot = gid >> 3;
-  bool          act = cslot < a.m.n_defer * B;
-  const int     rec = act ? cslot / B : 0, pos = cslot % B;
   int4          r0 = make_int4(0, -1, -1, -1), r1 = make_int4(-1, -1, -1, -1), r2 = make_int4(-1, -1, -1, -1), r3 = make_int4(-1, 0, 0, 0);
   if (act)
   {
@@ -1406,11 +1518,11 @@ reflux2d_mixed_lanes_kernel(StepArgs a)
       if (fine[f])
       {
         const float * p0 = reinterpret_cast<const float *>(a.reflux_buf) + ((size_t)rs[f] * B + fl) * 8;
-        F0[f] = p0[k];
-        F1[f] = p0[8 + k];
+        F0[f] = __ldcg(p0 + k);
+        F1[f] = __ldcg(p0 + 8 + k);
       }
       else
-        F0[f] = reinterpret_cast<const float *>(a.defer_buf)[((size_t)dslf * B + pos) * 32 + f * 8 + k];
+        F0[f] = __ldcg(reinterpret_cast<const float *>(a.defer_buf) + ((size_t)dslf * B + pos) * 32 + f * 8 + k);
     }
   }
   // the whole old state in every lane of the group
@@ -1568,6 +1680,15 @@ reflux2d_mixed_lanes_kernel(StepArgs a)
     }
     atomic_max_pos_warp(a.invdt, ins, (double)m_inv);
   }
+}
+
+template <int B>
+__global__ void __launch_bounds__(128)
+reflux2d_mixed_lanes_kernel(StepArgs a)
+{
+  const int  cslot = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 3);
+  const bool act = cslot < a.m.n_defer * B;
+  reflux2d_lanes<B>(a, act ? cslot / B : 0, cslot % B, act);
 }
 
 } // namespace g5

@@ -539,7 +539,8 @@ class GodunovImplemGB300:
         return self.tune_choice(mode)
 
     # reflux_layout (FP32-bulk 2D reflux pass): 0 eight lanes per deferred
-    # cell, 1 one thread per cell
+    # cell, 1 one thread per cell, 2 eight lanes per cell in the step
+    # kernel's tail
     SHAPE_KEYS = ("ctas_per_sm", "claim", "walk_cf_first", "reflux_layout")
 
     def tune_choice(self, mode="fp64") -> dict:
@@ -559,7 +560,7 @@ class GodunovImplemGB300:
         self.lib.g5_tune_report(self.ctx, MODES[mode], shapes, ms, n)
         return [(unpack_shape(int(shapes[i])), float(ms[i])) for i in range(n)]
 
-    def set_shape(self, mode="fp64", ctas_per_sm=0, claim=1, walk_cf_first=1, reflux_layout=0):
+    def set_shape(self, mode="fp64", ctas_per_sm=0, claim=1, walk_cf_first=1, reflux_layout=2):
         arr = (ctypes.c_int32 * 4)(ctas_per_sm, claim, walk_cf_first, reflux_layout)
         rc = self.lib.g5_set_shape(self.ctx, MODES[mode], arr)
         if rc != 0:
@@ -571,7 +572,7 @@ class GodunovImplemGB300:
 
 def unpack_shape(code: int) -> dict:
     """A packed launch shape of g5_tune (ctas_per_sm + 16 claim + 32 walk + 64 reflux)."""
-    return {"ctas_per_sm": code & 15, "claim": (code >> 4) & 1, "walk_cf_first": (code >> 5) & 1, "reflux_layout": (code >> 6) & 1}
+    return {"ctas_per_sm": code & 15, "claim": (code >> 4) & 1, "walk_cf_first": (code >> 5) & 1, "reflux_layout": (code >> 6) & 3}
 
 
 def tune_pick(ms, default_index, margin=0.02) -> int:

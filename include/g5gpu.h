@@ -315,9 +315,10 @@ int g5_status(G5Context * ctx, void * stream);
  * fixed).  Candidates: CTAs per SM of the persistent step kernel (1 up to the
  * occupancy maximum), dynamic block claiming on or off, the block walk order
  * (blocks with coarse/fine neighbours first, or table order) and, for the
- * FP32-bulk 2D pass over coarse/fine records, its layout (8 lanes or one
- * thread per deferred cell).  Every candidate computes the same values bit for
- * bit.  Each is timed twice on d_U -> d_U2 (3 steps after a warm-up, CUDA
+ * FP32-bulk 2D pass over coarse/fine records, its layout (a separate pass
+ * with 8 lanes or one thread per deferred cell, or 8 lanes per cell in the
+ * step kernel's tail, by the CTAs out of blocks).  Every candidate computes the
+ * same values bit for bit.  Each is timed twice on d_U -> d_U2 (3 steps after a warm-up, CUDA
  * events on `stream`), and g5_tune_pick chooses with a 2 % margin in favour of
  * the default shape.  The choice is kept by the context for that mode
  * (across g5_set_mesh) until the next g5_tune or g5_set_shape.  Synchronises
@@ -332,8 +333,11 @@ int g5_tune(G5Context * ctx, const double * d_U, double * d_U2, int mode, void *
 int g5_tune_pick(const float * ms, int n, int default_index, float margin);
 
 /* The launch shape a mode uses: out4 = {CTAs per SM, claim, walk order,
- * reflux layout (0: 8 lanes per deferred cell, 1: one thread per cell; the
- * FP32-bulk 2D pass only, the others take one thread per cell)}. */
+ * reflux layout (0: a separate pass, 8 lanes per deferred cell; 1: a separate
+ * pass, one thread per cell; 2 (the default): 8 lanes per cell in the step
+ * kernel's tail, by the CTAs out of blocks, where the FP32-bulk 2D full-mesh
+ * step has coarse/fine records, otherwise as 0; the FP64 form and 3D take a
+ * separate pass with one thread per cell)}. */
 int g5_tune_choice(const G5Context * ctx, int mode, int32_t * out4);
 
 /* The candidates and their times (ms per step) of the last g5_tune of a mode:

@@ -61,3 +61,4 @@ def test_tune_pick_selection_rule():
         tune_pick([0.0, 0.0], default_index=0)
     assert unpack_shape(4 + 16 + 32) == {"ctas_per_sm": 4, "claim": 1, "walk_cf_first": 1, "reflux_layout": 0}
     assert unpack_shape(2 + 64) == {"ctas_per_sm": 2, "claim": 0, "walk_cf_first": 0, "reflux_layout": 1}
+    assert unpack_shape(3 + 16 + 128) == {"ctas_per_sm": 3, "claim": 1, "walk_cf_first": 0, "reflux_layout": 2}

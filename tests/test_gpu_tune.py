@@ -1,7 +1,8 @@
 """g5_tune, the launch-shape autotuner: it searches CTAs per SM, block
 claiming, the block walk order and (FP32-bulk 2D with coarse/fine records) the
-reflux-pass layout, keeps the fastest, and every candidate shape gives the
-same state bit for bit."""
+reflux layout (a separate pass in two layouts, or the step kernel's tail),
+keeps the fastest, and every candidate shape gives the same state bit for
+bit."""
 import numpy as np
 import pytest
 
@@ -42,7 +43,7 @@ def test_every_tuned_shape_is_bit_identical(case, mode):
     choice = impl.tune(A, B, mode)
     assert set(choice) == set(GodunovImplemGB300.SHAPE_KEYS)
     report = impl.tune_report(mode)
-    n_layouts = 2 if (mode == "mixed" and t.dim == 2) else 1
+    n_layouts = 3 if (mode == "mixed" and t.dim == 2) else 1
     assert len(report) == max(s["ctas_per_sm"] for s, _ in report) * 2 * 2 * n_layouts
     assert all(ms > 0 for _, ms in report)
     n = t.n_owned
