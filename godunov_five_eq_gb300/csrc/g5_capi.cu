@@ -725,9 +725,10 @@ g5_set_mesh(G5Context * c, const G5Mesh * m)
             ok = add_tgt(F, j);
         }
       }
-      rc = ok ? 0 : 1;
+      // (a table whose blocks count off more counters than a row holds keeps
+      // the separate pass)
       c->n_fin = ok ? (int)init.size() : 0;
-      if (!rc)
+      if (c->n_fin > 0)
       {
         rc |= dev_upload(c, &c->d_fin_tgt, tgt.data(), tgt.size());
         rc |= dev_upload(c, &c->d_fin_rec, frec.data(), frec.size());
