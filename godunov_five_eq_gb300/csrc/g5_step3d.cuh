@@ -488,6 +488,100 @@ apply_dir_fp64(double * u2, const double * acc)
   u2[H::IW] += acc[H::FW];
 }
 
+// The FP32-bulk form's update of a cell's state u2 (old state on entry) from
+// its per-direction increments: hh + ll (exact float pairs) of the partial
+// densities, dA (source term included) of the volume fractions, the running
+// float-float sums es + et of energy and momentum, and the old volume
+// fractions af0, af1 as floats.  The partial densities and volume fractions
+// take the three directions combined when no per-direction clamp can trigger
+// (FP32 test with margin), otherwise direction by direction; then the
+// renormalisation and ID = IAD0 + IAD1.
+__device__ __forceinline__ void
+apply_mixed_3d(double * u2, const float (&hh)[3][2], const float (&ll)[3][2], const float (&dA)[3][2], const float (&es)[4],
+               const float (&et)[4], float af0, float af1)
+{
+  using H = V<3>;
+  const double eps = 1e-12, one_m_eps = 1.0 - 1e-12;
+#pragma unroll
+  for (int k = 0; k < 2; ++k)
+  {
+    const int   iv = k == 0 ? H::IAD0 : H::IAD1;
+    const float uf = d2f_fast(u2[iv]);
+    if (uf > 2.0f * (fabsf(hh[0][k]) + fabsf(hh[1][k])) + 2e-12f)
+    {
+      float s, t, s2, t2;
+      two_sum(hh[0][k], hh[1][k], s, t);
+      two_sum(s, hh[2][k], s2, t2);
+      two_sum(s2, t2 + (t + ll[0][k] + ll[1][k] + ll[2][k]), s2, t2);
+      u2[iv] += ff_to_d(s2, t2);
+      if (dlt_pos(u2[iv], eps))
+        u2[iv] = 0.0;
+    }
+    else
+    {
+#pragma unroll
+      for (int d = 0; d < 3; ++d)
+      {
+        u2[iv] = (u2[iv] + f2d_exact(hh[d][k])) + f2d_exact(ll[d][k]);
+        if (dlt_pos(u2[iv], eps))
+          u2[iv] = 0.0;
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 2; ++k)
+  {
+    const int   iv = k == 0 ? H::IA0 : H::IA1;
+    const float af = k == 0 ? af0 : af1;
+    const float m = 2.0f * (fabsf(dA[0][k]) + fabsf(dA[1][k])) + 2e-12f;
+    if (af > m && af + m < 1.0f)
+    {
+      u2[iv] += f2d_exact((dA[0][k] + dA[1][k]) + dA[2][k]);
+      if (dlt_pos(u2[iv], eps))
+        u2[iv] = 0.0;
+      if (dgt_pos(u2[iv], one_m_eps))
+        u2[iv] = 1.0;
+    }
+    else
+    {
+#pragma unroll
+      for (int d = 0; d < 3; ++d)
+      {
+        u2[iv] += f2d_exact(dA[d][k]);
+        if (dlt_pos(u2[iv], eps))
+          u2[iv] = 0.0;
+        if (dgt_pos(u2[iv], one_m_eps))
+          u2[iv] = 1.0;
+      }
+    }
+  }
+  const int ive[4] = { H::IE, H::IU, H::IV, H::IW };
+#pragma unroll
+  for (int e = 0; e < 4; ++e)
+  {
+    float s, t;
+    two_sum(es[e], et[e], s, t);
+    u2[ive[e]] += ff_to_d(s, t);
+  }
+  const double sa = u2[H::IA0] + u2[H::IA1];
+  const double d = sa - 1.0;
+  if (d != 0.0)
+  {
+    if ((__double_as_longlong(d) & 0x7FFFFFFFFFFFFFFFLL) < __double_as_longlong(1e-8))
+    {
+      u2[H::IA0] = fma(-u2[H::IA0], d, u2[H::IA0]);
+      u2[H::IA1] = fma(-u2[H::IA1], d, u2[H::IA1]);
+    }
+    else
+    {
+      const double inv = 1.0 / sa;
+      u2[H::IA0] *= inv;
+      u2[H::IA1] *= inv;
+    }
+  }
+  u2[H::ID] = u2[H::IAD0] + u2[H::IAD1];
+}
+
 // THINC, STIFF: compile-time cases of the FP32-bulk form (-1: tested at run
 // time, the FP64 form)
 template <bool MIXED, int THINC = -1, int STIFF = -1>
@@ -862,95 +956,14 @@ step3d_kernel(StepArgs a)
 
     if constexpr (MIXED)
     {
-      // partial densities and volume fractions: the three directions combined
-      // when no per-direction clamp can trigger (FP32 test with margin),
-      // otherwise applied direction by direction; energy and momentum in one
-      // exact float-float sum
-      const double eps = 1e-12, one_m_eps = 1.0 - 1e-12;
+      // the old state read again, then the update of the three directions
       {
         const double * base = a.U + (size_t)n * H::NV * NC + tid;
 #pragma unroll
         for (int v = 0; v < H::NV; ++v)
           u2[v] = base[v * NC];
       }
-#pragma unroll
-      for (int k = 0; k < 2; ++k)
-      {
-        const int   iv = k == 0 ? H::IAD0 : H::IAD1;
-        const float uf = d2f_fast(u2[iv]);
-        if (uf > 2.0f * (fabsf(hh[0][k]) + fabsf(hh[1][k])) + 2e-12f)
-        {
-          float s, t, s2, t2;
-          two_sum(hh[0][k], hh[1][k], s, t);
-          two_sum(s, hh[2][k], s2, t2);
-          two_sum(s2, t2 + (t + ll[0][k] + ll[1][k] + ll[2][k]), s2, t2);
-          u2[iv] += ff_to_d(s2, t2);
-          if (dlt_pos(u2[iv], eps))
-            u2[iv] = 0.0;
-        }
-        else
-        {
-#pragma unroll
-          for (int d = 0; d < 3; ++d)
-          {
-            u2[iv] = (u2[iv] + f2d_exact(hh[d][k])) + f2d_exact(ll[d][k]);
-            if (dlt_pos(u2[iv], eps))
-              u2[iv] = 0.0;
-          }
-        }
-      }
-#pragma unroll
-      for (int k = 0; k < 2; ++k)
-      {
-        const int   iv = k == 0 ? H::IA0 : H::IA1;
-        const float af = k == 0 ? af0 : af1;
-        const float m = 2.0f * (fabsf(dA[0][k]) + fabsf(dA[1][k])) + 2e-12f;
-        if (af > m && af + m < 1.0f)
-        {
-          u2[iv] += f2d_exact((dA[0][k] + dA[1][k]) + dA[2][k]);
-          if (dlt_pos(u2[iv], eps))
-            u2[iv] = 0.0;
-          if (dgt_pos(u2[iv], one_m_eps))
-            u2[iv] = 1.0;
-        }
-        else
-        {
-#pragma unroll
-          for (int d = 0; d < 3; ++d)
-          {
-            u2[iv] += f2d_exact(dA[d][k]);
-            if (dlt_pos(u2[iv], eps))
-              u2[iv] = 0.0;
-            if (dgt_pos(u2[iv], one_m_eps))
-              u2[iv] = 1.0;
-          }
-        }
-      }
-      const int ive[4] = { H::IE, H::IU, H::IV, H::IW };
-#pragma unroll
-      for (int e = 0; e < 4; ++e)
-      {
-        float s, t;
-        two_sum(es[e], et[e], s, t);
-        u2[ive[e]] += ff_to_d(s, t);
-      }
-      const double sa = u2[H::IA0] + u2[H::IA1];
-      const double d = sa - 1.0;
-      if (d != 0.0)
-      {
-        if ((__double_as_longlong(d) & 0x7FFFFFFFFFFFFFFFLL) < __double_as_longlong(1e-8))
-        {
-          u2[H::IA0] = fma(-u2[H::IA0], d, u2[H::IA0]);
-          u2[H::IA1] = fma(-u2[H::IA1], d, u2[H::IA1]);
-        }
-        else
-        {
-          const double inv = 1.0 / sa;
-          u2[H::IA0] *= inv;
-          u2[H::IA1] *= inv;
-        }
-      }
-      u2[H::ID] = u2[H::IAD0] + u2[H::IAD1];
+      apply_mixed_3d(u2, hh, ll, dA, es, et, af0, af1);
     }
     else
     {
@@ -1067,6 +1080,95 @@ reflux3d_kernel(StepArgs a)
     u2[v] = uin[v] = ub[v * NC];
   const int    ins = row[D::INST];
   const double dx = a.p.level_dx[row[D::LEVEL]];
+  if constexpr (MIXED)
+  {
+    // FP32-bulk form: per direction the two sides' fluxes as float pairs (a
+    // fine side is the float-float sum of its 2x2 fine faces, / 8; the
+    // records hold floats as doubles), their differences as exact float
+    // pairs, and the step kernel's update of the increments (apply_mixed_3d)
+    const int eosk = a.p.mg_any ? 2 : ((a.p.gpx[0] != 0.0 || a.p.gpx[1] != 0.0) ? 1 : 0);
+    float     fst0, fst1;
+    source_factors_mixed<3>(uin, a.p, eosk, fst0, fst1);
+    const float af0 = d2f_fast(uin[H::IA0]), af1 = d2f_fast(uin[H::IA1]);
+    const float a0f = af0 * fst0, a1f = af1 * fst1;
+    float       hh[3][2], ll[3][2], dA[3][2];
+    float       es[4] = { 0.f, 0.f, 0.f, 0.f }, et[4] = { 0.f, 0.f, 0.f, 0.f };
+    const int   ke[4] = { H::FE, H::FU, H::FV, H::FW };
+#pragma unroll
+    for (int dir = 0; dir < 3; ++dir)
+    {
+      const int e1 = dir == 0 ? 1 : 0, e2 = dir == 2 ? 1 : 2;
+      float     Fh[2][9], Fl[2][9];
+#pragma unroll
+      for (int side = 0; side < 2; ++side)
+      {
+        const int  fface = 2 * dir + side;
+        const bool fine = cc[dir] == (side ? B - 1 : 0) && dsl[fface] >= 0;
+        if (fine)
+        {
+          int ch[3], fl[3];
+          ch[dir] = side ? 0 : 1;
+          fl[dir] = 0;
+#pragma unroll
+          for (int e = 0; e < 3; ++e)
+            if (e != dir)
+            {
+              const int f = 2 * cc[e];
+              ch[e] = f / B;
+              fl[e] = f - ch[e] * B;
+            }
+          const int rs = row[D::RS + fface * D::NCF + ch[e1] + 2 * ch[e2]];
+          if (rs < 0)
+          {
+            raise_status(a.status, STATUS_MESH);
+            return;
+          }
+          const double * fb = a.reflux_buf + ((size_t)rs * B * B + fl[e1] + B * fl[e2]) * 9;
+#pragma unroll
+          for (int k = 0; k < 9; ++k)
+          {
+            const float v0 = d2f_fast(fb[k]), v1 = d2f_fast(fb[9 + k]);
+            const float v2 = d2f_fast(fb[B * 9 + k]), v3 = d2f_fast(fb[(B + 1) * 9 + k]);
+            float       s, t1, t2, t3;
+            two_sum(v0, v1, s, t1);
+            two_sum(s, v2, s, t2);
+            two_sum(s, v3, s, t3);
+            Fh[side][k] = 0.125f * s;
+            Fl[side][k] = 0.125f * ((t1 + t2) + t3);
+          }
+        }
+        else
+        {
+          const double * fr = own + fface * 9;
+#pragma unroll
+          for (int k = 0; k < 9; ++k)
+          {
+            Fh[side][k] = d2f_fast(fr[k]);
+            Fl[side][k] = 0.0f;
+          }
+        }
+      }
+      two_diff(Fh[0][H::FR0], Fh[1][H::FR0], hh[dir][0], ll[dir][0]);
+      ll[dir][0] += Fl[0][H::FR0] - Fl[1][H::FR0];
+      two_diff(Fh[0][H::FR1], Fh[1][H::FR1], hh[dir][1], ll[dir][1]);
+      ll[dir][1] += Fl[0][H::FR1] - Fl[1][H::FR1];
+#pragma unroll
+      for (int e = 0; e < 4; ++e)
+      {
+        float h, l, t;
+        two_diff(Fh[0][ke[e]], Fh[1][ke[e]], h, l);
+        l += Fl[0][ke[e]] - Fl[1][ke[e]];
+        two_sum(es[e], h, es[e], t);
+        et[e] += t + l;
+      }
+      const float usl = Fh[0][H::FUS] + Fl[0][H::FUS], usr = Fh[1][H::FUS] + Fl[1][H::FUS];
+      dA[dir][0] = (((Fh[0][H::FA0] + Fl[0][H::FA0]) - usl * a0f) - (Fh[1][H::FA0] + Fl[1][H::FA0])) + usr * a0f;
+      dA[dir][1] = (((Fh[0][H::FA1] + Fl[0][H::FA1]) - usl * a1f) - (Fh[1][H::FA1] + Fl[1][H::FA1])) + usr * a1f;
+    }
+    apply_mixed_3d(u2, hh, ll, dA, es, et, af0, af1);
+  }
+  else
+  {
   const double a0n = uin[H::IA0], a1n = uin[H::IA1];
   double       st0, st1;
   source_factors_fp64<3>(uin, a.p, st0, st1);
@@ -1147,6 +1249,7 @@ reflux3d_kernel(StepArgs a)
   u2[H::IA0] *= inv;
   u2[H::IA1] *= inv;
   u2[H::ID] = sum_alpha_rho;
+  }
   double * out = a.U2 + (size_t)n * H::NV * NC + cell;
   bool     finite = true;
   for (int v = 0; v < H::NV; ++v)
