@@ -79,3 +79,29 @@ def test_batched_rejects_bad_instance():
     impl.do_time_step_batched(A, B, dt, [])
     torch.cuda.synchronize()
     assert torch.all(B == SENTINEL)
+
+
+def test_tail_reflux_counters_over_many_steps():
+    """The FP32-bulk 2D step finishes the coarse/fine records in its tail by
+    arrival counters and ticket claims that reset themselves: 30 graph-replayed
+    steps of a two-instance AMR batch give the same bits as the separate
+    reflux pass, and the counters end where they started (a second run
+    repeats the first)."""
+    t, p, U = _amr_pair()
+    assert (t.nbr_rel != 0).any()
+    impl = GodunovImplemGB300(p, t)
+    n = t.n_owned
+
+    def run(layout):
+        impl.set_shape("mixed", reflux_layout=layout)
+        A = torch.from_numpy(np.ascontiguousarray(U).copy()).cuda()
+        B = torch.zeros_like(A)
+        impl.run(A, B, 30, "mixed")
+        torch.cuda.synchronize()
+        assert impl.status() == 0
+        return A.cpu().numpy()[:n]
+
+    tail = run(2)
+    assert np.array_equal(run(0), tail)
+    assert np.array_equal(run(2), tail)
+    impl.close()
