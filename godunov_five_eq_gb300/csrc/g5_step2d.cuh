@@ -681,362 +681,362 @@ step2d_kernel(StepArgs a)
     int next = iw;
     if (iw < nwalk)
     {
-    const int    n = a.work ? a.work[iw] : iw;
-    const int    fin_v = (fused && tid >= 16 && tid < 21) ? a.m.fin_tgt[n * 5 + tid - 16] : -1;
-    // (a block with no counter to count off skips the tail's barriers)
-    const bool   counts = fused && a.m.fin_tgt[n * 5] >= 0;
-    const int    lev = a.m.level[n];
-    const int    cx0 = a.m.coord[n * 3 + 0], cy0 = a.m.coord[n * 3 + 1];
-    // the next block is claimed now (the ticket's latency hides behind the gather)
-    const int    next_v = tid == 10 ? claim_next(a, iw, nwalk) : 0;
-    // coarse/fine slots: loaded now, stored to shared memory at the end of the
-    // gather (their latency hides behind it)
-    int slot_v = -1;
-    if (a.m.reflux_slot && tid < 8)
-      slot_v = tid < 4 ? a.m.reflux_slot[n * 4 + tid] : a.m.defer_slot[n * 4 + tid - 4];
-    if (tid == 8 || tid == 9)
-      slot_v = a.fill_twins ? a.m.twin_first[n + tid - 8] : 0;
-    const int    ins = a.m.inst ? a.m.inst[n] : 0;
-    const double dx = P.level_dx[lev];
-    R            dtdx_r;
-    if constexpr (MIXED)
-      dtdx_r = d2f_fast(a.dt[ins]) * __frcp_rn(d2f_fast(dx));
-    else
-      dtdx_r = a.dt[ins] / dx;
+      const int    n = a.work ? a.work[iw] : iw;
+      const int    fin_v = (fused && tid >= 16 && tid < 21) ? a.m.fin_tgt[n * 5 + tid - 16] : -1;
+      // (a block with no counter to count off skips the tail's barriers)
+      const bool   counts = fused && a.m.fin_tgt[n * 5] >= 0;
+      const int    lev = a.m.level[n];
+      const int    cx0 = a.m.coord[n * 3 + 0], cy0 = a.m.coord[n * 3 + 1];
+      // the next block is claimed now (the ticket's latency hides behind the gather)
+      const int    next_v = tid == 10 ? claim_next(a, iw, nwalk) : 0;
+      // coarse/fine slots: loaded now, stored to shared memory at the end of the
+      // gather (their latency hides behind it)
+      int slot_v = -1;
+      if (a.m.reflux_slot && tid < 8)
+        slot_v = tid < 4 ? a.m.reflux_slot[n * 4 + tid] : a.m.defer_slot[n * 4 + tid - 4];
+      if (tid == 8 || tid == 9)
+        slot_v = a.fill_twins ? a.m.twin_first[n + tid - 8] : 0;
+      const int    ins = a.m.inst ? a.m.inst[n] : 0;
+      const double dx = P.level_dx[lev];
+      R            dtdx_r;
+      if constexpr (MIXED)
+        dtdx_r = d2f_fast(a.dt[ins]) * __frcp_rn(d2f_fast(dx));
+      else
+        dtdx_r = a.dt[ins] / dx;
 
-    // ---------------- phase 1: own cell (coalesced) + halo gather -> primitives
-    // (the own cell's loads are in flight while the halo gather runs; its
-    // primitives are stored last)
-    const int ci = tid % B, cj = tid / B;
-    double    uin[H::NV];
-    {
-      const double * base = a.U + (size_t)n * H::NV * NC + tid;
-#pragma unroll
-      for (int v = 0; v < H::NV; ++v)
-        uin[v] = base[v * NC];
-    }
-    for (int h = tid; h < NHALO; h += NT)
-    {
-      int gx, gy;
-      halo_coords<B>(h, gx, gy);
-      double u[H::NV];
-      if (!gather_ghost_2d<B>(a, n, cx0, cy0, gx, gy, u))
+      // ---------------- phase 1: own cell (coalesced) + halo gather -> primitives
+      // (the own cell's loads are in flight while the halo gather runs; its
+      // primitives are stored last)
+      const int ci = tid % B, cj = tid / B;
+      double    uin[H::NV];
       {
-        raise_status(a.status, STATUS_MESH);
+        const double * base = a.U + (size_t)n * H::NV * NC + tid;
 #pragma unroll
         for (int v = 0; v < H::NV; ++v)
-          u[v] = uin[v];
+          uin[v] = base[v * NC];
       }
-      store_prim<B, MIXED>(sQ, (gx + 2) + G * (gy + 2), u, P, eosk);
-    }
-    store_prim<B, MIXED>(sQ, (ci + 2) + G * (cj + 2), uin, P, eosk);
-    if (tid < 10)
-      sSlot[tid] = slot_v;
-    if (tid == 10)
-      sNext = next_v;
-    __syncthreads();
-    // the next block of this CTA: its own cells and table rows into L2 while
-    // this block computes (its gather then hits L2 instead of HBM)
-    if (tid < 3 && sNext < nwalk)
-    {
-      const int nn = a.work ? a.work[sNext] : sNext;
-      if (tid == 0)
-        prefetch_l2_range(a.U + (size_t)nn * H::NV * NC, (unsigned)(H::NV * NC * sizeof(double)));
-      else if (tid == 1)
-        prefetch_l2_line(a.m.nbr + (size_t)nn * 36);
-      else
-        prefetch_l2_line(a.m.nbr_rel + (size_t)nn * 9);
-    }
-
-    // ---------------- phase 2: per face-neighbour cell slopes + Hancock source
-    // (the block, then the row or column beyond each face, without gaps: the
-    // ring's corners are never a face neighbour; r: the cell's index in the
-    // ring layout)
-    for (int h = tid; h < NC + 4 * B; h += NT)
-    {
-      int ri, rj;
-      if (h < NC)
+      for (int h = tid; h < NHALO; h += NT)
       {
-        ri = h % B;
-        rj = h / B;
-      }
-      else
-      {
-        const int i = h - NC, f = i / B, pa = i % B;
-        const int side = (f & 1) ? B : -1;
-        ri = f < 2 ? side : pa;
-        rj = f < 2 ? pa : side;
-      }
-      const int r = (ri + 1) + S * (rj + 1);
-      const int gi = (ri + 2) + G * (rj + 2);
-      R         q[5], dqx[5], dqy[5];
-      R st;
-      if constexpr (MIXED)
-        st = P.f_slope_type;
-      else
-        st = P.slope_type;
+        int gx, gy;
+        halo_coords<B>(h, gx, gy);
+        double u[H::NV];
+        if (!gather_ghost_2d<B>(a, n, cx0, cy0, gx, gy, u))
+        {
+          raise_status(a.status, STATUS_MESH);
 #pragma unroll
-      for (int k = 0; k < 5; ++k)
-      {
-        const R * Qk = sQ + k * GG;
-        q[k] = Qk[gi];
-        dqx[k] = slope_scalar<R>(q[k], Qk[gi + 1], Qk[gi - 1], st);
-        dqy[k] = slope_scalar<R>(q[k], Qk[gi + G], Qk[gi - G], st);
-        sRec[k * SS + r] = dqx[k];
-        sRec[(5 + k) * SS + r] = dqy[k];
+          for (int v = 0; v < H::NV; ++v)
+            u[v] = uin[v];
+        }
+        store_prim<B, MIXED>(sQ, (gx + 2) + G * (gy + 2), u, P, eosk);
       }
-      const R a0 = sQ[5 * GG + gi];
-      if (P.integrator == 0)
+      store_prim<B, MIXED>(sQ, (ci + 2) + G * (cj + 2), uin, P, eosk);
+      if (tid < 10)
+        sSlot[tid] = slot_v;
+      if (tid == 10)
+        sNext = next_v;
+      __syncthreads();
+      // the next block of this CTA: its own cells and table rows into L2 while
+      // this block computes (its gather then hits L2 instead of HBM)
+      if (tid < 3 && sNext < nwalk)
       {
-        // Hancock half-step source (ComputeFluxesAndStoreFunctor.cpp:174-199)
-        const R r0 = q[0], r1 = q[1], p = q[2], u = q[3], v = q[4];
-        const R rr = r0 + r1;
-        R       c;
-        if constexpr (MIXED)
-          c = sound_speed_eos(P, eosk, rr, p, a0, r0, r1);
+        const int nn = a.work ? a.work[sNext] : sNext;
+        if (tid == 0)
+          prefetch_l2_range(a.U + (size_t)nn * H::NV * NC, (unsigned)(H::NV * NC * sizeof(double)));
+        else if (tid == 1)
+          prefetch_l2_line(a.m.nbr + (size_t)nn * 36);
         else
-          c = sound_speed_mix(P, rr, p, a0, 1 - a0, r0, r1);
-        const R drx0 = dqx[0], drx1 = dqx[1], dpx = dqx[2], dux = dqx[3], dvx = dqx[4];
-        const R dry0 = dqy[0], dry1 = dqy[1], dpy = dqy[2], duy = dqy[3], dvy = dqy[4];
-        const R dtdy = dtdx_r;
-        const R sr0 = (-u * (drx0 + drx1) - dux * rr) * dtdx_r + (-v * (dry0 + dry1) - dvy * rr) * dtdy;
-        const R sr0_0 = sr0 * a0;
-        const R sr0_1 = sr0 * (R(1) - a0);
-        const R su0 = (-u * dux - dpx / rr) * dtdx_r + (-v * duy) * dtdy;
-        const R sv0 = (-u * dvx) * dtdx_r + (-v * dvy - dpy / rr) * dtdy;
-        const R sp0 = (-u * dpx - dux * rr * c * c) * dtdx_r + (-v * dpy - dvy * rr * c * c) * dtdy;
-        if constexpr (MIXED)
+          prefetch_l2_line(a.m.nbr_rel + (size_t)nn * 9);
+      }
+
+      // ---------------- phase 2: per face-neighbour cell slopes + Hancock source
+      // (the block, then the row or column beyond each face, without gaps: the
+      // ring's corners are never a face neighbour; r: the cell's index in the
+      // ring layout)
+      for (int h = tid; h < NC + 4 * B; h += NT)
+      {
+        int ri, rj;
+        if (h < NC)
         {
-          // the mixed form stores the predicted centre value q + hs
-          sRec[10 * SS + r] = q[0] + R(0.5) * sr0_0;
-          sRec[11 * SS + r] = q[1] + R(0.5) * sr0_1;
-          sRec[12 * SS + r] = q[2] + R(0.5) * sp0;
-          sRec[13 * SS + r] = q[3] + R(0.5) * su0;
-          sRec[14 * SS + r] = q[4] + R(0.5) * sv0;
+          ri = h % B;
+          rj = h / B;
         }
         else
         {
-          sRec[10 * SS + r] = R(0.5) * sr0_0;
-          sRec[11 * SS + r] = R(0.5) * sr0_1;
-          sRec[12 * SS + r] = R(0.5) * sp0;
-          sRec[13 * SS + r] = R(0.5) * su0;
-          sRec[14 * SS + r] = R(0.5) * sv0;
+          const int i = h - NC, f = i / B, pa = i % B;
+          const int side = (f & 1) ? B : -1;
+          ri = f < 2 ? side : pa;
+          rj = f < 2 ? pa : side;
         }
-      }
-      else if constexpr (MIXED)
-      {
+        const int r = (ri + 1) + S * (rj + 1);
+        const int gi = (ri + 2) + G * (rj + 2);
+        R         q[5], dqx[5], dqy[5];
+        R st;
+        if constexpr (MIXED)
+          st = P.f_slope_type;
+        else
+          st = P.slope_type;
 #pragma unroll
         for (int k = 0; k < 5; ++k)
-          sRec[(10 + k) * SS + r] = q[k];
+        {
+          const R * Qk = sQ + k * GG;
+          q[k] = Qk[gi];
+          dqx[k] = slope_scalar<R>(q[k], Qk[gi + 1], Qk[gi - 1], st);
+          dqy[k] = slope_scalar<R>(q[k], Qk[gi + G], Qk[gi - G], st);
+          sRec[k * SS + r] = dqx[k];
+          sRec[(5 + k) * SS + r] = dqy[k];
+        }
+        const R a0 = sQ[5 * GG + gi];
+        if (P.integrator == 0)
+        {
+          // Hancock half-step source (ComputeFluxesAndStoreFunctor.cpp:174-199)
+          const R r0 = q[0], r1 = q[1], p = q[2], u = q[3], v = q[4];
+          const R rr = r0 + r1;
+          R       c;
+          if constexpr (MIXED)
+            c = sound_speed_eos(P, eosk, rr, p, a0, r0, r1);
+          else
+            c = sound_speed_mix(P, rr, p, a0, 1 - a0, r0, r1);
+          const R drx0 = dqx[0], drx1 = dqx[1], dpx = dqx[2], dux = dqx[3], dvx = dqx[4];
+          const R dry0 = dqy[0], dry1 = dqy[1], dpy = dqy[2], duy = dqy[3], dvy = dqy[4];
+          const R dtdy = dtdx_r;
+          const R sr0 = (-u * (drx0 + drx1) - dux * rr) * dtdx_r + (-v * (dry0 + dry1) - dvy * rr) * dtdy;
+          const R sr0_0 = sr0 * a0;
+          const R sr0_1 = sr0 * (R(1) - a0);
+          const R su0 = (-u * dux - dpx / rr) * dtdx_r + (-v * duy) * dtdy;
+          const R sv0 = (-u * dvx) * dtdx_r + (-v * dvy - dpy / rr) * dtdy;
+          const R sp0 = (-u * dpx - dux * rr * c * c) * dtdx_r + (-v * dpy - dvy * rr * c * c) * dtdy;
+          if constexpr (MIXED)
+          {
+            // the mixed form stores the predicted centre value q + hs
+            sRec[10 * SS + r] = q[0] + R(0.5) * sr0_0;
+            sRec[11 * SS + r] = q[1] + R(0.5) * sr0_1;
+            sRec[12 * SS + r] = q[2] + R(0.5) * sp0;
+            sRec[13 * SS + r] = q[3] + R(0.5) * su0;
+            sRec[14 * SS + r] = q[4] + R(0.5) * sv0;
+          }
+          else
+          {
+            sRec[10 * SS + r] = R(0.5) * sr0_0;
+            sRec[11 * SS + r] = R(0.5) * sr0_1;
+            sRec[12 * SS + r] = R(0.5) * sp0;
+            sRec[13 * SS + r] = R(0.5) * su0;
+            sRec[14 * SS + r] = R(0.5) * sv0;
+          }
+        }
+        else if constexpr (MIXED)
+        {
+#pragma unroll
+          for (int k = 0; k < 5; ++k)
+            sRec[(10 + k) * SS + r] = q[k];
+        }
       }
-    }
-    __syncthreads();
+      __syncthreads();
 
-    // ---------------- phase 3: faces (X then Y) -> HLLC -> shared fluxes
-    if constexpr (MIXED)
-    {
+      // ---------------- phase 3: faces (X then Y) -> HLLC -> shared fluxes
+      if constexpr (MIXED)
+      {
+        for (int f = tid; f < 2 * NFF; f += NT)
+        {
+          if (f < NFF)
+            face_flux_mixed<B, 0, THINC, STIFF == 2>(sQ, sRec, sFx, f, dtdx_r, P);
+          else
+            face_flux_mixed<B, 1, THINC, STIFF == 2>(sQ, sRec, sFy, f - NFF, dtdx_r, P);
+        }
+      }
+      else
       for (int f = tid; f < 2 * NFF; f += NT)
       {
-        if (f < NFF)
-          face_flux_mixed<B, 0, THINC, STIFF == 2>(sQ, sRec, sFx, f, dtdx_r, P);
-        else
-          face_flux_mixed<B, 1, THINC, STIFF == 2>(sQ, sRec, sFy, f - NFF, dtdx_r, P);
-      }
-    }
-    else
-    for (int f = tid; f < 2 * NFF; f += NT)
-    {
-      const int dir = f >= NFF ? 1 : 0;
-      const int ff = f - dir * NFF;
-      int       li, lj, ri, rj;
-      if (dir == 0)
-      {
-        const int fi = ff % (B + 1), fj = ff / (B + 1);
-        li = fi - 1;
-        lj = fj;
-        ri = fi;
-        rj = fj;
-      }
-      else
-      {
-        const int fi = ff % B, fj = ff / B;
-        li = fi;
-        lj = fj - 1;
-        ri = fi;
-        rj = fj;
-      }
-      R qL[6], qR[6], fl[8];
-      face_state<B, MIXED>(sQ, sRec, li, lj, dir, +1, P, qL);
-      face_state<B, MIXED>(sQ, sRec, ri, rj, dir, -1, P, qR);
-      if (dir == 1)
-      {
-        R t = qL[3];
-        qL[3] = qL[4];
-        qL[4] = t;
-        t = qR[3];
-        qR[3] = qR[4];
-        qR[4] = t;
-      }
-      if constexpr (MIXED)
-        hllc_fp32<2>(qL, qR, P.f_xi[0], P.f_xi[1], P.f_gpx[0], P.f_gpx[1], P.f_smallr, P.f_smallp, P.f_smallc, fl);
-      else
-        hllc_fp64<2>(qL, qR, P, fl);
-      if (dir == 1)
-      {
-        const R t = fl[H::FU];
-        fl[H::FU] = fl[H::FV];
-        fl[H::FV] = t;
-      }
-      R * dst = dir == 0 ? sFx : sFy;
-#pragma unroll
-      for (int k = 0; k < 8; ++k)
-        dst[k * NFF + ff] = fl[k] * dtdx_r;
-    }
-    __syncthreads();
-
-    // ---------------- publish coarse/fine records (AMR only)
-    if (a.m.reflux_slot)
-    {
-#pragma unroll
-      for (int face = 0; face < 4; ++face)
-      {
-        const int rs = sSlot[face];
-        if (rs >= 0 && tid < B)
+        const int dir = f >= NFF ? 1 : 0;
+        const int ff = f - dir * NFF;
+        int       li, lj, ri, rj;
+        if (dir == 0)
         {
-          // fine block face next to a coarser neighbour: publish its B face fluxes
-          const int dir = face >> 1, side = face & 1;
-          const int idx = dir == 0 ? (side ? B : 0) + (B + 1) * tid : tid + B * (side ? B : 0);
-          const R * src = dir == 0 ? sFx : sFy;
-          // the mixed form keeps the float fluxes (the buffer read as floats)
-          R * dst = reinterpret_cast<R *>(a.reflux_buf) + ((size_t)rs * B + tid) * 8;
-#pragma unroll
-          for (int k = 0; k < 8; ++k)
-            dst[k] = src[k * NFF + idx];
+          const int fi = ff % (B + 1), fj = ff / (B + 1);
+          li = fi - 1;
+          lj = fj;
+          ri = fi;
+          rj = fj;
         }
-        const int ds = sSlot[4 + face];
-        if (ds >= 0 && tid < B)
+        else
         {
-          // coarse cell next to a finer face: save its four own face fluxes
-          const int dir = face >> 1, side = face & 1;
-          const int cx = dir == 0 ? (side ? B - 1 : 0) : tid;
-          const int cy = dir == 0 ? tid : (side ? B - 1 : 0);
-          R *       dst = reinterpret_cast<R *>(a.defer_buf) + ((size_t)ds * B + tid) * 32;
-          const int fxl = cx + (B + 1) * cy, fyl = cx + B * cy;
+          const int fi = ff % B, fj = ff / B;
+          li = fi;
+          lj = fj - 1;
+          ri = fi;
+          rj = fj;
+        }
+        R qL[6], qR[6], fl[8];
+        face_state<B, MIXED>(sQ, sRec, li, lj, dir, +1, P, qL);
+        face_state<B, MIXED>(sQ, sRec, ri, rj, dir, -1, P, qR);
+        if (dir == 1)
+        {
+          R t = qL[3];
+          qL[3] = qL[4];
+          qL[4] = t;
+          t = qR[3];
+          qR[3] = qR[4];
+          qR[4] = t;
+        }
+        if constexpr (MIXED)
+          hllc_fp32<2>(qL, qR, P.f_xi[0], P.f_xi[1], P.f_gpx[0], P.f_gpx[1], P.f_smallr, P.f_smallp, P.f_smallc, fl);
+        else
+          hllc_fp64<2>(qL, qR, P, fl);
+        if (dir == 1)
+        {
+          const R t = fl[H::FU];
+          fl[H::FU] = fl[H::FV];
+          fl[H::FV] = t;
+        }
+        R * dst = dir == 0 ? sFx : sFy;
 #pragma unroll
-          for (int k = 0; k < 8; ++k)
+        for (int k = 0; k < 8; ++k)
+          dst[k * NFF + ff] = fl[k] * dtdx_r;
+      }
+      __syncthreads();
+
+      // ---------------- publish coarse/fine records (AMR only)
+      if (a.m.reflux_slot)
+      {
+#pragma unroll
+        for (int face = 0; face < 4; ++face)
+        {
+          const int rs = sSlot[face];
+          if (rs >= 0 && tid < B)
           {
-            dst[0 * 8 + k] = sFx[k * NFF + fxl];
-            dst[1 * 8 + k] = sFx[k * NFF + fxl + 1];
-            dst[2 * 8 + k] = sFy[k * NFF + fyl];
-            dst[3 * 8 + k] = sFy[k * NFF + fyl + B];
+            // fine block face next to a coarser neighbour: publish its B face fluxes
+            const int dir = face >> 1, side = face & 1;
+            const int idx = dir == 0 ? (side ? B : 0) + (B + 1) * tid : tid + B * (side ? B : 0);
+            const R * src = dir == 0 ? sFx : sFy;
+            // the mixed form keeps the float fluxes (the buffer read as floats)
+            R * dst = reinterpret_cast<R *>(a.reflux_buf) + ((size_t)rs * B + tid) * 8;
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+              dst[k] = src[k * NFF + idx];
+          }
+          const int ds = sSlot[4 + face];
+          if (ds >= 0 && tid < B)
+          {
+            // coarse cell next to a finer face: save its four own face fluxes
+            const int dir = face >> 1, side = face & 1;
+            const int cx = dir == 0 ? (side ? B - 1 : 0) : tid;
+            const int cy = dir == 0 ? tid : (side ? B - 1 : 0);
+            R *       dst = reinterpret_cast<R *>(a.defer_buf) + ((size_t)ds * B + tid) * 32;
+            const int fxl = cx + (B + 1) * cy, fyl = cx + B * cy;
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+            {
+              dst[0 * 8 + k] = sFx[k * NFF + fxl];
+              dst[1 * 8 + k] = sFx[k * NFF + fxl + 1];
+              dst[2 * 8 + k] = sFy[k * NFF + fyl];
+              dst[3 * 8 + k] = sFy[k * NFF + fyl + B];
+            }
           }
         }
       }
-    }
 
-    // ---------------- phase 4: update of the owned cell (tid)
-    bool deferred = false;
-    if (a.m.defer_slot)
-    {
-      const int * dsl = sSlot + 4;
-      deferred = (ci == 0 && dsl[0] >= 0) || (ci == B - 1 && dsl[1] >= 0) || (cj == 0 && dsl[2] >= 0) ||
-                 (cj == B - 1 && dsl[3] >= 0);
-    }
-    DtT    m_inv = DtT(0);
-    double u2[H::NV];
-    if (!deferred)
-    {
-      if constexpr (MIXED)
-        m_inv = update_mixed<B>(uin, u2, sFx, sFy, ci, cj, d2f_fast(dx), P, eosk, a.invdt != nullptr);
-      else
-        m_inv = update_fp64<B>(uin, u2, sFx, sFy, ci, cj, dx, P, a.invdt != nullptr);
-      double * out = a.U2 + (size_t)n * H::NV * NC + tid;
-      bool     finite = true;
-#pragma unroll
-      for (int v = 0; v < H::NV; ++v)
+      // ---------------- phase 4: update of the owned cell (tid)
+      bool deferred = false;
+      if (a.m.defer_slot)
       {
-        out[v * NC] = u2[v];
-        finite = finite && finite_bits(u2[v]);
+        const int * dsl = sSlot + 4;
+        deferred = (ci == 0 && dsl[0] >= 0) || (ci == B - 1 && dsl[1] >= 0) || (cj == 0 && dsl[2] >= 0) ||
+                   (cj == B - 1 && dsl[3] >= 0);
       }
-      if (!finite)
-        raise_status(a.status, STATUS_NONPHYSICAL);
-    }
-    else
-    {
-#pragma unroll
-      for (int v = 0; v < H::NV; ++v)
-        u2[v] = uin[v]; // the reflux pass finishes the cell (and its twin cells)
-    }
-    if (sSlot[9] > sSlot[8])
-    {
-      // the solver loop's boundary fill of the outside blocks mirroring this
-      // block (FillOutside: the last applicable face's copy rule), from the
-      // new state staged in the (now free) slope area
-      double * sTw = reinterpret_cast<double *>(sRec);
-#pragma unroll
-      for (int v = 0; v < H::NV; ++v)
-        sTw[v * NC + tid] = u2[v];
-      __syncthreads();
-      for (int t = sSlot[8]; t < sSlot[9]; ++t)
+      DtT    m_inv = DtT(0);
+      double u2[H::NV];
+      if (!deferred)
       {
-        const int e = a.m.twin_list[t];
-        const int o = e >> 3, face = e & 7, dir = face >> 1, bc = P.bc[face];
-        const int edge = (face & 1) ? B - 1 : 0;
-        const int sx = dir == 0 ? (bc == 2 ? edge : B - 1 - ci) : ci;
-        const int sy = dir == 1 ? (bc == 2 ? edge : B - 1 - cj) : cj;
-        const double * src = sTw + sx + B * sy;
-        double *       dst = a.U2 + (size_t)o * H::NV * NC + tid;
+        if constexpr (MIXED)
+          m_inv = update_mixed<B>(uin, u2, sFx, sFy, ci, cj, d2f_fast(dx), P, eosk, a.invdt != nullptr);
+        else
+          m_inv = update_fp64<B>(uin, u2, sFx, sFy, ci, cj, dx, P, a.invdt != nullptr);
+        double * out = a.U2 + (size_t)n * H::NV * NC + tid;
+        bool     finite = true;
 #pragma unroll
         for (int v = 0; v < H::NV; ++v)
         {
-          const double val = src[v * NC];
-          dst[v * NC] = (bc == 3 && v == H::IU + dir) ? -val : val;
+          out[v * NC] = u2[v];
+          finite = finite && finite_bits(u2[v]);
         }
+        if (!finite)
+          raise_status(a.status, STATUS_NONPHYSICAL);
       }
-    }
-    if (a.invdt)
-    {
+      else
+      {
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1)
-        m_inv = fmax(m_inv, __shfl_xor_sync(0xffffffffu, m_inv, o));
-      if ((tid & 31) == 0)
-        sRed[tid >> 5] = m_inv;
-      __syncthreads();
-      if (tid == 0)
-      {
-        DtT mm = DtT(0);
-        for (int w = 0; w < NT / 32; ++w)
-          mm = fmax(mm, sRed[w]);
-        atomic_max_pos(a.invdt + ins, (double)mm);
+        for (int v = 0; v < H::NV; ++v)
+          u2[v] = uin[v]; // the reflux pass finishes the cell (and its twin cells)
       }
-    }
-    if (counts)
-    {
-      __syncthreads(); // every output of the block is written
-      if (tid >= 16 && tid < 21)
+      if (sSlot[9] > sSlot[8])
       {
-        int ready = -1;
-        if (fin_v >= 0)
+        // the solver loop's boundary fill of the outside blocks mirroring this
+        // block (FillOutside: the last applicable face's copy rule), from the
+        // new state staged in the (now free) slope area
+        double * sTw = reinterpret_cast<double *>(sRec);
+#pragma unroll
+        for (int v = 0; v < H::NV; ++v)
+          sTw[v * NC + tid] = u2[v];
+        __syncthreads();
+        for (int t = sSlot[8]; t < sSlot[9]; ++t)
         {
-          __threadfence();
-          if (atomicSub(a.m.fin_cnt + fin_v, 1u) == 1u)
+          const int e = a.m.twin_list[t];
+          const int o = e >> 3, face = e & 7, dir = face >> 1, bc = P.bc[face];
+          const int edge = (face & 1) ? B - 1 : 0;
+          const int sx = dir == 0 ? (bc == 2 ? edge : B - 1 - ci) : ci;
+          const int sy = dir == 1 ? (bc == 2 ? edge : B - 1 - cj) : cj;
+          const double * src = sTw + sx + B * sy;
+          double *       dst = a.U2 + (size_t)o * H::NV * NC + tid;
+#pragma unroll
+          for (int v = 0; v < H::NV; ++v)
           {
-            __threadfence();
-            ready = fin_v;
+            const double val = src[v * NC];
+            dst[v * NC] = (bc == 3 && v == H::IU + dir) ? -val : val;
           }
         }
-        sFin[tid - 16] = ready;
       }
-      if (tid == 0)
-        sFin[5] = 0;
-    }
-    next = sNext; // read before the barrier: the next block's claim overwrites it
-    if (!counts)
-    {
-      __syncthreads();
-      iw = next;
-      continue;
-    }
+      if (a.invdt)
+      {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+          m_inv = fmax(m_inv, __shfl_xor_sync(0xffffffffu, m_inv, o));
+        if ((tid & 31) == 0)
+          sRed[tid >> 5] = m_inv;
+        __syncthreads();
+        if (tid == 0)
+        {
+          DtT mm = DtT(0);
+          for (int w = 0; w < NT / 32; ++w)
+            mm = fmax(mm, sRed[w]);
+          atomic_max_pos(a.invdt + ins, (double)mm);
+        }
+      }
+      if (counts)
+      {
+        __syncthreads(); // every output of the block is written
+        if (tid >= 16 && tid < 21)
+        {
+          int ready = -1;
+          if (fin_v >= 0)
+          {
+            __threadfence();
+            if (atomicSub(a.m.fin_cnt + fin_v, 1u) == 1u)
+            {
+              __threadfence();
+              ready = fin_v;
+            }
+          }
+          sFin[tid - 16] = ready;
+        }
+        if (tid == 0)
+          sFin[5] = 0;
+      }
+      next = sNext; // read before the barrier: the next block's claim overwrites it
+      if (!counts)
+      {
+        __syncthreads();
+        iw = next;
+        continue;
+      }
     }
     else
     {
