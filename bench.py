@@ -465,6 +465,11 @@ def measure(name, args, world, local, flush, stream, steps, clocks=True, want_l1
         if args.no_tune and args.reflux_layout is not None:
             impl.set_shape(mode, reflux_layout=args.reflux_layout)
         shape = impl.tune(A, B, mode) if not args.no_tune else impl.tune_choice(mode)
+        # the tuner's candidates, fastest first: [ctas_per_sm, claim, walk_cf_first,
+        # reflux_layout, ms per step]
+        report = [] if args.no_tune else sorted(
+            ([s[k] for k in GodunovImplemGB300.SHAPE_KEYS] + [round(ms, 5)] for s, ms in impl.tune_report(mode)), key=lambda r: r[-1]
+        )
         impl.begin(A)
         for _ in range(args.warmup):
             impl.advance(A, B, mode)
@@ -485,7 +490,7 @@ def measure(name, args, world, local, flush, stream, steps, clocks=True, want_l1
         total_ms = max_over_ranks(total_ms, device="cuda")
         d_dt = impl.compute_dt_local(A)
         kern_ms = time_kernel(impl, A, B, d_dt, mode, max(5, min(steps, 20)), flush, stream)
-        res[mode] = dict(total_ms=total_ms, launches=launches, clocks=clk, kern_ms=kern_ms, impl=impl, shape=shape)
+        res[mode] = dict(total_ms=total_ms, launches=launches, clocks=clk, kern_ms=kern_ms, impl=impl, shape=shape, report=report)
         del A, B
     out = dict(desc=desc, t=t, p=p, U=U, cells=cells, res=res)
     out["value"] = whole_job_rate(world, cells, steps, res["mixed"]["total_ms"])
@@ -654,6 +659,7 @@ def main():
                 "l2": "flushed (512 MB write) before every timed step",
                 "parallelism": "replicas" if world > 1 else "single GPU",
                 "launch_shape": {mode: res[mode]["shape"] for mode in ("fp64", "mixed")},
+                "tuner_candidates_mixed": res["mixed"]["report"][:8],
             },
             "fp64_plain": {"value": value64, "unit": "cell-updates/s", "ms_per_step": res["fp64"]["total_ms"] / args.steps},
             "speedup_mixed_vs_fp64": value / value64,
