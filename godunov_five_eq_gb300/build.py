@@ -1,8 +1,9 @@
 """In-tree build of libg5gpu.so (sm_103a) with nvcc.
 
-Five translation units compiled in parallel:
+Six translation units compiled in parallel:
   g5_fp64.cu   FP64 kernels, --fmad=false (bit-reproducible reference arithmetic)
-  g5_mixed.cu  FP32-bulk kernels, --use_fast_math
+  g5_mixed.cu  FP32-bulk 2D kernels and the FP32-bulk dispatch, --use_fast_math
+  g5_mixed3d.cu FP32-bulk 3D kernels, --use_fast_math
   g5_capi.cu   the C ABI (include/g5gpu.h)
   g5_static.cu the allocation-free g5_step_static and its fixed scratch array
   g5_forest.cpp the host block forest of the dynamic AMR cycle
@@ -23,6 +24,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 UNITS = {
     "g5_fp64.cu": ["--fmad=false"],
     "g5_mixed.cu": ["--use_fast_math"],
+    "g5_mixed3d.cu": ["--use_fast_math"],
     "g5_capi.cu": [],
     "g5_static.cu": [],
     "g5_forest.cpp": [],

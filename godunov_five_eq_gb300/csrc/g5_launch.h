@@ -48,4 +48,9 @@ cudaError_t launch_derived(int dim, int b, const double * U, double * out, int q
 cudaError_t launch_pack_fields(int dim, int b, const double * U, double * out, const int * codes, int n, long long oct_begin,
                                long long num_octs, const PhysParams & p, cudaStream_t s);
 
+// the FP32-bulk 3D step of case v = 3 THINC + equation-of-state kind
+// (g5_mixed3d.cu) and the occupancy maximum of its kernels
+cudaError_t launch_step3d_mixed_case(int v, const StepArgs & a, int ctas_per_sm, cudaStream_t s, int * launches);
+int         step_max_ctas_per_sm_mixed3d();
+
 } // namespace g5

@@ -1,9 +1,10 @@
-// g5_mixed.cu — FP32-bulk instantiations (fast FP32 math; FP64 kept for the
-// pressure numerator, the accumulation into U2, the renormalisation and dt).
+// g5_mixed.cu — FP32-bulk instantiations of the 2D step (fast FP32 math; FP64
+// kept for the pressure numerator, the accumulation into U2, the
+// renormalisation and dt) and the dispatch of every FP32-bulk step; the 3D
+// kernels are in g5_mixed3d.cu.
 #include "g5_aux.cuh"
 #include "g5_launch.h"
 #include "g5_step2d.cuh"
-#include "g5_step3d.cuh"
 
 namespace g5
 {
@@ -23,19 +24,22 @@ num_sms_m()
   return n;
 }
 
-template <int B, bool THINC, int STIFF>
+// the persistent step kernel of one case (FUSED: the coarse/fine records
+// finished in its tail, m.fin_tgt set)
+template <int B, bool THINC, int STIFF, bool FUSED>
 static cudaError_t
-launch_step2d_m(const StepArgs & a, int ctas_per_sm, cudaStream_t s, int * launches)
+launch_step2d_kernel_m(const StepArgs & a, int ctas_per_sm, cudaStream_t s, int * launches)
 {
   using T = Step2DTraits<B, true>;
   static bool configured = false;
   static int  occ = 1;
   if (!configured)
   {
-    cudaError_t e = cudaFuncSetAttribute(step2d_kernel<B, true, THINC, STIFF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::smem_bytes);
+    cudaError_t e =
+      cudaFuncSetAttribute(step2d_kernel<B, true, THINC, STIFF, FUSED>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::smem_bytes);
     if (e != cudaSuccess)
       return e;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, step2d_kernel<B, true, THINC, STIFF>, T::NT, T::smem_bytes);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, step2d_kernel<B, true, THINC, STIFF, FUSED>, T::NT, T::smem_bytes);
     if (occ < 1)
       occ = 1;
     configured = true;
@@ -44,15 +48,21 @@ launch_step2d_m(const StepArgs & a, int ctas_per_sm, cudaStream_t s, int * launc
   int       grid = num_sms_m() * per_sm;
   if (grid > step_count(a))
     grid = step_count(a);
-  cudaError_t e = cudaSuccess;
-  if (grid >= 1)
-  {
-    step2d_kernel<B, true, THINC, STIFF><<<grid, T::NT, T::smem_bytes, s>>>(a);
-    ++*launches;
-    e = cudaGetLastError();
-    if (e != cudaSuccess)
-      return e;
-  }
+  if (grid < 1)
+    return cudaSuccess;
+  step2d_kernel<B, true, THINC, STIFF, FUSED><<<grid, T::NT, T::smem_bytes, s>>>(a);
+  ++*launches;
+  return cudaGetLastError();
+}
+
+template <int B, bool THINC, int STIFF>
+static cudaError_t
+launch_step2d_m(const StepArgs & a, int ctas_per_sm, cudaStream_t s, int * launches)
+{
+  cudaError_t e = a.m.fin_tgt ? launch_step2d_kernel_m<B, THINC, STIFF, true>(a, ctas_per_sm, s, launches)
+                              : launch_step2d_kernel_m<B, THINC, STIFF, false>(a, ctas_per_sm, s, launches);
+  if (e != cudaSuccess)
+    return e;
   if (a.m.fin_tgt)
     return e; // the step kernel's tail finished the deferred cells
   if (a.m.n_defer > 0 && a.reflux_layout == 1)
@@ -91,47 +101,13 @@ occupancy2d_m()
   one((const void *)step2d_kernel<B, true, true, 1>);
   one((const void *)step2d_kernel<B, true, false, 2>);
   one((const void *)step2d_kernel<B, true, true, 2>);
+  one((const void *)step2d_kernel<B, true, false, 0, true>);
+  one((const void *)step2d_kernel<B, true, false, 1, true>);
+  one((const void *)step2d_kernel<B, true, true, 0, true>);
+  one((const void *)step2d_kernel<B, true, true, 1, true>);
+  one((const void *)step2d_kernel<B, true, false, 2, true>);
+  one((const void *)step2d_kernel<B, true, true, 2, true>);
   return occ;
-}
-
-template <int THINC, int STIFF>
-static cudaError_t
-launch_step3d_m(const StepArgs & a, int ctas_per_sm, cudaStream_t s, int * launches)
-{
-  using T = Step3DTraits<true>;
-  static bool configured = false;
-  static int  occ = 1;
-  if (!configured)
-  {
-    cudaError_t e = cudaFuncSetAttribute(step3d_kernel<true, THINC, STIFF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::smem_bytes);
-    if (e != cudaSuccess)
-      return e;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, step3d_kernel<true, THINC, STIFF>, T::NT, T::smem_bytes);
-    if (occ < 1)
-      occ = 1;
-    configured = true;
-  }
-  const int per_sm = (ctas_per_sm > 0 && ctas_per_sm < occ) ? ctas_per_sm : occ;
-  int       grid = num_sms_m() * per_sm;
-  if (grid > step_count(a))
-    grid = step_count(a);
-  cudaError_t e = cudaSuccess;
-  if (grid >= 1)
-  {
-    step3d_kernel<true, THINC, STIFF><<<grid, T::NT, T::smem_bytes, s>>>(a);
-    ++*launches;
-    e = cudaGetLastError();
-    if (e != cudaSuccess)
-      return e;
-  }
-  if (a.m.n_defer > 0)
-  {
-    const int n = a.m.n_defer * 64;
-    reflux3d_kernel<true><<<(n + 31) / 32, 32, 0, s>>>(a);
-    ++*launches;
-    e = cudaGetLastError();
-  }
-  return e;
 }
 
 template <int DIM, int B>
@@ -171,17 +147,7 @@ launch_step_mixed(int dim, int b, const StepArgs & a, int ctas_per_sm, cudaStrea
   const int eosk = a.p.mg_any ? 2 : ((a.p.gpx[0] != 0.0 || a.p.gpx[1] != 0.0) ? 1 : 0);
   const int v = (a.p.thinc ? 3 : 0) + eosk;
   if (dim == 3 && b == 8)
-  {
-    switch (v)
-    {
-      case 0: return launch_step3d_m<0, 0>(a, ctas_per_sm, s, launches);
-      case 1: return launch_step3d_m<0, 1>(a, ctas_per_sm, s, launches);
-      case 2: return launch_step3d_m<0, 2>(a, ctas_per_sm, s, launches);
-      case 3: return launch_step3d_m<1, 0>(a, ctas_per_sm, s, launches);
-      case 4: return launch_step3d_m<1, 1>(a, ctas_per_sm, s, launches);
-      default: return launch_step3d_m<1, 2>(a, ctas_per_sm, s, launches);
-    }
-  }
+    return launch_step3d_mixed_case(v, a, ctas_per_sm, s, launches);
   if (dim == 2 && b == 16)
   {
     switch (v)
@@ -217,23 +183,7 @@ step_max_ctas_per_sm_mixed(int dim, int b)
   if (dim == 2 && b == 8)
     return occupancy2d_m<8>();
   if (dim == 3 && b == 8)
-  {
-    using T = Step3DTraits<true>;
-    int  occ = 1 << 20;
-    auto one = [&](const void * k) {
-      cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::smem_bytes);
-      int o = 0;
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k, T::NT, T::smem_bytes);
-      occ = o < occ ? o : occ;
-    };
-    one((const void *)step3d_kernel<true, 0, 0>);
-    one((const void *)step3d_kernel<true, 0, 1>);
-    one((const void *)step3d_kernel<true, 1, 0>);
-    one((const void *)step3d_kernel<true, 1, 1>);
-    one((const void *)step3d_kernel<true, 0, 2>);
-    one((const void *)step3d_kernel<true, 1, 2>);
-    return occ;
-  }
+    return step_max_ctas_per_sm_mixed3d();
   return 0;
 }
 

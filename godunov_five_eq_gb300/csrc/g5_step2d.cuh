@@ -638,8 +638,10 @@ finish_deferred_2d(const StepArgs & a, int j)
 // THINC, STIFF: the FP32-bulk form is compiled with and without the THINC
 // reconstruction and the stiffened-gas pressure path (P picks the kernel), so
 // a kernel carries only the code its case runs; the FP64 form tests both at
-// run time (STIFF = -1)
-template <int B, bool MIXED, bool THINC = false, int STIFF = -1>
+// run time (STIFF = -1).  FUSED: the FP32-bulk form finishing the coarse/fine
+// records in its tail (m.fin_tgt set; the kernel without it keeps the plain
+// block loop)
+template <int B, bool MIXED, bool THINC = false, int STIFF = -1, bool FUSED = false>
 __global__ void __launch_bounds__(B * B, MIXED ? (B == 16 ? 4 : 8) : (B == 16 ? 2 : 8))
 step2d_kernel(StepArgs a)
 {
@@ -667,7 +669,7 @@ step2d_kernel(StepArgs a)
   const int eosk = STIFF < 0 ? (P.mg_any ? 2 : ((P.gpx[0] != 0.0 || P.gpx[1] != 0.0) ? 1 : 0)) : STIFF;
 
   const int nwalk = step_count(a);
-  // reflux in the tail (FP32-bulk form, m.fin_tgt set): after its step a
+  // reflux in the tail (FP32-bulk form, FUSED, m.fin_tgt set): after its step a
   // block counts itself off the counters of the deferred blocks whose records
   // it completes (its own and those of the coarser blocks it publishes to);
   // a CTA out of blocks claims deferred blocks by ticket and counts a claim
@@ -675,7 +677,7 @@ step2d_kernel(StepArgs a)
   // cells.  Release: the barrier orders the CTA's writes before the counting
   // thread's device-scope fence and atomic; acquire: that thread's fence
   // after the atomic, then the barrier.
-  const bool fused = MIXED && a.m.fin_tgt != nullptr;
+  constexpr bool fused = MIXED && FUSED;
   for (int iw = blockIdx.x;;)
   {
     int next = iw;
