@@ -529,6 +529,15 @@ def measure(name, args, world, local, flush, stream, steps, clocks=True, want_l1
     bpc = BYTES_PER_CELL_2D if t.dim == 2 else BYTES_PER_CELL_3D
     achieved = cells * bpc / kern_s / 1e9
     traffic = ncu_traffic(name, "mixed", cells)
+    # the coarse/fine record pass runs only where a face has a finer neighbour
+    faces = [3, 5, 1, 7] if t.dim == 2 else [12, 14, 10, 16, 4, 22]
+    has_records = bool((t.nbr_rel[: t.n_owned][:, faces] > 0).any())
+    if t.dim == 2:
+        kernel_label = "step2d_kernel<16,mixed>" + (
+            ("" if not has_records else " (+reflux in its tail)" if res["mixed"]["shape"].get("reflux_layout") == 2 else " (+reflux2d)")
+        )
+    else:
+        kernel_label = "step3d_kernel<mixed>" + (" (+reflux3d)" if has_records else "")
     out["roofline"] = {
         "bound": "hbm",
         "achieved": achieved,
@@ -538,9 +547,7 @@ def measure(name, args, world, local, flush, stream, steps, clocks=True, want_l1
         "traffic": traffic,
         "traffic_source": (f"committed ncu capture profiles/{PROFILE_OF[name][0]} (dram read + write bytes per launch), scaled by cells" if traffic else None),
         "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback 6.8 TB/s",
-        "kernel": ("step2d_kernel<16,mixed> (+reflux in its tail)" if res["mixed"]["shape"].get("reflux_layout") == 2 else "step2d_kernel<16,mixed> (+reflux2d)")
-        if t.dim == 2
-        else "step3d_kernel<mixed> (+reflux3d)",
+        "kernel": kernel_label,
         "kernel_ms": res["mixed"]["kern_ms"],
         "algorithmic_bytes_per_launch": cells * bpc,
         "fp64_kernel_ms": res["fp64"]["kern_ms"],
