@@ -1131,6 +1131,32 @@ two_sum(float a, float b, float & hi, float & lo)
   lo = __fadd_rn(__fsub_rn(a, __fsub_rn(hi, bb)), __fsub_rn(b, bb));
 }
 
+// The same two transformations on two independent pairs at once, with the
+// packed FP32x2 arithmetic of sm_100+ (one issue slot for both lanes; each
+// lane rounds to nearest like the scalar form, so the results are the scalar
+// ones bit for bit).  x - y is formed as fma(y, -1, x), exact in its product.
+__device__ __forceinline__ float2
+fsub2_rn(float2 x, float2 y)
+{
+  return __ffma2_rn(y, make_float2(-1.0f, -1.0f), x);
+}
+
+__device__ __forceinline__ void
+two_diff2(float2 a, float2 b, float2 & hi, float2 & lo)
+{
+  hi = fsub2_rn(a, b);
+  const float2 bb = fsub2_rn(a, hi);
+  lo = __fadd2_rn(fsub2_rn(a, __fadd2_rn(hi, bb)), fsub2_rn(bb, b));
+}
+
+__device__ __forceinline__ void
+two_sum2(float2 a, float2 b, float2 & hi, float2 & lo)
+{
+  hi = __fadd2_rn(a, b);
+  const float2 bb = fsub2_rn(hi, a);
+  lo = __fadd2_rn(fsub2_rn(a, fsub2_rn(hi, bb)), fsub2_rn(b, bb));
+}
+
 // ordered comparisons of doubles against positive constants on the integer
 // pipe (IEEE doubles order like sign-magnitude integers; NaN never clamps to 0)
 __device__ __forceinline__ bool

@@ -592,8 +592,13 @@ update_mixed(const double * uin, double * u2, const float * sFx, const float * s
 #pragma unroll
   for (int k = 0; k < 5; ++k)
   {
-    two_diff(sFx[ks[k] * NFF + ilx], sFx[ks[k] * NFF + irx], h[0][k], l[0][k]);
-    two_diff(sFy[ks[k] * NFF + ily], sFy[ks[k] * NFF + iry], h[1][k], l[1][k]);
+    // both directions in one packed transformation
+    float2 hi, lo;
+    two_diff2(make_float2(sFx[ks[k] * NFF + ilx], sFy[ks[k] * NFF + ily]), make_float2(sFx[ks[k] * NFF + irx], sFy[ks[k] * NFF + iry]), hi, lo);
+    h[0][k] = hi.x;
+    h[1][k] = hi.y;
+    l[0][k] = lo.x;
+    l[1][k] = lo.y;
   }
   float dA[2][2];
   {
