@@ -935,16 +935,29 @@ step3d_kernel(StepArgs a)
         }
         else
         {
-          two_diff(sFd[H::FR0 * NFF + il], sFd[H::FR0 * NFF + ir], hh[dir][0], ll[dir][0]);
-          two_diff(sFd[H::FR1 * NFF + il], sFd[H::FR1 * NFF + ir], hh[dir][1], ll[dir][1]);
+          // two variables per packed FP32x2 transformation (bit-identical to
+          // the scalar form): the partial densities, then (E, rho u) and
+          // (rho v, rho w)
+          {
+            float2 h, l;
+            two_diff2(make_float2(sFd[H::FR0 * NFF + il], sFd[H::FR1 * NFF + il]), make_float2(sFd[H::FR0 * NFF + ir], sFd[H::FR1 * NFF + ir]), h, l);
+            hh[dir][0] = h.x;
+            hh[dir][1] = h.y;
+            ll[dir][0] = l.x;
+            ll[dir][1] = l.y;
+          }
           const int ke[4] = { H::FE, H::FU, H::FV, H::FW };
 #pragma unroll
-          for (int e = 0; e < 4; ++e)
+          for (int e = 0; e < 4; e += 2)
           {
-            float h, l, t;
-            two_diff(sFd[ke[e] * NFF + il], sFd[ke[e] * NFF + ir], h, l);
-            two_sum(es[e], h, es[e], t);
-            et[e] += t + l;
+            float2 h, l, s, t;
+            two_diff2(make_float2(sFd[ke[e] * NFF + il], sFd[ke[e + 1] * NFF + il]), make_float2(sFd[ke[e] * NFF + ir], sFd[ke[e + 1] * NFF + ir]), h, l);
+            two_sum2(make_float2(es[e], es[e + 1]), h, s, t);
+            const float2 tl = __fadd2_rn(make_float2(et[e], et[e + 1]), __fadd2_rn(t, l));
+            es[e] = s.x;
+            es[e + 1] = s.y;
+            et[e] = tl.x;
+            et[e + 1] = tl.y;
           }
           const float usl = sFd[H::FUS * NFF + il], usr = sFd[H::FUS * NFF + ir];
           dA[dir][0] = ((sFd[H::FA0 * NFF + il] - usl * a0f) - sFd[H::FA0 * NFF + ir]) + usr * a0f;
