@@ -602,6 +602,25 @@ slope_scalar(R q, R qPlus, R qMinus, R slope_type)
   return dq;
 }
 
+// slope_scalar of two independent (q, qPlus, qMinus) triples at once (FP32):
+// its differences and products on the packed FP32x2 pipe of sm_100+, each
+// lane rounded as the scalar operation is; |.|, min and the selects per lane
+__device__ __forceinline__ float2
+slope_pair(float2 q, float2 qPlus, float2 qMinus, float slope_type)
+{
+  if (!(slope_type == 1.0f || slope_type == 2.0f))
+    return make_float2(0.0f, 0.0f);
+  const float2 st = make_float2(slope_type, slope_type);
+  const float2 dlft = __fmul2_rn(st, __ffma2_rn(qMinus, make_float2(-1.0f, -1.0f), q));
+  const float2 drgt = __fmul2_rn(st, __ffma2_rn(q, make_float2(-1.0f, -1.0f), qPlus));
+  const float2 dcen = __fmul2_rn(make_float2(0.5f, 0.5f), __ffma2_rn(qMinus, make_float2(-1.0f, -1.0f), qPlus));
+  const float2 pr = __fmul2_rn(dlft, drgt);
+  const float2 sg = make_float2(dcen.x >= 0.0f ? 1.0f : -1.0f, dcen.y >= 0.0f ? 1.0f : -1.0f);
+  const float2 m = make_float2(fminf(pr.x <= 0.0f ? 0.0f : fminf(fabsf(dlft.x), fabsf(drgt.x)), fabsf(dcen.x)),
+                               fminf(pr.y <= 0.0f ? 0.0f : fminf(fabsf(dlft.y), fabsf(drgt.y)), fabsf(dcen.y)));
+  return __fmul2_rn(sg, m);
+}
+
 // ---------------------------------------------------------------------------
 // tanh: same algorithm as the oracle (Cody-Waite reduced Taylor expm1),
 // FP64, bit-reproducible on IEEE hardware without contraction.

@@ -330,15 +330,34 @@ face_state3(const typename Step3DTraits<MIXED>::R * sQ,
   }
   const bool hancock = P.integrator == 0;
   const R    off = R(0.5) * R(side);
-#pragma unroll
-  for (int k = 0; k < 6; ++k)
+  if constexpr (MIXED)
   {
-    const R * Qk = sQ + k * GGG;
-    const R   qc = Qk[gi];
-    const R   dq = slope_at<R>(Qk, gi, o, st);
-    R         t = qc + off * dq;
-    if constexpr (!MIXED)
+    // two components per packed slope evaluation
+#pragma unroll
+    for (int k = 0; k < 6; k += 2)
     {
+      const R *    Q0 = sQ + k * GGG;
+      const R *    Q1 = Q0 + GGG;
+      const float2 qc = make_float2(Q0[gi], Q1[gi]);
+      const float2 dq = slope_pair(qc, make_float2(Q0[gi + o], Q1[gi + o]), make_float2(Q0[gi - o], Q1[gi - o]), st);
+      q[k] = qc.x + off * dq.x;
+      q[k + 1] = qc.y + off * dq.y;
+      if (hancock)
+      {
+        q[k] += sHS[k * SSS + si];
+        q[k + 1] += sHS[(k + 1) * SSS + si];
+      }
+    }
+  }
+  else
+  {
+#pragma unroll
+    for (int k = 0; k < 6; ++k)
+    {
+      const R * Qk = sQ + k * GGG;
+      const R   qc = Qk[gi];
+      const R   dq = slope_at<R>(Qk, gi, o, st);
+      R         t = qc + off * dq;
       // the reference adds the zero-offset terms of the other directions,
       // ((q + o_x dq_x) + o_y dq_y) + o_z dq_z; they can only change the sign
       // of a zero, so they are evaluated only when a negative zero occurs
@@ -351,10 +370,10 @@ face_state3(const typename Step3DTraits<MIXED>::R * sQ,
         const R o0 = dir == 0 ? off : R(0), o1 = dir == 1 ? off : R(0), o2 = dir == 2 ? off : R(0);
         t = qc + o0 * dd[0] + o1 * dd[1] + o2 * dd[2];
       }
+      q[k] = t;
+      if (hancock)
+        q[k] += sHS[k * SSS + si];
     }
-    q[k] = t;
-    if (hancock)
-      q[k] += sHS[k * SSS + si];
   }
   const R a0 = sQ[6 * GGG + gi];
   q[6] = a0;
@@ -746,8 +765,18 @@ step3d_kernel(StepArgs a)
         {
           const R * Qk = sQ + k * GGG;
           q[k] = Qk[gi];
-          dq[0][k] = slope_at<R>(Qk, gi, 1, st);
-          dq[1][k] = slope_at<R>(Qk, gi, G, st);
+          if constexpr (MIXED)
+          {
+            // x and y in one packed evaluation, z alone
+            const float2 d = slope_pair(make_float2(q[k], q[k]), make_float2(Qk[gi + 1], Qk[gi + G]), make_float2(Qk[gi - 1], Qk[gi - G]), st);
+            dq[0][k] = d.x;
+            dq[1][k] = d.y;
+          }
+          else
+          {
+            dq[0][k] = slope_at<R>(Qk, gi, 1, st);
+            dq[1][k] = slope_at<R>(Qk, gi, G, st);
+          }
           dq[2][k] = slope_at<R>(Qk, gi, GG, st);
         }
         const R a0 = sQ[6 * GGG + gi];
