@@ -426,6 +426,7 @@ g5_create(const G5Params * params, G5Context ** out_ctx)
   if (!g5::eos_params_valid(params))
     return G5_ERR_ARG;
   G5Context * c = new G5Context;
+  c->shape[G5_MODE_FP64].reflux = 0; // the FP64 form has one record pass (the tuner's choice too)
   c->prm = *params;
   c->dim = params->dim;
   c->b = params->bsize;

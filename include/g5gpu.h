@@ -334,10 +334,11 @@ int g5_tune_pick(const float * ms, int n, int default_index, float margin);
 
 /* The launch shape a mode uses: out4 = {CTAs per SM, claim, walk order,
  * reflux layout (0: a separate pass, 8 lanes per deferred cell; 1: a separate
- * pass, one thread per cell; 2 (the default): 8 lanes per cell in the step
- * kernel's tail, by the CTAs out of blocks, where the FP32-bulk 2D full-mesh
- * step has coarse/fine records, otherwise as 0; the FP64 form and 3D take a
- * separate pass with one thread per cell)}. */
+ * pass, one thread per cell; 2 (the FP32-bulk form's default): 8 lanes per
+ * cell in the step kernel's tail, by the CTAs out of blocks, where the
+ * FP32-bulk 2D full-mesh step has coarse/fine records, otherwise as 0; the
+ * FP64 form (default 0) and 3D take a separate pass with one thread per
+ * cell whatever the layout)}. */
 int g5_tune_choice(const G5Context * ctx, int mode, int32_t * out4);
 
 /* The candidates and their times (ms per step) of the last g5_tune of a mode:
