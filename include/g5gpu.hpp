@@ -16,6 +16,8 @@
 //   compute_derived_quantity(U, q, o)  ComputeDerivedQuantities (output path)
 //   pack_output_fields(U, f, n, out)   the datasets of one output, packed in one pass
 //   do_time_step_host(hU, hU2, dt)     do_time_step on host-resident arrays
+//   tune(U, U2), tune_choice(), set_shape(s)  launch shape of the step (no
+//                                      counterpart: the reference's policies are fixed)
 // Errors from the C ABI are thrown as g5::Error (the reference aborts).
 #pragma once
 
@@ -347,6 +349,31 @@ public:
 
   //! device status word (G5_STATUS_* bits), cleared by the read
   int status() { return g5_status(m_ctx, m_stream); }
+
+  //! launch shape of the step for the current mesh and the context's mode:
+  //! every candidate timed on U -> U2 (U2 overwritten, the stream
+  //! synchronised), the fastest kept; returns {CTAs per SM, claim, walk, reflux layout}
+  std::vector<int32_t> tune(const g5::BlockArray & U, const g5::BlockArray & U2)
+  {
+    g5::check(g5_tune(m_ctx, U.data, U2.data, m_mode, m_stream), "g5_tune");
+    return tune_choice();
+  }
+
+  //! the launch shape in use for the context's mode
+  std::vector<int32_t> tune_choice() const
+  {
+    std::vector<int32_t> s(4);
+    g5::check(g5_tune_choice(m_ctx, m_mode, s.data()), "g5_tune_choice");
+    return s;
+  }
+
+  //! set the launch shape by hand ({CTAs per SM (0: occupancy maximum), claim, walk, reflux layout})
+  void set_shape(const std::vector<int32_t> & shape4)
+  {
+    if (shape4.size() != 4)
+      throw g5::Error(G5_ERR_ARG, "set_shape: four values");
+    g5::check(g5_set_shape(m_ctx, m_mode, shape4.data()), "g5_set_shape");
+  }
 
   G5Context * context() const { return m_ctx; }
 
