@@ -486,7 +486,8 @@ g5_destroy(G5Context * ctx)
 extern "C" int
 g5_set_mesh(G5Context * c, const G5Mesh * m)
 {
-  if (!c || !m || m->n_owned < 0 || m->n_outside < 0 || !m->level || !m->coord)
+  // (a table without blocks, a rank that owns none, may pass NULL arrays)
+  if (!c || !m || m->n_owned < 0 || m->n_outside < 0 || (m->n_owned + m->n_outside > 0 && (!m->level || !m->coord)))
     return G5_ERR_ARG;
   if (m->n_owned > 0 && (!m->nbr || !m->nbr_rel))
     return G5_ERR_ARG;

@@ -147,7 +147,9 @@ int g5_destroy(G5Context * ctx);
 
 /* Upload a block table and size the scratch memory: mirrors
  * GodunovImplemV0::resize_auxiliary_data (scheme/GodunovImplemV0.cpp:37-61).
- * Synchronous (allocates); call it outside stream capture. */
+ * Synchronous (allocates); call it outside stream capture.  A table without
+ * blocks (a rank that owns none) is accepted, its arrays may be NULL; the
+ * calls on it launch nothing (their device pointers must still be non-NULL). */
 int g5_set_mesh(G5Context * ctx, const G5Mesh * mesh);
 
 /* Device bytes held by the context: GodunovImplemBase::total_mem_size_in_bytes
